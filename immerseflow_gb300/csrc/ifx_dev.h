@@ -1,0 +1,98 @@
+// ifx_dev.h -- device-side layout shared by the host orchestration and the
+// CUDA kernels.
+//
+// Every kernel works on a batch of independent instances (a single solve is a
+// batch of one).  Work is described by tile lists: a tile is a 32x8 block of
+// cells of one grid level of one instance; a launch covers all tiles of all
+// instances that take part in a phase.  Per-instance reductions are written
+// as one partial per tile and summed per instance in a fixed order, so an
+// instance gives bit-identical results alone or inside any batch.
+//
+// Field layout in HBM: row-major, i fastest, with the reference's one-cell
+// ghost ring (src/include/ADSolver.cu:10), rows padded to a pitch that is a
+// multiple of 32 elements.  Face velocities live on cell-shaped arrays:
+// U[c] is the east face of cell c, V[c] its north face.
+#pragma once
+#include <cstdint>
+
+namespace ifx {
+
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 8;
+constexpr int TILE_THREADS = TILE_X * TILE_Y;
+constexpr int GHOST_BLOCK = 256;
+constexpr int NPART = 6;            // partial sums per tile
+constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
+constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
+constexpr double COARSE_OMEGA = 1.5;
+
+enum CellType : uint8_t { T_SOLID = 0, T_FLUID = 1, T_GHOST = 2, T_DOMAIN = 3 };
+// per-cell stencil bits: open faces, and (finest level) faces to an IBM ghost
+enum : uint8_t { B_E = 1, B_W = 2, B_N = 4, B_S = 8, G_E = 16, G_W = 32, G_N = 64, G_S = 128 };
+// per-instance iteration state
+enum : int { ST_ACTIVE = 0, ST_FINAL_IN_ALT = 1, ST_DONE = 2 };
+
+struct Tile {
+    int inst;  // instance index
+    int lev;   // index into the LevelDev array
+    int i0, j0;
+};
+
+// One boundary relation q[cell] = c + sum_k w[k] * q[nb[k]].  Domain ghosts
+// (one neighbour) carry the wall/inflow/slip/outflow rule; IBM ghosts carry
+// image-point weights (Dirichlet for u,v; Neumann for p).
+struct GhostDev {
+    int cell, inst, side, adj;  // side: -1 IBM ghost, 0..3 domain side, 4 corner
+    int nb[4];
+    double wu[4], wv[4], wp[4];
+    double cu, cv;               // static constants
+    int qi[2];                   // outflow face values feeding the constant (-1: none)
+    double qf[2];                // ... with these factors
+    int qown;                    // outflow face value owned (updated) by this entry, -1 none
+    double qh;                   // normal spacing for the convective outflow update
+};
+
+struct LevelDev {
+    int NX, NY, nx, ny, pitch;
+    int inst, depth, dirmask;    // dirmask bit s: side s Dirichlet for pressure
+    const double *kx, *ky, *ix, *iy, *dw, *dh;
+    const float *kxf, *kyf, *ixf, *iyf, *dwf, *dhf;
+    const uint8_t* bits;
+    void* e;   // correction, T*
+    void* e2;  // Jacobi partner, T*
+    void* r;   // right-hand side, T*
+    // prolongation tables from the next coarser level into this one
+    const int *pI, *pIn, *pJ, *pJn;
+    const double *pwx, *pwy;
+    const float *pwxf, *pwyf;
+    int child;   // LevelDev index of the next coarser level, -1 at the coarsest
+};
+
+struct InstDev {
+    int NX, NY, nx, ny, pitch;
+    int singular, dirmask, body, lev0, nlev;
+    int tile_beg, tile_cnt;      // level-0 tiles (for per-instance partial sums)
+    int ghost_beg, ghost_cnt;
+    double dt, re, dtre, idt, omega;
+    double ad_lim, ppe_tol;
+    int ad_itermax, ppe_itermax, first_step, mixed_inner;
+    double *u, *v, *u2, *v2, *Us, *Vs, *U, *V, *Nu, *Nv, *ru, *rv, *p, *b, *div, *iblank;
+    const double *dx, *dy, *fx, *gx, *fy, *gy, *xc, *yc, *xf, *yf;
+    const uint8_t* type;
+    const int* gidx;             // cell -> global ghost index (IBM ghosts), -1 otherwise
+    double *qbu, *qbv;
+    // mixed-precision predictor corrections
+    float *du, *dv, *du2, *dv2, *rfu, *rfv;
+    // body (ellipse), bit-exact predicate constants
+    double bcx, bcy, ba, bb, bcs, bsn, bia2, bib2, fref;
+};
+
+// Device-resident per-instance iteration state and diagnostics.
+struct InstState {
+    int pred_state, pred_iters, ppe_state, ppe_iters;
+    int status, pad0, pad1, pad2;
+    double pred_metric, ppe_rel, bmean, rmean, bnorm, pmean;
+    double max_div, cd, cl, flux_in, flux_out, area;
+};
+
+}  // namespace ifx

@@ -1,0 +1,191 @@
+/*
+ * immerseflow_gb300.h -- C ABI of the GB300-native fractional-step / ghost-cell
+ * immersed-boundary solver.
+ *
+ * The reference (ImmerseFlow++) exposes no library API: its boundary is the
+ * executable `main` (src/main.cu:75-102) plus the file surface (inputs.txt,
+ * xgrid/ygrid files, Tecplot outputs).  Each entry point below names the
+ * reference routine it replaces.  All functions return an ifx_status code
+ * instead of calling exit(1) (the reference's CHECK_CUDA_ERROR,
+ * src/header/globalVariables.cuh:91-107).  Host buffers are owned by the
+ * caller, device state by the solver handle.  A handle is used by one host
+ * thread at a time.
+ *
+ * Index convention (same as the reference, src/include/ADSolver.cu:10):
+ *   cells (i,j), i = 0..nx-1 fastest, nx = NX+2 (one ghost layer each side),
+ *   host arrays are dense: q[i + j*nx].
+ *   u faces: uf[i + (j-1)*(nx-1)], i = 0..nx-2, j = 1..ny-2  (east face of cell i)
+ *   v faces: vf[(i-1) + j*(nx-2)], i = 1..nx-2, j = 0..ny-2  (north face of cell j)
+ */
+#ifndef IMMERSEFLOW_GB300_H
+#define IMMERSEFLOW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef int ifx_status;
+#define IFX_OK                 0
+#define IFX_ERR_ARG            1  /* bad argument / size                       */
+#define IFX_ERR_IO             2  /* file cannot be opened or written          */
+#define IFX_ERR_PARSE          3  /* malformed inputs.txt or grid file         */
+#define IFX_ERR_CUDA           4  /* CUDA runtime error (message in last_error) */
+#define IFX_ERR_NOMEM          5  /* device or host allocation failed          */
+#define IFX_ERR_NOT_CONVERGED  6  /* an iteration cap was hit                  */
+#define IFX_ERR_DIVERGED       7  /* NaN/Inf detected in the state             */
+#define IFX_ERR_BUDGET         8  /* request does not fit the HBM budget       */
+#define IFX_ERR_STATE          9  /* call not valid in the current state       */
+#define IFX_ERR_NODEVICE      10  /* no CUDA device                            */
+
+/* ---------------------------------------------------------------- enums */
+#define IFX_MODE_REFERENCE 0  /* ADsolver-only semantics of the reference      */
+#define IFX_MODE_METHOD    1  /* full fractional step: predictor/PPE/projection */
+
+#define IFX_PREC_FP64  0      /* every kernel in FP64                          */
+#define IFX_PREC_MIXED 1      /* FP32 sweeps, FP64 residuals / defect correction */
+
+#define IFX_INIT_VORTEX  0    /* vortex in uniform flow, src/include/preSim.cu:70-73 */
+#define IFX_INIT_UNIFORM 1    /* u = bc_u[W], v = 0 in the fluid               */
+#define IFX_INIT_REST    2    /* u = v = 0                                     */
+
+#define IFX_SIDE_W 0
+#define IFX_SIDE_E 1
+#define IFX_SIDE_S 2
+#define IFX_SIDE_N 3
+
+#define IFX_BC_WALL    0      /* Dirichlet velocity (bc_u, bc_v), Neumann p     */
+#define IFX_BC_INFLOW  1      /* Dirichlet velocity (bc_u, bc_v), Neumann p     */
+#define IFX_BC_OUTFLOW 2      /* convective outflow, Dirichlet p = 0           */
+#define IFX_BC_SLIP    3      /* zero normal velocity, zero shear, Neumann p   */
+
+#define IFX_BODY_NONE    0
+#define IFX_BODY_ELLIPSE 1    /* ellipse / circle: centre, semi-axes a >= b, angle */
+
+#define IFX_FIELD_U        0  /* cell u, nx*ny                                 */
+#define IFX_FIELD_V        1  /* cell v, nx*ny                                 */
+#define IFX_FIELD_P        2  /* cell p, nx*ny                                 */
+#define IFX_FIELD_IBLANK   3  /* 1 fluid / 0 solid as double, nx*ny            */
+#define IFX_FIELD_UF       4  /* u faces, (nx-1)*(ny-2)                         */
+#define IFX_FIELD_VF       5  /* v faces, (nx-2)*(ny-1)                         */
+#define IFX_FIELD_CELLTYPE 6  /* 0 solid, 1 fluid, 2 IBM ghost, 3 domain ghost (as double) */
+#define IFX_FIELD_DIV      7  /* face divergence per fluid cell, nx*ny           */
+#define IFX_FIELD_XC       8  /* cell centres x, nx                             */
+#define IFX_FIELD_YC       9  /* cell centres y, ny                             */
+
+#define IFX_PATH_MAX 512
+
+/* --------------------------------------------------------------- config */
+/*
+ * Fields up to write_interval are the reference's CFDInput
+ * (src/header/globalVariables.cuh:15-33) read by the same keyword grammar
+ * (src/main.cu:10-59).  The rest are extension keywords that the reference
+ * grammar ignores.
+ */
+typedef struct ifx_config {
+    int    restart, restart_time;
+    int    nx, ny;                 /* interior cells, as written in inputs.txt */
+    double lx, ly;
+    int    w_ad, w_ppe, ad_itermax, ppe_itermax, ad_solver, ppe_solver;
+    double error_max, tmax, dt, re, mu;
+    int    write_interval;
+
+    int    mode;                   /* IFX_MODE_*                                */
+    int    precision;              /* IFX_PREC_*                                */
+    int    init;                   /* IFX_INIT_*                                */
+    int    bc_type[4];             /* per side W,E,S,N: IFX_BC_*                */
+    double bc_u[4], bc_v[4];       /* Dirichlet values per side                 */
+    double outflow_uc;             /* convective outflow speed                  */
+    int    body;                   /* IFX_BODY_*                                */
+    double body_cx, body_cy, body_a, body_b, body_angle_deg;
+    double ppe_tol;                /* method mode: ||r||_2 <= ppe_tol*||b||_2    */
+    double ad_tol;                 /* method mode: mean |Jacobi update| bound   */
+    int    mg_pre, mg_post;        /* multigrid smoothing sweeps                */
+    double mg_omega;               /* weighted-Jacobi factor                    */
+    int    mixed_inner;            /* FP32 predictor sweeps per FP64 residual   */
+    double force_ref_u, force_ref_len;   /* drag/lift normalisation          */
+    char   xgrid[IFX_PATH_MAX];    /* face-coordinate files (<idx> <coord>)     */
+    char   ygrid[IFX_PATH_MAX];
+} ifx_config;
+
+/* Per-instance statistics of the last ifx_step call. */
+typedef struct ifx_stats {
+    long long steps;               /* time steps done since creation            */
+    int    last_ad_iters;          /* predictor sweeps in the last step         */
+    int    last_ppe_iters;         /* PPE iterations (outer) in the last step   */
+    double last_ad_metric;         /* final predictor metric                    */
+    double last_ppe_residual;      /* final relative PPE residual               */
+    double max_div;                /* max |div U| over fluid cells after projection */
+    double cd, cl;                 /* drag and lift coefficients                */
+    double mass_flux_in, mass_flux_out;
+    long long ad_iters_total, ppe_iters_total;
+    long long kernel_launches;     /* kernels of this library launched so far   */
+    int    n_fluid, n_ibm_ghost, mg_levels;
+    int    status;                 /* sticky per-instance status (IFX_*)         */
+} ifx_stats;
+
+/* ------------------------------------------------------ library / errors */
+const char* ifx_status_string(ifx_status s);
+/* Message of the last failing call on this host thread. */
+const char* ifx_last_error(void);
+/* Library version string. */
+const char* ifx_version(void);
+
+/* ---------------------------------------------------------- file surface */
+/* Defaults = the reference's inputs/inputs.txt values, mode REFERENCE. */
+void       ifx_config_default(ifx_config* cfg);
+/* readInputFile (src/main.cu:10-59): keyword line, values on the next line.
+ * Grid paths default to xgrid.dat2 / ygrid.dat2 beside the inputs file
+ * (src/include/preSim.cu:268,281). */
+ifx_status ifx_config_read(const char* inputs_path, ifx_config* cfg);
+/* Grid-file loop of readGridData (src/include/preSim.cu:267-291):
+ * reads n lines "<index> <coordinate>". */
+ifx_status ifx_grid_read(const char* path, int n, double* coords);
+/* write_results_to_file (src/include/postSim.cu:41-66): Tecplot ASCII POINT. */
+ifx_status ifx_write_tecplot(const char* path, int nx, int ny, const double* x,
+                             const double* y, const double* q);
+
+/* ----------------------------------------------------------------- solver */
+typedef struct ifx_solver ifx_solver;
+
+/* allocation + readGridData + initializeData (src/main.cu:86-90,
+ * src/include/preSim.cu:147-240).  xf has cfg->nx+1 entries, yf cfg->ny+1. */
+ifx_status ifx_create(const ifx_config* cfg, const double* xf, const double* yf,
+                      ifx_solver** out);
+/* Same, reading inputs.txt and the grid files it names. */
+ifx_status ifx_create_from_file(const char* inputs_path, ifx_solver** out);
+/* Batched solver: n independent instances of uneven size, advanced together
+ * (no reference counterpart; the reference runs one instance per process). */
+ifx_status ifx_create_batch(int n, const ifx_config* cfgs, const double* const* xfs,
+                            const double* const* yfs, ifx_solver** out);
+int        ifx_num_instances(const ifx_solver* s);
+
+/* One reference time step is ImmerseFlow::ADsolver (src/include/ADSolver.cu:268-395)
+ * in REFERENCE mode; in METHOD mode it is predictor -> PPE -> projection. */
+ifx_status ifx_step(ifx_solver* s, int nsteps);
+/* ImmerseFlow::PPESolver (src/include/PPESolver.cu:137-205): Jacobi Laplace with
+ * p = 100 on the i=0 and j=0 ghosts, stopped on the signed residual sum. */
+ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
+
+/* Host <-> device field copies (saveDataToFile's D2H, src/include/postSim.cu:10-39). */
+ifx_status ifx_get_field(ifx_solver* s, int field, double* host, size_t n);
+ifx_status ifx_set_field(ifx_solver* s, int field, const double* host, size_t n);
+ifx_status ifx_get_field_i(ifx_solver* s, int inst, int field, double* host, size_t n);
+ifx_status ifx_set_field_i(ifx_solver* s, int inst, int field, const double* host, size_t n);
+/* Writes p.dat, uc.dat, vc.dat, final_results.dat into dir (src/include/postSim.cu:10-66). */
+ifx_status ifx_write_results(ifx_solver* s, const char* dir);
+ifx_status ifx_forces(ifx_solver* s, double* cd, double* cl);
+ifx_status ifx_get_stats(ifx_solver* s, int inst, ifx_stats* out);
+/* Device milliseconds of the last ifx_step call, timed with CUDA events on
+ * the solver's own stream. */
+ifx_status ifx_last_step_ms(ifx_solver* s, double* ms);
+ifx_status ifx_synchronize(ifx_solver* s);
+void       ifx_destroy(ifx_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMMERSEFLOW_GB300_H */
