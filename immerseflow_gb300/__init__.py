@@ -1,0 +1,218 @@
+"""GB300-native fractional-step / ghost-cell immersed-boundary solver.
+
+Python side of the C ABI in include/immerseflow_gb300.h.  The compute path is
+libimmerseflow_gb300.so (CUDA kernels for sm_103a + C++ host code); this
+module only loads it with ctypes and converts arrays.  There is no CPU
+fallback: if the library is missing or no GPU is present, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import Config, Stats, default_config
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libimmerseflow_gb300.so")
+_lib = None
+
+# every entry point of include/immerseflow_gb300.h with (restype, argtypes)
+_dp = C.POINTER(C.c_double)
+_SIGS = {
+    "ifx_status_string": (C.c_char_p, [C.c_int]),
+    "ifx_last_error": (C.c_char_p, []),
+    "ifx_version": (C.c_char_p, []),
+    "ifx_config_default": (None, [C.POINTER(Config)]),
+    "ifx_config_read": (C.c_int, [C.c_char_p, C.POINTER(Config)]),
+    "ifx_grid_read": (C.c_int, [C.c_char_p, C.c_int, _dp]),
+    "ifx_write_tecplot": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp, _dp, _dp]),
+    "ifx_create": (C.c_int, [C.POINTER(Config), _dp, _dp, C.POINTER(C.c_void_p)]),
+    "ifx_create_from_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "ifx_create_batch": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(_dp), C.POINTER(_dp),
+                                   C.POINTER(C.c_void_p)]),
+    "ifx_num_instances": (C.c_int, [C.c_void_p]),
+    "ifx_get_dims": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ifx_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_ppe_reference": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_get_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t]),
+    "ifx_set_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t]),
+    "ifx_get_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),
+    "ifx_set_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),
+    "ifx_write_results": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ifx_forces": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "ifx_get_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Stats)]),
+    "ifx_last_step_ms": (C.c_int, [C.c_void_p, _dp]),
+    "ifx_get_ibm_ghosts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_synchronize": (C.c_int, [C.c_void_p]),
+    "ifx_destroy": (None, [C.c_void_p]),
+}
+
+
+class IFXError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m immerseflow_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(st):
+    if st != capi.IFX_OK:
+        raise IFXError(st, lib().ifx_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def config_read(path):
+    """readInputFile (src/main.cu:10-59) with the extension keywords."""
+    c = Config()
+    _check(lib().ifx_config_read(os.fsencode(path), C.byref(c)))
+    return c
+
+
+def grid_read(path, n):
+    out = np.zeros(n)
+    _check(lib().ifx_grid_read(os.fsencode(path), n, _dptr(out)))
+    return out
+
+
+def write_tecplot(path, x, y, q):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    _check(lib().ifx_write_tecplot(os.fsencode(path), len(x), len(y), _dptr(x), _dptr(y), _dptr(q)))
+
+
+class Solver:
+    """One solver handle: a single instance, or a batch of instances."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def create(cls, cfg, xf, yf):
+        xf = np.ascontiguousarray(xf, np.float64)
+        yf = np.ascontiguousarray(yf, np.float64)
+        h = C.c_void_p()
+        _check(lib().ifx_create(C.byref(cfg), _dptr(xf), _dptr(yf), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_file(cls, inputs_path):
+        h = C.c_void_p()
+        _check(lib().ifx_create_from_file(os.fsencode(inputs_path), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def batch(cls, cfgs, xfs, yfs):
+        n = len(cfgs)
+        carr = (Config * n)(*cfgs)
+        xs = [np.ascontiguousarray(x, np.float64) for x in xfs]
+        ys = [np.ascontiguousarray(y, np.float64) for y in yfs]
+        xp = (_dp * n)(*[_dptr(x) for x in xs])
+        yp = (_dp * n)(*[_dptr(y) for y in ys])
+        h = C.c_void_p()
+        _check(lib().ifx_create_batch(n, carr, xp, yp, C.byref(h)))
+        s = cls(h.value)
+        s._keep = (xs, ys)
+        return s
+
+    @property
+    def n_instances(self):
+        return lib().ifx_num_instances(self._h)
+
+    def step(self, n=1):
+        _check(lib().ifx_step(self._h, n))
+
+    def ppe_reference(self):
+        it = C.c_int(0)
+        _check(lib().ifx_ppe_reference(self._h, C.byref(it)))
+        return it.value
+
+    def get(self, field, inst=0):
+        """Copy a field to the host; cell fields come back as [ny, nx]."""
+        nx, ny = self.grid_dims(inst)
+        shp = {capi.FIELD_UF: (ny - 2, nx - 1), capi.FIELD_VF: (ny - 1, nx - 2),
+               capi.FIELD_XC: (nx,), capi.FIELD_YC: (ny,)}.get(field, (ny, nx))
+        out = np.zeros(int(np.prod(shp)))
+        _check(lib().ifx_get_field_i(self._h, inst, field, _dptr(out), out.size))
+        return out.reshape(shp)
+
+    def set(self, field, arr, inst=0):
+        a = np.ascontiguousarray(arr, np.float64).ravel()
+        _check(lib().ifx_set_field_i(self._h, inst, field, _dptr(a), a.size))
+
+    def grid_dims(self, inst=0):
+        """(nx, ny) including the ghost ring."""
+        nx = C.c_int()
+        ny = C.c_int()
+        _check(lib().ifx_get_dims(self._h, inst, C.byref(nx), C.byref(ny)))
+        return nx.value, ny.value
+
+    def stats(self, inst=0):
+        st = Stats()
+        _check(lib().ifx_get_stats(self._h, inst, C.byref(st)))
+        return st
+
+    def ibm_ghosts(self, inst=0):
+        """IBM ghost table: cells, nb[4], Dirichlet weights, Neumann weights, BI/IP (dense indices)."""
+        n = C.c_int()
+        _check(lib().ifx_get_ibm_ghosts(self._h, inst, 0, None, None, None, None, None, C.byref(n)))
+        k = n.value
+        cells = np.zeros(k, np.int32)
+        nb = np.zeros(4 * k, np.int32)
+        wu, wp, bip = np.zeros(4 * k), np.zeros(4 * k), np.zeros(4 * k)
+        _check(lib().ifx_get_ibm_ghosts(self._h, inst, k, cells.ctypes.data, nb.ctypes.data, wu.ctypes.data,
+                                        wp.ctypes.data, bip.ctypes.data, C.byref(n)))
+        return cells, nb.reshape(k, 4), wu.reshape(k, 4), wp.reshape(k, 4), bip.reshape(k, 4)
+
+    def forces(self):
+        cd = C.c_double()
+        cl = C.c_double()
+        _check(lib().ifx_forces(self._h, C.byref(cd), C.byref(cl)))
+        return cd.value, cl.value
+
+    def last_step_ms(self):
+        ms = C.c_double()
+        _check(lib().ifx_last_step_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def write_results(self, directory):
+        _check(lib().ifx_write_results(self._h, os.fsencode(directory)))
+
+    def synchronize(self):
+        _check(lib().ifx_synchronize(self._h))
+
+    def close(self):
+        if self._h:
+            lib().ifx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+from .interface import ImmerseFlow  # noqa: E402  (mirror of the reference object)
+
+__all__ = ["Config", "Stats", "default_config", "Solver", "ImmerseFlow", "IFXError", "config_read",
+           "grid_read", "write_tecplot", "lib", "capi"]

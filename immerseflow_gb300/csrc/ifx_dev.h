@@ -66,6 +66,7 @@ struct LevelDev {
     const double *pwx, *pwy;
     const float *pwxf, *pwyf;
     int child;   // LevelDev index of the next coarser level, -1 at the coarsest
+    int parent;  // LevelDev index of the next finer level, -1 at the finest
 };
 
 struct InstDev {
@@ -75,9 +76,12 @@ struct InstDev {
     int ghost_beg, ghost_cnt;
     double dt, re, dtre, idt, omega;
     double ad_lim, ppe_tol;
-    int ad_itermax, ppe_itermax, first_step, mixed_inner;
+    int ad_itermax, ppe_itermax, n_fluid, mixed_inner;
+    double uc;                   // convective outflow speed
+    double area;                 // sum of fluid-cell areas
     double *u, *v, *u2, *v2, *Us, *Vs, *U, *V, *Nu, *Nv, *ru, *rv, *p, *b, *div, *iblank;
     const double *dx, *dy, *fx, *gx, *fy, *gy, *xc, *yc, *xf, *yf;
+    const double *kx, *ky, *ix, *iy;   // finest-level face coefficients and 1/width
     const uint8_t* type;
     const int* gidx;             // cell -> global ghost index (IBM ghosts), -1 otherwise
     double *qbu, *qbv;
@@ -90,9 +94,18 @@ struct InstDev {
 // Device-resident per-instance iteration state and diagnostics.
 struct InstState {
     int pred_state, pred_iters, ppe_state, ppe_iters;
-    int status, pad0, pad1, pad2;
+    int status, have_nold, pad1, pad2;
     double pred_metric, ppe_rel, bmean, rmean, bnorm, pmean;
-    double max_div, cd, cl, flux_in, flux_out, area;
+    double max_div, cd, cl, flux_in, flux_out, spare;
+};
+
+// Loop control for device-side convergence: reduce kernels vote, the last
+// block publishes the result (and sets the CUDA-graph conditional).
+struct LoopCtl {
+    int active;
+    unsigned int ticket;
+    int result;
+    int pad;
 };
 
 }  // namespace ifx

@@ -1,0 +1,102 @@
+// ifx_host.h -- host-side solver object behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/immerseflow_gb300.h"
+#include "ifx_dev.h"
+
+namespace ifx {
+
+extern thread_local std::string g_last_error;
+ifx_status set_error(ifx_status st, const std::string& msg);
+
+// One multigrid level of one instance, host copy.
+struct HostLevel {
+    int NX = 0, NY = 0, nx = 0, ny = 0, pitch = 0;
+    std::vector<double> dw, dh, xc, yc, kx, ky, ix, iy;
+    std::vector<uint8_t> act, bits;  // pitched
+    std::vector<int> pI, pIn, pJ, pJn;
+    std::vector<double> pwx, pwy;
+    // device
+    double *d_kx = nullptr, *d_ky = nullptr, *d_ix = nullptr, *d_iy = nullptr, *d_dw = nullptr, *d_dh = nullptr;
+    float *d_kxf = nullptr, *d_kyf = nullptr, *d_ixf = nullptr, *d_iyf = nullptr, *d_dwf = nullptr, *d_dhf = nullptr;
+    uint8_t* d_bits = nullptr;
+    void *d_e = nullptr, *d_e2 = nullptr, *d_r = nullptr;
+    int *d_pI = nullptr, *d_pIn = nullptr, *d_pJ = nullptr, *d_pJn = nullptr;
+    double *d_pwx = nullptr, *d_pwy = nullptr;
+    float *d_pwxf = nullptr, *d_pwyf = nullptr;
+};
+
+struct Instance {
+    ifx_config cfg;
+    int NX = 0, NY = 0, nx = 0, ny = 0, pitch = 0;
+    size_t ncell = 0;  // pitch * ny
+    std::vector<double> xf, yf, xc, yc, dx, dy, fx, gx, fy, gy;
+    std::vector<uint8_t> type;       // pitched, after tagging
+    std::vector<HostLevel> lev;
+    int n_fluid = 0, n_ibm = 0, lev_base = 0, tile_beg = 0, tile_cnt = 0, ghost_beg = 0, ghost_cnt = 0;
+    double area = 0.0;
+    bool singular = true;
+    int dirmask = 0;
+    double cs = 1.0, sn = 0.0, ia2 = 1.0, ib2 = 1.0;
+    int qstride = 0;
+    InstDev dev{};                   // device pointers (host copy of the InstDev entry)
+};
+
+}  // namespace ifx
+
+// The opaque handle of the C ABI.
+struct ifx_solver {
+    int mode = IFX_MODE_METHOD;
+    int prec = IFX_PREC_FP64;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    long long launches = 0;
+    std::vector<void*> allocs;       // every device allocation, freed at destroy
+    std::vector<ifx::Instance> inst;
+
+    // batched device tables
+    ifx::InstDev* dI = nullptr;
+    ifx::InstState* dS = nullptr;
+    ifx::InstState* hS = nullptr;    // pinned mirror
+    ifx::LevelDev* dLV = nullptr;
+    ifx::GhostDev* dG = nullptr;
+    int ng = 0, nibm = 0;
+    int* dIbm = nullptr;             // global indices of IBM ghost entries
+    double* dGval = nullptr;         // ghost gather scratch, 3 per entry
+    double* dBiIp = nullptr;         // BI/IP per IBM ghost (diagnostics, tests)
+    ifx::Tile* dT0 = nullptr;        // finest-level tiles of every instance
+    int nt0 = 0;
+    std::vector<ifx::Tile*> dTsm;    // per level >= 1: tiles of instances for which it is a middle level
+    std::vector<int> ntsm;
+    std::vector<ifx::Tile*> dTre;    // per level >= 1: tiles of instances that have the level
+    std::vector<int> ntre;
+    int* dCoarse = nullptr;          // LevelDev index of each instance's coarsest level
+    int lmax = 0;
+    int mg_pre = 2, mg_post = 2;
+    double* dPart = nullptr;         // NPART partials per finest-level tile
+    ifx::LoopCtl* dCtl = nullptr;
+    ifx::LoopCtl* hCtl = nullptr;    // pinned
+
+    // graph execution of one time step (conditional WHILE nodes for the loops)
+    bool use_graph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long graph_nodes_pre = 0, graph_nodes_pred = 0, graph_nodes_mid = 0, graph_nodes_ppe = 0,
+              graph_nodes_post = 0;
+
+    // REFERENCE mode state (one instance, dense rows)
+    double *r_u = nullptr, *r_v = nullptr, *r_ut = nullptr, *r_vt = nullptr, *r_p = nullptr, *r_pt = nullptr;
+    double *r_dx = nullptr, *r_dy = nullptr, *r_xc = nullptr, *r_yc = nullptr, *r_ib = nullptr;
+    double *r_coef = nullptr, *r_sx = nullptr, *r_sy = nullptr, *r_uf = nullptr, *r_vf = nullptr, *r_res = nullptr;
+    double* r_out = nullptr;         // device reduction results (+ ticket)
+    double* h_out = nullptr;         // pinned
+    int r_cur = 0;                   // 0: state in r_u/r_v, 1: in r_ut/r_vt
+    std::vector<int> r_iters;
+    long long steps_done = 0;
+};

@@ -1,0 +1,74 @@
+// ifx_kernels.h -- host-callable launchers of the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ifx_dev.h"
+
+namespace ifx {
+
+// ---- method path (kernels_method.cu)
+cudaError_t launch_step_begin(InstState* S, int n, cudaStream_t s);
+cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStream_t s);
+cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int comps, double* gval,
+                              cudaStream_t s);
+cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
+cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I,
+                              const InstState* S, double* part, int parity, cudaStream_t s);
+cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
+                               LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
+cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
+                            cudaStream_t s);
+cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
+template <typename T>
+cudaError_t launch_ppe_resid(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                             const GhostDev* G, double* part, cudaStream_t s);
+cudaError_t launch_ppe_reduce(const InstDev* I, InstState* S, const double* part, int ninst, LoopCtl* ctl,
+                              unsigned long long handle, cudaStream_t s);
+template <typename T>
+cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          const GhostDev* G, const int* ibm, int nibm, int flags, int src_alt, cudaStream_t s);
+template <typename T>
+cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                            const GhostDev* G, int fine_alt, int init_coarse, cudaStream_t s);
+template <typename T>
+cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
+                           int coarse_alt, cudaStream_t s);
+template <typename T>
+cudaError_t launch_coarse_solve(const int* levs, int n, const LevelDev* LV, const InstDev* I,
+                                const InstState* S, cudaStream_t s);
+cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
+cudaError_t launch_correct(const Tile* t, int nt, const InstDev* I, double* part, cudaStream_t s);
+cudaError_t launch_correct_reduce(const InstDev* I, InstState* S, const double* part, int ninst,
+                                  cudaStream_t s);
+cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_t s);
+
+// ---- immersed-boundary set-up (kernels_ibm.cu, built without FMA contraction)
+cudaError_t launch_tag(const InstDev* I, int inst, int n_cells, uint8_t* type, cudaStream_t s);
+cudaError_t launch_mark_ghosts(const InstDev* I, int inst, int n_interior, uint8_t* type, cudaStream_t s);
+cudaError_t launch_ghost_weights(GhostDev* G, const int* ibm, int nibm, const InstDev* I, double* bi_ip,
+                                 cudaStream_t s);
+
+// ---- reference path (kernels_ref.cu), one instance, dense rows (pitch = nx)
+struct RefDev {
+    int nx, ny;
+    double dt, re;
+    const double *dx, *dy, *iblank;
+    double *aP, *aE, *aW, *aN, *aS, *sx, *sy, *uf, *vf, *res;
+};
+cudaError_t launch_ref_coeffs(const RefDev& R, cudaStream_t s);
+cudaError_t launch_ref_velf(const RefDev& R, const double* u, const double* v, cudaStream_t s);
+cudaError_t launch_ref_bc(const RefDev& R, double* u, double* v, cudaStream_t s);
+cudaError_t launch_ref_source(const RefDev& R, const double* u, const double* v, cudaStream_t s);
+cudaError_t launch_ref_jacobi(const RefDev& R, const double* u, const double* v, double* un, double* vn,
+                              cudaStream_t s);
+// |u_old - u_new| + |v_old - v_new| summed over fluid interior cells -> out[0] (u), out[1] (v)
+cudaError_t launch_ref_resid(const RefDev& R, const double* uo, const double* un, const double* vo,
+                             const double* vn, double* out, cudaStream_t s);
+cudaError_t launch_ref_init(int nx, int ny, const double* xc, const double* yc, double* u, double* v,
+                            double* p, cudaStream_t s);
+// Jacobi Laplace (PPESolver intent): coefficients, BC, sweep, signed residual sum -> out[0]
+cudaError_t launch_ref_ppe_coeffs(const RefDev& R, cudaStream_t s);
+cudaError_t launch_ref_ppe_bc(const RefDev& R, double* p, cudaStream_t s);
+cudaError_t launch_ref_ppe_sweep(const RefDev& R, const double* p, double* pn, double* out, cudaStream_t s);
+
+}  // namespace ifx

@@ -1,0 +1,1367 @@
+// solver.cu -- host orchestration behind the C ABI (include/immerseflow_gb300.h).
+//
+// Replaces the reference's ImmerseFlow object (src/header/globalVariables.cuh:70-88):
+// allocation() + readGridData() + initializeData() become ifx_create*, the
+// per-step ADsolver() becomes ifx_step.  Differences by design:
+//  - all device memory is allocated once at creation (the reference does 11
+//    cudaMalloc/cudaFree per step and 2 per residual reduction);
+//  - one stream per solver, no cudaDeviceSynchronize after each launch;
+//  - convergence loops run on the device: reduce kernels vote and a CUDA
+//    graph with conditional WHILE nodes repeats the loop body, so a time step
+//    is one graph launch with no host round trip (a host-driven loop with the
+//    same semantics is kept for debugging, IFX_NO_GRAPH=1);
+//  - any number of instances of uneven size are advanced together.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ifx_host.h"
+#include "ifx_kernels.h"
+
+using namespace ifx;
+
+namespace {
+
+ifx_status cuerr(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) return set_error(IFX_ERR_NOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+    return set_error(IFX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(x)                                        \
+    do {                                                   \
+        cudaError_t e_ = (x);                              \
+        if (e_ != cudaSuccess) return cuerr(e_, #x);       \
+    } while (0)
+
+#define IFX_TRY(x)                                         \
+    do {                                                   \
+        ifx_status s_ = (x);                               \
+        if (s_ != IFX_OK) return s_;                       \
+    } while (0)
+
+template <typename T>
+ifx_status dalloc(ifx_solver* S, T** out, size_t n) {
+    void* p = nullptr;
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    CUDA_TRY(cudaMalloc(&p, bytes));
+    S->allocs.push_back(p);
+    CUDA_TRY(cudaMemsetAsync(p, 0, bytes, S->stream));
+    *out = (T*)p;
+    return IFX_OK;
+}
+
+template <typename T>
+ifx_status dupload(ifx_solver* S, T** out, const std::vector<T>& h) {
+    IFX_TRY(dalloc(S, out, h.size()));
+    if (!h.empty()) CUDA_TRY(cudaMemcpyAsync(*out, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, S->stream));
+    return IFX_OK;
+}
+
+std::vector<float> to_f(const std::vector<double>& v) {
+    std::vector<float> r(v.size());
+    for (size_t k = 0; k < v.size(); k++) r[k] = (float)v[k];
+    return r;
+}
+
+int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// ------------------------------------------------------------- grid
+
+// Face coordinates -> centres and widths (readGridData, src/include/preSim.cu:293-355;
+// widths are stored 1-D because they are separable).
+void build_grid(Instance& I, const double* xf, const double* yf) {
+    const int nx = I.nx, ny = I.ny;
+    I.xf.assign(xf, xf + I.NX + 1);
+    I.yf.assign(yf, yf + I.NY + 1);
+    I.xc.assign(nx, 0.0);
+    I.yc.assign(ny, 0.0);
+    for (int i = 1; i < nx - 1; i++) I.xc[i] = (xf[i - 1] + xf[i]) / 2.0;
+    for (int j = 1; j < ny - 1; j++) I.yc[j] = (yf[j - 1] + yf[j]) / 2.0;
+    I.xc[0] = -1 * I.xc[1];
+    I.yc[0] = -1 * I.yc[1];
+    I.xc[nx - 1] = xf[nx - 2] + (xf[nx - 2] - I.xc[nx - 2]);
+    I.yc[ny - 1] = yf[ny - 2] + (yf[ny - 2] - I.yc[ny - 2]);
+    I.dx.assign(nx, 0.0);
+    I.dy.assign(ny, 0.0);
+    for (int i = 1; i < nx - 1; i++) I.dx[i] = xf[i] - xf[i - 1];
+    for (int j = 1; j < ny - 1; j++) I.dy[j] = yf[j] - yf[j - 1];
+    I.dx[0] = I.dx[1];
+    I.dx[nx - 1] = I.dx[nx - 2];
+    I.dy[0] = I.dy[1];
+    I.dy[ny - 1] = I.dy[ny - 2];
+    I.fx.assign(nx, 0.0);
+    I.gx.assign(nx, 0.0);
+    I.fy.assign(ny, 0.0);
+    I.gy.assign(ny, 0.0);
+    for (int i = 0; i < nx - 1; i++) {
+        I.fx[i] = I.dx[i] / (I.dx[i] + I.dx[i + 1]);
+        I.gx[i] = I.dx[i + 1] / (I.dx[i] + I.dx[i + 1]);
+    }
+    for (int j = 0; j < ny - 1; j++) {
+        I.fy[j] = I.dy[j] / (I.dy[j] + I.dy[j + 1]);
+        I.gy[j] = I.dy[j + 1] / (I.dy[j] + I.dy[j + 1]);
+    }
+}
+
+// Multigrid hierarchy from the tagged finest level.  Coarse cells merge 2x2
+// children (ceil at odd sizes); a coarse cell is active when any child is.
+void build_levels(Instance& I) {
+    I.lev.clear();
+    HostLevel l0;
+    l0.NX = I.NX;
+    l0.NY = I.NY;
+    l0.nx = I.nx;
+    l0.ny = I.ny;
+    l0.pitch = I.pitch;
+    l0.dw = I.dx;
+    l0.dh = I.dy;
+    l0.xc.assign(I.nx, 0.0);
+    l0.yc.assign(I.ny, 0.0);
+    for (int i = 1; i < I.nx - 1; i++) l0.xc[i] = 0.5 * (I.xf[i - 1] + I.xf[i]);
+    for (int j = 1; j < I.ny - 1; j++) l0.yc[j] = 0.5 * (I.yf[j - 1] + I.yf[j]);
+    l0.xc[0] = I.xf[0] - 0.5 * l0.dw[0];
+    l0.xc[I.nx - 1] = I.xf[I.NX] + 0.5 * l0.dw[I.nx - 1];
+    l0.yc[0] = I.yf[0] - 0.5 * l0.dh[0];
+    l0.yc[I.ny - 1] = I.yf[I.NY] + 0.5 * l0.dh[I.ny - 1];
+    I.lev.push_back(l0);
+    while (true) {
+        const HostLevel& f = I.lev.back();
+        if (!(f.NX >= 4 && f.NY >= 4 && (I.lev.size() == 1 || f.NX * f.NY > 64))) break;
+        HostLevel c;
+        c.NX = (f.NX + 1) / 2;
+        c.NY = (f.NY + 1) / 2;
+        c.nx = c.NX + 2;
+        c.ny = c.NY + 2;
+        c.pitch = round_up(c.nx, 32);
+        c.dw.assign(c.nx, 0.0);
+        c.dh.assign(c.ny, 0.0);
+        for (int Ic = 1; Ic <= c.NX; Ic++) {
+            int i = 2 * Ic - 1;
+            c.dw[Ic] = f.dw[i] + (i + 1 <= f.NX ? f.dw[i + 1] : 0.0);
+        }
+        for (int Jc = 1; Jc <= c.NY; Jc++) {
+            int j = 2 * Jc - 1;
+            c.dh[Jc] = f.dh[j] + (j + 1 <= f.NY ? f.dh[j + 1] : 0.0);
+        }
+        c.dw[0] = c.dw[1];
+        c.dw[c.nx - 1] = c.dw[c.nx - 2];
+        c.dh[0] = c.dh[1];
+        c.dh[c.ny - 1] = c.dh[c.ny - 2];
+        c.xc.assign(c.nx, 0.0);
+        c.yc.assign(c.ny, 0.0);
+        double x0 = I.xf[0];
+        for (int Ic = 1; Ic <= c.NX; Ic++) {
+            c.xc[Ic] = x0 + 0.5 * c.dw[Ic];
+            x0 += c.dw[Ic];
+        }
+        double y0 = I.yf[0];
+        for (int Jc = 1; Jc <= c.NY; Jc++) {
+            c.yc[Jc] = y0 + 0.5 * c.dh[Jc];
+            y0 += c.dh[Jc];
+        }
+        c.xc[0] = I.xf[0] - 0.5 * c.dw[0];
+        c.xc[c.nx - 1] = x0 + 0.5 * c.dw[c.nx - 1];
+        c.yc[0] = I.yf[0] - 0.5 * c.dh[0];
+        c.yc[c.ny - 1] = y0 + 0.5 * c.dh[c.ny - 1];
+        I.lev.push_back(c);
+    }
+    for (size_t l = 0; l < I.lev.size(); l++) {
+        HostLevel& v = I.lev[l];
+        v.kx.assign(v.nx, 0.0);
+        v.ky.assign(v.ny, 0.0);
+        v.ix.assign(v.nx, 0.0);
+        v.iy.assign(v.ny, 0.0);
+        for (int i = 0; i < v.nx - 1; i++) v.kx[i] = 2.0 / (v.dw[i] + v.dw[i + 1]);
+        for (int j = 0; j < v.ny - 1; j++) v.ky[j] = 2.0 / (v.dh[j] + v.dh[j + 1]);
+        for (int i = 0; i < v.nx; i++) v.ix[i] = 1.0 / v.dw[i];
+        for (int j = 0; j < v.ny; j++) v.iy[j] = 1.0 / v.dh[j];
+        const size_t nn = (size_t)v.pitch * v.ny;
+        v.act.assign(nn, 0);
+        v.bits.assign(nn, 0);
+        if (l == 0) {
+            for (int j = 0; j < v.ny; j++)
+                for (int i = 0; i < v.nx; i++) v.act[i + j * v.pitch] = I.type[i + j * I.pitch] == T_FLUID;
+        } else {
+            const HostLevel& f = I.lev[l - 1];
+            for (int J = 1; J <= v.NY; J++)
+                for (int Ic = 1; Ic <= v.NX; Ic++) {
+                    uint8_t a = 0;
+                    for (int dj = 0; dj < 2; dj++)
+                        for (int di = 0; di < 2; di++) {
+                            int i = 2 * Ic - 1 + di, j = 2 * J - 1 + dj;
+                            if (i <= f.NX && j <= f.NY) a |= f.act[i + j * f.pitch];
+                        }
+                    v.act[Ic + J * v.pitch] = a;
+                }
+        }
+        for (int j = 1; j <= v.NY; j++)
+            for (int i = 1; i <= v.NX; i++) {
+                const int id = i + j * v.pitch;
+                if (!v.act[id]) continue;
+                uint8_t bt = 0;
+                auto probe = [&](int ni, int nj, uint8_t ob, uint8_t gb) {
+                    if (ni < 1 || ni > v.NX || nj < 1 || nj > v.NY) return;
+                    const int nid = ni + nj * v.pitch;
+                    if (l == 0) {
+                        const uint8_t t = I.type[nid];
+                        if (t == T_FLUID) bt |= ob;
+                        if (t == T_GHOST) bt |= (uint8_t)(ob | gb);
+                    } else if (v.act[nid]) {
+                        bt |= ob;
+                    }
+                };
+                probe(i + 1, j, B_E, G_E);
+                probe(i - 1, j, B_W, G_W);
+                probe(i, j + 1, B_N, G_N);
+                probe(i, j - 1, B_S, G_S);
+                v.bits[id] = bt;
+            }
+        if (l > 0) {
+            HostLevel& f = I.lev[l - 1];
+            f.pI.assign(f.nx, 0);
+            f.pIn.assign(f.nx, 0);
+            f.pwx.assign(f.nx, 0.0);
+            f.pJ.assign(f.ny, 0);
+            f.pJn.assign(f.ny, 0);
+            f.pwy.assign(f.ny, 0.0);
+            for (int i = 1; i <= f.NX; i++) {
+                int Ic = (i + 1) / 2;
+                int In = f.xc[i] < v.xc[Ic] ? Ic - 1 : Ic + 1;
+                double w = 0.0;
+                if (In < 1 || In > v.NX) In = Ic;
+                else w = (f.xc[i] - v.xc[Ic]) / (v.xc[In] - v.xc[Ic]);
+                f.pI[i] = Ic;
+                f.pIn[i] = In;
+                f.pwx[i] = w;
+            }
+            for (int j = 1; j <= f.NY; j++) {
+                int Jc = (j + 1) / 2;
+                int Jn = f.yc[j] < v.yc[Jc] ? Jc - 1 : Jc + 1;
+                double w = 0.0;
+                if (Jn < 1 || Jn > v.NY) Jn = Jc;
+                else w = (f.yc[j] - v.yc[Jc]) / (v.yc[Jn] - v.yc[Jc]);
+                f.pJ[j] = Jc;
+                f.pJn[j] = Jn;
+                f.pwy[j] = w;
+            }
+        }
+    }
+}
+
+// Domain ghost relations (wall/inflow/slip/outflow per side, corners from the
+// diagonal interior cell) and IBM ghost stubs, in row-major cell order.
+void build_ghosts(Instance& I, int inst, std::vector<GhostDev>& out, std::vector<int>& ibm_list) {
+    const int nx = I.nx, ny = I.ny, P = I.pitch;
+    const ifx_config& c = I.cfg;
+    I.ghost_beg = (int)out.size();
+    I.n_ibm = 0;
+    auto rule = [&](int side, int k_along, double* wu, double* wv, double* wp, double* cu, double* cv, int* qi,
+                    double* qf) {
+        const int bt = c.bc_type[side];
+        const bool normal_is_u = (side == IFX_SIDE_W || side == IFX_SIDE_E);
+        *qi = -1;
+        *qf = 0.0;
+        if (bt == IFX_BC_WALL || bt == IFX_BC_INFLOW) {
+            *wu = -1.0; *cu = 2.0 * c.bc_u[side];
+            *wv = -1.0; *cv = 2.0 * c.bc_v[side];
+            *wp = 1.0;
+        } else if (bt == IFX_BC_SLIP) {
+            if (normal_is_u) { *wu = -1.0; *wv = 1.0; }
+            else { *wu = 1.0; *wv = -1.0; }
+            *cu = *cv = 0.0;
+            *wp = 1.0;
+        } else {
+            *wu = -1.0; *wv = -1.0;
+            *cu = *cv = 0.0;
+            *qi = side * I.qstride + k_along;
+            *qf = 2.0;
+            *wp = -1.0;
+        }
+    };
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const int id = i + j * P;
+            const uint8_t t = I.type[id];
+            if (t != T_DOMAIN && t != T_GHOST) continue;
+            GhostDev g;
+            std::memset(&g, 0, sizeof(g));
+            g.cell = id;
+            g.inst = inst;
+            g.qi[0] = g.qi[1] = -1;
+            g.qown = -1;
+            g.adj = -1;
+            for (int k = 0; k < 4; k++) g.nb[k] = id;
+            if (t == T_GHOST) {
+                g.side = -1;
+                ibm_list.push_back((int)out.size());
+                I.n_ibm++;
+                out.push_back(g);
+                continue;
+            }
+            const bool W = i == 0, E = i == nx - 1, So = j == 0, N = j == ny - 1;
+            int sd;
+            if ((W || E) && (So || N)) sd = 4;
+            else if (W) sd = IFX_SIDE_W;
+            else if (E) sd = IFX_SIDE_E;
+            else if (So) sd = IFX_SIDE_S;
+            else sd = IFX_SIDE_N;
+            g.side = sd;
+            if (sd == 4) {
+                const int di = (i == 0) ? 1 : nx - 2, dj = (j == 0) ? 1 : ny - 2;
+                const int sa = (i == 0) ? IFX_SIDE_W : IFX_SIDE_E;
+                const int sb = (j == 0) ? IFX_SIDE_S : IFX_SIDE_N;
+                double wua, wva, wpa, cua, cva, qfa, wub, wvb, wpb, cub, cvb, qfb;
+                int qia, qib;
+                rule(sa, dj, &wua, &wva, &wpa, &cua, &cva, &qia, &qfa);
+                rule(sb, di, &wub, &wvb, &wpb, &cub, &cvb, &qib, &qfb);
+                g.nb[0] = di + dj * P;
+                g.wu[0] = 0.5 * (wua + wub);
+                g.wv[0] = 0.5 * (wva + wvb);
+                g.wp[0] = 0.5 * (wpa + wpb);
+                g.cu = 0.5 * (cua + cub);
+                g.cv = 0.5 * (cva + cvb);
+                g.qi[0] = qia;
+                g.qf[0] = 0.5 * qfa;
+                g.qi[1] = qib;
+                g.qf[1] = 0.5 * qfb;
+            } else {
+                int ai = i, aj = j;
+                if (sd == IFX_SIDE_W) ai = 1;
+                if (sd == IFX_SIDE_E) ai = nx - 2;
+                if (sd == IFX_SIDE_S) aj = 1;
+                if (sd == IFX_SIDE_N) aj = ny - 2;
+                const int k_along = (sd <= 1) ? j : i;
+                g.nb[0] = ai + aj * P;
+                g.adj = g.nb[0];
+                rule(sd, k_along, &g.wu[0], &g.wv[0], &g.wp[0], &g.cu, &g.cv, &g.qi[0], &g.qf[0]);
+                if (c.bc_type[sd] == IFX_BC_OUTFLOW) {
+                    g.qown = g.qi[0];
+                    g.qh = (sd <= 1) ? I.dx[ai] : I.dy[aj];
+                }
+            }
+            out.push_back(g);
+        }
+    I.ghost_cnt = (int)out.size() - I.ghost_beg;
+}
+
+// Host initial condition (same formulas as initializeKernel for the vortex,
+// src/include/preSim.cu:70-73).
+void initial_field(const Instance& I, std::vector<double>& u, std::vector<double>& v) {
+    const int nx = I.nx, ny = I.ny, P = I.pitch;
+    u.assign(I.ncell, 0.0);
+    v.assign(I.ncell, 0.0);
+    const ifx_config& c = I.cfg;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const int id = i + j * P;
+            const uint8_t t = I.type[id];
+            if (c.init == IFX_INIT_VORTEX) {
+                if (t == T_SOLID || t == T_GHOST) continue;
+                double r = std::sqrt(std::pow(I.xc[i] - 0.5, 2.0) + std::pow(I.yc[j] - 0.5, 2.0));
+                double r0 = 0.1;
+                u[id] = 1.0 - 0.25 * (I.yc[j] - 0.5) * std::exp((1.0 - std::pow(r / r0, 2.0)) / 2.0);
+                v[id] = 0.25 * (I.xc[i] - 0.5) * std::exp((1.0 - std::pow(r / r0, 2.0)) / 2.0);
+            } else if (c.init == IFX_INIT_UNIFORM) {
+                if (t == T_FLUID || t == T_DOMAIN) u[id] = c.bc_u[IFX_SIDE_W];
+            }
+        }
+}
+
+ifx_status validate(const ifx_config* c) {
+    if (c->nx < 4 || c->ny < 4) return set_error(IFX_ERR_ARG, "method mode needs nx, ny >= 4");
+    if (!(c->dt > 0) || !(c->re > 0)) return set_error(IFX_ERR_ARG, "dt and Re must be positive");
+    if (c->mg_pre < 1 || c->mg_post < 1) return set_error(IFX_ERR_ARG, "multigrid sweeps must be >= 1");
+    if (c->ad_itermax < 1 || c->ppe_itermax < 0) return set_error(IFX_ERR_ARG, "bad iteration caps");
+    if (c->body == IFX_BODY_ELLIPSE && !(c->body_a > 0 && c->body_b > 0))
+        return set_error(IFX_ERR_ARG, "body semi-axes must be positive");
+    for (int s = 0; s < 4; s++)
+        if (c->bc_type[s] < 0 || c->bc_type[s] > 3) return set_error(IFX_ERR_ARG, "bad boundary type");
+    return IFX_OK;
+}
+
+// -------------------------------------------------------- method: create
+
+template <typename T>
+ifx_status alloc_level_fields(ifx_solver* S, HostLevel& L) {
+    const size_t nn = (size_t)L.pitch * L.ny;
+    T *e = nullptr, *e2 = nullptr, *r = nullptr;
+    IFX_TRY(dalloc(S, &e, nn));
+    IFX_TRY(dalloc(S, &e2, nn));
+    IFX_TRY(dalloc(S, &r, nn));
+    L.d_e = e;
+    L.d_e2 = e2;
+    L.d_r = r;
+    return IFX_OK;
+}
+
+ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const double* const* xfs,
+                         const double* const* yfs) {
+    S->mode = IFX_MODE_METHOD;
+    S->prec = cfgs[0].precision;
+    S->mg_pre = cfgs[0].mg_pre;
+    S->mg_post = cfgs[0].mg_post;
+    for (int k = 0; k < n; k++) {
+        IFX_TRY(validate(&cfgs[k]));
+        if (cfgs[k].mode != IFX_MODE_METHOD) return set_error(IFX_ERR_ARG, "a batch holds method-mode instances only");
+        if (cfgs[k].precision != S->prec || cfgs[k].mg_pre != S->mg_pre || cfgs[k].mg_post != S->mg_post)
+            return set_error(IFX_ERR_ARG, "instances of one batch share precision and multigrid sweeps");
+    }
+    S->inst.resize(n);
+    std::vector<InstDev> hI(n);
+    for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        I.cfg = cfgs[k];
+        I.NX = I.cfg.nx;
+        I.NY = I.cfg.ny;
+        I.nx = I.NX + 2;
+        I.ny = I.NY + 2;
+        I.pitch = round_up(I.nx, 32);
+        I.ncell = (size_t)I.pitch * I.ny;
+        I.qstride = std::max(I.nx, I.ny);
+        build_grid(I, xfs[k], yfs[k]);
+        for (int s = 0; s < 4; s++)
+            if (I.cfg.bc_type[s] == IFX_BC_OUTFLOW) I.dirmask |= 1 << s;
+        I.singular = I.dirmask == 0;
+        if (I.cfg.body == IFX_BODY_ELLIPSE) {
+            const double th = I.cfg.body_angle_deg * M_PI / 180.0;
+            I.cs = std::cos(th);
+            I.sn = std::sin(th);
+            I.ia2 = 1.0 / (I.cfg.body_a * I.cfg.body_a);
+            I.ib2 = 1.0 / (I.cfg.body_b * I.cfg.body_b);
+        }
+        InstDev& d = I.dev;
+        std::memset(&d, 0, sizeof(d));
+        d.NX = I.NX; d.NY = I.NY; d.nx = I.nx; d.ny = I.ny; d.pitch = I.pitch;
+        d.singular = I.singular;
+        d.dirmask = I.dirmask;
+        d.body = I.cfg.body == IFX_BODY_ELLIPSE;
+        d.dt = I.cfg.dt;
+        d.re = I.cfg.re;
+        d.dtre = I.cfg.dt / I.cfg.re;
+        d.idt = 1.0 / I.cfg.dt;
+        d.omega = I.cfg.mg_omega;
+        d.ppe_tol = I.cfg.ppe_tol;
+        d.ad_itermax = I.cfg.ad_itermax;
+        d.ppe_itermax = I.cfg.ppe_itermax;
+        d.mixed_inner = I.cfg.mixed_inner;
+        d.uc = I.cfg.outflow_uc;
+        d.bcx = I.cfg.body_cx; d.bcy = I.cfg.body_cy; d.ba = I.cfg.body_a; d.bb = I.cfg.body_b;
+        d.bcs = I.cs; d.bsn = I.sn; d.bia2 = I.ia2; d.bib2 = I.ib2;
+        d.fref = 0.5 * I.cfg.force_ref_u * I.cfg.force_ref_u * I.cfg.force_ref_len;
+        const size_t nc = I.ncell;
+        IFX_TRY(dalloc(S, &d.u, nc)); IFX_TRY(dalloc(S, &d.v, nc));
+        IFX_TRY(dalloc(S, &d.u2, nc)); IFX_TRY(dalloc(S, &d.v2, nc));
+        IFX_TRY(dalloc(S, &d.Us, nc)); IFX_TRY(dalloc(S, &d.Vs, nc));
+        IFX_TRY(dalloc(S, &d.U, nc)); IFX_TRY(dalloc(S, &d.V, nc));
+        IFX_TRY(dalloc(S, &d.Nu, nc)); IFX_TRY(dalloc(S, &d.Nv, nc));
+        IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
+        IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
+        IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
+        double *xf_d = nullptr, *yf_d = nullptr, *xc_d = nullptr, *yc_d = nullptr, *dx_d = nullptr,
+               *dy_d = nullptr, *fx_d = nullptr, *gx_d = nullptr, *fy_d = nullptr, *gy_d = nullptr;
+        IFX_TRY(dupload(S, &xf_d, I.xf)); IFX_TRY(dupload(S, &yf_d, I.yf));
+        IFX_TRY(dupload(S, &xc_d, I.xc)); IFX_TRY(dupload(S, &yc_d, I.yc));
+        IFX_TRY(dupload(S, &dx_d, I.dx)); IFX_TRY(dupload(S, &dy_d, I.dy));
+        IFX_TRY(dupload(S, &fx_d, I.fx)); IFX_TRY(dupload(S, &gx_d, I.gx));
+        IFX_TRY(dupload(S, &fy_d, I.fy)); IFX_TRY(dupload(S, &gy_d, I.gy));
+        d.xf = xf_d; d.yf = yf_d; d.xc = xc_d; d.yc = yc_d; d.dx = dx_d; d.dy = dy_d;
+        d.fx = fx_d; d.gx = gx_d; d.fy = fy_d; d.gy = gy_d;
+        uint8_t* type_d = nullptr;
+        IFX_TRY(dalloc(S, &type_d, nc));
+        d.type = type_d;
+        IFX_TRY(dalloc(S, &d.qbu, 4 * (size_t)I.qstride));
+        IFX_TRY(dalloc(S, &d.qbv, 4 * (size_t)I.qstride));
+        hI[k] = d;
+    }
+    IFX_TRY(dalloc(S, &S->dI, n));
+    CUDA_TRY(cudaMemcpyAsync(S->dI, hI.data(), n * sizeof(InstDev), cudaMemcpyHostToDevice, S->stream));
+    // tagging on the device, then the type arrays back to the host
+    for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        uint8_t* type_d = const_cast<uint8_t*>(I.dev.type);
+        CUDA_TRY(launch_tag(S->dI, k, I.nx * I.ny, type_d, S->stream));
+        CUDA_TRY(launch_mark_ghosts(S->dI, k, I.NX * I.NY, type_d, S->stream));
+        S->launches += 2;
+        I.type.assign(I.ncell, 0);
+        CUDA_TRY(cudaMemcpyAsync(I.type.data(), type_d, I.ncell, cudaMemcpyDeviceToHost, S->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    // ghost tables, hierarchy, tiles
+    std::vector<GhostDev> hG;
+    std::vector<int> hIbm;
+    std::vector<LevelDev> hLV;
+    std::vector<Tile> hT0;
+    std::vector<int> hCoarse;
+    int lmax = 0;
+    for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        I.n_fluid = 0;
+        I.area = 0.0;
+        for (int j = 1; j <= I.NY; j++)
+            for (int i = 1; i <= I.NX; i++)
+                if (I.type[i + j * I.pitch] == T_FLUID) {
+                    I.n_fluid++;
+                    I.area += I.dx[i] * I.dy[j];
+                }
+        build_ghosts(I, k, hG, hIbm);
+        build_levels(I);
+        lmax = std::max(lmax, (int)I.lev.size());
+    }
+    S->lmax = lmax;
+    S->ng = (int)hG.size();
+    S->nibm = (int)hIbm.size();
+    IFX_TRY(dupload(S, &S->dG, hG));
+    IFX_TRY(dupload(S, &S->dIbm, hIbm));
+    IFX_TRY(dalloc(S, &S->dGval, 3 * (size_t)std::max(1, S->ng)));
+    IFX_TRY(dalloc(S, &S->dBiIp, 4 * (size_t)std::max(1, S->nibm)));
+    std::vector<std::vector<Tile>> tsm(lmax), tre(lmax);
+    for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        InstDev& d = I.dev;
+        I.lev_base = (int)hLV.size();
+        std::vector<int> gidx(I.ncell, -1);
+        for (int g = I.ghost_beg; g < I.ghost_beg + I.ghost_cnt; g++)
+            if (hG[g].side < 0) gidx[hG[g].cell] = g;
+        int* gidx_d = nullptr;
+        IFX_TRY(dupload(S, &gidx_d, gidx));
+        d.gidx = gidx_d;
+        const int nl = (int)I.lev.size();
+        for (int l = 0; l < nl; l++) {
+            HostLevel& L = I.lev[l];
+            IFX_TRY(dupload(S, &L.d_kx, L.kx)); IFX_TRY(dupload(S, &L.d_ky, L.ky));
+            IFX_TRY(dupload(S, &L.d_ix, L.ix)); IFX_TRY(dupload(S, &L.d_iy, L.iy));
+            IFX_TRY(dupload(S, &L.d_dw, L.dw)); IFX_TRY(dupload(S, &L.d_dh, L.dh));
+            IFX_TRY(dupload(S, &L.d_kxf, to_f(L.kx))); IFX_TRY(dupload(S, &L.d_kyf, to_f(L.ky)));
+            IFX_TRY(dupload(S, &L.d_ixf, to_f(L.ix))); IFX_TRY(dupload(S, &L.d_iyf, to_f(L.iy)));
+            IFX_TRY(dupload(S, &L.d_dwf, to_f(L.dw))); IFX_TRY(dupload(S, &L.d_dhf, to_f(L.dh)));
+            IFX_TRY(dupload(S, &L.d_bits, L.bits));
+            if (S->prec == IFX_PREC_FP64) IFX_TRY(alloc_level_fields<double>(S, L));
+            else IFX_TRY(alloc_level_fields<float>(S, L));
+            if (l + 1 < nl) {
+                IFX_TRY(dupload(S, &L.d_pI, L.pI)); IFX_TRY(dupload(S, &L.d_pIn, L.pIn));
+                IFX_TRY(dupload(S, &L.d_pJ, L.pJ)); IFX_TRY(dupload(S, &L.d_pJn, L.pJn));
+                IFX_TRY(dupload(S, &L.d_pwx, L.pwx)); IFX_TRY(dupload(S, &L.d_pwy, L.pwy));
+                IFX_TRY(dupload(S, &L.d_pwxf, to_f(L.pwx))); IFX_TRY(dupload(S, &L.d_pwyf, to_f(L.pwy)));
+            }
+            LevelDev ld;
+            std::memset(&ld, 0, sizeof(ld));
+            ld.NX = L.NX; ld.NY = L.NY; ld.nx = L.nx; ld.ny = L.ny; ld.pitch = L.pitch;
+            ld.inst = k;
+            ld.depth = l;
+            ld.dirmask = I.dirmask;
+            ld.kx = L.d_kx; ld.ky = L.d_ky; ld.ix = L.d_ix; ld.iy = L.d_iy; ld.dw = L.d_dw; ld.dh = L.d_dh;
+            ld.kxf = L.d_kxf; ld.kyf = L.d_kyf; ld.ixf = L.d_ixf; ld.iyf = L.d_iyf; ld.dwf = L.d_dwf; ld.dhf = L.d_dhf;
+            ld.bits = L.d_bits;
+            ld.e = L.d_e; ld.e2 = L.d_e2; ld.r = L.d_r;
+            ld.pI = L.d_pI; ld.pIn = L.d_pIn; ld.pJ = L.d_pJ; ld.pJn = L.d_pJn;
+            ld.pwx = L.d_pwx; ld.pwy = L.d_pwy; ld.pwxf = L.d_pwxf; ld.pwyf = L.d_pwyf;
+            ld.child = (l + 1 < nl) ? I.lev_base + l + 1 : -1;
+            ld.parent = (l > 0) ? I.lev_base + l - 1 : -1;
+            hLV.push_back(ld);
+            // tiles
+            const int lv = I.lev_base + l;
+            std::vector<Tile> tl;
+            for (int j0 = 0; j0 < L.ny; j0 += TILE_Y)
+                for (int i0 = 0; i0 < L.nx; i0 += TILE_X) tl.push_back(Tile{k, lv, i0, j0});
+            if (l == 0) {
+                I.tile_beg = (int)hT0.size();
+                I.tile_cnt = (int)tl.size();
+                hT0.insert(hT0.end(), tl.begin(), tl.end());
+            } else {
+                tre[l].insert(tre[l].end(), tl.begin(), tl.end());
+                if (l < nl - 1) tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
+            }
+        }
+        hCoarse.push_back(I.lev_base + nl - 1);
+        d.lev0 = I.lev_base;
+        d.nlev = nl;
+        d.tile_beg = I.tile_beg;
+        d.tile_cnt = I.tile_cnt;
+        d.ghost_beg = I.ghost_beg;
+        d.ghost_cnt = I.ghost_cnt;
+        d.n_fluid = I.n_fluid;
+        d.area = I.area;
+        d.ad_lim = I.cfg.ad_tol * std::max(1, I.n_fluid);
+        d.kx = I.lev[0].d_kx; d.ky = I.lev[0].d_ky; d.ix = I.lev[0].d_ix; d.iy = I.lev[0].d_iy;
+        hI[k] = d;
+    }
+    IFX_TRY(dupload(S, &S->dLV, hLV));
+    IFX_TRY(dupload(S, &S->dT0, hT0));
+    S->nt0 = (int)hT0.size();
+    S->dTsm.assign(lmax, nullptr);
+    S->dTre.assign(lmax, nullptr);
+    S->ntsm.assign(lmax, 0);
+    S->ntre.assign(lmax, 0);
+    for (int l = 1; l < lmax; l++) {
+        IFX_TRY(dupload(S, &S->dTsm[l], tsm[l]));
+        IFX_TRY(dupload(S, &S->dTre[l], tre[l]));
+        S->ntsm[l] = (int)tsm[l].size();
+        S->ntre[l] = (int)tre[l].size();
+    }
+    IFX_TRY(dupload(S, &S->dCoarse, hCoarse));
+    IFX_TRY(dalloc(S, &S->dPart, (size_t)S->nt0 * NPART));
+    IFX_TRY(dalloc(S, &S->dS, n));
+    IFX_TRY(dalloc(S, &S->dCtl, 1));
+    CUDA_TRY(cudaMallocHost((void**)&S->hS, n * sizeof(InstState)));
+    CUDA_TRY(cudaMallocHost((void**)&S->hCtl, sizeof(LoopCtl)));
+    std::memset(S->hS, 0, n * sizeof(InstState));
+    CUDA_TRY(cudaMemcpyAsync(S->dI, hI.data(), n * sizeof(InstDev), cudaMemcpyHostToDevice, S->stream));
+    // image-point weights of the IBM ghosts
+    CUDA_TRY(launch_ghost_weights(S->dG, S->dIbm, S->nibm, S->dI, S->dBiIp, S->stream));
+    S->launches++;
+    // initial field, outflow face values, ghosts and faces
+    for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        std::vector<double> u, v;
+        initial_field(I, u, v);
+        std::vector<double> qbu(4 * (size_t)I.qstride, 0.0), qbv(4 * (size_t)I.qstride, 0.0);
+        for (int g = I.ghost_beg; g < I.ghost_beg + I.ghost_cnt; g++)
+            if (hG[g].qown >= 0) {
+                qbu[hG[g].qown] = u[hG[g].adj];
+                qbv[hG[g].qown] = v[hG[g].adj];
+            }
+        CUDA_TRY(cudaMemcpyAsync(I.dev.u, u.data(), I.ncell * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.dev.v, v.data(), I.ncell * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.dev.u2, u.data(), I.ncell * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.dev.v2, v.data(), I.ncell * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.dev.qbu, qbu.data(), qbu.size() * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.dev.qbv, qbv.data(), qbv.size() * 8, cudaMemcpyHostToDevice, S->stream));
+        CUDA_TRY(cudaStreamSynchronize(S->stream));  // host vectors go out of scope
+    }
+    CUDA_TRY(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, S->stream));
+    CUDA_TRY(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 1, S->stream));
+    S->launches += 3;
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+// ------------------------------------------------------- method: step
+
+struct Seq {
+    ifx_solver* S;
+    long long n = 0;  // launches issued through this sequence
+    cudaError_t err = cudaSuccess;
+    void add(cudaError_t e) {
+        n++;
+        if (e != cudaSuccess && err == cudaSuccess) err = e;
+    }
+};
+
+template <typename T>
+void seq_vcycle(Seq& q) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int L = S->lmax;
+    std::vector<int> cur(L, 0);
+    // finest level: first sweep from zero, then the rest of the pre-smoothing
+    q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, 1, 0, st));
+    cur[0] = 1;
+    for (int k = 1; k < S->mg_pre; k++) {
+        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, 0, cur[0], st));
+        cur[0] ^= 1;
+    }
+    for (int l = 1; l < L; l++) {
+        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, cur[l - 1], 1, st));
+        cur[l] = 0;
+        if (S->ntsm[l] > 0)
+            for (int k = 1; k < S->mg_pre; k++) {
+                q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, nullptr, 0, 0, cur[l], st));
+                cur[l] ^= 1;
+            }
+    }
+    q.add(launch_coarse_solve<T>(S->dCoarse, (int)S->inst.size(), S->dLV, S->dI, S->dS, st));
+    for (int l = L - 2; l >= 0; l--) {
+        const Tile* tl = l == 0 ? S->dT0 : S->dTsm[l];
+        const int nt = l == 0 ? S->nt0 : S->ntsm[l];
+        if (nt == 0) continue;
+        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur[l], cur[l + 1], st));
+        for (int k = 0; k < S->mg_post; k++) {
+            const int flags = (l == 0 && k == S->mg_post - 1) ? 2 : 0;
+            if (l == 0)
+                q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, flags, cur[0], st));
+            else
+                q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, nullptr, 0, flags, cur[l], st));
+            cur[l] ^= 1;
+        }
+    }
+}
+
+void seq_pre(Seq& q) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    q.add(launch_step_begin(S->dS, n, st));
+    q.add(launch_outflow(S->dG, S->ng, S->dI, st));
+    q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
+    q.n++;  // ghost fill is two kernels
+    q.add(launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st));
+}
+
+void seq_pred_body(Seq& q, unsigned long long h) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st));
+    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st));
+    q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 1, st));
+    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 1, S->dCtl, h, st));
+}
+
+template <typename T>
+void seq_mid(Seq& q) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
+    q.n++;
+    q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
+    q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
+    q.add(launch_ppe_resid<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
+    q.add(launch_ppe_reduce(S->dI, S->dS, S->dPart, n, S->dCtl, 0ull, st));
+}
+
+template <typename T>
+void seq_ppe_body(Seq& q, unsigned long long h) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    seq_vcycle<T>(q);
+    q.add(launch_ppe_resid<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
+    q.add(launch_ppe_reduce(S->dI, S->dS, S->dPart, n, S->dCtl, h, st));
+}
+
+void seq_post(Seq& q) {
+    ifx_solver* S = q.S;
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    q.add(launch_p_finalize(S->dT0, S->nt0, S->dI, S->dS, st));
+    q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 4, S->dGval, st));
+    q.n++;
+    q.add(launch_correct(S->dT0, S->nt0, S->dI, S->dPart, st));
+    q.add(launch_correct_reduce(S->dI, S->dS, S->dPart, n, st));
+    q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
+    q.n++;
+    q.add(launch_forces(S->dI, S->dS, n, st));
+}
+
+int max_pred_pairs(const ifx_solver* S) {
+    int m = 1;
+    for (auto& I : S->inst) m = std::max(m, (I.cfg.ad_itermax + 1) / 2);
+    return m;
+}
+int max_ppe_bodies(const ifx_solver* S) {
+    int m = 1;
+    for (auto& I : S->inst) m = std::max(m, I.cfg.ppe_itermax + 1);
+    return m;
+}
+
+// Host-driven loop: run the body, read the vote, repeat.
+template <class F>
+ifx_status host_loop(ifx_solver* S, Seq& q, int maxit, F body) {
+    for (int k = 0; k < maxit; k++) {
+        body(q, 0ull);
+        if (q.err != cudaSuccess) return cuerr(q.err, "kernel launch");
+        CUDA_TRY(cudaMemcpyAsync(S->hCtl, S->dCtl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, S->stream));
+        CUDA_TRY(cudaStreamSynchronize(S->stream));
+        if (S->hCtl->result == 0) break;
+    }
+    return IFX_OK;
+}
+
+template <typename T>
+ifx_status step_method_host(ifx_solver* S) {
+    Seq q{S};
+    seq_pre(q);
+    IFX_TRY(host_loop(S, q, max_pred_pairs(S), [](Seq& qq, unsigned long long h) { seq_pred_body(qq, h); }));
+    seq_mid<T>(q);
+    CUDA_TRY(cudaMemcpyAsync(S->hCtl, S->dCtl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    if (S->hCtl->result != 0)
+        IFX_TRY(host_loop(S, q, max_ppe_bodies(S), [](Seq& qq, unsigned long long h) { seq_ppe_body<T>(qq, h); }));
+    seq_post(q);
+    if (q.err != cudaSuccess) return cuerr(q.err, "kernel launch");
+    S->launches += q.n;
+    return IFX_OK;
+}
+
+// ---- CUDA graph of one time step: linear segments captured to the graph,
+//      the two convergence loops as conditional WHILE nodes.
+struct GraphBuilder {
+    ifx_solver* S;
+    cudaGraph_t g;
+    std::vector<cudaGraphNode_t> frontier;
+    cudaError_t err = cudaSuccess;
+
+    template <class F>
+    long long segment(F fn) {
+        Seq q{S};
+        if (err != cudaSuccess) return 0;
+        err = cudaStreamBeginCaptureToGraph(S->stream, g, frontier.empty() ? nullptr : frontier.data(), nullptr,
+                                            frontier.size(), cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) return 0;
+        fn(q);
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaStreamCaptureStatus cs;
+        cudaError_t e2 = cudaStreamGetCaptureInfo(S->stream, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        std::vector<cudaGraphNode_t> nf;
+        if (e2 == cudaSuccess)
+            for (size_t k = 0; k < nd; k++) nf.push_back(deps[k]);
+        cudaGraph_t out = nullptr;
+        cudaError_t e3 = cudaStreamEndCapture(S->stream, &out);
+        if (q.err != cudaSuccess) err = q.err;
+        else if (e2 != cudaSuccess) err = e2;
+        else if (e3 != cudaSuccess) err = e3;
+        frontier = nf;
+        return q.n;
+    }
+
+    template <class F>
+    long long loop(F body) {
+        if (err != cudaSuccess) return 0;
+        cudaGraphConditionalHandle h;
+        err = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+        if (err != cudaSuccess) return 0;
+        cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        err = cudaGraphAddNode(&node, g, frontier.empty() ? nullptr : frontier.data(), nullptr, frontier.size(), &p);
+        if (err != cudaSuccess) return 0;
+        cudaGraph_t body_g = p.conditional.phGraph_out[0];
+        Seq q{S};
+        err = cudaStreamBeginCaptureToGraph(S->stream, body_g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) return 0;
+        body(q, (unsigned long long)h);
+        cudaGraph_t out = nullptr;
+        cudaError_t e3 = cudaStreamEndCapture(S->stream, &out);
+        if (q.err != cudaSuccess) err = q.err;
+        else if (e3 != cudaSuccess) err = e3;
+        frontier.assign(1, node);
+        return q.n;
+    }
+};
+
+template <typename T>
+ifx_status build_graph(ifx_solver* S) {
+    GraphBuilder b{S, nullptr, {}, cudaSuccess};
+    CUDA_TRY(cudaGraphCreate(&b.g, 0));
+    S->graph = b.g;
+    S->graph_nodes_pre = b.segment([](Seq& q) { seq_pre(q); });
+    S->graph_nodes_pred = b.loop([](Seq& q, unsigned long long h) { seq_pred_body(q, h); });
+    S->graph_nodes_mid = b.segment([](Seq& q) { seq_mid<T>(q); });
+    S->graph_nodes_ppe = b.loop([](Seq& q, unsigned long long h) { seq_ppe_body<T>(q, h); });
+    S->graph_nodes_post = b.segment([](Seq& q) { seq_post(q); });
+    if (b.err != cudaSuccess) return cuerr(b.err, "graph capture");
+    CUDA_TRY(cudaGraphInstantiate(&S->gexec, S->graph, 0));
+    return IFX_OK;
+}
+
+ifx_status check_states(ifx_solver* S) {
+    const int n = (int)S->inst.size();
+    CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, n * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    ifx_status worst = IFX_OK;
+    for (int k = 0; k < n; k++) {
+        const InstState& s = S->hS[k];
+        if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric))
+            worst = IFX_ERR_DIVERGED;
+    }
+    return worst;
+}
+
+template <typename T>
+ifx_status step_method(ifx_solver* S, int nsteps) {
+    const char* ng = std::getenv("IFX_NO_GRAPH");
+    if (ng && ng[0] == '1') S->use_graph = false;
+    CUDA_TRY(cudaEventRecord(S->ev0, S->stream));
+    if (S->use_graph) {
+        if (!S->gexec) IFX_TRY(build_graph<T>(S));
+        for (int s = 0; s < nsteps; s++) CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
+    } else {
+        for (int s = 0; s < nsteps; s++) IFX_TRY(step_method_host<T>(S));
+    }
+    CUDA_TRY(cudaEventRecord(S->ev1, S->stream));
+    CUDA_TRY(cudaEventSynchronize(S->ev1));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+    S->last_ms = ms;
+    S->steps_done += nsteps;
+    ifx_status st = check_states(S);
+    if (S->use_graph) {
+        // kernels executed by the graph: fixed segments plus loop bodies
+        int pairs = 0, bodies = 0;
+        for (size_t k = 0; k < S->inst.size(); k++) {
+            pairs = std::max(pairs, (S->hS[k].pred_iters + 1) / 2);
+            bodies = std::max(bodies, S->hS[k].ppe_iters);
+        }
+        bodies = std::max(bodies, 1);
+        S->launches += (long long)nsteps * (S->graph_nodes_pre + pairs * S->graph_nodes_pred + S->graph_nodes_mid +
+                                            bodies * S->graph_nodes_ppe + S->graph_nodes_post);
+    }
+    for (size_t k = 0; k < S->inst.size(); k++) {
+        if (st != IFX_OK) S->hS[k].status = st;
+    }
+    if (st != IFX_OK) return set_error(st, "non-finite value in the solver state");
+    return IFX_OK;
+}
+
+// ---------------------------------------------------- reference mode
+
+ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf, const double* yf) {
+    S->mode = IFX_MODE_REFERENCE;
+    S->inst.resize(1);
+    Instance& I = S->inst[0];
+    I.cfg = *c;
+    I.NX = c->nx;
+    I.NY = c->ny;
+    I.nx = I.NX + 2;
+    I.ny = I.NY + 2;
+    I.pitch = I.nx;
+    I.ncell = (size_t)I.nx * I.ny;
+    if (I.NX < 2 || I.NY < 2) return set_error(IFX_ERR_ARG, "reference mode needs nx, ny >= 2");
+    build_grid(I, xf, yf);
+    const int nx = I.nx, ny = I.ny;
+    const size_t n = I.ncell;
+    // readGridData's full dx/dy arrays (src/include/preSim.cu:328-355)
+    std::vector<double> dx(n), dy(n), ib(n, 1.0);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            dx[i + j * nx] = I.dx[i];
+            dy[i + j * nx] = I.dy[j];
+        }
+    if (c->body == IFX_BODY_ELLIPSE) {
+        // extension: the reference's iBlank kernel is fixed to 1 (src/include/preSim.cu:133)
+        const double th = c->body_angle_deg * M_PI / 180.0, cs = std::cos(th), sn = std::sin(th);
+        const double ia2 = 1.0 / (c->body_a * c->body_a), ib2 = 1.0 / (c->body_b * c->body_b);
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                // built with -ffp-contract=off: same rounding as the device predicate
+                const double ddx = I.xc[i] - c->body_cx, ddy = I.yc[j] - c->body_cy;
+                const double xr = ddx * cs + ddy * sn, yr = ddy * cs - ddx * sn;
+                const double f = xr * xr * ia2 + yr * yr * ib2;
+                ib[i + j * nx] = f < 1.0 ? 0.0 : 1.0;
+            }
+    }
+    IFX_TRY(dalloc(S, &S->r_u, n)); IFX_TRY(dalloc(S, &S->r_v, n));
+    IFX_TRY(dalloc(S, &S->r_ut, n)); IFX_TRY(dalloc(S, &S->r_vt, n));
+    IFX_TRY(dalloc(S, &S->r_p, n)); IFX_TRY(dalloc(S, &S->r_pt, n));
+    IFX_TRY(dupload(S, &S->r_dx, dx)); IFX_TRY(dupload(S, &S->r_dy, dy));
+    IFX_TRY(dupload(S, &S->r_xc, I.xc)); IFX_TRY(dupload(S, &S->r_yc, I.yc));
+    IFX_TRY(dupload(S, &S->r_ib, ib));
+    IFX_TRY(dalloc(S, &S->r_coef, 5 * n));
+    IFX_TRY(dalloc(S, &S->r_sx, n)); IFX_TRY(dalloc(S, &S->r_sy, n));
+    IFX_TRY(dalloc(S, &S->r_uf, (size_t)(nx - 1) * (ny - 1)));
+    IFX_TRY(dalloc(S, &S->r_vf, (size_t)(nx - 1) * (ny - 1)));
+    IFX_TRY(dalloc(S, &S->r_res, 2 * ((n + 255) / 256) + 2));
+    IFX_TRY(dalloc(S, &S->r_out, 4));
+    CUDA_TRY(cudaMallocHost((void**)&S->h_out, 4 * sizeof(double)));
+    // initializeData (src/include/preSim.cu:201-217)
+    CUDA_TRY(launch_ref_init(nx, ny, S->r_xc, S->r_yc, S->r_u, S->r_v, S->r_p, S->stream));
+    CUDA_TRY(cudaMemcpyAsync(S->r_ut, S->r_u, n * 8, cudaMemcpyDeviceToDevice, S->stream));
+    CUDA_TRY(cudaMemcpyAsync(S->r_vt, S->r_v, n * 8, cudaMemcpyDeviceToDevice, S->stream));
+    S->launches++;
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+RefDev refdev(ifx_solver* S) {
+    const Instance& I = S->inst[0];
+    const size_t n = I.ncell;
+    RefDev R;
+    R.nx = I.nx;
+    R.ny = I.ny;
+    R.dt = I.cfg.dt;
+    R.re = I.cfg.re;
+    R.dx = S->r_dx;
+    R.dy = S->r_dy;
+    R.iblank = S->r_ib;
+    R.aP = S->r_coef;
+    R.aE = S->r_coef + n;
+    R.aW = S->r_coef + 2 * n;
+    R.aN = S->r_coef + 3 * n;
+    R.aS = S->r_coef + 4 * n;
+    R.sx = S->r_sx;
+    R.sy = S->r_sy;
+    R.uf = S->r_uf;
+    R.vf = S->r_vf;
+    R.res = S->r_res;
+    return R;
+}
+
+// nsteps x ADsolver (src/include/ADSolver.cu:268-395).
+ifx_status step_reference(ifx_solver* S, int nsteps) {
+    const Instance& I = S->inst[0];
+    RefDev R = refdev(S);
+    cudaStream_t st = S->stream;
+    CUDA_TRY(cudaEventRecord(S->ev0, st));
+    CUDA_TRY(launch_ref_coeffs(R, st));
+    S->launches++;
+    for (int s = 0; s < nsteps; s++) {
+        double* cu = S->r_cur ? S->r_ut : S->r_u;
+        double* cv = S->r_cur ? S->r_vt : S->r_v;
+        CUDA_TRY(launch_ref_velf(R, cu, cv, st));
+        CUDA_TRY(launch_ref_bc(R, cu, cv, st));
+        CUDA_TRY(launch_ref_source(R, cu, cv, st));
+        S->launches += 3;
+        double ures = 1.0, vres = 1.0;
+        int it = 0;
+        // pow(10.0, -6.0) at src/include/ADSolver.cu:315
+        while (ures + vres > 1e-6 && it < I.cfg.ad_itermax) {
+            double* tu = S->r_cur ? S->r_u : S->r_ut;
+            double* tv = S->r_cur ? S->r_v : S->r_vt;
+            CUDA_TRY(launch_ref_bc(R, cu, cv, st));
+            CUDA_TRY(launch_ref_velf(R, cu, cv, st));
+            CUDA_TRY(launch_ref_jacobi(R, cu, cv, tu, tv, st));
+            CUDA_TRY(launch_ref_bc(R, cu, cv, st));
+            CUDA_TRY(launch_ref_resid(R, cu, tu, cv, tv, S->r_out, st));
+            S->launches += 5;
+            S->r_cur ^= 1;
+            cu = tu;
+            cv = tv;
+            CUDA_TRY(cudaMemcpyAsync(S->h_out, S->r_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            ures = S->h_out[0];
+            vres = S->h_out[1];
+            it++;
+        }
+        S->r_iters.push_back(it);
+    }
+    CUDA_TRY(cudaEventRecord(S->ev1, st));
+    CUDA_TRY(cudaEventSynchronize(S->ev1));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+    S->last_ms = ms;
+    S->steps_done += nsteps;
+    return IFX_OK;
+}
+
+ifx_status ppe_reference(ifx_solver* S, int* iters) {
+    const Instance& I = S->inst[0];
+    RefDev R = refdev(S);
+    cudaStream_t st = S->stream;
+    CUDA_TRY(launch_ref_ppe_coeffs(R, st));
+    CUDA_TRY(launch_ref_ppe_bc(R, S->r_p, st));
+    S->launches += 2;
+    double* cur = S->r_p;
+    double* tmp = S->r_pt;
+    double residual = 1.0;
+    int it = 0;
+    // pow(10.0, -6.0) at src/include/PPESolver.cu:172
+    while (residual > 1e-6 && it < I.cfg.ppe_itermax) {
+        CUDA_TRY(launch_ref_ppe_sweep(R, cur, tmp, S->r_out, st));
+        S->launches += 2;
+        std::swap(cur, tmp);
+        CUDA_TRY(cudaMemcpyAsync(S->h_out, S->r_out, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        residual = S->h_out[0];
+        it++;
+    }
+    CUDA_TRY(launch_ref_ppe_bc(R, cur, st));
+    S->launches++;
+    if (cur != S->r_p) CUDA_TRY(cudaMemcpyAsync(S->r_p, cur, I.ncell * 8, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (iters) *iters = it;
+    return IFX_OK;
+}
+
+// ------------------------------------------------------------ fields
+
+ifx_status field_size(const Instance& I, int field, size_t* n) {
+    switch (field) {
+        case IFX_FIELD_U: case IFX_FIELD_V: case IFX_FIELD_P: case IFX_FIELD_IBLANK:
+        case IFX_FIELD_CELLTYPE: case IFX_FIELD_DIV:
+            *n = (size_t)I.nx * I.ny; return IFX_OK;
+        case IFX_FIELD_UF: *n = (size_t)(I.nx - 1) * (I.ny - 2); return IFX_OK;
+        case IFX_FIELD_VF: *n = (size_t)(I.nx - 2) * (I.ny - 1); return IFX_OK;
+        case IFX_FIELD_XC: *n = I.nx; return IFX_OK;
+        case IFX_FIELD_YC: *n = I.ny; return IFX_OK;
+    }
+    return set_error(IFX_ERR_ARG, "unknown field id");
+}
+
+ifx_status get_pitched(ifx_solver* S, const Instance& I, const double* src, double* host) {
+    CUDA_TRY(cudaMemcpy2DAsync(host, I.nx * sizeof(double), src, I.pitch * sizeof(double), I.nx * sizeof(double),
+                               I.ny, cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+
+static ifx_status new_solver(ifx_solver** out) {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return set_error(IFX_ERR_NODEVICE, "no CUDA device available");
+    ifx_solver* S = new ifx_solver();
+    CUDA_TRY(cudaGetDevice(&S->device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&S->ev0));
+    CUDA_TRY(cudaEventCreate(&S->ev1));
+    *out = S;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_create_batch(int n, const ifx_config* cfgs, const double* const* xfs,
+                                       const double* const* yfs, ifx_solver** out) {
+    if (!out || n < 1 || !cfgs || !xfs || !yfs) return set_error(IFX_ERR_ARG, "ifx_create_batch: bad argument");
+    *out = nullptr;
+    for (int k = 0; k < n; k++)
+        if (!xfs[k] || !yfs[k]) return set_error(IFX_ERR_ARG, "ifx_create_batch: null grid");
+    ifx_solver* S = nullptr;
+    IFX_TRY(new_solver(&S));
+    ifx_status st;
+    if (n == 1 && cfgs[0].mode == IFX_MODE_REFERENCE) st = create_reference(S, &cfgs[0], xfs[0], yfs[0]);
+    else st = create_method(S, n, cfgs, xfs, yfs);
+    if (st != IFX_OK) {
+        std::string msg = ifx::g_last_error;
+        ifx_destroy(S);
+        return set_error(st, msg);
+    }
+    *out = S;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_create(const ifx_config* cfg, const double* xf, const double* yf, ifx_solver** out) {
+    if (!cfg) return set_error(IFX_ERR_ARG, "ifx_create: null config");
+    const double* xs[1] = {xf};
+    const double* ys[1] = {yf};
+    return ifx_create_batch(1, cfg, xs, ys, out);
+}
+
+extern "C" ifx_status ifx_create_from_file(const char* inputs_path, ifx_solver** out) {
+    ifx_config c;
+    IFX_TRY(ifx_config_read(inputs_path, &c));
+    std::vector<double> xf(c.nx + 1), yf(c.ny + 1);
+    IFX_TRY(ifx_grid_read(c.xgrid, c.nx + 1, xf.data()));
+    IFX_TRY(ifx_grid_read(c.ygrid, c.ny + 1, yf.data()));
+    return ifx_create(&c, xf.data(), yf.data(), out);
+}
+
+extern "C" int ifx_num_instances(const ifx_solver* s) { return s ? (int)s->inst.size() : 0; }
+
+extern "C" ifx_status ifx_get_dims(const ifx_solver* S, int inst, int* nx, int* ny) {
+    if (!S || !nx || !ny || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_dims: bad argument");
+    *nx = S->inst[inst].nx;
+    *ny = S->inst[inst].ny;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_step(ifx_solver* S, int nsteps) {
+    if (!S || nsteps < 0) return set_error(IFX_ERR_ARG, "ifx_step: bad argument");
+    if (nsteps == 0) return IFX_OK;
+    CUDA_TRY(cudaSetDevice(S->device));
+    if (S->mode == IFX_MODE_REFERENCE) return step_reference(S, nsteps);
+    if (S->prec == IFX_PREC_FP64) return step_method<double>(S, nsteps);
+    return step_method<float>(S, nsteps);
+}
+
+extern "C" ifx_status ifx_ppe_reference(ifx_solver* S, int* iters) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_ppe_reference: null solver");
+    if (S->mode != IFX_MODE_REFERENCE) return set_error(IFX_ERR_STATE, "ifx_ppe_reference needs a REFERENCE-mode solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    return ppe_reference(S, iters);
+}
+
+extern "C" ifx_status ifx_get_field_i(ifx_solver* S, int inst, int field, double* host, size_t n) {
+    if (!S || !host || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_field: bad argument");
+    const Instance& I = S->inst[inst];
+    size_t need;
+    IFX_TRY(field_size(I, field, &need));
+    if (n != need) return set_error(IFX_ERR_ARG, "ifx_get_field: size mismatch, expected " + std::to_string(need));
+    CUDA_TRY(cudaSetDevice(S->device));
+    const int nx = I.nx, ny = I.ny;
+    if (field == IFX_FIELD_XC) { std::memcpy(host, I.xc.data(), nx * 8); return IFX_OK; }
+    if (field == IFX_FIELD_YC) { std::memcpy(host, I.yc.data(), ny * 8); return IFX_OK; }
+    if (S->mode == IFX_MODE_REFERENCE) {
+        const double* src = nullptr;
+        if (field == IFX_FIELD_U) src = S->r_cur ? S->r_ut : S->r_u;
+        else if (field == IFX_FIELD_V) src = S->r_cur ? S->r_vt : S->r_v;
+        else if (field == IFX_FIELD_P) src = S->r_p;
+        else if (field == IFX_FIELD_IBLANK) src = S->r_ib;
+        else if (field == IFX_FIELD_UF) src = S->r_uf;
+        else if (field == IFX_FIELD_VF) src = S->r_vf;
+        else return set_error(IFX_ERR_ARG, "field not available in REFERENCE mode");
+        CUDA_TRY(cudaMemcpyAsync(host, src, n * 8, cudaMemcpyDeviceToHost, S->stream));
+        CUDA_TRY(cudaStreamSynchronize(S->stream));
+        return IFX_OK;
+    }
+    const InstDev& d = I.dev;
+    switch (field) {
+        case IFX_FIELD_U: return get_pitched(S, I, d.u, host);
+        case IFX_FIELD_V: return get_pitched(S, I, d.v, host);
+        case IFX_FIELD_P: return get_pitched(S, I, d.p, host);
+        case IFX_FIELD_IBLANK: return get_pitched(S, I, d.iblank, host);
+        case IFX_FIELD_DIV: return get_pitched(S, I, d.div, host);
+        case IFX_FIELD_CELLTYPE:
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) host[i + j * nx] = I.type[i + j * I.pitch];
+            return IFX_OK;
+        case IFX_FIELD_UF:
+        case IFX_FIELD_VF: {
+            std::vector<double> full((size_t)nx * ny);
+            IFX_TRY(get_pitched(S, I, field == IFX_FIELD_UF ? d.U : d.V, full.data()));
+            if (field == IFX_FIELD_UF) {
+                for (int j = 1; j < ny - 1; j++)
+                    for (int i = 0; i < nx - 1; i++) host[i + (j - 1) * (nx - 1)] = full[i + j * nx];
+            } else {
+                for (int j = 0; j < ny - 1; j++)
+                    for (int i = 1; i < nx - 1; i++) host[(i - 1) + j * (nx - 2)] = full[i + j * nx];
+            }
+            return IFX_OK;
+        }
+    }
+    return set_error(IFX_ERR_ARG, "unknown field");
+}
+
+extern "C" ifx_status ifx_get_field(ifx_solver* S, int field, double* host, size_t n) {
+    return ifx_get_field_i(S, 0, field, host, n);
+}
+
+extern "C" ifx_status ifx_set_field_i(ifx_solver* S, int inst, int field, const double* host, size_t n) {
+    if (!S || !host || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_set_field: bad argument");
+    const Instance& I = S->inst[inst];
+    if (field != IFX_FIELD_U && field != IFX_FIELD_V && field != IFX_FIELD_P)
+        return set_error(IFX_ERR_ARG, "ifx_set_field: only u, v, p can be set");
+    if (n != (size_t)I.nx * I.ny) return set_error(IFX_ERR_ARG, "ifx_set_field: size mismatch");
+    CUDA_TRY(cudaSetDevice(S->device));
+    double* dst;
+    size_t pitch = I.pitch;
+    if (S->mode == IFX_MODE_REFERENCE) {
+        dst = field == IFX_FIELD_U ? (S->r_cur ? S->r_ut : S->r_u) : field == IFX_FIELD_V ? (S->r_cur ? S->r_vt : S->r_v) : S->r_p;
+    } else {
+        dst = field == IFX_FIELD_U ? I.dev.u : field == IFX_FIELD_V ? I.dev.v : I.dev.p;
+    }
+    CUDA_TRY(cudaMemcpy2DAsync(dst, pitch * 8, host, I.nx * 8, I.nx * 8, I.ny, cudaMemcpyHostToDevice, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_set_field(ifx_solver* S, int field, const double* host, size_t n) {
+    return ifx_set_field_i(S, 0, field, host, n);
+}
+
+extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
+    if (!S || !dir) return set_error(IFX_ERR_ARG, "ifx_write_results: bad argument");
+    const Instance& I = S->inst[0];
+    const size_t n = (size_t)I.nx * I.ny;
+    std::vector<double> q(n);
+    const std::string d(dir);
+    struct { int f; const char* name; } outs[4] = {
+        {IFX_FIELD_P, "/p.dat"}, {IFX_FIELD_U, "/uc.dat"}, {IFX_FIELD_V, "/vc.dat"}, {IFX_FIELD_IBLANK, "/final_results.dat"}};
+    for (auto& o : outs) {
+        IFX_TRY(ifx_get_field(S, o.f, q.data(), n));
+        IFX_TRY(ifx_write_tecplot((d + o.name).c_str(), I.nx, I.ny, I.xc.data(), I.yc.data(), q.data()));
+    }
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_stats(ifx_solver* S, int inst, ifx_stats* out) {
+    if (!S || !out || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_stats: bad argument");
+    std::memset(out, 0, sizeof(*out));
+    out->steps = S->steps_done;
+    out->kernel_launches = S->launches;
+    const Instance& I = S->inst[inst];
+    if (S->mode == IFX_MODE_REFERENCE) {
+        out->last_ad_iters = S->r_iters.empty() ? 0 : S->r_iters.back();
+        for (int it : S->r_iters) out->ad_iters_total += it;
+        out->n_fluid = I.NX * I.NY;
+        return IFX_OK;
+    }
+    CUDA_TRY(cudaSetDevice(S->device));
+    CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, S->inst.size() * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    const InstState& s = S->hS[inst];
+    out->last_ad_iters = s.pred_iters;
+    out->last_ppe_iters = s.ppe_iters;
+    out->last_ad_metric = s.pred_metric;
+    out->last_ppe_residual = s.ppe_rel;
+    out->max_div = s.max_div;
+    out->cd = s.cd;
+    out->cl = s.cl;
+    out->mass_flux_in = s.flux_in;
+    out->mass_flux_out = s.flux_out;
+    out->n_fluid = I.n_fluid;
+    out->n_ibm_ghost = I.n_ibm;
+    out->mg_levels = (int)I.lev.size();
+    out->status = s.status;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_forces(ifx_solver* S, double* cd, double* cl) {
+    ifx_stats st;
+    IFX_TRY(ifx_get_stats(S, 0, &st));
+    if (cd) *cd = st.cd;
+    if (cl) *cl = st.cl;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* cells, int* nb, double* wu,
+                                         double* wp, double* bi_ip, int* count) {
+    if (!S || !count || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_ibm_ghosts: bad argument");
+    const Instance& I = S->inst[inst];
+    *count = (S->mode == IFX_MODE_METHOD) ? I.n_ibm : 0;
+    if (*count == 0 || cap <= 0) return IFX_OK;
+    CUDA_TRY(cudaSetDevice(S->device));
+    std::vector<GhostDev> g(I.ghost_cnt);
+    std::vector<double> bip(4 * (size_t)std::max(1, S->nibm));
+    CUDA_TRY(cudaMemcpyAsync(g.data(), S->dG + I.ghost_beg, g.size() * sizeof(GhostDev), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaMemcpyAsync(bip.data(), S->dBiIp, bip.size() * sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    // position of this instance's first IBM ghost in the global IBM list
+    int ibase = 0;
+    for (int k = 0; k < inst; k++) ibase += S->inst[k].n_ibm;
+    auto dense = [&](int c) { return (c % I.pitch) + (c / I.pitch) * I.nx; };
+    int q = 0;
+    for (const GhostDev& e : g) {
+        if (e.side >= 0) continue;
+        if (q >= cap) break;
+        if (cells) cells[q] = dense(e.cell);
+        for (int k = 0; k < 4; k++) {
+            if (nb) nb[4 * q + k] = dense(e.nb[k]);
+            if (wu) wu[4 * q + k] = e.wu[k];
+            if (wp) wp[4 * q + k] = e.wp[k];
+        }
+        if (bi_ip)
+            for (int k = 0; k < 4; k++) bi_ip[4 * q + k] = bip[4 * (size_t)(ibase + q) + k];
+        q++;
+    }
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_last_step_ms(ifx_solver* S, double* ms) {
+    if (!S || !ms) return set_error(IFX_ERR_ARG, "ifx_last_step_ms: bad argument");
+    *ms = S->last_ms;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_synchronize(ifx_solver* S) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_synchronize: null solver");
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+extern "C" void ifx_destroy(ifx_solver* S) {
+    if (!S) return;
+    cudaSetDevice(S->device);
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    if (S->graph) cudaGraphDestroy(S->graph);
+    for (void* p : S->allocs) cudaFree(p);
+    if (S->hS) cudaFreeHost(S->hS);
+    if (S->hCtl) cudaFreeHost(S->hCtl);
+    if (S->h_out) cudaFreeHost(S->h_out);
+    if (S->ev0) cudaEventDestroy(S->ev0);
+    if (S->ev1) cudaEventDestroy(S->ev1);
+    if (S->stream) cudaStreamDestroy(S->stream);
+    delete S;
+}

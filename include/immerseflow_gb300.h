@@ -162,6 +162,8 @@ ifx_status ifx_create_from_file(const char* inputs_path, ifx_solver** out);
 ifx_status ifx_create_batch(int n, const ifx_config* cfgs, const double* const* xfs,
                             const double* const* yfs, ifx_solver** out);
 int        ifx_num_instances(const ifx_solver* s);
+/* Grid size of instance inst including the ghost ring (nx = NX+2, ny = NY+2). */
+ifx_status ifx_get_dims(const ifx_solver* s, int inst, int* nx, int* ny);
 
 /* One reference time step is ImmerseFlow::ADsolver (src/include/ADSolver.cu:268-395)
  * in REFERENCE mode; in METHOD mode it is predictor -> PPE -> projection. */
@@ -178,6 +180,15 @@ ifx_status ifx_set_field_i(ifx_solver* s, int inst, int field, const double* hos
 /* Writes p.dat, uc.dat, vc.dat, final_results.dat into dir (src/include/postSim.cu:10-66). */
 ifx_status ifx_write_results(ifx_solver* s, const char* dir);
 ifx_status ifx_forces(ifx_solver* s, double* cd, double* cl);
+/* Immersed-boundary ghost table of instance inst (no reference counterpart:
+ * the reference has no ghost-cell code, src/include/preSim.cu:110-136).
+ * Writes up to cap entries in row-major cell order: dense cell index
+ * (i + j*nx), the 4 image-point stencil cells, Dirichlet (velocity) and
+ * Neumann (pressure) weights, and body-intercept / image-point coordinates
+ * (bi_ip[4k..4k+3] = BIx, BIy, IPx, IPy).  Any output may be NULL.
+ * *count receives the number of ghost cells. */
+ifx_status ifx_get_ibm_ghosts(ifx_solver* s, int inst, int cap, int* cells, int* nb, double* wu,
+                              double* wp, double* bi_ip, int* count);
 ifx_status ifx_get_stats(ifx_solver* s, int inst, ifx_stats* out);
 /* Device milliseconds of the last ifx_step call, timed with CUDA events on
  * the solver's own stream. */

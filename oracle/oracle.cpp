@@ -620,7 +620,8 @@ void build_levels(orc_solver* S) {
     // coarsen while the level is large and both sides can halve
     while (true) {
         const Level& f = S->L.back();
-        if (!(f.NX * f.NY > 64 && f.NX >= 4 && f.NY >= 4)) break;
+        // the finest level is always coarsened once (method mode needs NX, NY >= 4)
+        if (!(f.NX >= 4 && f.NY >= 4 && (S->L.size() == 1 || f.NX * f.NY > 64))) break;
         Level c;
         c.NX = (f.NX + 1) / 2; c.NY = (f.NY + 1) / 2;
         c.nx = c.NX + 2; c.ny = c.NY + 2;
@@ -712,6 +713,10 @@ void build_levels(orc_solver* S) {
     }
 }
 
+// A cell takes part in the pressure multigrid when it is active and has at
+// least one open face (the CUDA path encodes exactly this in its stencil bits).
+inline bool live(const Level& v, int id) { return v.act[id] && (v.bits[id] & 0x0F); }
+
 // Laplacian of e at active cell (i,j) of a level, and its diagonal.  On the
 // finest level a face to an IBM ghost uses the ghost's image-point value
 // evaluated from the same iterate (ghost unknowns eliminated).
@@ -760,7 +765,7 @@ void smooth(orc_solver* S, int l, bool zero_init) {
     for (int j = 1; j <= v.NY; j++)
         for (int i = 1; i <= v.NX; i++) {
             int id = IDX(i, j, v.nx);
-            if (!v.act[id]) continue;
+            if (!live(v, id)) continue;
             double Le, D;
             lap(S, v, v.e.data(), i, j, &Le, &D, l == 0);
             if (zero_init) v.e2[id] = -om * v.r[id] * rcp_approx(D);
@@ -788,7 +793,7 @@ void coarse_solve(orc_solver* S, int l) {
                 for (int i = 1; i <= v.NX; i++) {
                     if (((i + j) & 1) != col) continue;
                     int id = IDX(i, j, v.nx);
-                    if (!v.act[id]) continue;
+                    if (!live(v, id)) continue;
                     double Le, D;
                     lap(S, v, v.e.data(), i, j, &Le, &D);
                     v.e[id] = v.e[id] + om * (Le - v.r[id]) * rcp_approx(D);
@@ -808,12 +813,12 @@ void restrict_res(orc_solver* S, int l) {
                     int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
                     if (i > f.NX || j > f.NY) continue;
                     int id = IDX(i, j, f.nx);
-                    if (!f.act[id]) continue;
+                    if (!live(f, id)) continue;
                     double Le, D;
                     lap(S, f, f.e.data(), i, j, &Le, &D, l == 0);
                     acc += (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
                 }
-            c.r[cid] = c.act[cid] ? acc / (c.dw[I] * c.dh[J]) : 0.0;
+            c.r[cid] = live(c, cid) ? acc / (c.dw[I] * c.dh[J]) : 0.0;
         }
 }
 
@@ -824,15 +829,15 @@ void prolong_add(orc_solver* S, int l) {
     for (int j = 1; j <= f.NY; j++)
         for (int i = 1; i <= f.NX; i++) {
             int id = IDX(i, j, f.nx);
-            if (!f.act[id]) continue;
+            if (!live(f, id)) continue;
             int I = f.pI[i], In = f.pIn[i], J = f.pJ[j], Jn = f.pJn[j];
             double wx = f.pwx[i], wy = f.pwy[j];
             double w00 = (1.0 - wx) * (1.0 - wy), w10 = wx * (1.0 - wy), w01 = (1.0 - wx) * wy, w11 = wx * wy;
             int c00 = IDX(I, J, c.nx), c10 = IDX(In, J, c.nx), c01 = IDX(I, Jn, c.nx), c11 = IDX(In, Jn, c.nx);
-            w00 = c.act[c00] ? w00 : 0.0;
-            w10 = c.act[c10] ? w10 : 0.0;
-            w01 = c.act[c01] ? w01 : 0.0;
-            w11 = c.act[c11] ? w11 : 0.0;
+            w00 = live(c, c00) ? w00 : 0.0;
+            w10 = live(c, c10) ? w10 : 0.0;
+            w01 = live(c, c01) ? w01 : 0.0;
+            w11 = live(c, c11) ? w11 : 0.0;
             double sw = w00 + w10 + w01 + w11;
             double val = (w00 * c.e[c00] + w10 * c.e[c10] + w01 * c.e[c01] + w11 * c.e[c11]) / sw;
             f.e[id] += val;

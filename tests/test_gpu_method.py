@@ -1,0 +1,133 @@
+"""METHOD mode (fractional step + ghost-cell IBM) on the GPU against the oracle.
+
+Tolerances:
+  - iBlank, cell types, ghost cells, image-point stencils and weights: bit-exact
+    (the set-up kernels are built without FMA contraction, like the oracle);
+  - FP64 fields after several steps: 1e-10 relative to the field's max
+    (FMA contraction in the step kernels, sums reduced in another order);
+  - a batched instance equals the same instance run alone, bit for bit;
+  - graph execution equals the host-driven loop, bit for bit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import immerseflow_gb300 as ifx
+from immerseflow_gb300 import _capi as capi
+from immerseflow_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+FIELD_RTOL = 1e-10
+
+
+def small_cylinder(prec=capi.PREC_FP64, nx=96, ny=64, angle=0.0, b=0.5):
+    return cases.external(nx, ny, 12.0, 8.0, 4.0, 4.0, 0.5, b, angle, 100.0, 1e-2, prec, ratio=4.0, width=1.0)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("angle,b", [(0.0, 0.5), (17.0, 0.15), (-30.0, 0.3)])
+def test_tagging_and_ghost_table_bit_exact(oracle, angle, b):
+    cfg, xf, yf = small_cylinder(angle=angle, b=b)
+    s = ifx.Solver.create(cfg, xf, yf)
+    o = oracle.method(cfg, xf, yf)
+    assert np.array_equal(s.get(capi.FIELD_IBLANK), o.get(capi.FIELD_IBLANK))
+    assert np.array_equal(s.get(capi.FIELD_CELLTYPE), o.get(capi.FIELD_CELLTYPE))
+    cells, nb, wu, wp, bip = s.ibm_ghosts()
+    oc, onb, owu, owp, obi, oip = o.ghosts()
+    assert len(cells) > 0
+    assert np.array_equal(cells, oc)
+    assert np.array_equal(nb, onb)
+    assert np.array_equal(wu, owu)
+    assert np.array_equal(wp, owp)
+    assert np.array_equal(bip[:, :2], obi) and np.array_equal(bip[:, 2:], oip)
+
+
+def _compare(s, o, fields=(capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF, capi.FIELD_VF), tol=FIELD_RTOL):
+    for f in fields:
+        a, b = s.get(f), o.get(f)
+        assert rel(a, b) <= tol, (f, rel(a, b))
+
+
+def test_cavity_vs_oracle(oracle):
+    cfg, xf, yf = cases.cavity(n=64)
+    s = ifx.Solver.create(cfg, xf, yf)
+    o = oracle.method(cfg, xf, yf)
+    for k in range(4):
+        s.step(1)
+        o.step(1)
+        st, so = s.stats(), o.stats()
+        assert st.last_ad_iters == so.last_ad_iters
+        assert st.last_ppe_iters == so.last_ppe_iters
+        assert st.last_ppe_residual <= cfg.ppe_tol
+    _compare(s, o)
+    assert s.stats().max_div < 1e-5
+
+
+def test_cylinder_vs_oracle(oracle):
+    cfg, xf, yf = small_cylinder()
+    s = ifx.Solver.create(cfg, xf, yf)
+    o = oracle.method(cfg, xf, yf)
+    for k in range(3):
+        s.step(1)
+        o.step(1)
+        st, so = s.stats(), o.stats()
+        assert st.last_ad_iters == so.last_ad_iters
+        assert abs(st.last_ppe_iters - so.last_ppe_iters) <= 1
+    _compare(s, o, tol=1e-9)
+    st, so = s.stats(), o.stats()
+    assert abs(st.cd - so.cd) <= 1e-8 * abs(so.cd)
+    assert abs(st.cl - so.cl) <= 1e-8 * max(abs(so.cd), 1.0)
+
+
+def test_rotated_ellipse_stretched_vs_oracle(oracle):
+    cfg, xf, yf = small_cylinder(nx=80, ny=72, angle=20.0, b=0.2)
+    s = ifx.Solver.create(cfg, xf, yf)
+    o = oracle.method(cfg, xf, yf)
+    s.step(3)
+    o.step(3)
+    _compare(s, o, tol=1e-9)
+
+
+def test_graph_equals_host_loop():
+    cfg, xf, yf = small_cylinder()
+    a = ifx.Solver.create(cfg, xf, yf)
+    a.step(3)
+    os.environ["IFX_NO_GRAPH"] = "1"
+    try:
+        b = ifx.Solver.create(cfg, xf, yf)
+        b.step(3)
+    finally:
+        del os.environ["IFX_NO_GRAPH"]
+    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+        assert np.array_equal(a.get(f), b.get(f))
+
+
+def test_batch_member_equals_alone():
+    specs = [small_cylinder(nx=96, ny=64), cases.cavity(n=40), small_cylinder(nx=70, ny=90, angle=25.0, b=0.25)]
+    batch = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+    assert batch.n_instances == 3
+    batch.step(3)
+    for k, (c, x, y) in enumerate(specs):
+        alone = ifx.Solver.create(c, x, y)
+        alone.step(3)
+        for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+            assert np.array_equal(batch.get(f, inst=k), alone.get(f)), (k, f)
+        assert batch.stats(k).last_ppe_iters == alone.stats().last_ppe_iters
+
+
+def test_mixed_precision_close_to_fp64():
+    cfg64, xf, yf = small_cylinder()
+    cfg32, _, _ = small_cylinder(prec=capi.PREC_MIXED)
+    a = ifx.Solver.create(cfg64, xf, yf)
+    b = ifx.Solver.create(cfg32, xf, yf)
+    a.step(5)
+    b.step(5)
+    for f in (capi.FIELD_U, capi.FIELD_V):
+        ua, ub = a.get(f), b.get(f)
+        assert np.linalg.norm(ub - ua) / np.linalg.norm(ua) <= 1e-6, f
+    cda, cdb = a.stats().cd, b.stats().cd
+    assert abs(cda - cdb) <= 1e-3 * abs(cda)
