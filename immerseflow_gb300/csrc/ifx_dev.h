@@ -61,10 +61,13 @@ struct LevelDev {
     void* e;   // correction, T*
     void* e2;  // Jacobi partner, T*
     void* r;   // right-hand side, T*
-    // prolongation tables from the next coarser level into this one
+    // prolongation tables from the next coarser level into this one; at a
+    // domain boundary the neighbour is the cell itself mirrored with sign
+    // psx/psy (+1 Neumann, -1 Dirichlet)
     const int *pI, *pIn, *pJ, *pJn;
     const double *pwx, *pwy;
     const float *pwxf, *pwyf;
+    const signed char *psx, *psy;
     int child;   // LevelDev index of the next coarser level, -1 at the coarsest
     int parent;  // LevelDev index of the next finer level, -1 at the finest
 };
@@ -85,6 +88,8 @@ struct InstDev {
     const uint8_t* type;
     const int* gidx;             // cell -> global ghost index (IBM ghosts), -1 otherwise
     double *qbu, *qbv;
+    // BiCGSTAB vectors of the pressure solve (FP64)
+    double *kr, *krh, *kp, *kv, *ks, *kt, *kph, *ksh;
     // mixed-precision predictor corrections
     float *du, *dv, *du2, *dv2, *rfu, *rfv;
     // body (ellipse), bit-exact predicate constants
@@ -95,7 +100,8 @@ struct InstDev {
 struct InstState {
     int pred_state, pred_iters, ppe_state, ppe_iters;
     int status, have_nold, pad1, pad2;
-    double pred_metric, ppe_rel, bmean, rmean, bnorm, pmean;
+    double pred_metric, ppe_rel, bmean, bnorm, pmean;
+    double rho, alpha, omega, beta;           // BiCGSTAB scalars
     double max_div, cd, cl, flux_in, flux_out, spare;
 };
 

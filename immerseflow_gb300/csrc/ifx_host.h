@@ -20,6 +20,7 @@ struct HostLevel {
     std::vector<uint8_t> act, bits;  // pitched
     std::vector<int> pI, pIn, pJ, pJn;
     std::vector<double> pwx, pwy;
+    std::vector<signed char> psx, psy;
     // device
     double *d_kx = nullptr, *d_ky = nullptr, *d_ix = nullptr, *d_iy = nullptr, *d_dw = nullptr, *d_dh = nullptr;
     float *d_kxf = nullptr, *d_kyf = nullptr, *d_ixf = nullptr, *d_iyf = nullptr, *d_dwf = nullptr, *d_dhf = nullptr;
@@ -28,6 +29,7 @@ struct HostLevel {
     int *d_pI = nullptr, *d_pIn = nullptr, *d_pJ = nullptr, *d_pJn = nullptr;
     double *d_pwx = nullptr, *d_pwy = nullptr;
     float *d_pwxf = nullptr, *d_pwyf = nullptr;
+    signed char *d_psx = nullptr, *d_psy = nullptr;
 };
 
 struct Instance {

@@ -19,17 +19,29 @@ cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* par
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
                             cudaStream_t s);
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
+cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                              const GhostDev* G, double* part, cudaStream_t s);
+cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
+                                 LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 template <typename T>
-cudaError_t launch_ppe_resid(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                             const GhostDev* G, double* part, cudaStream_t s);
-cudaError_t launch_ppe_reduce(const InstDev* I, InstState* S, const double* part, int ninst, LoopCtl* ctl,
-                              unsigned long long handle, cudaStream_t s);
+cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          cudaStream_t s);
+template <typename T>
+cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                              const GhostDev* G, double* part, int e_alt, int which, cudaStream_t s);
+cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
+                               cudaStream_t s);
+template <typename T>
+cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          cudaStream_t s);
+cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          double* part, cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          const GhostDev* G, const int* ibm, int nibm, int flags, int src_alt, cudaStream_t s);
+                          const GhostDev* G, int flags, int src_alt, cudaStream_t s);
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                            const GhostDev* G, int fine_alt, int init_coarse, cudaStream_t s);
+                            const GhostDev* G, int fine_alt, cudaStream_t s);
 template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
                            int coarse_alt, cudaStream_t s);

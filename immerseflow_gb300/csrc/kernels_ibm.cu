@@ -238,6 +238,19 @@ __global__ void k_ghost_weights(GhostDev* __restrict__ G, const int* __restrict_
             wN[k] = w;
         }
     }
+    // pressure: nodes that are IBM ghosts themselves are dropped so that every
+    // ghost pressure is a linear function of fluid cells
+    double keep = 0.0;
+    for (int k = 0; k < 4; k++)
+        if (k != gk && in.type[g.nb[k]] != T_GHOST) keep += wN[k];
+    if (!(keep > 0.05)) {
+        const double wb[4] = {(1 - xi) * (1 - eta), xi * (1 - eta), (1 - xi) * eta, xi * eta};
+        keep = 0.0;
+        for (int k = 0; k < 4; k++) {
+            wN[k] = wb[k];
+            if (k != gk && in.type[g.nb[k]] != T_GHOST) keep += wb[k];
+        }
+    }
     for (int k = 0; k < 4; k++) {
         if (k == gk) {
             g.wu[k] = g.wv[k] = g.wp[k] = 0.0;
@@ -245,7 +258,7 @@ __global__ void k_ghost_weights(GhostDev* __restrict__ G, const int* __restrict_
         }
         g.wu[k] = -wD[k];
         g.wv[k] = -wD[k];
-        g.wp[k] = wN[k];
+        g.wp[k] = (in.type[g.nb[k]] != T_GHOST) ? wN[k] / keep : 0.0;
     }
     g.cu = g.cv = 0.0;
 }

@@ -129,16 +129,17 @@ __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* q
 }
 
 // Image-point value of the IBM ghost at global entry gid, from field e;
-// ws receives the weight on cell `self`.
-template <typename T>
-__device__ __forceinline__ T ghost_eval(const GhostDev* G, int gid, const T* e, int self, T& ws) {
+// ws receives the weight on cell `self`.  Pressure stencils reference fluid
+// cells only, so this is an exact linear function of the fluid values.
+template <typename TC, typename TE>
+__device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
     const GhostDev& g = G[gid];
-    T acc = (T)0;
-    ws = (T)0;
+    TC acc = (TC)0;
+    ws = (TC)0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const T w = (T)g.wp[k];
-        acc += w * e[g.nb[k]];
+        const TC w = (TC)g.wp[k];
+        acc += w * (TC)e[g.nb[k]];
         if (g.nb[k] == self) ws += w;
     }
     return acc;
@@ -146,37 +147,38 @@ __device__ __forceinline__ T ghost_eval(const GhostDev* G, int gid, const T* e, 
 
 // Pressure-type Laplacian at live cell (i,j): Le = sum c (e_nb - e) with
 // closed faces dropped, Dirichlet sides adding 2c to the diagonal, and (finest
-// level) faces to IBM ghosts using the ghost's image-point value.  D is the
-// diagonal of the ghost-eliminated operator.
-template <typename T, bool LVL0>
-__device__ __forceinline__ void lap(const LevelDev& L, const T* __restrict__ e, int i, int j, int id,
-                                    uint8_t bt, const GhostDev* G, const int* gidx, T& Le, T& D) {
-    const T* kx = LvA<T>::kx(L);
-    const T* ky = LvA<T>::ky(L);
-    const T* ix = LvA<T>::ix(L);
-    const T* iy = LvA<T>::iy(L);
-    const T cE = kx[i] * ix[i], cW = kx[i - 1] * ix[i];
-    const T cN = ky[j] * iy[j], cS = ky[j - 1] * iy[j];
-    const T ce = (bt & B_E) ? cE : (T)0, cw = (bt & B_W) ? cW : (T)0;
-    const T cn = (bt & B_N) ? cN : (T)0, cs = (bt & B_S) ? cS : (T)0;
-    T dd = ce + cw + cn + cs;
+// level) faces to IBM ghosts using the ghost's image-point value (ghost
+// unknowns eliminated).  D is the diagonal of that operator.  Coefficients
+// and arithmetic in TC, field values of type TE.
+template <typename TC, typename TE, bool LVL0>
+__device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id,
+                                    uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+    const TC* kx = LvA<TC>::kx(L);
+    const TC* ky = LvA<TC>::ky(L);
+    const TC* ix = LvA<TC>::ix(L);
+    const TC* iy = LvA<TC>::iy(L);
+    const TC cE = kx[i] * ix[i], cW = kx[i - 1] * ix[i];
+    const TC cN = ky[j] * iy[j], cS = ky[j - 1] * iy[j];
+    const TC ce = (bt & B_E) ? cE : (TC)0, cw = (bt & B_W) ? cW : (TC)0;
+    const TC cn = (bt & B_N) ? cN : (TC)0, cs = (bt & B_S) ? cS : (TC)0;
+    TC dd = ce + cw + cn + cs;
     if (L.dirmask) {
-        if (i == L.NX && (L.dirmask & (1 << 1))) dd += (T)2 * cE;
-        if (i == 1 && (L.dirmask & (1 << 0))) dd += (T)2 * cW;
-        if (j == L.NY && (L.dirmask & (1 << 3))) dd += (T)2 * cN;
-        if (j == 1 && (L.dirmask & (1 << 2))) dd += (T)2 * cS;
+        if (i == L.NX && (L.dirmask & (1 << 1))) dd += (TC)2 * cE;
+        if (i == 1 && (L.dirmask & (1 << 0))) dd += (TC)2 * cW;
+        if (j == L.NY && (L.dirmask & (1 << 3))) dd += (TC)2 * cN;
+        if (j == 1 && (L.dirmask & (1 << 2))) dd += (TC)2 * cS;
     }
     const int P = L.pitch;
-    T eE = e[id + 1], eW = e[id - 1], eN = e[id + P], eS = e[id - P];
-    T dm = dd;
+    TC eE = (TC)e[id + 1], eW = (TC)e[id - 1], eN = (TC)e[id + P], eS = (TC)e[id - P];
+    TC dm = dd;
     if (LVL0 && (bt & 0xF0)) {
-        T ws;
-        if (bt & G_E) { eE = ghost_eval<T>(G, gidx[id + 1], e, id, ws); dm -= ce * ws; }
-        if (bt & G_W) { eW = ghost_eval<T>(G, gidx[id - 1], e, id, ws); dm -= cw * ws; }
-        if (bt & G_N) { eN = ghost_eval<T>(G, gidx[id + P], e, id, ws); dm -= cn * ws; }
-        if (bt & G_S) { eS = ghost_eval<T>(G, gidx[id - P], e, id, ws); dm -= cs * ws; }
+        TC ws;
+        if (bt & G_E) { eE = ghost_eval<TC, TE>(G, gidx[id + 1], e, id, ws); dm -= ce * ws; }
+        if (bt & G_W) { eW = ghost_eval<TC, TE>(G, gidx[id - 1], e, id, ws); dm -= cw * ws; }
+        if (bt & G_N) { eN = ghost_eval<TC, TE>(G, gidx[id + P], e, id, ws); dm -= cn * ws; }
+        if (bt & G_S) { eS = ghost_eval<TC, TE>(G, gidx[id - P], e, id, ws); dm -= cs * ws; }
     }
-    Le = ce * eE + cw * eW + cn * eN + cs * eS - dd * e[id];
+    Le = ce * eE + cw * eW + cn * eN + cs * eS - dd * (TC)e[id];
     D = dm;
 }
 
@@ -431,66 +433,79 @@ __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restric
 }
 
 // ------------------------------------------------------------------ PPE
+//
+// BiCGSTAB in FP64 on L p = b (ghost-eliminated finest-level operator),
+// preconditioned by one multigrid V-cycle in T.  Per-instance scalars live
+// in InstState; every reduction is per instance over its tiles, fixed order.
 
-// FP64 residual r = (b - mean b) - L p on the finest level, stored in T.
-template <typename T>
-__global__ void k_ppe_resid(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                            const GhostDev* __restrict__ G, double* __restrict__ part) {
+__device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, uint8_t& bt) {
+    if (i < 1 || i > L.NX || j < 1 || j > L.NY) return false;
+    id = i + j * L.pitch;
+    bt = L.bits[id];
+    return (bt & 0x0F) != 0;
+}
+
+// r = (b - mean b) - L p, rh = r, p_dir = v = 0.
+// partials: 0 (r,r)  1 (b,b)  2 (rh,r)  3 (p,area)
+__global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                             const GhostDev* __restrict__ G, double* __restrict__ part) {
     const Tile t = tiles[blockIdx.x];
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
     const LevelDev& L = LV[in.lev0];
-    int i, j;
+    int i, j, id;
+    uint8_t bt;
     tile_ij(t, i, j);
-    double acc[NPART] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
-        const int id = i + j * in.pitch;
-        const uint8_t bt = L.bits[id];
-        if (bt & 0x0F) {
-            double Lp, D;
-            lap<double, true>(L, in.p, i, j, id, bt, G, in.gidx, Lp, D);
-            const double bb = in.b[id] - st.bmean;
-            const double r = bb - Lp;
-            ((T*)L.r)[id] = (T)r;
-            const double a = in.dx[i] * in.dy[j];
-            acc[0] = r * a;
-            acc[1] = r;
-            acc[2] = r * r;
-            acc[3] = bb * bb;
-            acc[4] = in.p[id] * a;
-            acc[5] = 1.0;
-        }
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        double Lp, D;
+        lap<double, double, true>(L, in.p, i, j, id, bt, G, in.gidx, Lp, D);
+        const double bb = in.b[id] - st.bmean;
+        const double r = bb - Lp;
+        in.kr[id] = r;
+        in.krh[id] = r;
+        in.kp[id] = 0.0;
+        in.kv[id] = 0.0;
+        acc[0] = r * r;
+        acc[1] = bb * bb;
+        acc[2] = r * r;
+        acc[3] = in.p[id] * (in.dx[i] * in.dy[j]);
     }
-    __shared__ double out[NPART];
-    block_sum<NPART>(acc, out);
-    if (threadIdx.x < NPART) part[(size_t)blockIdx.x * NPART + threadIdx.x] = out[threadIdx.x];
+    __shared__ double out[4];
+    block_sum<4>(acc, out);
+    if (threadIdx.x < 4) part[(size_t)blockIdx.x * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
-__global__ void k_ppe_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
-                             const double* __restrict__ part, LoopCtl* ctl, unsigned long long handle) {
+// Convergence test on ||r||, then rho, beta for the next direction.  Votes.
+__global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                                const double* __restrict__ part, int start, LoopCtl* ctl,
+                                unsigned long long handle) {
     const int k = blockIdx.x;
     const InstDev& in = I[k];
     bool active = false;
     if (S[k].ppe_state == ST_ACTIVE) {
-        double r[NPART];
-        inst_sum<NPART>(part, in.tile_beg, in.tile_cnt, r);
+        double r[4];
+        inst_sum<4>(part, in.tile_beg, in.tile_cnt, r);
         if (threadIdx.x == 0) {
-            const double rm = in.singular ? r[0] / in.area : 0.0;
-            double rn2 = r[2] - 2.0 * rm * r[1] + rm * rm * r[5];
-            rn2 = rn2 > 0.0 ? rn2 : 0.0;
-            const double bn = sqrt(r[3]);
-            const double rel = sqrt(rn2) / (bn > 1e-300 ? bn : 1e-300);
-            S[k].rmean = rm;
-            S[k].bnorm = bn;
-            S[k].ppe_rel = rel;
-            S[k].pmean = r[4] / in.area;
-            const int it = S[k].ppe_iters;
-            if (rel <= in.ppe_tol || it >= in.ppe_itermax) {
-                S[k].ppe_state = ST_DONE;
+            InstState& st = S[k];
+            if (start) {
+                st.bnorm = sqrt(r[1]);
+                st.rho = st.alpha = st.omega = 1.0;
+                st.ppe_iters = 0;
             } else {
-                S[k].ppe_iters = it + 1;
+                st.ppe_iters += 1;
+            }
+            const double rel = sqrt(r[0]) / (st.bnorm > 1e-300 ? st.bnorm : 1e-300);
+            st.ppe_rel = rel;
+            st.pmean = r[3] / in.area;
+            if (rel <= in.ppe_tol || st.ppe_iters >= in.ppe_itermax) {
+                st.ppe_state = ST_DONE;
+            } else {
+                const double rho1 = r[2];
+                st.beta = (rho1 / st.rho) * (st.alpha / st.omega);
+                st.rho = rho1;
                 active = true;
             }
         }
@@ -498,68 +513,151 @@ __global__ void k_ppe_reduce(const InstDev* __restrict__ I, InstState* __restric
     if (threadIdx.x == 0) loop_vote(ctl, active, handle);
 }
 
-// Weighted-Jacobi sweep on one multigrid level (tiles of that level for all
-// instances), plus on the finest level the IBM ghost entries.
-// flags: 1 = start from e = 0, 2 = add the result into p (finest level).
+// p_dir = r + beta (p_dir - omega v); preconditioner input.
 template <typename T>
-__global__ void k_smooth(const Tile* __restrict__ tiles, int ntiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         const GhostDev* __restrict__ G, const int* __restrict__ ibm, int nibm, int flags,
-                         int src_alt) {
-    const bool zero = flags & 1, addp = flags & 2;
-    if ((int)blockIdx.x < ntiles) {
-        const Tile t = tiles[blockIdx.x];
-        const LevelDev& L = LV[t.lev];
-        const InstState& st = S[L.inst];
-        if (st.ppe_state != ST_ACTIVE) return;
-        int i, j;
-        tile_ij(t, i, j);
-        if (i < 1 || i > L.NX || j < 1 || j > L.NY) return;
-        const int id = i + j * L.pitch;
-        const uint8_t bt = L.bits[id];
-        if (!(bt & 0x0F)) return;
-        const T* src = (const T*)(src_alt ? L.e2 : L.e);
-        T* dst = (T*)(src_alt ? L.e : L.e2);
-        const T om = (T)I[L.inst].omega;
-        T r = ((const T*)L.r)[id];
-        if (L.depth == 0 && I[L.inst].singular) r = (T)((double)r - st.rmean);
-        T Le, D;
-        if (L.depth == 0) lap<T, true>(L, src, i, j, id, bt, G, I[L.inst].gidx, Le, D);
-        else lap<T, false>(L, src, i, j, id, bt, G, nullptr, Le, D);
-        T val;
-        if (zero) val = -om * r * rcpa(D);
-        else val = src[id] + om * (Le - r) * rcpa(D);
-        dst[id] = val;
-        if (addp) I[L.inst].p[id] += (double)val;
-    } else {
-        const int g = ((int)blockIdx.x - ntiles) * blockDim.x + threadIdx.x;
-        if (g >= nibm) return;
-        const GhostDev& gh = G[ibm[g]];
-        const InstState& st = S[gh.inst];
-        if (st.ppe_state != ST_ACTIVE) return;
-        const LevelDev& L = LV[I[gh.inst].lev0];
-        const T* src = (const T*)(src_alt ? L.e2 : L.e);
-        T* dst = (T*)(src_alt ? L.e : L.e2);
-        T val = (T)0;
-        if (!zero) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) val += (T)gh.wp[k] * src[gh.nb[k]];
+__global__ void k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S) {
+    const Tile t = tiles[blockIdx.x];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const double pd = in.kr[id] + st.beta * (in.kp[id] - st.omega * in.kv[id]);
+    in.kp[id] = pd;
+    ((T*)L.r)[id] = (T)pd;
+}
+
+// y = L z with z the preconditioned vector (V-cycle result in T), stored in
+// FP64 as zo; partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
+template <typename T>
+__global__ void k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) {
+    const Tile t = tiles[blockIdx.x];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    const T* z = (const T*)(e_alt ? L.e2 : L.e);
+    double* zo = which == 0 ? in.kph : in.ksh;
+    double* y = which == 0 ? in.kv : in.kt;
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    double acc[2] = {0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        double Lz, D;
+        lap<double, T, true>(L, z, i, j, id, bt, G, in.gidx, Lz, D);
+        zo[id] = (double)z[id];
+        y[id] = Lz;
+        if (which == 0) {
+            acc[0] = in.krh[id] * Lz;
+        } else {
+            acc[0] = Lz * in.ks[id];
+            acc[1] = Lz * Lz;
         }
-        dst[gh.cell] = val;
-        if (addp) I[gh.inst].p[gh.cell] += (double)val;
+    }
+    __shared__ double out[2];
+    block_sum<2>(acc, out);
+    if (threadIdx.x < 2) part[(size_t)blockIdx.x * NPART + threadIdx.x] = out[threadIdx.x];
+}
+
+// alpha = rho / (rh, v)   (which = 0)   or   omega = (t, s) / (t, t)   (which = 1)
+__global__ void k_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                              const double* __restrict__ part, int which) {
+    const int k = blockIdx.x;
+    const InstDev& in = I[k];
+    if (S[k].ppe_state != ST_ACTIVE) return;
+    double r[2];
+    inst_sum<2>(part, in.tile_beg, in.tile_cnt, r);
+    if (threadIdx.x == 0) {
+        if (which == 0) S[k].alpha = r[0] != 0.0 ? S[k].rho / r[0] : 0.0;
+        else S[k].omega = r[1] != 0.0 ? r[0] / r[1] : 0.0;
     }
 }
 
+// s = r - alpha v; preconditioner input.
+template <typename T>
+__global__ void k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S) {
+    const Tile t = tiles[blockIdx.x];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const double sv = in.kr[id] - st.alpha * in.kv[id];
+    in.ks[id] = sv;
+    ((T*)L.r)[id] = (T)sv;
+}
+
+// p += alpha ph + omega sh ; r = s - omega t.
+// partials: 0 (r,r)  1 unused  2 (rh,r)  3 (p,area)
+__global__ void k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                         double* __restrict__ part) {
+    const Tile t = tiles[blockIdx.x];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        const double pn = in.p[id] + st.alpha * in.kph[id] + st.omega * in.ksh[id];
+        in.p[id] = pn;
+        const double r = in.ks[id] - st.omega * in.kt[id];
+        in.kr[id] = r;
+        acc[0] = r * r;
+        acc[2] = in.krh[id] * r;
+        acc[3] = pn * (in.dx[i] * in.dy[j]);
+    }
+    __shared__ double out[4];
+    block_sum<4>(acc, out);
+    if (threadIdx.x < 4) part[(size_t)blockIdx.x * NPART + threadIdx.x] = out[threadIdx.x];
+}
+
+// Weighted-Jacobi sweep on one multigrid level (tiles of that level for all
+// instances).  flags: 1 = start from e = 0.
+template <typename T>
+__global__ void k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                         const GhostDev* __restrict__ G, int flags, int src_alt) {
+    const Tile t = tiles[blockIdx.x];
+    const LevelDev& L = LV[t.lev];
+    if (S[L.inst].ppe_state != ST_ACTIVE) return;
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const T* src = (const T*)(src_alt ? L.e2 : L.e);
+    T* dst = (T*)(src_alt ? L.e : L.e2);
+    const T om = (T)I[L.inst].omega;
+    const T r = ((const T*)L.r)[id];
+    T Le, D;
+    if (L.depth == 0) lap<T, T, true>(L, src, i, j, id, bt, G, I[L.inst].gidx, Le, D);
+    else lap<T, T, false>(L, src, i, j, id, bt, G, nullptr, Le, D);
+    dst[id] = (flags & 1) ? -om * r * rcpa(D) : src[id] + om * (Le - r) * rcpa(D);
+}
+
 // Restriction of the fine residual (area weighted) onto coarse tiles, fused
-// with the first (zero-start) smoothing sweep of the coarse level.
+// with the first (zero-start) smoothing sweep of a middle coarse level.
 template <typename T>
 __global__ void k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                           const GhostDev* __restrict__ G, int fine_alt, int init_coarse) {
+                           const GhostDev* __restrict__ G, int fine_alt) {
     const Tile t = tiles[blockIdx.x];
     const LevelDev& C = LV[t.lev];
-    const InstState& st = S[C.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
+    if (S[C.inst].ppe_state != ST_ACTIVE) return;
     const LevelDev& F = LV[C.parent];
     int I0, J0;
     tile_ij(t, I0, J0);
@@ -575,7 +673,6 @@ __global__ void k_restrict(const Tile* __restrict__ tiles, const LevelDev* __res
     const T* fr = (const T*)F.r;
     const T* fdw = LvA<T>::dw(F);
     const T* fdh = LvA<T>::dh(F);
-    const bool sing0 = F.depth == 0 && I[C.inst].singular;
     T acc = (T)0;
 #pragma unroll
     for (int dj = 0; dj < 2; dj++)
@@ -587,17 +684,15 @@ __global__ void k_restrict(const Tile* __restrict__ tiles, const LevelDev* __res
             const uint8_t bt = F.bits[id];
             if (!(bt & 0x0F)) continue;
             T Le, D;
-            if (F.depth == 0) lap<T, true>(F, fe, i, j, id, bt, G, I[C.inst].gidx, Le, D);
-            else lap<T, false>(F, fe, i, j, id, bt, G, nullptr, Le, D);
-            T r = fr[id];
-            if (sing0) r = (T)((double)r - st.rmean);
-            acc += (r - Le) * (fdw[i] * fdh[j]);
+            if (F.depth == 0) lap<T, T, true>(F, fe, i, j, id, bt, G, I[C.inst].gidx, Le, D);
+            else lap<T, T, false>(F, fe, i, j, id, bt, G, nullptr, Le, D);
+            acc += (fr[id] - Le) * (fdw[i] * fdh[j]);
         }
     const T rv = acc / (LvA<T>::dw(C)[I0] * LvA<T>::dh(C)[J0]);
     rc[cid] = rv;
-    if (init_coarse && C.child >= 0) {  // middle level: fused first sweep from zero
+    if (C.child >= 0) {  // middle level: fused first sweep from zero
         T Le, D;
-        lap<T, false>(C, (const T*)C.e, I0, J0, cid, cb, G, nullptr, Le, D);
+        lap<T, T, false>(C, (const T*)C.e, I0, J0, cid, cb, G, nullptr, Le, D);
         ((T*)C.e)[cid] = -(T)I[C.inst].omega * rv * rcpa(D);
     }
 }
@@ -610,16 +705,16 @@ __global__ void k_prolong(const Tile* __restrict__ tiles, const LevelDev* __rest
     const LevelDev& F = LV[t.lev];
     if (S[F.inst].ppe_state != ST_ACTIVE) return;
     const LevelDev& C = LV[F.child];
-    int i, j;
+    int i, j, id;
+    uint8_t bt;
     tile_ij(t, i, j);
-    if (i < 1 || i > F.NX || j < 1 || j > F.NY) return;
-    const int id = i + j * F.pitch;
-    if (!(F.bits[id] & 0x0F)) return;
+    if (!live0(F, i, j, id, bt)) return;
     // the coarsest level's solution is always in e; a middle level's in the buffer its sweeps ended on
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
     T* fe = (T*)(fine_alt ? F.e2 : F.e);
     const int I0 = F.pI[i], In = F.pIn[i], J0 = F.pJ[j], Jn = F.pJn[j];
     const T wx = LvA<T>::pwx(F)[i], wy = LvA<T>::pwy(F)[j];
+    const T sx = (T)F.psx[i], sy = (T)F.psy[j];
     T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
     const int CP = C.pitch;
     const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
@@ -628,7 +723,7 @@ __global__ void k_prolong(const Tile* __restrict__ tiles, const LevelDev* __rest
     w01 = (C.bits[c01] & 0x0F) ? w01 : (T)0;
     w11 = (C.bits[c11] & 0x0F) ? w11 : (T)0;
     const T sw = w00 + w10 + w01 + w11;
-    const T val = (w00 * ce[c00] + w10 * ce[c10] + w01 * ce[c01] + w11 * ce[c11]) / sw;
+    const T val = (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
     fe[id] += val;
 }
 
@@ -654,7 +749,7 @@ __global__ void k_coarse_solve(const int* __restrict__ levs, const LevelDev* __r
                 const uint8_t bt = L.bits[id];
                 if (!(bt & 0x0F)) continue;
                 T Le, D;
-                lap<T, false>(L, e, i, j, id, bt, nullptr, nullptr, Le, D);
+                lap<T, T, false>(L, e, i, j, id, bt, nullptr, nullptr, Le, D);
                 e[id] = e[id] + om * (Le - r[id]) * rcpa(D);
             }
             __syncthreads();
@@ -876,30 +971,56 @@ cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part
     k_rhs_reduce<<<ninst, 256, 0, s>>>(I, S, part);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_ppe_resid(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                             const GhostDev* G, double* part, cudaStream_t s) {
-    k_ppe_resid<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part);
+cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                              const GhostDev* G, double* part, cudaStream_t s) {
+    k_bicg_start<<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part);
     return cudaGetLastError();
 }
-cudaError_t launch_ppe_reduce(const InstDev* I, InstState* S, const double* part, int ninst, LoopCtl* ctl,
-                              unsigned long long handle, cudaStream_t s) {
-    k_ppe_reduce<<<ninst, 256, 0, s>>>(I, S, part, ctl, handle);
+cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
+                                 LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
+    k_bicg_reduce_r<<<ninst, 256, 0, s>>>(I, S, part, start, ctl, handle);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          cudaStream_t s) {
+    k_bicg_p<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                              const GhostDev* G, double* part, int e_alt, int which, cudaStream_t s) {
+    k_bicg_apply<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
+    return cudaGetLastError();
+}
+cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
+                               cudaStream_t s) {
+    k_bicg_scalar<<<ninst, 256, 0, s>>>(I, S, part, which);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          cudaStream_t s) {
+    k_bicg_s<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+    return cudaGetLastError();
+}
+cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                          double* part, cudaStream_t s) {
+    k_bicg_x<<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          const GhostDev* G, const int* ibm, int nibm, int flags, int src_alt, cudaStream_t s) {
-    const int nb = nt + nblk(nibm, TILE_THREADS);
-    if (nb == 0) return cudaSuccess;
-    k_smooth<T><<<nb, TILE_THREADS, 0, s>>>(t, nt, LV, I, S, G, ibm, nibm, flags, src_alt);
+                          const GhostDev* G, int flags, int src_alt, cudaStream_t s) {
+    if (nt == 0) return cudaSuccess;
+    k_smooth<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                            const GhostDev* G, int fine_alt, int init_coarse, cudaStream_t s) {
+                            const GhostDev* G, int fine_alt, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_restrict<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt, init_coarse);
+    k_restrict<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     return cudaGetLastError();
 }
 template <typename T>
@@ -934,18 +1055,16 @@ cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_
     return cudaGetLastError();
 }
 
-template cudaError_t launch_ppe_resid<double>(const Tile*, int, const LevelDev*, const InstDev*,
-                                              const InstState*, const GhostDev*, double*, cudaStream_t);
-template cudaError_t launch_ppe_resid<float>(const Tile*, int, const LevelDev*, const InstDev*,
-                                             const InstState*, const GhostDev*, double*, cudaStream_t);
-template cudaError_t launch_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                           const GhostDev*, const int*, int, int, int, cudaStream_t);
-template cudaError_t launch_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                          const GhostDev*, const int*, int, int, int, cudaStream_t);
-template cudaError_t launch_restrict<double>(const Tile*, int, const LevelDev*, const InstDev*,
-                                             const InstState*, const GhostDev*, int, int, cudaStream_t);
-template cudaError_t launch_restrict<float>(const Tile*, int, const LevelDev*, const InstDev*,
-                                            const InstState*, const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_bicg_p<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
+template cudaError_t launch_bicg_s<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
+template cudaError_t launch_bicg_apply<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
+template cudaError_t launch_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_restrict<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, cudaStream_t);
+template cudaError_t launch_bicg_p<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
+template cudaError_t launch_bicg_s<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
+template cudaError_t launch_bicg_apply<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
+template cudaError_t launch_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_restrict<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, cudaStream_t);
 template cudaError_t launch_prolong<double>(const Tile*, int, const LevelDev*, const InstState*, int, int,
                                             cudaStream_t);
 template cudaError_t launch_prolong<float>(const Tile*, int, const LevelDev*, const InstState*, int, int,

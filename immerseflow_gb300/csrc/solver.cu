@@ -227,28 +227,37 @@ void build_levels(Instance& I) {
             f.pI.assign(f.nx, 0);
             f.pIn.assign(f.nx, 0);
             f.pwx.assign(f.nx, 0.0);
+            f.psx.assign(f.nx, 1);
             f.pJ.assign(f.ny, 0);
             f.pJn.assign(f.ny, 0);
             f.pwy.assign(f.ny, 0.0);
+            f.psy.assign(f.ny, 1);
+            // ring centres are the mirror images of the first/last interior
+            // centres: the neighbour beyond a domain side is the cell itself
+            // with sign +1 (Neumann) or -1 (Dirichlet)
             for (int i = 1; i <= f.NX; i++) {
                 int Ic = (i + 1) / 2;
                 int In = f.xc[i] < v.xc[Ic] ? Ic - 1 : Ic + 1;
-                double w = 0.0;
-                if (In < 1 || In > v.NX) In = Ic;
-                else w = (f.xc[i] - v.xc[Ic]) / (v.xc[In] - v.xc[Ic]);
+                double w = (f.xc[i] - v.xc[Ic]) / (v.xc[In] - v.xc[Ic]);
+                signed char sg = 1;
+                if (In < 1) { sg = (I.dirmask & (1 << IFX_SIDE_W)) ? -1 : 1; In = Ic; }
+                if (In > v.NX) { sg = (I.dirmask & (1 << IFX_SIDE_E)) ? -1 : 1; In = Ic; }
                 f.pI[i] = Ic;
                 f.pIn[i] = In;
                 f.pwx[i] = w;
+                f.psx[i] = sg;
             }
             for (int j = 1; j <= f.NY; j++) {
                 int Jc = (j + 1) / 2;
                 int Jn = f.yc[j] < v.yc[Jc] ? Jc - 1 : Jc + 1;
-                double w = 0.0;
-                if (Jn < 1 || Jn > v.NY) Jn = Jc;
-                else w = (f.yc[j] - v.yc[Jc]) / (v.yc[Jn] - v.yc[Jc]);
+                double w = (f.yc[j] - v.yc[Jc]) / (v.yc[Jn] - v.yc[Jc]);
+                signed char sg = 1;
+                if (Jn < 1) { sg = (I.dirmask & (1 << IFX_SIDE_S)) ? -1 : 1; Jn = Jc; }
+                if (Jn > v.NY) { sg = (I.dirmask & (1 << IFX_SIDE_N)) ? -1 : 1; Jn = Jc; }
                 f.pJ[j] = Jc;
                 f.pJn[j] = Jn;
                 f.pwy[j] = w;
+                f.psy[j] = sg;
             }
         }
     }
@@ -463,6 +472,10 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
         IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
         IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
+        IFX_TRY(dalloc(S, &d.kr, nc)); IFX_TRY(dalloc(S, &d.krh, nc));
+        IFX_TRY(dalloc(S, &d.kp, nc)); IFX_TRY(dalloc(S, &d.kv, nc));
+        IFX_TRY(dalloc(S, &d.ks, nc)); IFX_TRY(dalloc(S, &d.kt, nc));
+        IFX_TRY(dalloc(S, &d.kph, nc)); IFX_TRY(dalloc(S, &d.ksh, nc));
         double *xf_d = nullptr, *yf_d = nullptr, *xc_d = nullptr, *yc_d = nullptr, *dx_d = nullptr,
                *dy_d = nullptr, *fx_d = nullptr, *gx_d = nullptr, *fy_d = nullptr, *gy_d = nullptr;
         IFX_TRY(dupload(S, &xf_d, I.xf)); IFX_TRY(dupload(S, &yf_d, I.yf));
@@ -548,6 +561,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
                 IFX_TRY(dupload(S, &L.d_pJ, L.pJ)); IFX_TRY(dupload(S, &L.d_pJn, L.pJn));
                 IFX_TRY(dupload(S, &L.d_pwx, L.pwx)); IFX_TRY(dupload(S, &L.d_pwy, L.pwy));
                 IFX_TRY(dupload(S, &L.d_pwxf, to_f(L.pwx))); IFX_TRY(dupload(S, &L.d_pwyf, to_f(L.pwy)));
+                IFX_TRY(dupload(S, &L.d_psx, L.psx)); IFX_TRY(dupload(S, &L.d_psy, L.psy));
             }
             LevelDev ld;
             std::memset(&ld, 0, sizeof(ld));
@@ -561,6 +575,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ld.e = L.d_e; ld.e2 = L.d_e2; ld.r = L.d_r;
             ld.pI = L.d_pI; ld.pIn = L.d_pIn; ld.pJ = L.d_pJ; ld.pJn = L.d_pJn;
             ld.pwx = L.d_pwx; ld.pwy = L.d_pwy; ld.pwxf = L.d_pwxf; ld.pwyf = L.d_pwyf;
+            ld.psx = L.d_psx; ld.psy = L.d_psy;
             ld.child = (l + 1 < nl) ? I.lev_base + l + 1 : -1;
             ld.parent = (l > 0) ? I.lev_base + l - 1 : -1;
             hLV.push_back(ld);
@@ -653,25 +668,27 @@ struct Seq {
     }
 };
 
+// One V-cycle on the correction equation; returns which buffer (0: e,
+// 1: e2) holds the finest-level result.
 template <typename T>
-void seq_vcycle(Seq& q) {
+int seq_vcycle(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int L = S->lmax;
     std::vector<int> cur(L, 0);
     // finest level: first sweep from zero, then the rest of the pre-smoothing
-    q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, 1, 0, st));
+    q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, st));
     cur[0] = 1;
     for (int k = 1; k < S->mg_pre; k++) {
-        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, 0, cur[0], st));
+        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur[0], st));
         cur[0] ^= 1;
     }
     for (int l = 1; l < L; l++) {
-        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, cur[l - 1], 1, st));
+        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, cur[l - 1], st));
         cur[l] = 0;
         if (S->ntsm[l] > 0)
             for (int k = 1; k < S->mg_pre; k++) {
-                q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, nullptr, 0, 0, cur[l], st));
+                q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, 0, cur[l], st));
                 cur[l] ^= 1;
             }
     }
@@ -682,14 +699,11 @@ void seq_vcycle(Seq& q) {
         if (nt == 0) continue;
         q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur[l], cur[l + 1], st));
         for (int k = 0; k < S->mg_post; k++) {
-            const int flags = (l == 0 && k == S->mg_post - 1) ? 2 : 0;
-            if (l == 0)
-                q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, S->dIbm, S->nibm, flags, cur[0], st));
-            else
-                q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, nullptr, 0, flags, cur[l], st));
+            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur[l], st));
             cur[l] ^= 1;
         }
     }
+    return cur[0];
 }
 
 void seq_pre(Seq& q) {
@@ -722,18 +736,26 @@ void seq_mid(Seq& q) {
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
     q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
-    q.add(launch_ppe_resid<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
-    q.add(launch_ppe_reduce(S->dI, S->dS, S->dPart, n, S->dCtl, 0ull, st));
+    q.add(launch_bicg_start(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, S->dCtl, 0ull, st));
 }
 
+// One BiCGSTAB iteration with two V-cycle preconditioner applications.
 template <typename T>
 void seq_ppe_body(Seq& q, unsigned long long h) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    seq_vcycle<T>(q);
-    q.add(launch_ppe_resid<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
-    q.add(launch_ppe_reduce(S->dI, S->dS, S->dPart, n, S->dCtl, h, st));
+    q.add(launch_bicg_p<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
+    int e1 = seq_vcycle<T>(q);
+    q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, st));
+    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 0, st));
+    q.add(launch_bicg_s<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
+    int e2 = seq_vcycle<T>(q);
+    q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, st));
+    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st));
+    q.add(launch_bicg_x(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dPart, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st));
 }
 
 void seq_post(Seq& q) {

@@ -421,9 +421,10 @@ struct Level {
     std::vector<double> dw, dh, xc, yc, kx, ky, ix, iy;  // widths, centres, face coeffs, 1/width
     std::vector<uint8_t> act, bits;
     std::vector<double> e, e2, r;
-    // prolongation from level+1 into this level
+    // prolongation from level+1 into this level; at a domain boundary the
+    // neighbour is the cell itself mirrored with sign psx/psy (+1 Neumann, -1 Dirichlet)
     std::vector<int> pI, pIn, pJ, pJn;
-    std::vector<double> pwx, pwy;
+    std::vector<double> pwx, pwy, psx, psy;
 };
 
 }  // namespace
@@ -593,11 +594,24 @@ void build_ghosts(orc_solver* S) {
                         wD[k] = w; wN[k] = w;
                     }
                 }
+                // pressure: nodes that are IBM ghosts themselves are dropped so
+                // that every ghost pressure is a linear function of fluid cells
+                double keep = 0.0;
+                for (int k = 0; k < 4; k++)
+                    if (k != gk && S->type[g.nb[k]] != T_GHOST) keep += wN[k];
+                if (!(keep > 0.05)) {
+                    double wb[4] = {(1 - xi) * (1 - eta), xi * (1 - eta), (1 - xi) * eta, xi * eta};
+                    keep = 0.0;
+                    for (int k = 0; k < 4; k++) {
+                        wN[k] = wb[k];
+                        if (k != gk && S->type[g.nb[k]] != T_GHOST) keep += wb[k];
+                    }
+                }
                 for (int k = 0; k < 4; k++) {
                     if (k == gk) { g.wu[k] = g.wv[k] = g.wp[k] = 0.0; continue; }
                     g.wu[k] = -wD[k];
                     g.wv[k] = -wD[k];
-                    g.wp[k] = wN[k];
+                    g.wp[k] = (S->type[g.nb[k]] != T_GHOST) ? wN[k] / keep : 0.0;
                 }
                 S->ghosts.push_back(g);
             }
@@ -691,23 +705,26 @@ void build_levels(orc_solver* S) {
         if (l > 0) {
             // prolongation tables: level l -> level l-1
             Level& f = S->L[l - 1];
-            f.pI.assign(f.nx, 0); f.pIn.assign(f.nx, 0); f.pwx.assign(f.nx, 0.0);
-            f.pJ.assign(f.ny, 0); f.pJn.assign(f.ny, 0); f.pwy.assign(f.ny, 0.0);
+            f.pI.assign(f.nx, 0); f.pIn.assign(f.nx, 0); f.pwx.assign(f.nx, 0.0); f.psx.assign(f.nx, 1.0);
+            f.pJ.assign(f.ny, 0); f.pJn.assign(f.ny, 0); f.pwy.assign(f.ny, 0.0); f.psy.assign(f.ny, 1.0);
             for (int i = 1; i <= f.NX; i++) {
                 int I = (i + 1) / 2;
                 int In = f.xc[i] < v.xc[I] ? I - 1 : I + 1;
-                double w = 0.0;
-                if (In < 1 || In > v.NX) In = I;
-                else w = (f.xc[i] - v.xc[I]) / (v.xc[In] - v.xc[I]);
-                f.pI[i] = I; f.pIn[i] = In; f.pwx[i] = w;
+                // ring centres are the mirror images of the first/last interior centres
+                double w = (f.xc[i] - v.xc[I]) / (v.xc[In] - v.xc[I]);
+                double sg = 1.0;
+                if (In < 1) { sg = S->dir[IFX_SIDE_W] ? -1.0 : 1.0; In = I; }
+                if (In > v.NX) { sg = S->dir[IFX_SIDE_E] ? -1.0 : 1.0; In = I; }
+                f.pI[i] = I; f.pIn[i] = In; f.pwx[i] = w; f.psx[i] = sg;
             }
             for (int j = 1; j <= f.NY; j++) {
                 int J = (j + 1) / 2;
                 int Jn = f.yc[j] < v.yc[J] ? J - 1 : J + 1;
-                double w = 0.0;
-                if (Jn < 1 || Jn > v.NY) Jn = J;
-                else w = (f.yc[j] - v.yc[J]) / (v.yc[Jn] - v.yc[J]);
-                f.pJ[j] = J; f.pJn[j] = Jn; f.pwy[j] = w;
+                double w = (f.yc[j] - v.yc[J]) / (v.yc[Jn] - v.yc[J]);
+                double sg = 1.0;
+                if (Jn < 1) { sg = S->dir[IFX_SIDE_S] ? -1.0 : 1.0; Jn = J; }
+                if (Jn > v.NY) { sg = S->dir[IFX_SIDE_N] ? -1.0 : 1.0; Jn = J; }
+                f.pJ[j] = J; f.pJn[j] = Jn; f.pwy[j] = w; f.psy[j] = sg;
             }
         }
     }
@@ -771,15 +788,6 @@ void smooth(orc_solver* S, int l, bool zero_init) {
             if (zero_init) v.e2[id] = -om * v.r[id] * rcp_approx(D);
             else v.e2[id] = v.e[id] + om * (Le - v.r[id]) * rcp_approx(D);
         }
-    if (l == 0) {
-        for (auto& g : S->ghosts) {
-            if (g.side >= 0) continue;
-            if (zero_init) { v.e2[g.cell] = 0.0; continue; }
-            double acc = 0.0;
-            for (int k = 0; k < 4; k++) acc += g.wp[k] * v.e[g.nb[k]];
-            v.e2[g.cell] = acc;
-        }
-    }
     std::swap(v.e, v.e2);
 }
 
@@ -832,6 +840,7 @@ void prolong_add(orc_solver* S, int l) {
             if (!live(f, id)) continue;
             int I = f.pI[i], In = f.pIn[i], J = f.pJ[j], Jn = f.pJn[j];
             double wx = f.pwx[i], wy = f.pwy[j];
+            double sx = f.psx[i], sy = f.psy[j];
             double w00 = (1.0 - wx) * (1.0 - wy), w10 = wx * (1.0 - wy), w01 = (1.0 - wx) * wy, w11 = wx * wy;
             int c00 = IDX(I, J, c.nx), c10 = IDX(In, J, c.nx), c01 = IDX(I, Jn, c.nx), c11 = IDX(In, Jn, c.nx);
             w00 = live(c, c00) ? w00 : 0.0;
@@ -839,7 +848,7 @@ void prolong_add(orc_solver* S, int l) {
             w01 = live(c, c01) ? w01 : 0.0;
             w11 = live(c, c11) ? w11 : 0.0;
             double sw = w00 + w10 + w01 + w11;
-            double val = (w00 * c.e[c00] + w10 * c.e[c10] + w01 * c.e[c01] + w11 * c.e[c11]) / sw;
+            double val = (w00 * c.e[c00] + sx * w10 * c.e[c10] + sy * w01 * c.e[c01] + (sx * sy) * w11 * c.e[c11]) / sw;
             f.e[id] += val;
         }
 }
@@ -1050,51 +1059,64 @@ void method_step(orc_solver* S) {
         for (int id = 0; id < n; id++)
             if (S->type[id] == T_FLUID) S->b[id] -= mb;
     }
-    double bn = 0.0;
-    for (int id = 0; id < n; id++)
-        if (S->type[id] == T_FLUID) bn += S->b[id] * S->b[id];
-    bn = std::sqrt(bn);
-    // 6. pressure: FP64 defect correction around multigrid V-cycles
+    // 6. pressure: BiCGSTAB in FP64 on the ghost-eliminated operator,
+    //    preconditioned by one multigrid V-cycle
     Level& L0 = S->L[0];
+    auto apply_A = [&](const double* x, double* y) {
+#pragma omp parallel for schedule(static) num_threads(S->nthreads)
+        for (int j = 1; j < ny - 1; j++)
+            for (int i = 1; i < nx - 1; i++) {
+                int id = IDX(i, j, nx);
+                if (!live(L0, id)) { y[id] = 0.0; continue; }
+                double Lx, D;
+                lap(S, L0, x, i, j, &Lx, &D, true);
+                y[id] = Lx;
+            }
+    };
+    auto precond = [&](const double* in, double* out) {
+        for (int id = 0; id < n; id++) L0.r[id] = live(L0, id) ? in[id] : 0.0;
+        vcycle(S, 0);
+        for (int id = 0; id < n; id++) out[id] = live(L0, id) ? L0.e[id] : 0.0;
+    };
+    auto dot = [&](const double* a1, const double* a2) {
+        double acc = 0.0;
+        for (int id = 0; id < n; id++)
+            if (live(L0, id)) acc += a1[id] * a2[id];
+        return acc;
+    };
+    std::vector<double> r(n, 0.0), rh(n, 0.0), pd(n, 0.0), vv(n, 0.0), sv(n, 0.0), tv(n, 0.0), ph(n, 0.0),
+        sh(n, 0.0), Ax(n, 0.0);
+    apply_A(S->p.data(), Ax.data());
+    for (int id = 0; id < n; id++) {
+        r[id] = live(L0, id) ? S->b[id] - Ax[id] : 0.0;
+        rh[id] = r[id];
+    }
+    const double bn = std::sqrt(dot(S->b.data(), S->b.data()));
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
     int pit = 0;
     double rel = 0.0;
     while (true) {
-        // residual
-        double rs = 0.0, rsum = 0.0;
-        for (int j = 1; j < ny - 1; j++)
-            for (int i = 1; i < nx - 1; i++) {
-                int id = IDX(i, j, nx);
-                if (S->type[id] != T_FLUID) { L0.r[id] = 0.0; continue; }
-                double Lp, D;
-                lap(S, L0, S->p.data(), i, j, &Lp, &D, true);
-                L0.r[id] = S->b[id] - Lp;
-                rsum += L0.r[id] * (S->dx[i] * S->dy[j]);
-            }
-        if (S->singular) {
-            double mr = rsum / asum;
-            for (int id = 0; id < n; id++)
-                if (S->type[id] == T_FLUID) L0.r[id] -= mr;
-        }
-        for (int id = 0; id < n; id++)
-            if (S->type[id] == T_FLUID) rs += L0.r[id] * L0.r[id];
-
-        rel = std::sqrt(rs) / std::max(bn, 1e-300);
+        rel = std::sqrt(dot(r.data(), r.data())) / std::max(bn, 1e-300);
         if (rel <= c.ppe_tol || pit >= c.ppe_itermax) break;
-        vcycle(S, 0);
-        for (int id = 0; id < n; id++)
-            if (S->type[id] == T_FLUID || S->type[id] == T_GHOST) S->p[id] += L0.e[id];
+        const double rho1 = dot(rh.data(), r.data());
+        const double beta = (rho1 / rho) * (alpha / omega);
+        rho = rho1;
+        for (int id = 0; id < n; id++) pd[id] = r[id] + beta * (pd[id] - omega * vv[id]);
+        precond(pd.data(), ph.data());
+        apply_A(ph.data(), vv.data());
+        const double rv = dot(rh.data(), vv.data());
+        alpha = rv != 0.0 ? rho / rv : 0.0;
+        for (int id = 0; id < n; id++) sv[id] = r[id] - alpha * vv[id];
+        precond(sv.data(), sh.data());
+        apply_A(sh.data(), tv.data());
+        const double ts = dot(tv.data(), sv.data()), tt = dot(tv.data(), tv.data());
+        omega = tt != 0.0 ? ts / tt : 0.0;
+        for (int id = 0; id < n; id++) {
+            if (!live(L0, id)) continue;
+            S->p[id] += alpha * ph[id] + omega * sh[id];
+            r[id] = sv[id] - omega * tv[id];
+        }
         pit++;
-    }
-    if (S->singular) {
-        double ps = 0.0;
-        for (int j = 1; j < ny - 1; j++)
-            for (int i = 1; i < nx - 1; i++) {
-                int id = IDX(i, j, nx);
-                if (S->type[id] == T_FLUID) ps += S->p[id] * (S->dx[i] * S->dy[j]);
-            }
-        double mp = ps / asum;
-        for (int id = 0; id < n; id++)
-            if (S->type[id] == T_FLUID || S->type[id] == T_GHOST) S->p[id] -= mp;
     }
     S->st.last_ppe_iters = pit;
     S->st.last_ppe_residual = rel;
