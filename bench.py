@@ -1,0 +1,290 @@
+#!/usr/bin/env python3
+"""Benchmark: Mcell-updates/s of the fractional step on one GB300.
+
+Workload (one "step" = one full time step: predictor, pressure solve to
+||r|| <= 1e-8 ||b||, projection, ghost refresh, drag/lift):
+  flow past a circular cylinder, D=1 at (10,10) in a 30x20 domain,
+  tanh-stretched 384x256 grid, uniform inflow u=1, convective outflow,
+  slip top/bottom, Re=100, dt=5e-3, ghost-cell immersed boundary.
+Synthetic: the grid and the impulsively started flow are generated here.
+
+value     : interior cells x steps / device time of the timed steps (CUDA
+            events on the solver's stream), mixed precision (FP32 multigrid
+            inside FP64 BiCGSTAB), L2 flushed before every step;
+e2e       : same metric through the C ABI with the state copied from pinned
+            host buffers and the result copied back every step, wall clock;
+plain_fp64: the same steps with every kernel in FP64;
+roofline  : the finest-level smoothing sweep (dominant kernel) timed alone;
+cpu_baseline: the CPU oracle (same scheme, FP64, all host threads).
+
+--impl reference times the CPU restatement of the reference scheme (the
+reference's own code is CUDA-only) on the same workload.
+Under torchrun with N>1 every rank advances its own replica (weak scaling,
+no collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-updates/s"
+WORKLOAD = "cylinder D=1, 30x20 domain, 384x256 tanh-stretched, Re=100, dt=5e-3, ghost-cell IBM"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.p = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax = float(t[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if t[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the roofline kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "smooth_l0_cylinder_384x256.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle
+
+    nthreads = nthreads or os.cpu_count() or 1
+    o = _oracle.Oracle().method(cfg, xf, yf, nthreads)
+    o.step(warm)
+    n = 0
+    t0 = time.perf_counter()
+    while n < min_steps or time.perf_counter() - t0 < seconds:
+        o.step(1)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n, dt, nthreads
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    import numpy as np
+
+    from immerseflow_gb300 import _capi as capi
+    from immerseflow_gb300 import cases
+
+    cfg_m, xf, yf = cases.cylinder(precision=capi.PREC_MIXED)
+    cells = cfg_m.nx * cfg_m.ny
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import _oracle
+
+        nth = os.cpu_count() or 1
+        o = _oracle.Oracle().method(cfg64, xf, yf, nth)
+        o.step(args.warmup)
+        t0 = time.perf_counter()
+        o.step(args.steps)
+        dt = time.perf_counter() - t0
+        val = cells * args.steps / dt / 1e6
+        line = {"metric": METRIC, "value": val, "unit": METRIC, "impl": "reference", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "grid": [384, 256], "solver": "CPU restatement (oracle), FP64"},
+                "cpu_baseline": {"value": val, "unit": METRIC, "cores": nth, "kind": "port",
+                                 "sample": f"{args.steps} time steps after {args.warmup} warm-up steps"},
+                "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    import immerseflow_gb300 as ifx
+
+    flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def flush():
+        flush_buf.zero_()
+        torch.cuda.synchronize()
+
+    def timed(prec):
+        cfg, _, _ = cases.cylinder(precision=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        for _ in range(args.warmup):
+            flush()
+            s.step(1)
+        l0 = s.stats().kernel_launches
+        barrier()
+        clk = Clocks(local)
+        clk.start()
+        ms = []
+        for _ in range(args.steps):
+            flush()
+            s.step(1)
+            ms.append(s.last_step_ms())
+        clocks = clk.stop()
+        barrier()
+        total = sum(ms)
+        launches = s.stats().kernel_launches - l0
+        return s, total, launches, clocks
+
+    s, total_ms, launches, clocks = timed(capi.PREC_MIXED)
+    st = s.stats()
+    u_m, v_m = s.get(capi.FIELD_U), s.get(capi.FIELD_V)
+    cd_m, cl_m = st.cd, st.cl
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = world * cells * args.steps / (total_ms * 1e-3) / 1e6
+
+    # plain FP64 path on the same steps
+    s64, total64, launches64, _ = timed(capi.PREC_FP64)
+    st64 = s64.stats()
+    u64, v64 = s64.get(capi.FIELD_U), s64.get(capi.FIELD_V)
+    err_u = float(np.sqrt(np.sum((u_m - u64) ** 2 + (v_m - v64) ** 2) / np.sum(u64 ** 2 + v64 ** 2)))
+    err_cd = abs(cd_m - st64.cd) / abs(st64.cd)
+    value64 = world * cells * args.steps / (total64 * 1e-3) / 1e6
+
+    # end to end through the C ABI: pinned host state in, result out, every step
+    nx, ny = s.grid_dims()
+    host = {f: torch.empty(nx * ny, dtype=torch.float64, pin_memory=True).numpy() for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P)}
+    for f, a in host.items():
+        a[:] = s.get(f).ravel()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for f, a in host.items():
+            s.set(f, a)
+        s.step(1)
+        for f, a in host.items():
+            lib_out = s.get(f).ravel()
+            a[:] = lib_out
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = world * cells * args.steps / e2e_s / 1e6
+    nbytes = 3 * nx * ny * 8
+
+    # roofline of the dominant kernel (finest-level smoothing sweep, FP32 in the mixed path)
+    k_ms, k_cells = s.profile_kernel(0, reps=200)
+    bytes_per_launch = k_cells * (3 * 4 + 1)
+    achieved = bytes_per_launch / (k_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = committed_traffic()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 multigrid + f64 BiCGSTAB/state", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [384, 256], "cells": cells, "parallelism": f"replicas x{world}",
+                   "precision": "mixed", "ppe_tol": cfg_m.ppe_tol, "l2": "flushed before every timed step (256 MB write)",
+                   "avg_ppe_iters_last_step": st.last_ppe_iters, "avg_predictor_sweeps_last_step": st.last_ad_iters},
+        "plain_fp64": {"value": value64, "ms_per_step": total64 / args.steps, "gpu_launches": launches64,
+                       "speedup_mixed_over_fp64": value / value64},
+        "accuracy_vs_fp64": {"rel_l2_velocity": err_u, "cd_rel_err": err_cd, "cd": cd_m, "cd_fp64": st64.cd},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_smooth<float> finest level", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "bytes_per_cell": 13, "cells_per_launch": k_cells, "ms_per_launch": k_ms,
+                     "note": "working set ~30 MB is L2-resident; launch-latency bound at this size"},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
+        n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": cells * n / dt / 1e6, "unit": METRIC, "cores": nth, "kind": "port",
+                                "sample": f"{n} time steps of the same workload after 1 warm-up step ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

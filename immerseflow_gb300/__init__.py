@@ -46,6 +46,7 @@ _SIGS = {
     "ifx_get_ibm_ghosts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_synchronize": (C.c_int, [C.c_void_p]),
+    "ifx_profile_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "ifx_destroy": (None, [C.c_void_p]),
 }
 
@@ -196,6 +197,13 @@ class Solver:
 
     def write_results(self, directory):
         _check(lib().ifx_write_results(self._h, os.fsencode(directory)))
+
+    def profile_kernel(self, kernel, reps=50):
+        """(mean ms per launch, interior cells per launch) of one step kernel."""
+        ms = C.c_double()
+        cells = C.c_longlong()
+        _check(lib().ifx_profile_kernel(self._h, kernel, reps, C.byref(ms), C.byref(cells)))
+        return ms.value, cells.value
 
     def synchronize(self):
         _check(lib().ifx_synchronize(self._h))

@@ -1366,6 +1366,43 @@ extern "C" ifx_status ifx_last_step_ms(ifx_solver* S, double* ms) {
     return IFX_OK;
 }
 
+template <typename T>
+static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms) {
+    cudaStream_t st = S->stream;
+    const int n = (int)S->inst.size();
+    CUDA_TRY(launch_step_begin(S->dS, n, st));
+    auto one = [&]() -> cudaError_t {
+        switch (kernel) {
+            case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, st);
+            case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, st);
+            case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
+            default: return launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st);
+        }
+    };
+    CUDA_TRY(one());  // warm
+    CUDA_TRY(cudaEventRecord(S->ev0, st));
+    for (int k = 0; k < reps; k++) CUDA_TRY(one());
+    CUDA_TRY(cudaEventRecord(S->ev1, st));
+    CUDA_TRY(cudaEventSynchronize(S->ev1));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, S->ev0, S->ev1));
+    *ms = t / reps;
+    S->launches += reps + 2;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, double* ms_per_launch,
+                                         long long* cells) {
+    if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 3) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_profile_kernel needs a METHOD-mode solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    long long c = 0;
+    for (auto& I : S->inst) c += (long long)I.NX * I.NY;
+    if (cells) *cells = c;
+    if (S->prec == IFX_PREC_FP64) return profile_kernel<double>(S, kernel, reps, ms_per_launch);
+    return profile_kernel<float>(S, kernel, reps, ms_per_launch);
+}
+
 extern "C" ifx_status ifx_synchronize(ifx_solver* S) {
     if (!S) return set_error(IFX_ERR_ARG, "ifx_synchronize: null solver");
     CUDA_TRY(cudaStreamSynchronize(S->stream));

@@ -194,6 +194,14 @@ ifx_status ifx_get_stats(ifx_solver* s, int inst, ifx_stats* out);
  * the solver's own stream. */
 ifx_status ifx_last_step_ms(ifx_solver* s, double* ms);
 ifx_status ifx_synchronize(ifx_solver* s);
+/* Measurement hook (no reference counterpart): launches one kernel of the
+ * time step `reps` times back to back on the solver's stream and returns the
+ * mean device time per launch (CUDA events).  kernel: 0 finest-level
+ * multigrid smoothing sweep, 1 FP64 pressure operator apply (BiCGSTAB),
+ * 2 predictor Jacobi sweep, 3 convection / predictor right-hand side.
+ * *cells receives the interior cells one launch covers.  Scratch buffers and
+ * the per-step iteration state are overwritten; the flow state is not. */
+ifx_status ifx_profile_kernel(ifx_solver* s, int kernel, int reps, double* ms_per_launch, long long* cells);
 void       ifx_destroy(ifx_solver* s);
 
 #ifdef __cplusplus

@@ -1118,6 +1118,18 @@ void method_step(orc_solver* S) {
         }
         pit++;
     }
+    if (S->singular) {
+        // Neumann nullspace: zero area-weighted mean over the fluid
+        double ps = 0.0;
+        for (int j = 1; j < ny - 1; j++)
+            for (int i = 1; i < nx - 1; i++) {
+                int id = IDX(i, j, nx);
+                if (live(L0, id)) ps += S->p[id] * (S->dx[i] * S->dy[j]);
+            }
+        double mp = ps / asum;
+        for (int id = 0; id < n; id++)
+            if (S->type[id] == T_FLUID || S->type[id] == T_GHOST) S->p[id] -= mp;
+    }
     S->st.last_ppe_iters = pit;
     S->st.last_ppe_residual = rel;
     S->st.ppe_iters_total += pit;
