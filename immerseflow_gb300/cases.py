@@ -26,7 +26,7 @@ def uniform_faces(n, length, x0=0.0):
     return np.linspace(x0, x0 + length, n + 1)
 
 
-def tanh_faces(n, length, centre, ratio=8.0, width=1.5):
+def tanh_faces(n, length, centre, ratio=4.0, width=3.0):
     """n cells on [0, length], finest at `centre`.  The cell size grows with
     the distance d from the centre as 1 + (ratio-1) tanh(d/width); faces are
     placed at equal increments of the integrated cell density."""
@@ -72,7 +72,7 @@ def cavity(n=128, re=100.0, dt=1e-3, precision=capi.PREC_FP64):
     return c, uniform_faces(n, 1.0), uniform_faces(n, 1.0)
 
 
-def external(nx, ny, lx, ly, cx, cy, a, b, angle_deg, re, dt, precision=capi.PREC_FP64, ratio=8.0, width=1.5):
+def external(nx, ny, lx, ly, cx, cy, a, b, angle_deg, re, dt, precision=capi.PREC_FP64, ratio=4.0, width=3.0):
     c = _method_cfg(precision)
     c.nx, c.ny = nx, ny
     c.lx, c.ly = lx, ly
