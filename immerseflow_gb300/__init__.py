@@ -35,6 +35,8 @@ _SIGS = {
     "ifx_get_dims": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ifx_step": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_ppe_reference": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_ppe_reference_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                            C.c_double, C.POINTER(C.c_int), C.c_void_p]),
     "ifx_get_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t]),
     "ifx_set_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t]),
     "ifx_get_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),

@@ -26,6 +26,7 @@ SOURCES = [
     ("kernels_ref.cu", []),
     ("solver.cu", []),
     ("io.cpp", ["-x", "cu"]),
+    ("noalloc.cu", []),
 ]
 
 

@@ -172,6 +172,29 @@ ifx_status ifx_step(ifx_solver* s, int nsteps);
  * p = 100 on the i=0 and j=0 ghosts, stopped on the signed residual sum. */
 ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
 
+/* Largest grid (cells including the ghost ring, nx*ny) that
+ * ifx_ppe_reference_noalloc accepts: 132 x 132, i.e. the 128 x 128 interior of the
+ * cavity configuration.  Its scratch is ~0.84 MB of device memory per GPU. */
+#define IFX_NOALLOC_MAX_CELLS (132 * 132)
+/* Pressure solve for callers that cannot allocate device memory (a plug-in
+ * whose host application owns every device allocation, work issued while a
+ * stream is captured into a graph, a service that budgets device memory up
+ * front).  No counterpart in the reference: it is the solve of ifx_ppe_reference
+ * (PPESolver's Jacobi Laplace with p = 100 on the i=0 / j=0 ghosts, stopped when
+ * the signed residual sum drops to tol or after itermax sweeps) run on buffers
+ * the caller owns: d_dx, d_dy (nx*ny each, the full width arrays of readGridData,
+ * src/include/preSim.cu:328-355) and d_p (nx*ny, initial pressure in, solution
+ * out), all device pointers; stream is a cudaStream_t (NULL: default stream).
+ * It calls no cudaMalloc/cudaFree: its scratch is one fixed device array inside
+ * this library, present on every GPU that loads the library until exit, so
+ * nx*ny above IFX_NOALLOC_MAX_CELLS returns IFX_ERR_ARG.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the array, so
+ * calls that overlap on the GPU (other streams, other threads) race: serialise
+ * them. */
+ifx_status ifx_ppe_reference_noalloc(const double* d_dx, const double* d_dy, int nx, int ny, double* d_p,
+                                     int itermax, double tol, int* iters, void* stream);
+
 /* Host <-> device field copies (saveDataToFile's D2H, src/include/postSim.cu:10-39). */
 ifx_status ifx_get_field(ifx_solver* s, int field, double* host, size_t n);
 ifx_status ifx_set_field(ifx_solver* s, int field, const double* host, size_t n);
