@@ -7,6 +7,7 @@
 
 #include "../../include/immerseflow_gb300.h"
 #include "ifx_dev.h"
+#include "ifx_persist.h"
 
 namespace ifx {
 
@@ -84,6 +85,12 @@ struct ifx_solver {
     double* dPart = nullptr;         // NPART partials per finest-level tile
     ifx::LoopCtl* dCtl = nullptr;
     ifx::LoopCtl* hCtl = nullptr;    // pinned
+
+    // persistent execution: one cooperative launch per ifx_step call
+    ifx::GridBar* dBar = nullptr;
+    ifx::PersistPlan plan{};
+    int persist_grid = 0;            // 0: cooperative launch unavailable
+    bool poisoned = false;           // a grid barrier timed out: the handle refuses further steps
 
     // graph execution of one time step (conditional WHILE nodes for the loops)
     bool use_graph = true;

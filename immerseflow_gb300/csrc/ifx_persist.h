@@ -1,0 +1,46 @@
+// ifx_persist.h -- plan of the persistent per-step kernel (kernels_persist.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ifx_dev.h"
+
+namespace ifx {
+
+constexpr int kMaxLevels = 16;
+
+// Grid barrier state (zeroed once at allocation; counters return to zero
+// after every barrier, the generation only grows).
+struct GridBar {
+    unsigned int gen;
+    unsigned int pad0[31];
+    unsigned int top;
+    unsigned int pad1[31];
+    unsigned int sub[64 * 32];  // one counter per group of 32 blocks, 128 B apart
+    unsigned int err;
+    unsigned int pad2[31];
+};
+
+struct PersistPlan {
+    const InstDev* I;
+    InstState* S;
+    const LevelDev* LV;
+    const GhostDev* G;
+    double* gval;
+    double* part;
+    const Tile* t0;
+    const Tile* tsm[kMaxLevels];
+    const Tile* tre[kMaxLevels];
+    const int* coarse;
+    GridBar* bar;
+    int nt0, ng, ninst, lmax, mg_pre, mg_post;
+    int ntsm[kMaxLevels];
+    int ntre[kMaxLevels];
+    int pred_pairs, ppe_bodies, nsteps;
+};
+
+template <typename T>
+cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s);
+template <typename T>
+cudaError_t persist_occupancy(int* blocks_per_sm);
+
+}  // namespace ifx

@@ -1,0 +1,228 @@
+// kernels_persist.cu -- one cooperative launch per time step.
+//
+// At the benchmark sizes a phase of the step (a smoothing sweep, a
+// reduction) touches ~100k cells held in L2 and takes about a microsecond of
+// work, so one launch per phase (~1000 per step) is bound by launch and drain
+// latency.  This kernel keeps a grid of co-resident blocks (cooperative
+// launch, numSMs x occupancy) for the whole step and separates dependent
+// phases by a software grid barrier instead of kernel boundaries.  Every
+// phase calls the same device bodies as the per-phase kernels
+// (method_body.cuh), with the same work decomposition, so both paths give
+// bit-identical results; the convergence loops are plain loops whose exit
+// test every block evaluates from the per-instance states after a barrier.
+//
+// The barrier spins on a generation counter with a bounded number of
+// iterations: on timeout it raises an error flag, every block leaves at its
+// next barrier, and the host reports the failure (the GPU is left usable).
+#include <cuda_runtime.h>
+
+#include "ifx_persist.h"
+#include "method_body.cuh"
+
+namespace ifx {
+
+namespace {
+
+constexpr long long kSpinLimit = 1ll << 22;  // x ~64 ns sleep: ~0.3 s per barrier at most
+
+__device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(const volatile unsigned int*)p; }
+
+// Two-level barrier: blocks arrive on one of up to 64 group counters (32
+// blocks each, one 128-B line per counter); the last of a group arrives on
+// the top counter; the last group flips the generation.
+__device__ __forceinline__ bool grid_barrier(GridBar* b) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int nb = gridDim.x;
+        const unsigned int gen = vload(&b->gen);
+        __threadfence();
+        const unsigned int grp = blockIdx.x >> 5;
+        const unsigned int ngrp = (nb + 31) >> 5;
+        const unsigned int gsize = min(32u, nb - grp * 32u);
+        const unsigned int a = atomicAdd(&b->sub[grp * 32], 1u);
+        if (a == gsize - 1) {
+            b->sub[grp * 32] = 0u;
+            __threadfence();
+            const unsigned int t = atomicAdd(&b->top, 1u);
+            if (t == ngrp - 1) {
+                b->top = 0u;
+                __threadfence();
+                atomicAdd(&b->gen, 1u);
+            }
+        }
+        long long spins = 0;
+        while (vload(&b->gen) == gen) {
+            if (++spins > kSpinLimit) {
+                atomicExch(&b->err, 1u);
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return vload(&b->err) == 0u;
+}
+
+// Loop-exit tests: every block must take the same decision, so the states
+// written by other blocks before the last barrier are read with volatile loads.
+__device__ __forceinline__ bool any_pred_active(const InstState* S, int n) {
+    int a = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].pred_state == ST_ACTIVE);
+    return __syncthreads_or(a) != 0;
+}
+__device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
+    int a = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].ppe_state == ST_ACTIVE);
+    return __syncthreads_or(a) != 0;
+}
+
+#define BAR()                                   \
+    do {                                        \
+        if (!grid_barrier(P.bar)) return false; \
+    } while (0)
+#define FOR_VB(n) for (int vb = blockIdx.x; vb < (n); vb += gridDim.x)
+
+__device__ __forceinline__ int nchunks(int n) { return (n + TILE_THREADS - 1) / TILE_THREADS; }
+
+__device__ bool ghost_fill(const PersistPlan& P, int comps) {
+    FOR_VB(nchunks(P.ng)) b_ghost_gather(P.G, P.ng, P.I, comps, P.gval, vb);
+    BAR();
+    FOR_VB(nchunks(P.ng)) b_ghost_scatter(P.G, P.ng, P.I, comps, P.gval, vb);
+    BAR();
+    return true;
+}
+
+// One V-cycle; *res receives the buffer (0: e, 1: e2) of the finest-level result.
+template <typename T>
+__device__ bool vcycle(const PersistPlan& P, int* res) {
+    int cur[kMaxLevels];
+    FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 1, 0, vb);
+    BAR();
+    cur[0] = 1;
+    for (int k = 1; k < P.mg_pre; k++) {
+        FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 0, cur[0], vb);
+        BAR();
+        cur[0] ^= 1;
+    }
+    for (int l = 1; l < P.lmax; l++) {
+        FOR_VB(P.ntre[l]) b_restrict<T>(P.tre[l], P.LV, P.I, P.S, P.G, cur[l - 1], vb);
+        BAR();
+        cur[l] = 0;
+        if (P.ntsm[l] > 0)
+            for (int k = 1; k < P.mg_pre; k++) {
+                FOR_VB(P.ntsm[l]) b_smooth<T>(P.tsm[l], P.LV, P.I, P.S, P.G, 0, cur[l], vb);
+                BAR();
+                cur[l] ^= 1;
+            }
+    }
+    FOR_VB(P.ninst) b_coarse_solve<T>(P.coarse, P.LV, P.I, P.S, vb);
+    BAR();
+    for (int l = P.lmax - 2; l >= 0; l--) {
+        const Tile* tl = l == 0 ? P.t0 : P.tsm[l];
+        const int nt = l == 0 ? P.nt0 : P.ntsm[l];
+        if (nt == 0) continue;
+        FOR_VB(nt) b_prolong<T>(tl, P.LV, P.S, cur[l], cur[l + 1], vb);
+        BAR();
+        for (int k = 0; k < P.mg_post; k++) {
+            FOR_VB(nt) b_smooth<T>(tl, P.LV, P.I, P.S, P.G, 0, cur[l], vb);
+            BAR();
+            cur[l] ^= 1;
+        }
+    }
+    *res = cur[0];
+    return true;
+}
+
+template <typename T>
+__device__ bool one_step(const PersistPlan& P) {
+    const int n = P.ninst;
+    FOR_VB(nchunks(n)) b_step_begin(P.S, n, vb);
+    FOR_VB(nchunks(P.ng)) b_outflow(P.G, P.ng, P.I, vb);
+    BAR();
+    if (!ghost_fill(P, 3)) return false;
+    FOR_VB(P.nt0) b_conv_rhs(P.t0, P.I, P.S, vb);
+    BAR();
+    // predictor: pairs of Jacobi sweeps until every instance converged
+    const int npred = P.nt0 + nchunks(P.ng);
+    for (int pair = 0; pair < P.pred_pairs; pair++) {
+        FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 0, vb);
+        BAR();
+        FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 0, nullptr, 0ull, vb);
+        BAR();
+        FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 1, vb);
+        BAR();
+        FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 1, nullptr, 0ull, vb);
+        BAR();
+        if (!any_pred_active(P.S, n)) break;
+    }
+    if (!ghost_fill(P, 3)) return false;
+    FOR_VB(P.nt0) b_face_rhs(P.t0, P.I, P.part, 0, vb);
+    BAR();
+    FOR_VB(n) b_rhs_reduce(P.I, P.S, P.part, vb);
+    BAR();
+    FOR_VB(P.nt0) b_bicg_start(P.t0, P.LV, P.I, P.S, P.G, P.part, vb);
+    BAR();
+    FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 1, nullptr, 0ull, vb);
+    BAR();
+    // pressure: BiCGSTAB iterations until every instance converged
+    for (int it = 0; it < P.ppe_bodies; it++) {
+        if (!any_ppe_active(P.S, n)) break;
+        FOR_VB(P.nt0) b_bicg_p<T>(P.t0, P.LV, P.I, P.S, vb);
+        BAR();
+        int e1 = 0, e2 = 0;
+        if (!vcycle<T>(P, &e1)) return false;
+        FOR_VB(P.nt0) b_bicg_apply<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, e1, 0, vb);
+        BAR();
+        FOR_VB(n) b_bicg_scalar(P.I, P.S, P.part, 0, vb);
+        BAR();
+        FOR_VB(P.nt0) b_bicg_s<T>(P.t0, P.LV, P.I, P.S, vb);
+        BAR();
+        if (!vcycle<T>(P, &e2)) return false;
+        FOR_VB(P.nt0) b_bicg_apply<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, e2, 1, vb);
+        BAR();
+        FOR_VB(n) b_bicg_scalar(P.I, P.S, P.part, 1, vb);
+        BAR();
+        FOR_VB(P.nt0) b_bicg_x(P.t0, P.LV, P.I, P.S, P.part, vb);
+        BAR();
+        FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 0, nullptr, 0ull, vb);
+        BAR();
+    }
+    FOR_VB(P.nt0) b_p_finalize(P.t0, P.I, P.S, vb);
+    BAR();
+    if (!ghost_fill(P, 4)) return false;
+    FOR_VB(P.nt0) b_correct(P.t0, P.I, P.part, vb);
+    BAR();
+    FOR_VB(n) b_correct_reduce(P.I, P.S, P.part, vb);
+    BAR();
+    if (!ghost_fill(P, 3)) return false;
+    FOR_VB(n) b_forces(P.I, P.S, vb);
+    BAR();
+    return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS) k_persist_step(PersistPlan P) {
+    for (int s = 0; s < P.nsteps; s++)
+        if (!one_step<T>(P)) return;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) {
+    void* args[] = {(void*)&P};
+    return cudaLaunchCooperativeKernel((const void*)k_persist_step<T>, dim3(grid), dim3(TILE_THREADS), args, 0, s);
+}
+
+template <typename T>
+cudaError_t persist_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_persist_step<T>, TILE_THREADS, 0);
+}
+
+template cudaError_t launch_persist_step<double>(const PersistPlan&, int, cudaStream_t);
+template cudaError_t launch_persist_step<float>(const PersistPlan&, int, cudaStream_t);
+template cudaError_t persist_occupancy<double>(int*);
+template cudaError_t persist_occupancy<float>(int*);
+
+}  // namespace ifx

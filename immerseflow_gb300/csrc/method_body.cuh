@@ -1,0 +1,940 @@
+// kernels_method.cu -- sm_103a kernels of the fractional step with ghost-cell
+// IBM, batched over instances.
+//
+// The method (written because the reference leaves it unimplemented:
+// src/include/AD_PPE_Correction.cu:1-12, src/include/PPESolver.cu:73-135):
+//   predictor  (I - dt/Re L) q* = q^n - dt (3/2 N^n - 1/2 N^{n-1})     Jacobi,
+//              convection N in the reference's face-flux form
+//              (src/include/ADSolver.cu:46-79) with face velocities U, V;
+//   pressure   L p = div(U*)/dt, BiCGSTAB in FP64 preconditioned by a
+//              multigrid V-cycle in T (weighted Jacobi smoothing,
+//              area-weighted restriction, bilinear prolongation, RB-SOR on
+//              the coarsest level);
+//   projection u = u* - dt grad p (cells), U = U* - dt dp/dn (faces).
+// Coefficients follow the reference's 2/(dx_i (dx_i + dx_nb)) form
+// (src/include/ADSolver.cu:34-39).  Every phase has a CPU twin in the
+// oracle (oracle/oracle.cpp, method_step).
+//
+// Precision: state in FP64; multigrid corrections in T (double for the plain
+// path, float for the mixed path).
+
+// method_body.cuh -- device bodies of the fractional-step kernels.
+//
+// Each phase of the time step is a __device__ function b_*(..., vb) that
+// processes one "virtual block" vb: a tile (32x8 cells of one level of one
+// instance), a chunk of ghost relations, or one instance.  The same bodies
+// run as ordinary kernels (one launch per phase, kernels_method.cu; used by
+// the CUDA-graph path) and inside the persistent per-step kernel
+// (kernels_persist.cu), so both paths compute bit-identical results.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ifx_dev.h"
+#include "ifx_kernels.h"
+
+
+namespace ifx {
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ double rcpa(double d) { return (double)__frcp_rn((float)d); }
+__device__ __forceinline__ float rcpa(float d) { return __frcp_rn(d); }
+
+template <typename T> struct LvA;
+template <> struct LvA<double> {
+    static __device__ __forceinline__ const double* kx(const LevelDev& L) { return L.kx; }
+    static __device__ __forceinline__ const double* ky(const LevelDev& L) { return L.ky; }
+    static __device__ __forceinline__ const double* ix(const LevelDev& L) { return L.ix; }
+    static __device__ __forceinline__ const double* iy(const LevelDev& L) { return L.iy; }
+    static __device__ __forceinline__ const double* dw(const LevelDev& L) { return L.dw; }
+    static __device__ __forceinline__ const double* dh(const LevelDev& L) { return L.dh; }
+    static __device__ __forceinline__ const double* pwx(const LevelDev& L) { return L.pwx; }
+    static __device__ __forceinline__ const double* pwy(const LevelDev& L) { return L.pwy; }
+};
+template <> struct LvA<float> {
+    static __device__ __forceinline__ const float* kx(const LevelDev& L) { return L.kxf; }
+    static __device__ __forceinline__ const float* ky(const LevelDev& L) { return L.kyf; }
+    static __device__ __forceinline__ const float* ix(const LevelDev& L) { return L.ixf; }
+    static __device__ __forceinline__ const float* iy(const LevelDev& L) { return L.iyf; }
+    static __device__ __forceinline__ const float* dw(const LevelDev& L) { return L.dwf; }
+    static __device__ __forceinline__ const float* dh(const LevelDev& L) { return L.dhf; }
+    static __device__ __forceinline__ const float* pwx(const LevelDev& L) { return L.pwxf; }
+    static __device__ __forceinline__ const float* pwy(const LevelDev& L) { return L.pwyf; }
+};
+
+__device__ __forceinline__ void tile_ij(const Tile& t, int& i, int& j) {
+    i = t.i0 + (int)(threadIdx.x & 31);
+    j = t.j0 + (int)(threadIdx.x >> 5);
+}
+
+// Deterministic block sum of NV values; result valid in thread 0..NV-1 as out[k].
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* out) {
+    __shared__ double sh[NV][32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (l == 0) sh[k][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int q = 0; q < nw; q++) s += sh[threadIdx.x][q];
+        out[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ double block_max(double v) {
+    __shared__ double sh[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double m = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nw; q++) m = fmax(m, sh[q]);
+    __syncthreads();
+    return m;
+}
+
+// Per-instance sum of the level-0 tile partials, fixed order; valid in all threads.
+template <int NV>
+__device__ __forceinline__ void inst_sum(const double* part, int beg, int cnt, double (&res)[NV]) {
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k] = 0.0;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; k++) acc[k] += part[(size_t)(beg + t) * NPART + k];
+    __shared__ double out[NV];
+    block_sum<NV>(acc, out);
+#pragma unroll
+    for (int k = 0; k < NV; k++) res[k] = out[k];
+}
+
+__device__ __forceinline__ void loop_vote(LoopCtl* ctl, bool active, unsigned long long handle) {
+    // thread 0 of each voting block; no-op inside the persistent kernel (ctl == nullptr)
+    if (!ctl) return;
+    if (active) atomicAdd(&ctl->active, 1);
+    __threadfence();
+    unsigned int t = atomicAdd(&ctl->ticket, 1u);
+    if (t == gridDim.x - 1) {
+        __threadfence();
+        int a = atomicAdd(&ctl->active, 0);
+        ctl->result = a;
+        ctl->active = 0;
+        ctl->ticket = 0u;
+        __threadfence();
+        if (handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, a > 0 ? 1u : 0u);
+    }
+}
+
+__device__ __forceinline__ double ghost_const(const GhostDev& g, const double* qb, double c0) {
+    if (g.qi[0] >= 0) c0 += g.qf[0] * qb[g.qi[0]];
+    if (g.qi[1] >= 0) c0 += g.qf[1] * qb[g.qi[1]];
+    return c0;
+}
+
+// Image-point value of the IBM ghost at global entry gid, from field e;
+// ws receives the weight on cell `self`.  Pressure stencils reference fluid
+// cells only, so this is an exact linear function of the fluid values.
+template <typename TC, typename TE>
+__device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
+    const GhostDev& g = G[gid];
+    TC acc = (TC)0;
+    ws = (TC)0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const TC w = (TC)g.wp[k];
+        acc += w * (TC)e[g.nb[k]];
+        if (g.nb[k] == self) ws += w;
+    }
+    return acc;
+}
+
+// Pressure-type Laplacian at live cell (i,j): Le = sum c (e_nb - e) with
+// closed faces dropped, Dirichlet sides adding 2c to the diagonal, and (finest
+// level) faces to IBM ghosts using the ghost's image-point value (ghost
+// unknowns eliminated).  D is the diagonal of that operator.  Coefficients
+// and arithmetic in TC, field values of type TE.
+template <typename TC, typename TE, bool LVL0>
+__device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id,
+                                    uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+    const TC* kx = LvA<TC>::kx(L);
+    const TC* ky = LvA<TC>::ky(L);
+    const TC* ix = LvA<TC>::ix(L);
+    const TC* iy = LvA<TC>::iy(L);
+    const TC cE = kx[i] * ix[i], cW = kx[i - 1] * ix[i];
+    const TC cN = ky[j] * iy[j], cS = ky[j - 1] * iy[j];
+    const TC ce = (bt & B_E) ? cE : (TC)0, cw = (bt & B_W) ? cW : (TC)0;
+    const TC cn = (bt & B_N) ? cN : (TC)0, cs = (bt & B_S) ? cS : (TC)0;
+    TC dd = ce + cw + cn + cs;
+    if (L.dirmask) {
+        if (i == L.NX && (L.dirmask & (1 << 1))) dd += (TC)2 * cE;
+        if (i == 1 && (L.dirmask & (1 << 0))) dd += (TC)2 * cW;
+        if (j == L.NY && (L.dirmask & (1 << 3))) dd += (TC)2 * cN;
+        if (j == 1 && (L.dirmask & (1 << 2))) dd += (TC)2 * cS;
+    }
+    const int P = L.pitch;
+    TC eE = (TC)e[id + 1], eW = (TC)e[id - 1], eN = (TC)e[id + P], eS = (TC)e[id - P];
+    TC dm = dd;
+    if (LVL0 && (bt & 0xF0)) {
+        TC ws;
+        if (bt & G_E) { eE = ghost_eval<TC, TE>(G, gidx[id + 1], e, id, ws); dm -= ce * ws; }
+        if (bt & G_W) { eW = ghost_eval<TC, TE>(G, gidx[id - 1], e, id, ws); dm -= cw * ws; }
+        if (bt & G_N) { eN = ghost_eval<TC, TE>(G, gidx[id + P], e, id, ws); dm -= cn * ws; }
+        if (bt & G_S) { eS = ghost_eval<TC, TE>(G, gidx[id - P], e, id, ws); dm -= cs * ws; }
+    }
+    Le = ce * eE + cw * eW + cn * eN + cs * eS - dd * (TC)e[id];
+    D = dm;
+}
+
+// ------------------------------------------------------ step bookkeeping
+
+__device__ __forceinline__ void b_step_begin(InstState* S, int n, int vb) {
+    int k = vb * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    S[k].pred_state = ST_ACTIVE;
+    S[k].pred_iters = 0;
+    S[k].ppe_state = ST_ACTIVE;
+    S[k].ppe_iters = 0;
+}
+
+// Convective outflow: advance the boundary face value of every outflow
+// edge ghost (dq/dt + Uc dq/dn = 0, explicit).
+__device__ __forceinline__ void b_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I, int vb) {
+    int g = vb * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const GhostDev& gh = G[g];
+    if (gh.qown < 0) return;
+    const InstDev& in = I[gh.inst];
+    double fac = in.dt * in.uc * 2.0 / gh.qh;
+    in.qbu[gh.qown] = in.qbu[gh.qown] - fac * (in.qbu[gh.qown] - in.u[gh.adj]);
+    in.qbv[gh.qown] = in.qbv[gh.qown] - fac * (in.qbv[gh.qown] - in.v[gh.adj]);
+}
+
+// Ghost refresh in two passes (gather, then scatter) so that ghost-to-ghost
+// references read the old values, exactly like one Jacobi pass.
+// comps: bit0 u, bit1 v, bit2 p.
+__device__ __forceinline__ void b_ghost_gather(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
+                               int comps, double* __restrict__ gval, int vb) {
+    int g = vb * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const GhostDev& gh = G[g];
+    const InstDev& in = I[gh.inst];
+    if (comps & 1) {
+        double a = ghost_const(gh, in.qbu, gh.cu);
+#pragma unroll
+        for (int k = 0; k < 4; k++) a += gh.wu[k] * in.u[gh.nb[k]];
+        gval[3 * (size_t)g] = a;
+    }
+    if (comps & 2) {
+        double a = ghost_const(gh, in.qbv, gh.cv);
+#pragma unroll
+        for (int k = 0; k < 4; k++) a += gh.wv[k] * in.v[gh.nb[k]];
+        gval[3 * (size_t)g + 1] = a;
+    }
+    if (comps & 4) {
+        double a = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) a += gh.wp[k] * in.p[gh.nb[k]];
+        gval[3 * (size_t)g + 2] = a;
+    }
+}
+
+__device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
+                                int comps, const double* __restrict__ gval, int vb) {
+    int g = vb * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const GhostDev& gh = G[g];
+    const InstDev& in = I[gh.inst];
+    if (comps & 1) in.u[gh.cell] = gval[3 * (size_t)g];
+    if (comps & 2) in.v[gh.cell] = gval[3 * (size_t)g + 1];
+    if (comps & 4) in.p[gh.cell] = gval[3 * (size_t)g + 2];
+}
+
+// ------------------------------------------------------------- predictor
+
+// Convective term in face-flux form and the AB2 right-hand side.
+__device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+                           const InstState* __restrict__ S, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    int i, j;
+    tile_ij(t, i, j);
+    if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
+    const int P = in.pitch, id = i + j * P;
+    if (in.type[id] != T_FLUID) {
+        in.ru[id] = 0.0;
+        in.rv[id] = 0.0;
+        return;
+    }
+    const double* u = in.u;
+    const double* v = in.v;
+    const double gxi = in.gx[i], fxi = in.fx[i], gxw = in.gx[i - 1], fxw = in.fx[i - 1];
+    const double gyj = in.gy[j], fyj = in.fy[j], gys = in.gy[j - 1], fys = in.fy[j - 1];
+    const double ixi = in.ix[i], iyj = in.iy[j];
+    const double Ue = in.U[id], Uw = in.U[id - 1], Vn = in.V[id], Vs = in.V[id - P];
+    const double ue = u[id] * gxi + u[id + 1] * fxi, uw = u[id - 1] * gxw + u[id] * fxw;
+    const double un = u[id] * gyj + u[id + P] * fyj, us = u[id - P] * gys + u[id] * fys;
+    const double ve = v[id] * gxi + v[id + 1] * fxi, vw = v[id - 1] * gxw + v[id] * fxw;
+    const double vn = v[id] * gyj + v[id + P] * fyj, vs = v[id - P] * gys + v[id] * fys;
+    const double Nu = (ue * Ue - uw * Uw) * ixi + (un * Vn - us * Vs) * iyj;
+    const double Nv = (ve * Ue - vw * Uw) * ixi + (vn * Vn - vs * Vs) * iyj;
+    const bool ab2 = S[t.inst].have_nold != 0;
+    const double cu = ab2 ? 1.5 * Nu - 0.5 * in.Nu[id] : Nu;
+    const double cv = ab2 ? 1.5 * Nv - 0.5 * in.Nv[id] : Nv;
+    in.ru[id] = u[id] - in.dt * cu;
+    in.rv[id] = v[id] - in.dt * cv;
+    in.Nu[id] = Nu;
+    in.Nv[id] = Nv;
+}
+
+// One Jacobi sweep of the predictor for u and v, fluid cells and every
+// ghost relation; parity 0 reads (u,v) and writes (u2,v2), parity 1 the
+// reverse.  An instance that converged on the parity-0 sweep copies its
+// result back on the parity-1 sweep.
+__device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
+                             int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                             double* __restrict__ part, int parity, int vb) {
+    if ((int)vb < ntiles) {
+        const Tile t = tiles[vb];
+        const InstDev& in = I[t.inst];
+        const int st = S[t.inst].pred_state;
+        if (st == ST_DONE) return;
+        const double* su = parity ? in.u2 : in.u;
+        const double* sv = parity ? in.v2 : in.v;
+        double* du = parity ? in.u : in.u2;
+        double* dv = parity ? in.v : in.v2;
+        int i, j;
+        tile_ij(t, i, j);
+        const bool ok = i >= 1 && i <= in.NX && j >= 1 && j <= in.NY;
+        const int P = in.pitch, id = i + j * P;
+        const bool fl = ok && in.type[id] == T_FLUID;
+        if (st == ST_FINAL_IN_ALT) {
+            if (fl) {
+                du[id] = su[id];
+                dv[id] = sv[id];
+            }
+            return;
+        }
+        double m[1] = {0.0};
+        if (fl) {
+            const double ixi = in.ix[i], iyj = in.iy[j];
+            const double aE = in.dtre * (in.kx[i] * ixi), aW = in.dtre * (in.kx[i - 1] * ixi);
+            const double aN = in.dtre * (in.ky[j] * iyj), aS = in.dtre * (in.ky[j - 1] * iyj);
+            const double aP = 1.0 + aE + aW + aN + aS;
+            const double di = rcpa(aP);
+            const double dU = (in.ru[id] + aE * su[id + 1] + aW * su[id - 1] + aN * su[id + P] + aS * su[id - P] -
+                               aP * su[id]) * di;
+            const double dV = (in.rv[id] + aE * sv[id + 1] + aW * sv[id - 1] + aN * sv[id + P] + aS * sv[id - P] -
+                               aP * sv[id]) * di;
+            du[id] = su[id] + dU;
+            dv[id] = sv[id] + dV;
+            m[0] = fabs(dU) + fabs(dV);
+        }
+        __shared__ double out[1];
+        block_sum<1>(m, out);
+        if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
+    } else {
+        const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
+        if (g >= ng) return;
+        const GhostDev& gh = G[g];
+        const InstDev& in = I[gh.inst];
+        const int st = S[gh.inst].pred_state;
+        if (st == ST_DONE) return;
+        const double* su = parity ? in.u2 : in.u;
+        const double* sv = parity ? in.v2 : in.v;
+        double* du = parity ? in.u : in.u2;
+        double* dv = parity ? in.v : in.v2;
+        if (st == ST_FINAL_IN_ALT) {
+            du[gh.cell] = su[gh.cell];
+            dv[gh.cell] = sv[gh.cell];
+            return;
+        }
+        double au = ghost_const(gh, in.qbu, gh.cu), av = ghost_const(gh, in.qbv, gh.cv);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            au += gh.wu[k] * su[gh.nb[k]];
+            av += gh.wv[k] * sv[gh.nb[k]];
+        }
+        du[gh.cell] = au;
+        dv[gh.cell] = av;
+    }
+}
+
+__device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                              const double* __restrict__ part, int parity, LoopCtl* ctl,
+                              unsigned long long handle, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    const int st = S[k].pred_state;
+    bool active = false;
+    if (st == ST_ACTIVE) {
+        double r[1];
+        inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
+        if (threadIdx.x == 0) {
+            const int it = S[k].pred_iters + 1;
+            S[k].pred_iters = it;
+            S[k].pred_metric = r[0] / (double)(in.n_fluid > 0 ? in.n_fluid : 1);
+            const bool done = r[0] <= in.ad_lim || it >= in.ad_itermax;
+            if (done) S[k].pred_state = parity == 0 ? ST_FINAL_IN_ALT : ST_DONE;
+            active = !done;
+        }
+    } else if (st == ST_FINAL_IN_ALT) {
+        if (threadIdx.x == 0) S[k].pred_state = ST_DONE;
+    }
+    if (threadIdx.x == 0) loop_vote(ctl, active, handle);
+}
+
+// -------------------------------------------------- faces and PPE source
+
+__device__ __forceinline__ double face_u(const InstDev& in, const double* u, int i, int id) {
+    if (in.type[id] == T_FLUID || in.type[id + 1] == T_FLUID) return u[id] * in.gx[i] + u[id + 1] * in.fx[i];
+    return 0.0;
+}
+__device__ __forceinline__ double face_v(const InstDev& in, const double* v, int j, int id) {
+    const int P = in.pitch;
+    if (in.type[id] == T_FLUID || in.type[id + P] == T_FLUID) return v[id] * in.gy[j] + v[id + P] * in.fy[j];
+    return 0.0;
+}
+
+// Face velocities of the predicted field (into Us,Vs, or into U,V when
+// to_final), the pressure source div(U*)/dt and its area-weighted sum.
+__device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+                           double* __restrict__ part, int to_final, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    int i, j;
+    tile_ij(t, i, j);
+    const int P = in.pitch, id = i + j * P;
+    double* Uo = to_final ? in.U : in.Us;
+    double* Vo = to_final ? in.V : in.Vs;
+    if (i <= in.nx - 2 && j >= 1 && j <= in.NY) Uo[id] = face_u(in, in.u, i, id);
+    if (j <= in.ny - 2 && i >= 1 && i <= in.NX) Vo[id] = face_v(in, in.v, j, id);
+    double acc[1] = {0.0};
+    if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
+        if (in.type[id] == T_FLUID) {
+            const double Ue = face_u(in, in.u, i, id), Uw = face_u(in, in.u, i - 1, id - 1);
+            const double Vn = face_v(in, in.v, j, id), Vs = face_v(in, in.v, j - 1, id - P);
+            const double d = (Ue - Uw) * in.ix[i] + (Vn - Vs) * in.iy[j];
+            const double b = d / in.dt;
+            in.b[id] = b;
+            acc[0] = b * (in.dx[i] * in.dy[j]);
+        } else {
+            in.b[id] = 0.0;
+        }
+    }
+    __shared__ double out[1];
+    block_sum<1>(acc, out);
+    if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
+}
+
+__device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                             const double* __restrict__ part, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    double r[1];
+    inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
+    if (threadIdx.x == 0) S[k].bmean = in.singular ? r[0] / in.area : 0.0;
+}
+
+// ------------------------------------------------------------------ PPE
+//
+// BiCGSTAB in FP64 on L p = b (ghost-eliminated finest-level operator),
+// preconditioned by one multigrid V-cycle in T.  Per-instance scalars live
+// in InstState; every reduction is per instance over its tiles, fixed order.
+
+__device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, uint8_t& bt) {
+    if (i < 1 || i > L.NX || j < 1 || j > L.NY) return false;
+    id = i + j * L.pitch;
+    bt = L.bits[id];
+    return (bt & 0x0F) != 0;
+}
+
+// r = (b - mean b) - L p, rh = r, p_dir = v = 0.
+// partials: 0 (r,r)  1 (b,b)  2 (rh,r)  3 (p,area)
+__device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        double Lp, D;
+        lap<double, double, true>(L, in.p, i, j, id, bt, G, in.gidx, Lp, D);
+        const double bb = in.b[id] - st.bmean;
+        const double r = bb - Lp;
+        in.kr[id] = r;
+        in.krh[id] = r;
+        in.kp[id] = 0.0;
+        in.kv[id] = 0.0;
+        acc[0] = r * r;
+        acc[1] = bb * bb;
+        acc[2] = r * r;
+        acc[3] = in.p[id] * (in.dx[i] * in.dy[j]);
+    }
+    __shared__ double out[4];
+    block_sum<4>(acc, out);
+    if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
+}
+
+// Convergence test on ||r||, then rho, beta for the next direction.  Votes.
+__device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                                const double* __restrict__ part, int start, LoopCtl* ctl,
+                                unsigned long long handle, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    bool active = false;
+    if (S[k].ppe_state == ST_ACTIVE) {
+        double r[4];
+        inst_sum<4>(part, in.tile_beg, in.tile_cnt, r);
+        if (threadIdx.x == 0) {
+            InstState& st = S[k];
+            if (start) {
+                st.bnorm = sqrt(r[1]);
+                st.rho = st.alpha = st.omega = 1.0;
+                st.ppe_iters = 0;
+            } else {
+                st.ppe_iters += 1;
+            }
+            const double rel = sqrt(r[0]) / (st.bnorm > 1e-300 ? st.bnorm : 1e-300);
+            st.ppe_rel = rel;
+            st.pmean = r[3] / in.area;
+            if (rel <= in.ppe_tol || st.ppe_iters >= in.ppe_itermax) {
+                st.ppe_state = ST_DONE;
+            } else {
+                const double rho1 = r[2];
+                st.beta = (rho1 / st.rho) * (st.alpha / st.omega);
+                st.rho = rho1;
+                active = true;
+            }
+        }
+    }
+    if (threadIdx.x == 0) loop_vote(ctl, active, handle);
+}
+
+// p_dir = r + beta (p_dir - omega v); preconditioner input.
+template <typename T>
+__device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const double pd = in.kr[id] + st.beta * (in.kp[id] - st.omega * in.kv[id]);
+    in.kp[id] = pd;
+    ((T*)L.r)[id] = (T)pd;
+}
+
+// y = L z with z the preconditioned vector (V-cycle result in T), stored in
+// FP64 as zo; partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
+template <typename T>
+__device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    const T* z = (const T*)(e_alt ? L.e2 : L.e);
+    double* zo = which == 0 ? in.kph : in.ksh;
+    double* y = which == 0 ? in.kv : in.kt;
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    double acc[2] = {0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        double Lz, D;
+        lap<double, T, true>(L, z, i, j, id, bt, G, in.gidx, Lz, D);
+        zo[id] = (double)z[id];
+        y[id] = Lz;
+        if (which == 0) {
+            acc[0] = in.krh[id] * Lz;
+        } else {
+            acc[0] = Lz * in.ks[id];
+            acc[1] = Lz * Lz;
+        }
+    }
+    __shared__ double out[2];
+    block_sum<2>(acc, out);
+    if (threadIdx.x < 2) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
+}
+
+// alpha = rho / (rh, v)   (which = 0)   or   omega = (t, s) / (t, t)   (which = 1)
+__device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                              const double* __restrict__ part, int which, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    if (S[k].ppe_state != ST_ACTIVE) return;
+    double r[2];
+    inst_sum<2>(part, in.tile_beg, in.tile_cnt, r);
+    if (threadIdx.x == 0) {
+        if (which == 0) S[k].alpha = r[0] != 0.0 ? S[k].rho / r[0] : 0.0;
+        else S[k].omega = r[1] != 0.0 ? r[0] / r[1] : 0.0;
+    }
+}
+
+// s = r - alpha v; preconditioner input.
+template <typename T>
+__device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const double sv = in.kr[id] - st.alpha * in.kv[id];
+    in.ks[id] = sv;
+    ((T*)L.r)[id] = (T)sv;
+}
+
+// p += alpha ph + omega sh ; r = s - omega t.
+// partials: 0 (r,r)  1 unused  2 (rh,r)  3 (p,area)
+__device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                         double* __restrict__ part, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[in.lev0];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (live0(L, i, j, id, bt)) {
+        const double pn = in.p[id] + st.alpha * in.kph[id] + st.omega * in.ksh[id];
+        in.p[id] = pn;
+        const double r = in.ks[id] - st.omega * in.kt[id];
+        in.kr[id] = r;
+        acc[0] = r * r;
+        acc[2] = in.krh[id] * r;
+        acc[3] = pn * (in.dx[i] * in.dy[j]);
+    }
+    __shared__ double out[4];
+    block_sum<4>(acc, out);
+    if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
+}
+
+// Weighted-Jacobi sweep on one multigrid level (tiles of that level for all
+// instances).  flags: 1 = start from e = 0.
+template <typename T>
+__device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                         const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
+    const Tile t = tiles[vb];
+    const LevelDev& L = LV[t.lev];
+    if (S[L.inst].ppe_state != ST_ACTIVE) return;
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(L, i, j, id, bt)) return;
+    const T* src = (const T*)(src_alt ? L.e2 : L.e);
+    T* dst = (T*)(src_alt ? L.e : L.e2);
+    const T om = (T)I[L.inst].omega;
+    const T r = ((const T*)L.r)[id];
+    T Le, D;
+    if (L.depth == 0) lap<T, T, true>(L, src, i, j, id, bt, G, I[L.inst].gidx, Le, D);
+    else lap<T, T, false>(L, src, i, j, id, bt, G, nullptr, Le, D);
+    dst[id] = (flags & 1) ? -om * r * rcpa(D) : src[id] + om * (Le - r) * rcpa(D);
+}
+
+// Restriction of the fine residual (area weighted) onto coarse tiles, fused
+// with the first (zero-start) smoothing sweep of a middle coarse level.
+template <typename T>
+__device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                           const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                           const GhostDev* __restrict__ G, int fine_alt, int vb) {
+    const Tile t = tiles[vb];
+    const LevelDev& C = LV[t.lev];
+    if (S[C.inst].ppe_state != ST_ACTIVE) return;
+    const LevelDev& F = LV[C.parent];
+    int I0, J0;
+    tile_ij(t, I0, J0);
+    if (I0 < 1 || I0 > C.NX || J0 < 1 || J0 > C.NY) return;
+    const int cid = I0 + J0 * C.pitch;
+    const uint8_t cb = C.bits[cid];
+    T* rc = (T*)C.r;
+    if (!(cb & 0x0F)) {
+        rc[cid] = (T)0;
+        return;
+    }
+    const T* fe = (const T*)(fine_alt ? F.e2 : F.e);
+    const T* fr = (const T*)F.r;
+    const T* fdw = LvA<T>::dw(F);
+    const T* fdh = LvA<T>::dh(F);
+    T acc = (T)0;
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+        for (int di = 0; di < 2; di++) {
+            const int i = 2 * I0 - 1 + di, j = 2 * J0 - 1 + dj;
+            if (i > F.NX || j > F.NY) continue;
+            const int id = i + j * F.pitch;
+            const uint8_t bt = F.bits[id];
+            if (!(bt & 0x0F)) continue;
+            T Le, D;
+            if (F.depth == 0) lap<T, T, true>(F, fe, i, j, id, bt, G, I[C.inst].gidx, Le, D);
+            else lap<T, T, false>(F, fe, i, j, id, bt, G, nullptr, Le, D);
+            acc += (fr[id] - Le) * (fdw[i] * fdh[j]);
+        }
+    const T rv = acc / (LvA<T>::dw(C)[I0] * LvA<T>::dh(C)[J0]);
+    rc[cid] = rv;
+    if (C.child >= 0) {  // middle level: fused first sweep from zero
+        T Le, D;
+        lap<T, T, false>(C, (const T*)C.e, I0, J0, cid, cb, G, nullptr, Le, D);
+        ((T*)C.e)[cid] = -(T)I[C.inst].omega * rv * rcpa(D);
+    }
+}
+
+// Bilinear prolongation of the coarse correction, added on the fine level.
+template <typename T>
+__device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                          const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
+    const Tile t = tiles[vb];
+    const LevelDev& F = LV[t.lev];
+    if (S[F.inst].ppe_state != ST_ACTIVE) return;
+    const LevelDev& C = LV[F.child];
+    int i, j, id;
+    uint8_t bt;
+    tile_ij(t, i, j);
+    if (!live0(F, i, j, id, bt)) return;
+    // the coarsest level's solution is always in e; a middle level's in the buffer its sweeps ended on
+    const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
+    T* fe = (T*)(fine_alt ? F.e2 : F.e);
+    const int I0 = F.pI[i], In = F.pIn[i], J0 = F.pJ[j], Jn = F.pJn[j];
+    const T wx = LvA<T>::pwx(F)[i], wy = LvA<T>::pwy(F)[j];
+    const T sx = (T)F.psx[i], sy = (T)F.psy[j];
+    T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
+    const int CP = C.pitch;
+    const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
+    w00 = (C.bits[c00] & 0x0F) ? w00 : (T)0;
+    w10 = (C.bits[c10] & 0x0F) ? w10 : (T)0;
+    w01 = (C.bits[c01] & 0x0F) ? w01 : (T)0;
+    w11 = (C.bits[c11] & 0x0F) ? w11 : (T)0;
+    const T sw = w00 + w10 + w01 + w11;
+    const T val = (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
+    fe[id] += val;
+}
+
+// Coarsest level: e = 0, then red-black SOR sweeps, one block per instance.
+template <typename T>
+__device__ __forceinline__ void b_coarse_solve(const int* __restrict__ levs, const LevelDev* __restrict__ LV,
+                               const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
+    const LevelDev& L = LV[levs[vb]];
+    if (S[L.inst].ppe_state != ST_ACTIVE) return;
+    T* e = (T*)L.e;
+    const T* r = (const T*)L.r;
+    const int n = L.pitch * L.ny;
+    for (int id = threadIdx.x; id < n; id += blockDim.x) e[id] = (T)0;
+    __syncthreads();
+    const T om = (T)COARSE_OMEGA;
+    const int NXY = L.NX * L.NY;
+    for (int it = 0; it < COARSE_SWEEPS; it++) {
+        for (int col = 0; col < 2; col++) {
+            for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
+                const int i = 1 + q % L.NX, j = 1 + q / L.NX;
+                if (((i + j) & 1) != col) continue;
+                const int id = i + j * L.pitch;
+                const uint8_t bt = L.bits[id];
+                if (!(bt & 0x0F)) continue;
+                T Le, D;
+                lap<T, T, false>(L, e, i, j, id, bt, nullptr, nullptr, Le, D);
+                e[id] = e[id] + om * (Le - r[id]) * rcpa(D);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ------------------------------------------------------------ projection
+
+__device__ __forceinline__ void b_p_finalize(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+                             const InstState* __restrict__ S, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    if (!in.singular) return;
+    int i, j;
+    tile_ij(t, i, j);
+    if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
+    const int id = i + j * in.pitch;
+    const uint8_t ty = in.type[id];
+    if (ty == T_FLUID || ty == T_GHOST) in.p[id] -= S[t.inst].pmean;
+}
+
+__device__ __forceinline__ double corr_u(const InstDev& in, int i, int id) {
+    const bool act = in.type[id] == T_FLUID || in.type[id + 1] == T_FLUID;
+    if (!act) return in.Us[id];
+    if (i == 0 && !(in.dirmask & 1)) return in.Us[id];
+    if (i == in.nx - 2 && !(in.dirmask & 2)) return in.Us[id];
+    return in.Us[id] - in.dt * in.kx[i] * (in.p[id + 1] - in.p[id]);
+}
+__device__ __forceinline__ double corr_v(const InstDev& in, int j, int id) {
+    const int P = in.pitch;
+    const bool act = in.type[id] == T_FLUID || in.type[id + P] == T_FLUID;
+    if (!act) return in.Vs[id];
+    if (j == 0 && !(in.dirmask & 4)) return in.Vs[id];
+    if (j == in.ny - 2 && !(in.dirmask & 8)) return in.Vs[id];
+    return in.Vs[id] - in.dt * in.ky[j] * (in.p[id + P] - in.p[id]);
+}
+
+// Projection of cell and face velocities; divergence and boundary fluxes.
+__device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+                          double* __restrict__ part, int vb) {
+    const Tile t = tiles[vb];
+    const InstDev& in = I[t.inst];
+    int i, j;
+    tile_ij(t, i, j);
+    const int P = in.pitch, id = i + j * P;
+    double dmax = 0.0, fl[2] = {0.0, 0.0};
+    if (i <= in.nx - 2 && j >= 1 && j <= in.NY) {
+        const double Un = corr_u(in, i, id);
+        in.U[id] = Un;
+        if (i == 0) fl[0] += Un * in.dy[j];
+        if (i == in.nx - 2) fl[1] += Un * in.dy[j];
+    }
+    if (j <= in.ny - 2 && i >= 1 && i <= in.NX) {
+        const double Vn = corr_v(in, j, id);
+        in.V[id] = Vn;
+        if (j == 0) fl[0] += Vn * in.dx[i];
+        if (j == in.ny - 2) fl[1] += Vn * in.dx[i];
+    }
+    if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
+        if (in.type[id] == T_FLUID) {
+            const double* p = in.p;
+            const double ixi = in.ix[i], iyj = in.iy[j];
+            const double pe = p[id] * in.gx[i] + p[id + 1] * in.fx[i];
+            const double pw = p[id - 1] * in.gx[i - 1] + p[id] * in.fx[i - 1];
+            const double pn = p[id] * in.gy[j] + p[id + P] * in.fy[j];
+            const double ps = p[id - P] * in.gy[j - 1] + p[id] * in.fy[j - 1];
+            in.u[id] -= in.dt * (pe - pw) * ixi;
+            in.v[id] -= in.dt * (pn - ps) * iyj;
+            const double d = (corr_u(in, i, id) - corr_u(in, i - 1, id - 1)) * ixi +
+                             (corr_v(in, j, id) - corr_v(in, j - 1, id - P)) * iyj;
+            in.div[id] = d;
+            dmax = fabs(d);
+        } else {
+            in.div[id] = 0.0;
+        }
+    }
+    const double m = block_max(dmax);
+    __shared__ double out[2];
+    block_sum<2>(fl, out);
+    if (threadIdx.x == 0) {
+        part[(size_t)vb * NPART] = m;
+        part[(size_t)vb * NPART + 1] = out[0];
+        part[(size_t)vb * NPART + 2] = out[1];
+    }
+}
+
+__device__ __forceinline__ void b_correct_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                                 const double* __restrict__ part, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    double m = 0.0, a[2] = {0.0, 0.0};
+    for (int t = threadIdx.x; t < in.tile_cnt; t += blockDim.x) {
+        const double* q = part + (size_t)(in.tile_beg + t) * NPART;
+        m = fmax(m, q[0]);
+        a[0] += q[1];
+        a[1] += q[2];
+    }
+    const double mm = block_max(m);
+    __shared__ double out[2];
+    block_sum<2>(a, out);
+    if (threadIdx.x == 0) {
+        S[k].max_div = mm;
+        S[k].flux_in = out[0];
+        S[k].flux_out = out[1];
+        S[k].have_nold = 1;
+    }
+}
+
+// ---------------------------------------------------------------- forces
+
+__device__ __forceinline__ int locate(const double* c, int n, double x) {
+    // last index in [1, n-2] with c[idx] <= x, minus nothing; 0 when x < c[1]; clamp to [0, n-2]
+    int lo = 1, hi = n - 1;  // search [1, n-1)
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (c[mid] <= x) lo = mid + 1;
+        else hi = mid;
+    }
+    int i0 = lo - 1;
+    if (i0 < 0) i0 = 0;
+    if (i0 > n - 2) i0 = n - 2;
+    return i0;
+}
+
+__device__ __forceinline__ double sample(const InstDev& in, const double* q, double x, double y) {
+    const int i0 = locate(in.xc, in.nx, x), j0 = locate(in.yc, in.ny, y);
+    const double xi = (x - in.xc[i0]) / (in.xc[i0 + 1] - in.xc[i0]);
+    const double et = (y - in.yc[j0]) / (in.yc[j0 + 1] - in.yc[j0]);
+    const int P = in.pitch, id = i0 + j0 * P;
+    return (1 - xi) * (1 - et) * q[id] + xi * (1 - et) * q[id + 1] + (1 - xi) * et * q[id + P] +
+           xi * et * q[id + P + 1];
+}
+
+// Drag and lift from body-surface samples: pressure by bilinear sampling of
+// the ghost-filled field, wall shear from a probe 1.5 cells along the normal.
+__device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
+    const int k = vb;
+    const InstDev& in = I[k];
+    if (!in.body) {
+        if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
+        return;
+    }
+    const double a = in.ba, b = in.bb, mu = 1.0 / in.re;
+    const double dth = 2.0 * M_PI / FORCE_SAMPLES;
+    double F[2] = {0.0, 0.0};
+    for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
+        const double t = dth * (q + 0.5);
+        const double ct = cos(t), st = sin(t);
+        const double lx = a * ct, ly = b * st;
+        double nlx = ct / a, nly = st / b;
+        const double nl = sqrt(nlx * nlx + nly * nly);
+        nlx /= nl;
+        nly /= nl;
+        const double xs = in.bcx + lx * in.bcs - ly * in.bsn;
+        const double ys = in.bcy + lx * in.bsn + ly * in.bcs;
+        const double nxw = nlx * in.bcs - nly * in.bsn, nyw = nlx * in.bsn + nly * in.bcs;
+        const double ds = sqrt(a * a * st * st + b * b * ct * ct) * dth;
+        const int i0 = locate(in.xc, in.nx, xs), j0 = locate(in.yc, in.ny, ys);
+        const double h = fmax(in.dx[i0], in.dy[j0]);
+        const double del = 1.5 * h;
+        const double ps = sample(in, in.p, xs, ys);
+        const double up = sample(in, in.u, xs + del * nxw, ys + del * nyw);
+        const double vp = sample(in, in.v, xs + del * nxw, ys + del * nyw);
+        F[0] += (-ps * nxw + mu * up / del) * ds;
+        F[1] += (-ps * nyw + mu * vp / del) * ds;
+    }
+    __shared__ double out[2];
+    block_sum<2>(F, out);
+    if (threadIdx.x == 0) {
+        S[k].cd = out[0] / in.fref;
+        S[k].cl = out[1] / in.fref;
+    }
+}
+
+}  // namespace ifx

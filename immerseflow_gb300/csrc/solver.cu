@@ -409,6 +409,51 @@ ifx_status alloc_level_fields(ifx_solver* S, HostLevel& L) {
     return IFX_OK;
 }
 
+int max_pred_pairs(const ifx_solver* S);
+int max_ppe_bodies(const ifx_solver* S);
+
+// Plan and grid of the persistent per-step kernel (co-resident blocks only).
+ifx_status setup_persistent(ifx_solver* S) {
+    if (S->lmax > kMaxLevels) return IFX_OK;
+    int coop = 0, sms = 0, bps = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, S->device));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device));
+    if (!coop) return IFX_OK;
+    if (S->prec == IFX_PREC_FP64) CUDA_TRY(persist_occupancy<double>(&bps));
+    else CUDA_TRY(persist_occupancy<float>(&bps));
+    if (bps < 1) return IFX_OK;
+    S->persist_grid = sms * std::min(bps, 4);
+    if (S->persist_grid > 64 * 32) S->persist_grid = 64 * 32;
+    IFX_TRY(dalloc(S, &S->dBar, 1));
+    PersistPlan& P = S->plan;
+    std::memset(&P, 0, sizeof(P));
+    P.I = S->dI;
+    P.S = S->dS;
+    P.LV = S->dLV;
+    P.G = S->dG;
+    P.gval = S->dGval;
+    P.part = S->dPart;
+    P.t0 = S->dT0;
+    P.nt0 = S->nt0;
+    for (int l = 1; l < S->lmax; l++) {
+        P.tsm[l] = S->dTsm[l];
+        P.ntsm[l] = S->ntsm[l];
+        P.tre[l] = S->dTre[l];
+        P.ntre[l] = S->ntre[l];
+    }
+    P.coarse = S->dCoarse;
+    P.bar = S->dBar;
+    P.ng = S->ng;
+    P.ninst = (int)S->inst.size();
+    P.lmax = S->lmax;
+    P.mg_pre = S->mg_pre;
+    P.mg_post = S->mg_post;
+    P.pred_pairs = max_pred_pairs(S);
+    P.ppe_bodies = max_ppe_bodies(S);
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
 ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const double* const* xfs,
                          const double* const* yfs) {
     S->mode = IFX_MODE_METHOD;
@@ -653,6 +698,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     CUDA_TRY(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 1, S->stream));
     S->launches += 3;
     CUDA_TRY(cudaStreamSynchronize(S->stream));
+    IFX_TRY(setup_persistent(S));
     return IFX_OK;
 }
 
@@ -899,12 +945,28 @@ ifx_status check_states(ifx_solver* S) {
     return worst;
 }
 
+// Execution mode from IFX_EXEC: "persistent" (default when cooperative
+// launch is available), "graph", or "host" (IFX_NO_GRAPH=1 also selects host).
+int exec_mode(const ifx_solver* S) {
+    const char* e = std::getenv("IFX_EXEC");
+    const char* ng = std::getenv("IFX_NO_GRAPH");
+    if (ng && ng[0] == '1') return 2;
+    if (e && std::strcmp(e, "host") == 0) return 2;
+    if (e && std::strcmp(e, "graph") == 0) return 1;
+    return S->persist_grid > 0 ? 0 : 1;
+}
+
 template <typename T>
 ifx_status step_method(ifx_solver* S, int nsteps) {
-    const char* ng = std::getenv("IFX_NO_GRAPH");
-    if (ng && ng[0] == '1') S->use_graph = false;
+    if (S->poisoned) return set_error(IFX_ERR_STATE, "a grid barrier timed out earlier; recreate the solver");
+    const int mode = exec_mode(S);
+    S->use_graph = mode == 1;
     CUDA_TRY(cudaEventRecord(S->ev0, S->stream));
-    if (S->use_graph) {
+    if (mode == 0) {
+        S->plan.nsteps = nsteps;
+        CUDA_TRY(launch_persist_step<T>(S->plan, S->persist_grid, S->stream));
+        S->launches += 1;
+    } else if (S->use_graph) {
         if (!S->gexec) IFX_TRY(build_graph<T>(S));
         for (int s = 0; s < nsteps; s++) CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
     } else {
@@ -916,6 +978,14 @@ ifx_status step_method(ifx_solver* S, int nsteps) {
     CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
     S->last_ms = ms;
     S->steps_done += nsteps;
+    if (mode == 0) {
+        unsigned int err = 0;
+        CUDA_TRY(cudaMemcpy(&err, &S->dBar->err, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err) {
+            S->poisoned = true;
+            return set_error(IFX_ERR_CUDA, "persistent step: grid barrier timed out");
+        }
+    }
     ifx_status st = check_states(S);
     if (S->use_graph) {
         // kernels executed by the graph: fixed segments plus loop bodies

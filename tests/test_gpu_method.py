@@ -6,7 +6,7 @@ Tolerances:
   - FP64 fields after several steps: 1e-10 relative to the field's max
     (FMA contraction in the step kernels, sums reduced in another order);
   - a batched instance equals the same instance run alone, bit for bit;
-  - graph execution equals the host-driven loop, bit for bit.
+  - persistent, graph and host-loop execution agree bit for bit.
 """
 import os
 
@@ -92,18 +92,39 @@ def test_rotated_ellipse_stretched_vs_oracle(oracle):
     _compare(s, o, tol=1e-9)
 
 
-def test_graph_equals_host_loop():
-    cfg, xf, yf = small_cylinder()
-    a = ifx.Solver.create(cfg, xf, yf)
-    a.step(3)
-    os.environ["IFX_NO_GRAPH"] = "1"
+def _run_mode(mode, specs, nsteps):
+    os.environ["IFX_EXEC"] = mode
     try:
-        b = ifx.Solver.create(cfg, xf, yf)
-        b.step(3)
+        if len(specs) == 1:
+            s = ifx.Solver.create(*specs[0])
+        else:
+            s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+        s.step(nsteps)
+        return s
     finally:
-        del os.environ["IFX_NO_GRAPH"]
-    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
-        assert np.array_equal(a.get(f), b.get(f))
+        del os.environ["IFX_EXEC"]
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_execution_modes_bit_identical(prec):
+    """Persistent per-step kernel, CUDA graph and host-driven loop run the same
+    device bodies: the results must agree bit for bit."""
+    specs = [small_cylinder(prec=prec)]
+    runs = {m: _run_mode(m, specs, 3) for m in ("persistent", "graph", "host")}
+    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF):
+        a = runs["persistent"].get(f)
+        assert np.array_equal(a, runs["graph"].get(f)), f
+        assert np.array_equal(a, runs["host"].get(f)), f
+    assert runs["persistent"].stats().last_ppe_iters == runs["graph"].stats().last_ppe_iters
+
+
+def test_persistent_batch_equals_graph_batch():
+    specs = [small_cylinder(nx=96, ny=64), cases.cavity(n=40), small_cylinder(nx=70, ny=90, angle=25.0, b=0.25)]
+    a = _run_mode("persistent", specs, 2)
+    b = _run_mode("graph", specs, 2)
+    for k in range(3):
+        for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+            assert np.array_equal(a.get(f, inst=k), b.get(f, inst=k)), (k, f)
 
 
 def test_batch_member_equals_alone():
