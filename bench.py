@@ -275,6 +275,10 @@ def main():
     # one phase alone: the finest-level smoothing sweep, FP32 in the mixed path
     k_ms, k_cells = s.profile_kernel(0, reps=200)
     k_bw = k_cells * (3 * 4 + 1) / (k_ms * 1e-3) / 1e9
+    try:
+        bar_us = s.profile_kernel(4, reps=5)[0] * 1e3
+    except Exception:
+        bar_us = None
 
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -295,7 +299,7 @@ def main():
                      "note": "working set ~30 MB is L2-resident; grid-barrier/latency bound at this size"},
         "phase_roofline": {"kernel": "k_smooth<float> finest level, launched alone", "bytes_per_cell": 13,
                            "cells_per_launch": k_cells, "ms_per_launch": k_ms, "achieved_gbs": k_bw,
-                           "frac": k_bw / peak},
+                           "frac": k_bw / peak, "grid_barrier_us": bar_us},
         "iterations": {"ppe_mean": sum(pits) / len(pits), "predictor_mean": sum(adits) / len(adits),
                        "ppe_mean_fp64": sum(pits64) / len(pits64)},
         "clocks": clocks,

@@ -25,12 +25,26 @@ constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
 constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
 constexpr double COARSE_OMEGA = 1.5;
+constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one block per instance
+constexpr int COARSE_SMEM_CELLS = 1024;  // coarsest level (with ghost ring) staged in shared memory
 
 enum CellType : uint8_t { T_SOLID = 0, T_FLUID = 1, T_GHOST = 2, T_DOMAIN = 3 };
 // per-cell stencil bits: open faces, and (finest level) faces to an IBM ghost
 enum : uint8_t { B_E = 1, B_W = 2, B_N = 4, B_S = 8, G_E = 16, G_W = 32, G_N = 64, G_S = 128 };
 // per-instance iteration state
 enum : int { ST_ACTIVE = 0, ST_FINAL_IN_ALT = 1, ST_DONE = 2 };
+
+#if defined(__CUDACC__)
+#define IFX_HD __host__ __device__
+#else
+#define IFX_HD
+#endif
+
+// Buffer (0: e, 1: e2) that holds a level's multigrid correction after its
+// pre- and after its post-smoothing (the finest level starts from a
+// zero-start sweep into e2; coarser levels from the fused restriction into e).
+IFX_HD inline int parity_after_pre(int depth, int pre) { return depth == 0 ? (pre & 1) : ((pre - 1) & 1); }
+IFX_HD inline int parity_after_post(int depth, int pre, int post) { return (parity_after_pre(depth, pre) + post) & 1; }
 
 struct Tile {
     int inst;  // instance index
@@ -70,6 +84,15 @@ struct LevelDev {
     const signed char *psx, *psy;
     int child;   // LevelDev index of the next coarser level, -1 at the coarsest
     int parent;  // LevelDev index of the next finer level, -1 at the finest
+    int tbeg, tcnt;  // this level's tiles in the all-levels tile table
+};
+
+// One body-surface sample for drag/lift (stationary body: built once).
+// Pressure is sampled bilinearly at the surface point (base cell c0,
+// weights xi0/et0), velocity at a probe del along the normal (c1, xi1/et1).
+struct ForceSample {
+    int c0, c1;
+    double xi0, et0, xi1, et1, nx, ny, ds, del;
 };
 
 struct InstDev {
@@ -94,6 +117,7 @@ struct InstDev {
     float *du, *dv, *du2, *dv2, *rfu, *rfv;
     // body (ellipse), bit-exact predicate constants
     double bcx, bcy, ba, bb, bcs, bsn, bia2, bib2, fref;
+    const ForceSample* fs;       // FORCE_SAMPLES entries when body != 0
 };
 
 // Device-resident per-instance iteration state and diagnostics.

@@ -79,7 +79,8 @@ struct ifx_solver {
     std::vector<int> ntsm;
     std::vector<ifx::Tile*> dTre;    // per level >= 1: tiles of instances that have the level
     std::vector<int> ntre;
-    int* dCoarse = nullptr;          // LevelDev index of each instance's coarsest level
+    ifx::Tile* dTall = nullptr;      // tiles of every level of every instance
+    int* dSub = nullptr;             // LevelDev index of each instance's first small level
     int lmax = 0;
     int mg_pre = 2, mg_post = 2;
     double* dPart = nullptr;         // NPART partials per finest-level tile

@@ -30,7 +30,8 @@ struct PersistPlan {
     const Tile* t0;
     const Tile* tsm[kMaxLevels];
     const Tile* tre[kMaxLevels];
-    const int* coarse;
+    const Tile* tall;   // tiles of every level, per-level ranges in LevelDev
+    const int* sub;     // per instance: LevelDev index of its first small level
     GridBar* bar;
     int nt0, ng, ninst, lmax, mg_pre, mg_post;
     int ntsm[kMaxLevels];
@@ -42,5 +43,6 @@ template <typename T>
 cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s);
 template <typename T>
 cudaError_t persist_occupancy(int* blocks_per_sm);
+cudaError_t launch_barrier_bench(GridBar* bar, int grid, int reps, cudaStream_t s);
 
 }  // namespace ifx

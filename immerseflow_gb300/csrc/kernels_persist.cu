@@ -93,44 +93,46 @@ __device__ bool ghost_fill(const PersistPlan& P, int comps) {
     return true;
 }
 
-// One V-cycle; *res receives the buffer (0: e, 1: e2) of the finest-level result.
+// One V-cycle; *res receives the buffer (0: e, 1: e2) of the finest-level
+// result.  Levels with at most SUB_MAX_CELLS cells run inside b_subcycle.
 template <typename T>
 __device__ bool vcycle(const PersistPlan& P, int* res) {
-    int cur[kMaxLevels];
     FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 1, 0, vb);
     BAR();
-    cur[0] = 1;
+    int cur0 = 1;
     for (int k = 1; k < P.mg_pre; k++) {
-        FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 0, cur[0], vb);
+        FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 0, cur0, vb);
         BAR();
-        cur[0] ^= 1;
+        cur0 ^= 1;
     }
     for (int l = 1; l < P.lmax; l++) {
-        FOR_VB(P.ntre[l]) b_restrict<T>(P.tre[l], P.LV, P.I, P.S, P.G, cur[l - 1], vb);
+        if (P.ntre[l] == 0) break;
+        FOR_VB(P.ntre[l]) b_restrict<T>(P.tre[l], P.LV, P.I, P.S, P.G, parity_after_pre(l - 1, P.mg_pre), vb);
         BAR();
-        cur[l] = 0;
-        if (P.ntsm[l] > 0)
-            for (int k = 1; k < P.mg_pre; k++) {
-                FOR_VB(P.ntsm[l]) b_smooth<T>(P.tsm[l], P.LV, P.I, P.S, P.G, 0, cur[l], vb);
-                BAR();
-                cur[l] ^= 1;
-            }
+        int cur = 0;
+        for (int k = 1; k < P.mg_pre; k++) {
+            FOR_VB(P.ntsm[l]) b_smooth<T>(P.tsm[l], P.LV, P.I, P.S, P.G, 0, cur, vb);
+            BAR();
+            cur ^= 1;
+        }
     }
-    FOR_VB(P.ninst) b_coarse_solve<T>(P.coarse, P.LV, P.I, P.S, vb);
+    FOR_VB(P.ninst) b_subcycle<T>(P.tall, P.sub, P.LV, P.I, P.S, P.G, P.mg_pre, P.mg_post, vb);
     BAR();
     for (int l = P.lmax - 2; l >= 0; l--) {
         const Tile* tl = l == 0 ? P.t0 : P.tsm[l];
         const int nt = l == 0 ? P.nt0 : P.ntsm[l];
         if (nt == 0) continue;
-        FOR_VB(nt) b_prolong<T>(tl, P.LV, P.S, cur[l], cur[l + 1], vb);
+        int cur = parity_after_pre(l, P.mg_pre);
+        FOR_VB(nt) b_prolong<T>(tl, P.LV, P.S, cur, parity_after_post(l + 1, P.mg_pre, P.mg_post), vb);
         BAR();
         for (int k = 0; k < P.mg_post; k++) {
-            FOR_VB(nt) b_smooth<T>(tl, P.LV, P.I, P.S, P.G, 0, cur[l], vb);
+            FOR_VB(nt) b_smooth<T>(tl, P.LV, P.I, P.S, P.G, 0, cur, vb);
             BAR();
-            cur[l] ^= 1;
+            cur ^= 1;
         }
+        if (l == 0) cur0 = cur;
     }
-    *res = cur[0];
+    *res = cur0;
     return true;
 }
 
@@ -207,7 +209,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_persist_step(PersistPlan P) {
         if (!one_step<T>(P)) return;
 }
 
+// Measurement: `reps` grid barriers back to back (no work between them).
+__global__ void __launch_bounds__(TILE_THREADS) k_barrier_bench(GridBar* bar, int reps) {
+    for (int r = 0; r < reps; r++)
+        if (!grid_barrier(bar)) return;
+}
+
 }  // namespace
+
+cudaError_t launch_barrier_bench(GridBar* bar, int grid, int reps, cudaStream_t s) {
+    void* args[] = {(void*)&bar, (void*)&reps};
+    return cudaLaunchCooperativeKernel((const void*)k_barrier_bench, dim3(grid), dim3(TILE_THREADS), args, 0, s);
+}
 
 template <typename T>
 cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) {

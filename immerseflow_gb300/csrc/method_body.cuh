@@ -739,19 +739,68 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
     fe[id] += val;
 }
 
-// Coarsest level: e = 0, then red-black SOR sweeps, one block per instance.
+// Coarsest level: e = 0, then red-black SOR sweeps.  Levels that fit are
+// staged in shared memory (same arithmetic, in the same order, as the
+// global-memory form below).
 template <typename T>
-__device__ __forceinline__ void b_coarse_solve(const int* __restrict__ levs, const LevelDev* __restrict__ LV,
-                               const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
-    const LevelDev& L = LV[levs[vb]];
-    if (S[L.inst].ppe_state != ST_ACTIVE) return;
+__device__ void coarse_solve_level(const LevelDev& L) {
     T* e = (T*)L.e;
     const T* r = (const T*)L.r;
+    const T om = (T)COARSE_OMEGA;
+    const int NXY = L.NX * L.NY;
+    const int nx = L.nx, ncell = L.nx * L.ny;
+    if (ncell <= COARSE_SMEM_CELLS && L.nx <= 256 && L.ny <= 256) {
+        __shared__ T se[COARSE_SMEM_CELLS], sr[COARSE_SMEM_CELLS];
+        __shared__ uint8_t sb[COARSE_SMEM_CELLS];
+        __shared__ T skx[256], sky[256], six[256], siy[256];
+        const T* kx = LvA<T>::kx(L);
+        const T* ky = LvA<T>::ky(L);
+        const T* ix = LvA<T>::ix(L);
+        const T* iy = LvA<T>::iy(L);
+        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+            const int i = q % nx, j = q / nx, id = i + j * L.pitch;
+            se[q] = (T)0;
+            sr[q] = r[id];
+            sb[q] = L.bits[id];
+        }
+        for (int q = threadIdx.x; q < L.nx; q += blockDim.x) { skx[q] = kx[q]; six[q] = ix[q]; }
+        for (int q = threadIdx.x; q < L.ny; q += blockDim.x) { sky[q] = ky[q]; siy[q] = iy[q]; }
+        __syncthreads();
+        for (int it = 0; it < COARSE_SWEEPS; it++) {
+            for (int col = 0; col < 2; col++) {
+                for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
+                    const int i = 1 + q % L.NX, j = 1 + q / L.NX;
+                    if (((i + j) & 1) != col) continue;
+                    const int id = i + j * nx;
+                    const uint8_t bt = sb[id];
+                    if (!(bt & 0x0F)) continue;
+                    const T cE = skx[i] * six[i], cW = skx[i - 1] * six[i];
+                    const T cN = sky[j] * siy[j], cS = sky[j - 1] * siy[j];
+                    const T ce = (bt & B_E) ? cE : (T)0, cw = (bt & B_W) ? cW : (T)0;
+                    const T cn = (bt & B_N) ? cN : (T)0, cs = (bt & B_S) ? cS : (T)0;
+                    T dd = ce + cw + cn + cs;
+                    if (L.dirmask) {
+                        if (i == L.NX && (L.dirmask & (1 << 1))) dd += (T)2 * cE;
+                        if (i == 1 && (L.dirmask & (1 << 0))) dd += (T)2 * cW;
+                        if (j == L.NY && (L.dirmask & (1 << 3))) dd += (T)2 * cN;
+                        if (j == 1 && (L.dirmask & (1 << 2))) dd += (T)2 * cS;
+                    }
+                    const T Le = ce * se[id + 1] + cw * se[id - 1] + cn * se[id + nx] + cs * se[id - nx] - dd * se[id];
+                    se[id] = se[id] + om * (Le - sr[id]) * rcpa(dd);
+                }
+                __syncthreads();
+            }
+        }
+        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+            const int i = q % nx, j = q / nx;
+            e[i + j * L.pitch] = se[q];
+        }
+        __syncthreads();
+        return;
+    }
     const int n = L.pitch * L.ny;
     for (int id = threadIdx.x; id < n; id += blockDim.x) e[id] = (T)0;
     __syncthreads();
-    const T om = (T)COARSE_OMEGA;
-    const int NXY = L.NX * L.NY;
     for (int it = 0; it < COARSE_SWEEPS; it++) {
         for (int col = 0; col < 2; col++) {
             for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
@@ -765,6 +814,52 @@ __device__ __forceinline__ void b_coarse_solve(const int* __restrict__ levs, con
                 e[id] = e[id] + om * (Le - r[id]) * rcpa(D);
             }
             __syncthreads();
+        }
+    }
+}
+
+// Small coarse levels of one instance (vb = instance) in one block: the
+// restriction into the first small level, its smoothing, every coarser level
+// down to the RB-SOR solve and back up.  Same per-cell bodies and order as
+// the tile phases; tiles of a level are processed one after another.
+template <typename T>
+__device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const int* __restrict__ sub,
+                                           const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
+                                           const InstState* __restrict__ S, const GhostDev* __restrict__ G,
+                                           int pre, int post, int vb) {
+    const int k = vb;
+    if (S[k].ppe_state != ST_ACTIVE) return;
+    const InstDev& in = I[k];
+    const int lb = sub[k];
+    const int top = in.lev0 + in.nlev - 1;
+    // descend: restriction into each small level, then its pre-smoothing
+    for (int lv = lb; lv <= top; lv++) {
+        const LevelDev& C = LV[lv];
+        const int fa = parity_after_pre(C.depth - 1, pre);
+        for (int t = C.tbeg; t < C.tbeg + C.tcnt; t++) b_restrict<T>(tall, LV, I, S, G, fa, t);
+        __syncthreads();
+        if (lv == top) {
+            coarse_solve_level<T>(C);
+            break;
+        }
+        int cur = 0;
+        for (int q = 1; q < pre; q++) {
+            for (int t = C.tbeg; t < C.tbeg + C.tcnt; t++) b_smooth<T>(tall, LV, I, S, G, 0, cur, t);
+            __syncthreads();
+            cur ^= 1;
+        }
+    }
+    // ascend: prolongation into each small middle level, then its post-smoothing
+    for (int lv = top - 1; lv >= lb; lv--) {
+        const LevelDev& F = LV[lv];
+        int cur = parity_after_pre(F.depth, pre);
+        for (int t = F.tbeg; t < F.tbeg + F.tcnt; t++)
+            b_prolong<T>(tall, LV, S, cur, parity_after_post(F.depth + 1, pre, post), t);
+        __syncthreads();
+        for (int q = 0; q < post; q++) {
+            for (int t = F.tbeg; t < F.tbeg + F.tcnt; t++) b_smooth<T>(tall, LV, I, S, G, 0, cur, t);
+            __syncthreads();
+            cur ^= 1;
         }
     }
 }
@@ -897,7 +992,12 @@ __device__ __forceinline__ double sample(const InstDev& in, const double* q, dou
 }
 
 // Drag and lift from body-surface samples: pressure by bilinear sampling of
-// the ghost-filled field, wall shear from a probe 1.5 cells along the normal.
+// the ghost-filled field, wall shear from a probe 1.5 cells along the normal
+// (sample geometry precomputed once; the body does not move).
+__device__ __forceinline__ double bil(const double* q, int c, int P, double xi, double et) {
+    return (1 - xi) * (1 - et) * q[c] + xi * (1 - et) * q[c + 1] + (1 - xi) * et * q[c + P] + xi * et * q[c + P + 1];
+}
+
 __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
@@ -905,29 +1005,16 @@ __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstStat
         if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
         return;
     }
-    const double a = in.ba, b = in.bb, mu = 1.0 / in.re;
-    const double dth = 2.0 * M_PI / FORCE_SAMPLES;
+    const double mu = 1.0 / in.re;
+    const int P = in.pitch;
     double F[2] = {0.0, 0.0};
     for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
-        const double t = dth * (q + 0.5);
-        const double ct = cos(t), st = sin(t);
-        const double lx = a * ct, ly = b * st;
-        double nlx = ct / a, nly = st / b;
-        const double nl = sqrt(nlx * nlx + nly * nly);
-        nlx /= nl;
-        nly /= nl;
-        const double xs = in.bcx + lx * in.bcs - ly * in.bsn;
-        const double ys = in.bcy + lx * in.bsn + ly * in.bcs;
-        const double nxw = nlx * in.bcs - nly * in.bsn, nyw = nlx * in.bsn + nly * in.bcs;
-        const double ds = sqrt(a * a * st * st + b * b * ct * ct) * dth;
-        const int i0 = locate(in.xc, in.nx, xs), j0 = locate(in.yc, in.ny, ys);
-        const double h = fmax(in.dx[i0], in.dy[j0]);
-        const double del = 1.5 * h;
-        const double ps = sample(in, in.p, xs, ys);
-        const double up = sample(in, in.u, xs + del * nxw, ys + del * nyw);
-        const double vp = sample(in, in.v, xs + del * nxw, ys + del * nyw);
-        F[0] += (-ps * nxw + mu * up / del) * ds;
-        F[1] += (-ps * nyw + mu * vp / del) * ds;
+        const ForceSample f = in.fs[q];
+        const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
+        const double up = bil(in.u, f.c1, P, f.xi1, f.et1);
+        const double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
+        F[0] += (-ps * f.nx + mu * up / f.del) * f.ds;
+        F[1] += (-ps * f.ny + mu * vp / f.del) * f.ds;
     }
     __shared__ double out[2];
     block_sum<2>(F, out);

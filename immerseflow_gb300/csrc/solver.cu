@@ -359,6 +359,53 @@ void build_ghosts(Instance& I, int inst, std::vector<GhostDev>& out, std::vector
     I.ghost_cnt = (int)out.size() - I.ghost_beg;
 }
 
+// Body-surface samples for drag/lift: parametric points on the ellipse,
+// outward normal, arc-length weight, and bilinear bases/weights of the
+// pressure sample and of the velocity probe (same formulas as the oracle).
+std::vector<ForceSample> build_force_table(const Instance& I) {
+    std::vector<ForceSample> out;
+    if (I.cfg.body != IFX_BODY_ELLIPSE) return out;
+    const int nx = I.nx, ny = I.ny, P = I.pitch;
+    auto locate = [](const std::vector<double>& cc, int n, double x) {
+        int i0 = (int)(std::upper_bound(cc.begin() + 1, cc.begin() + n - 1, x) - cc.begin()) - 1;
+        return std::min(std::max(i0, 0), n - 2);
+    };
+    const double a = I.cfg.body_a, b = I.cfg.body_b;
+    const double dth = 2.0 * M_PI / FORCE_SAMPLES;
+    out.resize(FORCE_SAMPLES);
+    for (int k = 0; k < FORCE_SAMPLES; k++) {
+        double t = dth * (k + 0.5);
+        double ct = std::cos(t), st = std::sin(t);
+        double lx = a * ct, ly = b * st;
+        double nlx = ct / a, nly = st / b;
+        double nl = std::sqrt(nlx * nlx + nly * nly);
+        nlx /= nl;
+        nly /= nl;
+        double xs = I.cfg.body_cx + lx * I.cs - ly * I.sn;
+        double ys = I.cfg.body_cy + lx * I.sn + ly * I.cs;
+        double nxw = nlx * I.cs - nly * I.sn, nyw = nlx * I.sn + nly * I.cs;
+        double ds = std::sqrt(a * a * st * st + b * b * ct * ct) * dth;
+        int i0 = locate(I.xc, nx, xs), j0 = locate(I.yc, ny, ys);
+        double h = std::max(I.dx[i0], I.dy[j0]);
+        double del = 1.5 * h;
+        ForceSample f;
+        f.c0 = i0 + j0 * P;
+        f.xi0 = (xs - I.xc[i0]) / (I.xc[i0 + 1] - I.xc[i0]);
+        f.et0 = (ys - I.yc[j0]) / (I.yc[j0 + 1] - I.yc[j0]);
+        double xq = xs + del * nxw, yq = ys + del * nyw;
+        int i1 = locate(I.xc, nx, xq), j1 = locate(I.yc, ny, yq);
+        f.c1 = i1 + j1 * P;
+        f.xi1 = (xq - I.xc[i1]) / (I.xc[i1 + 1] - I.xc[i1]);
+        f.et1 = (yq - I.yc[j1]) / (I.yc[j1 + 1] - I.yc[j1]);
+        f.nx = nxw;
+        f.ny = nyw;
+        f.ds = ds;
+        f.del = del;
+        out[k] = f;
+    }
+    return out;
+}
+
 // Host initial condition (same formulas as initializeKernel for the vortex,
 // src/include/preSim.cu:70-73).
 void initial_field(const Instance& I, std::vector<double>& u, std::vector<double>& v) {
@@ -441,7 +488,8 @@ ifx_status setup_persistent(ifx_solver* S) {
         P.tre[l] = S->dTre[l];
         P.ntre[l] = S->ntre[l];
     }
-    P.coarse = S->dCoarse;
+    P.tall = S->dTall;
+    P.sub = S->dSub;
     P.bar = S->dBar;
     P.ng = S->ng;
     P.ninst = (int)S->inst.size();
@@ -555,7 +603,6 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     std::vector<int> hIbm;
     std::vector<LevelDev> hLV;
     std::vector<Tile> hT0;
-    std::vector<int> hCoarse;
     int lmax = 0;
     for (int k = 0; k < n; k++) {
         Instance& I = S->inst[k];
@@ -579,6 +626,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     IFX_TRY(dalloc(S, &S->dGval, 3 * (size_t)std::max(1, S->ng)));
     IFX_TRY(dalloc(S, &S->dBiIp, 4 * (size_t)std::max(1, S->nibm)));
     std::vector<std::vector<Tile>> tsm(lmax), tre(lmax);
+    std::vector<Tile> hTall;
+    std::vector<int> hSub;
     for (int k = 0; k < n; k++) {
         Instance& I = S->inst[k];
         InstDev& d = I.dev;
@@ -590,6 +639,10 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dupload(S, &gidx_d, gidx));
         d.gidx = gidx_d;
         const int nl = (int)I.lev.size();
+        // first level handled inside one block per instance (>= 1, <= coarsest)
+        int lb = nl - 1;
+        for (int l = 1; l < nl; l++)
+            if ((long long)I.lev[l].NX * I.lev[l].NY <= SUB_MAX_CELLS) { lb = l; break; }
         for (int l = 0; l < nl; l++) {
             HostLevel& L = I.lev[l];
             IFX_TRY(dupload(S, &L.d_kx, L.kx)); IFX_TRY(dupload(S, &L.d_ky, L.ky));
@@ -623,22 +676,25 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ld.psx = L.d_psx; ld.psy = L.d_psy;
             ld.child = (l + 1 < nl) ? I.lev_base + l + 1 : -1;
             ld.parent = (l > 0) ? I.lev_base + l - 1 : -1;
-            hLV.push_back(ld);
             // tiles
             const int lv = I.lev_base + l;
             std::vector<Tile> tl;
             for (int j0 = 0; j0 < L.ny; j0 += TILE_Y)
                 for (int i0 = 0; i0 < L.nx; i0 += TILE_X) tl.push_back(Tile{k, lv, i0, j0});
+            ld.tbeg = (int)hTall.size();
+            ld.tcnt = (int)tl.size();
+            hTall.insert(hTall.end(), tl.begin(), tl.end());
+            hLV.push_back(ld);
             if (l == 0) {
                 I.tile_beg = (int)hT0.size();
                 I.tile_cnt = (int)tl.size();
                 hT0.insert(hT0.end(), tl.begin(), tl.end());
-            } else {
+            } else if (l < lb) {
                 tre[l].insert(tre[l].end(), tl.begin(), tl.end());
-                if (l < nl - 1) tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
+                tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
             }
         }
-        hCoarse.push_back(I.lev_base + nl - 1);
+        hSub.push_back(I.lev_base + lb);
         d.lev0 = I.lev_base;
         d.nlev = nl;
         d.tile_beg = I.tile_beg;
@@ -648,6 +704,12 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         d.n_fluid = I.n_fluid;
         d.area = I.area;
         d.ad_lim = I.cfg.ad_tol * std::max(1, I.n_fluid);
+        {
+            std::vector<ForceSample> fs = build_force_table(I);
+            ForceSample* fs_d = nullptr;
+            if (!fs.empty()) IFX_TRY(dupload(S, &fs_d, fs));
+            d.fs = fs_d;
+        }
         d.kx = I.lev[0].d_kx; d.ky = I.lev[0].d_ky; d.ix = I.lev[0].d_ix; d.iy = I.lev[0].d_iy;
         hI[k] = d;
     }
@@ -664,7 +726,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         S->ntsm[l] = (int)tsm[l].size();
         S->ntre[l] = (int)tre[l].size();
     }
-    IFX_TRY(dupload(S, &S->dCoarse, hCoarse));
+    IFX_TRY(dupload(S, &S->dTall, hTall));
+    IFX_TRY(dupload(S, &S->dSub, hSub));
     IFX_TRY(dalloc(S, &S->dPart, (size_t)S->nt0 * NPART));
     IFX_TRY(dalloc(S, &S->dS, n));
     IFX_TRY(dalloc(S, &S->dCtl, 1));
@@ -720,36 +783,39 @@ template <typename T>
 int seq_vcycle(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
-    const int L = S->lmax;
-    std::vector<int> cur(L, 0);
+    const int L = S->lmax, pre = S->mg_pre, post = S->mg_post;
     // finest level: first sweep from zero, then the rest of the pre-smoothing
     q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, st));
-    cur[0] = 1;
-    for (int k = 1; k < S->mg_pre; k++) {
-        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur[0], st));
-        cur[0] ^= 1;
+    int cur0 = 1;
+    for (int k = 1; k < pre; k++) {
+        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur0, st));
+        cur0 ^= 1;
     }
+    // large coarse levels: one launch per phase
     for (int l = 1; l < L; l++) {
-        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, cur[l - 1], st));
-        cur[l] = 0;
-        if (S->ntsm[l] > 0)
-            for (int k = 1; k < S->mg_pre; k++) {
-                q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, 0, cur[l], st));
-                cur[l] ^= 1;
-            }
+        if (S->ntre[l] == 0) break;
+        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, parity_after_pre(l - 1, pre), st));
+        int cur = 0;
+        for (int k = 1; k < pre; k++) {
+            q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, 0, cur, st));
+            cur ^= 1;
+        }
     }
-    q.add(launch_coarse_solve<T>(S->dCoarse, (int)S->inst.size(), S->dLV, S->dI, S->dS, st));
+    // small levels of every instance: one block each
+    q.add(launch_subcycle<T>(S->dTall, S->dSub, (int)S->inst.size(), S->dLV, S->dI, S->dS, S->dG, pre, post, st));
     for (int l = L - 2; l >= 0; l--) {
         const Tile* tl = l == 0 ? S->dT0 : S->dTsm[l];
         const int nt = l == 0 ? S->nt0 : S->ntsm[l];
         if (nt == 0) continue;
-        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur[l], cur[l + 1], st));
-        for (int k = 0; k < S->mg_post; k++) {
-            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur[l], st));
-            cur[l] ^= 1;
+        int cur = parity_after_pre(l, pre);
+        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), st));
+        for (int k = 0; k < post; k++) {
+            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur, st));
+            cur ^= 1;
         }
+        if (l == 0) cur0 = cur;
     }
-    return cur[0];
+    return cur0;
 }
 
 void seq_pre(Seq& q) {
@@ -1446,6 +1512,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
             case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, st);
             case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, st);
             case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
+            case 4: return launch_barrier_bench(S->dBar, S->persist_grid, 1000, st);
             default: return launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st);
         }
     };
@@ -1456,14 +1523,15 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
     CUDA_TRY(cudaEventSynchronize(S->ev1));
     float t = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&t, S->ev0, S->ev1));
-    *ms = t / reps;
+    *ms = kernel == 4 ? t / reps / 1000.0 : t / reps;
     S->launches += reps + 2;
     return IFX_OK;
 }
 
 extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, double* ms_per_launch,
                                          long long* cells) {
-    if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 3) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
+    if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 4) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
+    if (kernel == 4 && S->persist_grid == 0) return set_error(IFX_ERR_STATE, "cooperative launch unavailable");
     if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_profile_kernel needs a METHOD-mode solver");
     CUDA_TRY(cudaSetDevice(S->device));
     long long c = 0;
