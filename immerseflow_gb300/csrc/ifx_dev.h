@@ -46,7 +46,7 @@ enum : int { ST_ACTIVE = 0, ST_FINAL_IN_ALT = 1, ST_DONE = 2 };
 IFX_HD inline int parity_after_pre(int depth, int pre) { return depth == 0 ? (pre & 1) : ((pre - 1) & 1); }
 IFX_HD inline int parity_after_post(int depth, int pre, int post) { return (parity_after_pre(depth, pre) + post) & 1; }
 
-struct Tile {
+struct alignas(16) Tile {
     int inst;  // instance index
     int lev;   // index into the LevelDev array
     int i0, j0;
@@ -55,7 +55,7 @@ struct Tile {
 // One boundary relation q[cell] = c + sum_k w[k] * q[nb[k]].  Domain ghosts
 // (one neighbour) carry the wall/inflow/slip/outflow rule; IBM ghosts carry
 // image-point weights (Dirichlet for u,v; Neumann for p).
-struct GhostDev {
+struct alignas(16) GhostDev {
     int cell, inst, side, adj;  // side: -1 IBM ghost, 0..3 domain side, 4 corner
     int nb[4];
     double wu[4], wv[4], wp[4];
@@ -66,7 +66,7 @@ struct GhostDev {
     double qh;                   // normal spacing for the convective outflow update
 };
 
-struct LevelDev {
+struct alignas(16) LevelDev {
     int NX, NY, nx, ny, pitch;
     int inst, depth, dirmask;    // dirmask bit s: side s Dirichlet for pressure
     const double *kx, *ky, *ix, *iy, *dw, *dh;
@@ -90,12 +90,12 @@ struct LevelDev {
 // One body-surface sample for drag/lift (stationary body: built once).
 // Pressure is sampled bilinearly at the surface point (base cell c0,
 // weights xi0/et0), velocity at a probe del along the normal (c1, xi1/et1).
-struct ForceSample {
+struct alignas(16) ForceSample {
     int c0, c1;
     double xi0, et0, xi1, et1, nx, ny, ds, del;
 };
 
-struct InstDev {
+struct alignas(16) InstDev {
     int NX, NY, nx, ny, pitch;
     int singular, dirmask, body, lev0, nlev;
     int tile_beg, tile_cnt;      // level-0 tiles (for per-instance partial sums)

@@ -11,13 +11,10 @@ constexpr int kMaxLevels = 16;
 // Grid barrier state (zeroed once at allocation; counters return to zero
 // after every barrier, the generation only grows).
 struct GridBar {
-    unsigned int gen;
-    unsigned int pad0[31];
-    unsigned int top;
-    unsigned int pad1[31];
-    unsigned int sub[64 * 32];  // one counter per group of 32 blocks, 128 B apart
+    unsigned long long count;   // arrivals since the launch (reset before each launch)
+    unsigned long long pad0[15];
     unsigned int err;
-    unsigned int pad2[31];
+    unsigned int pad1[31];
 };
 
 struct PersistPlan {

@@ -23,42 +23,32 @@ namespace ifx {
 
 namespace {
 
-constexpr long long kSpinLimit = 1ll << 22;  // x ~64 ns sleep: ~0.3 s per barrier at most
+constexpr long long kSpinLimit = 1ll << 23;  // x ~50-100 ns per poll: well under a second per barrier
 
 __device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(const volatile unsigned int*)p; }
 
-// Two-level barrier: blocks arrive on one of up to 64 group counters (32
-// blocks each, one 128-B line per counter); the last of a group arrives on
-// the top counter; the last group flips the generation.
-__device__ __forceinline__ bool grid_barrier(GridBar* b) {
+// Flat barrier on a monotonically increasing 64-bit arrival counter: the
+// k-th barrier of the launch is passed once the counter reaches
+// gridDim.x * k.  Arrival is a release add, the wait an acquire poll, so the
+// critical path is one atomic and one poll; the counter never needs a reset
+// inside the launch (the host zeroes it before each launch).
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epoch) {
     __syncthreads();
+    epoch += 1;
     if (threadIdx.x == 0) {
-        const unsigned int nb = gridDim.x;
-        const unsigned int gen = vload(&b->gen);
-        __threadfence();
-        const unsigned int grp = blockIdx.x >> 5;
-        const unsigned int ngrp = (nb + 31) >> 5;
-        const unsigned int gsize = min(32u, nb - grp * 32u);
-        const unsigned int a = atomicAdd(&b->sub[grp * 32], 1u);
-        if (a == gsize - 1) {
-            b->sub[grp * 32] = 0u;
-            __threadfence();
-            const unsigned int t = atomicAdd(&b->top, 1u);
-            if (t == ngrp - 1) {
-                b->top = 0u;
-                __threadfence();
-                atomicAdd(&b->gen, 1u);
-            }
-        }
+        const unsigned long long target = epoch * (unsigned long long)gridDim.x;
+        unsigned long long v;
+        asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(v) : "l"(&b->count) : "memory");
         long long spins = 0;
-        while (vload(&b->gen) == gen) {
+        while (true) {
+            asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(&b->count) : "memory");
+            if (v >= target) break;
             if (++spins > kSpinLimit) {
                 atomicExch(&b->err, 1u);
                 break;
             }
-            __nanosleep(64);
+            __nanosleep(32);
         }
-        __threadfence();
     }
     __syncthreads();
     return vload(&b->err) == 0u;
@@ -77,15 +67,15 @@ __device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
     return __syncthreads_or(a) != 0;
 }
 
-#define BAR()                                   \
-    do {                                        \
-        if (!grid_barrier(P.bar)) return false; \
+#define BAR()                                          \
+    do {                                               \
+        if (!grid_barrier(P.bar, ep)) return false;    \
     } while (0)
 #define FOR_VB(n) for (int vb = blockIdx.x; vb < (n); vb += gridDim.x)
 
 __device__ __forceinline__ int nchunks(int n) { return (n + TILE_THREADS - 1) / TILE_THREADS; }
 
-__device__ bool ghost_fill(const PersistPlan& P, int comps) {
+__device__ bool ghost_fill(const PersistPlan& P, int comps, unsigned long long& ep) {
     FOR_VB(nchunks(P.ng)) b_ghost_gather(P.G, P.ng, P.I, comps, P.gval, vb);
     BAR();
     FOR_VB(nchunks(P.ng)) b_ghost_scatter(P.G, P.ng, P.I, comps, P.gval, vb);
@@ -96,7 +86,7 @@ __device__ bool ghost_fill(const PersistPlan& P, int comps) {
 // One V-cycle; *res receives the buffer (0: e, 1: e2) of the finest-level
 // result.  Levels with at most SUB_MAX_CELLS cells run inside b_subcycle.
 template <typename T>
-__device__ bool vcycle(const PersistPlan& P, int* res) {
+__device__ bool vcycle(const PersistPlan& P, int* res, unsigned long long& ep) {
     FOR_VB(P.nt0) b_smooth<T>(P.t0, P.LV, P.I, P.S, P.G, 1, 0, vb);
     BAR();
     int cur0 = 1;
@@ -137,12 +127,12 @@ __device__ bool vcycle(const PersistPlan& P, int* res) {
 }
 
 template <typename T>
-__device__ bool one_step(const PersistPlan& P) {
+__device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     const int n = P.ninst;
     FOR_VB(nchunks(n)) b_step_begin(P.S, n, vb);
     FOR_VB(nchunks(P.ng)) b_outflow(P.G, P.ng, P.I, vb);
     BAR();
-    if (!ghost_fill(P, 3)) return false;
+    if (!ghost_fill(P, 3, ep)) return false;
     FOR_VB(P.nt0) b_conv_rhs(P.t0, P.I, P.S, vb);
     BAR();
     // predictor: pairs of Jacobi sweeps until every instance converged
@@ -158,7 +148,7 @@ __device__ bool one_step(const PersistPlan& P) {
         BAR();
         if (!any_pred_active(P.S, n)) break;
     }
-    if (!ghost_fill(P, 3)) return false;
+    if (!ghost_fill(P, 3, ep)) return false;
     FOR_VB(P.nt0) b_face_rhs(P.t0, P.I, P.part, 0, vb);
     BAR();
     FOR_VB(n) b_rhs_reduce(P.I, P.S, P.part, vb);
@@ -173,14 +163,14 @@ __device__ bool one_step(const PersistPlan& P) {
         FOR_VB(P.nt0) b_bicg_p<T>(P.t0, P.LV, P.I, P.S, vb);
         BAR();
         int e1 = 0, e2 = 0;
-        if (!vcycle<T>(P, &e1)) return false;
+        if (!vcycle<T>(P, &e1, ep)) return false;
         FOR_VB(P.nt0) b_bicg_apply<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, e1, 0, vb);
         BAR();
         FOR_VB(n) b_bicg_scalar(P.I, P.S, P.part, 0, vb);
         BAR();
         FOR_VB(P.nt0) b_bicg_s<T>(P.t0, P.LV, P.I, P.S, vb);
         BAR();
-        if (!vcycle<T>(P, &e2)) return false;
+        if (!vcycle<T>(P, &e2, ep)) return false;
         FOR_VB(P.nt0) b_bicg_apply<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, e2, 1, vb);
         BAR();
         FOR_VB(n) b_bicg_scalar(P.I, P.S, P.part, 1, vb);
@@ -192,12 +182,12 @@ __device__ bool one_step(const PersistPlan& P) {
     }
     FOR_VB(P.nt0) b_p_finalize(P.t0, P.I, P.S, vb);
     BAR();
-    if (!ghost_fill(P, 4)) return false;
+    if (!ghost_fill(P, 4, ep)) return false;
     FOR_VB(P.nt0) b_correct(P.t0, P.I, P.part, vb);
     BAR();
     FOR_VB(n) b_correct_reduce(P.I, P.S, P.part, vb);
     BAR();
-    if (!ghost_fill(P, 3)) return false;
+    if (!ghost_fill(P, 3, ep)) return false;
     FOR_VB(n) b_forces(P.I, P.S, vb);
     BAR();
     return true;
@@ -205,25 +195,31 @@ __device__ bool one_step(const PersistPlan& P) {
 
 template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS) k_persist_step(PersistPlan P) {
+    unsigned long long ep = 0;
     for (int s = 0; s < P.nsteps; s++)
-        if (!one_step<T>(P)) return;
+        if (!one_step<T>(P, ep)) return;
 }
 
 // Measurement: `reps` grid barriers back to back (no work between them).
 __global__ void __launch_bounds__(TILE_THREADS) k_barrier_bench(GridBar* bar, int reps) {
+    unsigned long long ep = 0;
     for (int r = 0; r < reps; r++)
-        if (!grid_barrier(bar)) return;
+        if (!grid_barrier(bar, ep)) return;
 }
 
 }  // namespace
 
 cudaError_t launch_barrier_bench(GridBar* bar, int grid, int reps, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&bar->count, 0, sizeof(bar->count), s);
+    if (e != cudaSuccess) return e;
     void* args[] = {(void*)&bar, (void*)&reps};
     return cudaLaunchCooperativeKernel((const void*)k_barrier_bench, dim3(grid), dim3(TILE_THREADS), args, 0, s);
 }
 
 template <typename T>
 cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&P.bar->count, 0, sizeof(P.bar->count), s);
+    if (e != cudaSuccess) return e;
     void* args[] = {(void*)&P};
     return cudaLaunchCooperativeKernel((const void*)k_persist_step<T>, dim3(grid), dim3(TILE_THREADS), args, 0, s);
 }

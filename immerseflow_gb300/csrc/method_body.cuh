@@ -35,6 +35,20 @@
 
 namespace ifx {
 
+// Read-only data (tile lists, level / instance / ghost tables, stencil bytes,
+// metric arrays) does not change during a time step: load it through the
+// read-only data path.  Structs are 16-byte aligned and loaded by value.
+template <typename S>
+__device__ __forceinline__ S ldg_struct(const S* p) {
+    static_assert(sizeof(S) % 16 == 0, "16-byte multiple");
+    S out;
+    const int4* src = reinterpret_cast<const int4*>(p);
+    int4* dst = reinterpret_cast<int4*>(&out);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(S) / 16); k++) dst[k] = __ldg(src + k);
+    return out;
+}
+
 // ---------------------------------------------------------------- helpers
 
 __device__ __forceinline__ double rcpa(double d) { return (double)__frcp_rn((float)d); }
@@ -145,7 +159,7 @@ __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* q
 // cells only, so this is an exact linear function of the fluid values.
 template <typename TC, typename TE>
 __device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
-    const GhostDev& g = G[gid];
+    const GhostDev g = ldg_struct(&G[gid]);
     TC acc = (TC)0;
     ws = (TC)0;
 #pragma unroll
@@ -169,8 +183,9 @@ __device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e,
     const TC* ky = LvA<TC>::ky(L);
     const TC* ix = LvA<TC>::ix(L);
     const TC* iy = LvA<TC>::iy(L);
-    const TC cE = kx[i] * ix[i], cW = kx[i - 1] * ix[i];
-    const TC cN = ky[j] * iy[j], cS = ky[j - 1] * iy[j];
+    const TC ixi = __ldg(&ix[i]), iyj = __ldg(&iy[j]);
+    const TC cE = __ldg(&kx[i]) * ixi, cW = __ldg(&kx[i - 1]) * ixi;
+    const TC cN = __ldg(&ky[j]) * iyj, cS = __ldg(&ky[j - 1]) * iyj;
     const TC ce = (bt & B_E) ? cE : (TC)0, cw = (bt & B_W) ? cW : (TC)0;
     const TC cn = (bt & B_N) ? cN : (TC)0, cs = (bt & B_S) ? cS : (TC)0;
     TC dd = ce + cw + cn + cs;
@@ -210,9 +225,9 @@ __device__ __forceinline__ void b_step_begin(InstState* S, int n, int vb) {
 __device__ __forceinline__ void b_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev& gh = G[g];
+    const GhostDev gh = ldg_struct(&G[g]);
     if (gh.qown < 0) return;
-    const InstDev& in = I[gh.inst];
+    const InstDev in = ldg_struct(&I[gh.inst]);
     double fac = in.dt * in.uc * 2.0 / gh.qh;
     in.qbu[gh.qown] = in.qbu[gh.qown] - fac * (in.qbu[gh.qown] - in.u[gh.adj]);
     in.qbv[gh.qown] = in.qbv[gh.qown] - fac * (in.qbv[gh.qown] - in.v[gh.adj]);
@@ -225,8 +240,8 @@ __device__ __forceinline__ void b_ghost_gather(const GhostDev* __restrict__ G, i
                                int comps, double* __restrict__ gval, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev& gh = G[g];
-    const InstDev& in = I[gh.inst];
+    const GhostDev gh = ldg_struct(&G[g]);
+    const InstDev in = ldg_struct(&I[gh.inst]);
     if (comps & 1) {
         double a = ghost_const(gh, in.qbu, gh.cu);
 #pragma unroll
@@ -251,8 +266,8 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
                                 int comps, const double* __restrict__ gval, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev& gh = G[g];
-    const InstDev& in = I[gh.inst];
+    const GhostDev gh = ldg_struct(&G[g]);
+    const InstDev in = ldg_struct(&I[gh.inst]);
     if (comps & 1) in.u[gh.cell] = gval[3 * (size_t)g];
     if (comps & 2) in.v[gh.cell] = gval[3 * (size_t)g + 1];
     if (comps & 4) in.p[gh.cell] = gval[3 * (size_t)g + 2];
@@ -263,22 +278,22 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
 // Convective term in face-flux form and the AB2 right-hand side.
 __device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     int i, j;
     tile_ij(t, i, j);
     if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
     const int P = in.pitch, id = i + j * P;
-    if (in.type[id] != T_FLUID) {
+    if (__ldg(&in.type[id]) != T_FLUID) {
         in.ru[id] = 0.0;
         in.rv[id] = 0.0;
         return;
     }
     const double* u = in.u;
     const double* v = in.v;
-    const double gxi = in.gx[i], fxi = in.fx[i], gxw = in.gx[i - 1], fxw = in.fx[i - 1];
-    const double gyj = in.gy[j], fyj = in.fy[j], gys = in.gy[j - 1], fys = in.fy[j - 1];
-    const double ixi = in.ix[i], iyj = in.iy[j];
+    const double gxi = __ldg(&in.gx[i]), fxi = __ldg(&in.fx[i]), gxw = __ldg(&in.gx[i - 1]), fxw = __ldg(&in.fx[i - 1]);
+    const double gyj = __ldg(&in.gy[j]), fyj = __ldg(&in.fy[j]), gys = __ldg(&in.gy[j - 1]), fys = __ldg(&in.fy[j - 1]);
+    const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
     const double Ue = in.U[id], Uw = in.U[id - 1], Vn = in.V[id], Vs = in.V[id - P];
     const double ue = u[id] * gxi + u[id + 1] * fxi, uw = u[id - 1] * gxw + u[id] * fxw;
     const double un = u[id] * gyj + u[id + P] * fyj, us = u[id - P] * gys + u[id] * fys;
@@ -303,8 +318,8 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              double* __restrict__ part, int parity, int vb) {
     if ((int)vb < ntiles) {
-        const Tile t = tiles[vb];
-        const InstDev& in = I[t.inst];
+        const Tile t = ldg_struct(&tiles[vb]);
+        const InstDev in = ldg_struct(&I[t.inst]);
         const int st = S[t.inst].pred_state;
         if (st == ST_DONE) return;
         const double* su = parity ? in.u2 : in.u;
@@ -315,7 +330,7 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
         tile_ij(t, i, j);
         const bool ok = i >= 1 && i <= in.NX && j >= 1 && j <= in.NY;
         const int P = in.pitch, id = i + j * P;
-        const bool fl = ok && in.type[id] == T_FLUID;
+        const bool fl = ok && __ldg(&in.type[id]) == T_FLUID;
         if (st == ST_FINAL_IN_ALT) {
             if (fl) {
                 du[id] = su[id];
@@ -325,9 +340,9 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
         }
         double m[1] = {0.0};
         if (fl) {
-            const double ixi = in.ix[i], iyj = in.iy[j];
-            const double aE = in.dtre * (in.kx[i] * ixi), aW = in.dtre * (in.kx[i - 1] * ixi);
-            const double aN = in.dtre * (in.ky[j] * iyj), aS = in.dtre * (in.ky[j - 1] * iyj);
+            const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
+            const double aE = in.dtre * (__ldg(&in.kx[i]) * ixi), aW = in.dtre * (__ldg(&in.kx[i - 1]) * ixi);
+            const double aN = in.dtre * (__ldg(&in.ky[j]) * iyj), aS = in.dtre * (__ldg(&in.ky[j - 1]) * iyj);
             const double aP = 1.0 + aE + aW + aN + aS;
             const double di = rcpa(aP);
             const double dU = (in.ru[id] + aE * su[id + 1] + aW * su[id - 1] + aN * su[id + P] + aS * su[id - P] -
@@ -344,8 +359,8 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
     } else {
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
-        const GhostDev& gh = G[g];
-        const InstDev& in = I[gh.inst];
+        const GhostDev gh = ldg_struct(&G[g]);
+        const InstDev in = ldg_struct(&I[gh.inst]);
         const int st = S[gh.inst].pred_state;
         if (st == ST_DONE) return;
         const double* su = parity ? in.u2 : in.u;
@@ -372,7 +387,7 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     const int st = S[k].pred_state;
     bool active = false;
     if (st == ST_ACTIVE) {
@@ -395,12 +410,12 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
 // -------------------------------------------------- faces and PPE source
 
 __device__ __forceinline__ double face_u(const InstDev& in, const double* u, int i, int id) {
-    if (in.type[id] == T_FLUID || in.type[id + 1] == T_FLUID) return u[id] * in.gx[i] + u[id + 1] * in.fx[i];
+    if (__ldg(&in.type[id]) == T_FLUID || __ldg(&in.type[id + 1]) == T_FLUID) return u[id] * __ldg(&in.gx[i]) + u[id + 1] * __ldg(&in.fx[i]);
     return 0.0;
 }
 __device__ __forceinline__ double face_v(const InstDev& in, const double* v, int j, int id) {
     const int P = in.pitch;
-    if (in.type[id] == T_FLUID || in.type[id + P] == T_FLUID) return v[id] * in.gy[j] + v[id + P] * in.fy[j];
+    if (__ldg(&in.type[id]) == T_FLUID || __ldg(&in.type[id + P]) == T_FLUID) return v[id] * __ldg(&in.gy[j]) + v[id + P] * __ldg(&in.fy[j]);
     return 0.0;
 }
 
@@ -408,8 +423,8 @@ __device__ __forceinline__ double face_v(const InstDev& in, const double* v, int
 // to_final), the pressure source div(U*)/dt and its area-weighted sum.
 __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            double* __restrict__ part, int to_final, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -419,13 +434,13 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
     if (j <= in.ny - 2 && i >= 1 && i <= in.NX) Vo[id] = face_v(in, in.v, j, id);
     double acc[1] = {0.0};
     if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
-        if (in.type[id] == T_FLUID) {
+        if (__ldg(&in.type[id]) == T_FLUID) {
             const double Ue = face_u(in, in.u, i, id), Uw = face_u(in, in.u, i - 1, id - 1);
             const double Vn = face_v(in, in.v, j, id), Vs = face_v(in, in.v, j - 1, id - P);
-            const double d = (Ue - Uw) * in.ix[i] + (Vn - Vs) * in.iy[j];
+            const double d = (Ue - Uw) * __ldg(&in.ix[i]) + (Vn - Vs) * __ldg(&in.iy[j]);
             const double b = d / in.dt;
             in.b[id] = b;
-            acc[0] = b * (in.dx[i] * in.dy[j]);
+            acc[0] = b * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
         } else {
             in.b[id] = 0.0;
         }
@@ -438,7 +453,7 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
 __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     double r[1];
     inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
     if (threadIdx.x == 0) S[k].bmean = in.singular ? r[0] / in.area : 0.0;
@@ -453,7 +468,7 @@ __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, Inst
 __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, uint8_t& bt) {
     if (i < 1 || i > L.NX || j < 1 || j > L.NY) return false;
     id = i + j * L.pitch;
-    bt = L.bits[id];
+    bt = __ldg(&L.bits[id]);
     return (bt & 0x0F) != 0;
 }
 
@@ -462,11 +477,11 @@ __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, 
 __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev L = ldg_struct(&LV[in.lev0]);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -483,7 +498,7 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
         acc[0] = r * r;
         acc[1] = bb * bb;
         acc[2] = r * r;
-        acc[3] = in.p[id] * (in.dx[i] * in.dy[j]);
+        acc[3] = in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];
     block_sum<4>(acc, out);
@@ -495,7 +510,7 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
                                 const double* __restrict__ part, int start, LoopCtl* ctl,
                                 unsigned long long handle, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     bool active = false;
     if (S[k].ppe_state == ST_ACTIVE) {
         double r[4];
@@ -529,11 +544,11 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
 template <typename T>
 __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev L = ldg_struct(&LV[in.lev0]);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -549,11 +564,11 @@ template <typename T>
 __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev L = ldg_struct(&LV[in.lev0]);
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
     double* zo = which == 0 ? in.kph : in.ksh;
     double* y = which == 0 ? in.kv : in.kt;
@@ -582,7 +597,7 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
 __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int which, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     if (S[k].ppe_state != ST_ACTIVE) return;
     double r[2];
     inst_sum<2>(part, in.tile_beg, in.tile_cnt, r);
@@ -596,11 +611,11 @@ __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, Ins
 template <typename T>
 __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev L = ldg_struct(&LV[in.lev0]);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -615,11 +630,11 @@ __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const L
 __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          double* __restrict__ part, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev L = ldg_struct(&LV[in.lev0]);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -631,7 +646,7 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
         in.kr[id] = r;
         acc[0] = r * r;
         acc[2] = in.krh[id] * r;
-        acc[3] = pn * (in.dx[i] * in.dy[j]);
+        acc[3] = pn * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];
     block_sum<4>(acc, out);
@@ -644,8 +659,8 @@ template <typename T>
 __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
-    const Tile t = tiles[vb];
-    const LevelDev& L = LV[t.lev];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev L = ldg_struct(&LV[t.lev]);
     if (S[L.inst].ppe_state != ST_ACTIVE) return;
     int i, j, id;
     uint8_t bt;
@@ -667,15 +682,15 @@ template <typename T>
 __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt, int vb) {
-    const Tile t = tiles[vb];
-    const LevelDev& C = LV[t.lev];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev C = ldg_struct(&LV[t.lev]);
     if (S[C.inst].ppe_state != ST_ACTIVE) return;
-    const LevelDev& F = LV[C.parent];
+    const LevelDev F = ldg_struct(&LV[C.parent]);
     int I0, J0;
     tile_ij(t, I0, J0);
     if (I0 < 1 || I0 > C.NX || J0 < 1 || J0 > C.NY) return;
     const int cid = I0 + J0 * C.pitch;
-    const uint8_t cb = C.bits[cid];
+    const uint8_t cb = __ldg(&C.bits[cid]);
     T* rc = (T*)C.r;
     if (!(cb & 0x0F)) {
         rc[cid] = (T)0;
@@ -684,7 +699,7 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     const T* fe = (const T*)(fine_alt ? F.e2 : F.e);
     const T* fr = (const T*)F.r;
     const T* fdw = LvA<T>::dw(F);
-    const T* fdh = LvA<T>::dh(F);
+    const T* fdh = LvA<T>::dh(F);  // read through __ldg below
     T acc = (T)0;
 #pragma unroll
     for (int dj = 0; dj < 2; dj++)
@@ -693,14 +708,14 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
             const int i = 2 * I0 - 1 + di, j = 2 * J0 - 1 + dj;
             if (i > F.NX || j > F.NY) continue;
             const int id = i + j * F.pitch;
-            const uint8_t bt = F.bits[id];
+            const uint8_t bt = __ldg(&F.bits[id]);
             if (!(bt & 0x0F)) continue;
             T Le, D;
             if (F.depth == 0) lap<T, T, true>(F, fe, i, j, id, bt, G, I[C.inst].gidx, Le, D);
             else lap<T, T, false>(F, fe, i, j, id, bt, G, nullptr, Le, D);
-            acc += (fr[id] - Le) * (fdw[i] * fdh[j]);
+            acc += (fr[id] - Le) * (__ldg(&fdw[i]) * __ldg(&fdh[j]));
         }
-    const T rv = acc / (LvA<T>::dw(C)[I0] * LvA<T>::dh(C)[J0]);
+    const T rv = acc / (__ldg(&LvA<T>::dw(C)[I0]) * __ldg(&LvA<T>::dh(C)[J0]));
     rc[cid] = rv;
     if (C.child >= 0) {  // middle level: fused first sweep from zero
         T Le, D;
@@ -713,10 +728,10 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
 template <typename T>
 __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
-    const Tile t = tiles[vb];
-    const LevelDev& F = LV[t.lev];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev F = ldg_struct(&LV[t.lev]);
     if (S[F.inst].ppe_state != ST_ACTIVE) return;
-    const LevelDev& C = LV[F.child];
+    const LevelDev C = ldg_struct(&LV[F.child]);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -724,16 +739,16 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
     // the coarsest level's solution is always in e; a middle level's in the buffer its sweeps ended on
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
     T* fe = (T*)(fine_alt ? F.e2 : F.e);
-    const int I0 = F.pI[i], In = F.pIn[i], J0 = F.pJ[j], Jn = F.pJn[j];
-    const T wx = LvA<T>::pwx(F)[i], wy = LvA<T>::pwy(F)[j];
-    const T sx = (T)F.psx[i], sy = (T)F.psy[j];
+    const int I0 = __ldg(&F.pI[i]), In = __ldg(&F.pIn[i]), J0 = __ldg(&F.pJ[j]), Jn = __ldg(&F.pJn[j]);
+    const T wx = __ldg(&LvA<T>::pwx(F)[i]), wy = __ldg(&LvA<T>::pwy(F)[j]);
+    const T sx = (T)__ldg(&F.psx[i]), sy = (T)__ldg(&F.psy[j]);
     T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
     const int CP = C.pitch;
     const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
-    w00 = (C.bits[c00] & 0x0F) ? w00 : (T)0;
-    w10 = (C.bits[c10] & 0x0F) ? w10 : (T)0;
-    w01 = (C.bits[c01] & 0x0F) ? w01 : (T)0;
-    w11 = (C.bits[c11] & 0x0F) ? w11 : (T)0;
+    w00 = (__ldg(&C.bits[c00]) & 0x0F) ? w00 : (T)0;
+    w10 = (__ldg(&C.bits[c10]) & 0x0F) ? w10 : (T)0;
+    w01 = (__ldg(&C.bits[c01]) & 0x0F) ? w01 : (T)0;
+    w11 = (__ldg(&C.bits[c11]) & 0x0F) ? w11 : (T)0;
     const T sw = w00 + w10 + w01 + w11;
     const T val = (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
     fe[id] += val;
@@ -761,7 +776,7 @@ __device__ void coarse_solve_level(const LevelDev& L) {
             const int i = q % nx, j = q / nx, id = i + j * L.pitch;
             se[q] = (T)0;
             sr[q] = r[id];
-            sb[q] = L.bits[id];
+            sb[q] = __ldg(&L.bits[id]);
         }
         for (int q = threadIdx.x; q < L.nx; q += blockDim.x) { skx[q] = kx[q]; six[q] = ix[q]; }
         for (int q = threadIdx.x; q < L.ny; q += blockDim.x) { sky[q] = ky[q]; siy[q] = iy[q]; }
@@ -807,7 +822,7 @@ __device__ void coarse_solve_level(const LevelDev& L) {
                 const int i = 1 + q % L.NX, j = 1 + q / L.NX;
                 if (((i + j) & 1) != col) continue;
                 const int id = i + j * L.pitch;
-                const uint8_t bt = L.bits[id];
+                const uint8_t bt = __ldg(&L.bits[id]);
                 if (!(bt & 0x0F)) continue;
                 T Le, D;
                 lap<T, T, false>(L, e, i, j, id, bt, nullptr, nullptr, Le, D);
@@ -829,12 +844,12 @@ __device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const 
                                            int pre, int post, int vb) {
     const int k = vb;
     if (S[k].ppe_state != ST_ACTIVE) return;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     const int lb = sub[k];
     const int top = in.lev0 + in.nlev - 1;
     // descend: restriction into each small level, then its pre-smoothing
     for (int lv = lb; lv <= top; lv++) {
-        const LevelDev& C = LV[lv];
+        const LevelDev C = ldg_struct(&LV[lv]);
         const int fa = parity_after_pre(C.depth - 1, pre);
         for (int t = C.tbeg; t < C.tbeg + C.tcnt; t++) b_restrict<T>(tall, LV, I, S, G, fa, t);
         __syncthreads();
@@ -851,7 +866,7 @@ __device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const 
     }
     // ascend: prolongation into each small middle level, then its post-smoothing
     for (int lv = top - 1; lv >= lb; lv--) {
-        const LevelDev& F = LV[lv];
+        const LevelDev F = ldg_struct(&LV[lv]);
         int cur = parity_after_pre(F.depth, pre);
         for (int t = F.tbeg; t < F.tbeg + F.tcnt; t++)
             b_prolong<T>(tall, LV, S, cur, parity_after_post(F.depth + 1, pre, post), t);
@@ -868,38 +883,38 @@ __device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const 
 
 __device__ __forceinline__ void b_p_finalize(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                              const InstState* __restrict__ S, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     if (!in.singular) return;
     int i, j;
     tile_ij(t, i, j);
     if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
     const int id = i + j * in.pitch;
-    const uint8_t ty = in.type[id];
+    const uint8_t ty = __ldg(&in.type[id]);
     if (ty == T_FLUID || ty == T_GHOST) in.p[id] -= S[t.inst].pmean;
 }
 
 __device__ __forceinline__ double corr_u(const InstDev& in, int i, int id) {
-    const bool act = in.type[id] == T_FLUID || in.type[id + 1] == T_FLUID;
+    const bool act = __ldg(&in.type[id]) == T_FLUID || __ldg(&in.type[id + 1]) == T_FLUID;
     if (!act) return in.Us[id];
     if (i == 0 && !(in.dirmask & 1)) return in.Us[id];
     if (i == in.nx - 2 && !(in.dirmask & 2)) return in.Us[id];
-    return in.Us[id] - in.dt * in.kx[i] * (in.p[id + 1] - in.p[id]);
+    return in.Us[id] - in.dt * __ldg(&in.kx[i]) * (in.p[id + 1] - in.p[id]);
 }
 __device__ __forceinline__ double corr_v(const InstDev& in, int j, int id) {
     const int P = in.pitch;
-    const bool act = in.type[id] == T_FLUID || in.type[id + P] == T_FLUID;
+    const bool act = __ldg(&in.type[id]) == T_FLUID || __ldg(&in.type[id + P]) == T_FLUID;
     if (!act) return in.Vs[id];
     if (j == 0 && !(in.dirmask & 4)) return in.Vs[id];
     if (j == in.ny - 2 && !(in.dirmask & 8)) return in.Vs[id];
-    return in.Vs[id] - in.dt * in.ky[j] * (in.p[id + P] - in.p[id]);
+    return in.Vs[id] - in.dt * __ldg(&in.ky[j]) * (in.p[id + P] - in.p[id]);
 }
 
 // Projection of cell and face velocities; divergence and boundary fluxes.
 __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                           double* __restrict__ part, int vb) {
-    const Tile t = tiles[vb];
-    const InstDev& in = I[t.inst];
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev in = ldg_struct(&I[t.inst]);
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -907,23 +922,23 @@ __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const 
     if (i <= in.nx - 2 && j >= 1 && j <= in.NY) {
         const double Un = corr_u(in, i, id);
         in.U[id] = Un;
-        if (i == 0) fl[0] += Un * in.dy[j];
-        if (i == in.nx - 2) fl[1] += Un * in.dy[j];
+        if (i == 0) fl[0] += Un * __ldg(&in.dy[j]);
+        if (i == in.nx - 2) fl[1] += Un * __ldg(&in.dy[j]);
     }
     if (j <= in.ny - 2 && i >= 1 && i <= in.NX) {
         const double Vn = corr_v(in, j, id);
         in.V[id] = Vn;
-        if (j == 0) fl[0] += Vn * in.dx[i];
-        if (j == in.ny - 2) fl[1] += Vn * in.dx[i];
+        if (j == 0) fl[0] += Vn * __ldg(&in.dx[i]);
+        if (j == in.ny - 2) fl[1] += Vn * __ldg(&in.dx[i]);
     }
     if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
-        if (in.type[id] == T_FLUID) {
+        if (__ldg(&in.type[id]) == T_FLUID) {
             const double* p = in.p;
-            const double ixi = in.ix[i], iyj = in.iy[j];
-            const double pe = p[id] * in.gx[i] + p[id + 1] * in.fx[i];
-            const double pw = p[id - 1] * in.gx[i - 1] + p[id] * in.fx[i - 1];
-            const double pn = p[id] * in.gy[j] + p[id + P] * in.fy[j];
-            const double ps = p[id - P] * in.gy[j - 1] + p[id] * in.fy[j - 1];
+            const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
+            const double pe = p[id] * __ldg(&in.gx[i]) + p[id + 1] * __ldg(&in.fx[i]);
+            const double pw = p[id - 1] * __ldg(&in.gx[i - 1]) + p[id] * __ldg(&in.fx[i - 1]);
+            const double pn = p[id] * __ldg(&in.gy[j]) + p[id + P] * __ldg(&in.fy[j]);
+            const double ps = p[id - P] * __ldg(&in.gy[j - 1]) + p[id] * __ldg(&in.fy[j - 1]);
             in.u[id] -= in.dt * (pe - pw) * ixi;
             in.v[id] -= in.dt * (pn - ps) * iyj;
             const double d = (corr_u(in, i, id) - corr_u(in, i - 1, id - 1)) * ixi +
@@ -947,7 +962,7 @@ __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const 
 __device__ __forceinline__ void b_correct_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                  const double* __restrict__ part, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     double m = 0.0, a[2] = {0.0, 0.0};
     for (int t = threadIdx.x; t < in.tile_cnt; t += blockDim.x) {
         const double* q = part + (size_t)(in.tile_beg + t) * NPART;
@@ -984,8 +999,8 @@ __device__ __forceinline__ int locate(const double* c, int n, double x) {
 
 __device__ __forceinline__ double sample(const InstDev& in, const double* q, double x, double y) {
     const int i0 = locate(in.xc, in.nx, x), j0 = locate(in.yc, in.ny, y);
-    const double xi = (x - in.xc[i0]) / (in.xc[i0 + 1] - in.xc[i0]);
-    const double et = (y - in.yc[j0]) / (in.yc[j0 + 1] - in.yc[j0]);
+    const double xi = (x - __ldg(&in.xc[i0])) / (__ldg(&in.xc[i0 + 1]) - __ldg(&in.xc[i0]));
+    const double et = (y - __ldg(&in.yc[j0])) / (__ldg(&in.yc[j0 + 1]) - __ldg(&in.yc[j0]));
     const int P = in.pitch, id = i0 + j0 * P;
     return (1 - xi) * (1 - et) * q[id] + xi * (1 - et) * q[id + 1] + (1 - xi) * et * q[id + P] +
            xi * et * q[id + P + 1];
@@ -1000,7 +1015,7 @@ __device__ __forceinline__ double bil(const double* q, int c, int P, double xi, 
 
 __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
     const int k = vb;
-    const InstDev& in = I[k];
+    const InstDev in = ldg_struct(&I[k]);
     if (!in.body) {
         if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
         return;
@@ -1009,7 +1024,7 @@ __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstStat
     const int P = in.pitch;
     double F[2] = {0.0, 0.0};
     for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
-        const ForceSample f = in.fs[q];
+        const ForceSample f = ldg_struct(&in.fs[q]);
         const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
         const double up = bil(in.u, f.c1, P, f.xi1, f.et1);
         const double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
