@@ -48,6 +48,7 @@ _SIGS = {
     "ifx_get_ibm_ghosts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_synchronize": (C.c_int, [C.c_void_p]),
+    "ifx_trace_step": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int)]),
     "ifx_profile_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "ifx_destroy": (None, [C.c_void_p]),
 }
@@ -206,6 +207,13 @@ class Solver:
         cells = C.c_longlong()
         _check(lib().ifx_profile_kernel(self._h, kernel, reps, C.byref(ms), C.byref(cells)))
         return ms.value, cells.value
+
+    def trace_step(self, cap=4096):
+        """One persistent time step; microseconds between consecutive grid barriers."""
+        us = np.zeros(cap)
+        n = C.c_int()
+        _check(lib().ifx_trace_step(self._h, cap, _dptr(us), C.byref(n)))
+        return us[:n.value]
 
     def synchronize(self):
         _check(lib().ifx_synchronize(self._h))

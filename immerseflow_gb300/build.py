@@ -48,7 +48,7 @@ def _stale(target, deps):
 def build(verbose=False, ptxas_info=False):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(CLI), exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "immerseflow_gb300.h"))
     jobs = []
     objs = []

@@ -26,7 +26,9 @@ constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
 constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
 constexpr double COARSE_OMEGA = 1.5;
 constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one block per instance
-constexpr int COARSE_SMEM_CELLS = 1024;  // coarsest level (with ghost ring) staged in shared memory
+constexpr int SUB_SMEM_MAX = 96 * 1024;  // shared memory for those levels (fields, metrics, tables)
+constexpr int kSubLevels = 16;           // at most this many levels per instance
+constexpr int SUB_COARSE_PER_THREAD = 4;  // coarsest-level cells per thread in the RB-SOR solve
 
 enum CellType : uint8_t { T_SOLID = 0, T_FLUID = 1, T_GHOST = 2, T_DOMAIN = 3 };
 // per-cell stencil bits: open faces, and (finest level) faces to an IBM ghost
@@ -45,6 +47,49 @@ enum : int { ST_ACTIVE = 0, ST_FINAL_IN_ALT = 1, ST_DONE = 2 };
 // zero-start sweep into e2; coarser levels from the fused restriction into e).
 IFX_HD inline int parity_after_pre(int depth, int pre) { return depth == 0 ? (pre & 1) : ((pre - 1) & 1); }
 IFX_HD inline int parity_after_post(int depth, int pre, int post) { return (parity_after_pre(depth, pre) + post) & 1; }
+
+// Shared-memory layout (byte offsets) of one small multigrid level staged for
+// the sub-cycle: fields e, e2, r (n = nx*ny cells of tsize bytes), the 1-D
+// metric arrays kx ix dw (nx) and ky iy dh (ny), the prolongation tables from
+// the next coarser level (pwx pI pIn psx: nx; pwy pJ pJn psy: ny) and the
+// stencil bytes; every array starts on a 16-byte boundary.
+struct SubLayout {
+    size_t e, e2, r, kx, ix, dw, pwx, ky, iy, dh, pwy, pI, pIn, pJ, pJn, b, psx, psy, bytes;
+};
+IFX_HD inline size_t sub_al16(size_t x) { return (x + 15) & ~(size_t)15; }
+IFX_HD inline SubLayout sub_layout(int nx, int ny, int tsize) {
+    SubLayout L;
+    const size_t n = (size_t)nx * ny, ts = (size_t)tsize, X = (size_t)nx, Y = (size_t)ny;
+    size_t o = 0;
+    L.e = o;   o += sub_al16(n * ts);
+    L.e2 = o;  o += sub_al16(n * ts);
+    L.r = o;   o += sub_al16(n * ts);
+    L.kx = o;  o += sub_al16(X * ts);
+    L.ix = o;  o += sub_al16(X * ts);
+    L.dw = o;  o += sub_al16(X * ts);
+    L.pwx = o; o += sub_al16(X * ts);
+    L.ky = o;  o += sub_al16(Y * ts);
+    L.iy = o;  o += sub_al16(Y * ts);
+    L.dh = o;  o += sub_al16(Y * ts);
+    L.pwy = o; o += sub_al16(Y * ts);
+    L.pI = o;  o += sub_al16(X * 4);
+    L.pIn = o; o += sub_al16(X * 4);
+    L.pJ = o;  o += sub_al16(Y * 4);
+    L.pJn = o; o += sub_al16(Y * 4);
+    L.b = o;   o += sub_al16(n);
+    L.psx = o; o += sub_al16(X);
+    L.psy = o; o += sub_al16(Y);
+    L.bytes = o;
+    return L;
+}
+IFX_HD inline size_t sub_level_bytes(int nx, int ny, int tsize) { return sub_layout(nx, ny, tsize).bytes; }
+// Header of a staged level at the start of the sub-cycle's shared memory.
+struct SubHdr {
+    SubLayout o;
+    unsigned base;  // byte offset of the level's arrays
+    int NX, NY, nx, ny, dirmask, child, depth, ns;
+};
+constexpr size_t SUB_HDR_BYTES = (kSubLevels * sizeof(SubHdr) + 15) & ~(size_t)15;
 
 struct alignas(16) Tile {
     int inst;  // instance index

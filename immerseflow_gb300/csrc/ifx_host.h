@@ -82,6 +82,7 @@ struct ifx_solver {
     ifx::Tile* dTall = nullptr;      // tiles of every level of every instance
     int* dSub = nullptr;             // LevelDev index of each instance's first small level
     int lmax = 0;
+    int sub_bytes = 0;  // dynamic shared memory of the small-level sub-cycle
     int mg_pre = 2, mg_post = 2;
     double* dPart = nullptr;         // NPART partials per finest-level tile
     ifx::LoopCtl* dCtl = nullptr;

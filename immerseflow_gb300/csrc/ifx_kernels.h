@@ -46,8 +46,11 @@ template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
                            int coarse_alt, cudaStream_t s);
 template <typename T>
-cudaError_t launch_subcycle(const Tile* tall, const int* sub, int ninst, const LevelDev* LV, const InstDev* I,
-                            const InstState* S, const GhostDev* G, int pre, int post, cudaStream_t s);
+cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
+                            int pre, int post, int smem_bytes, cudaStream_t s);
+// Allows k_subcycle<T> `bytes` of dynamic shared memory (above the 48 KB default).
+template <typename T>
+cudaError_t subcycle_smem_limit(int bytes);
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
 cudaError_t launch_correct(const Tile* t, int nt, const InstDev* I, double* part, cudaStream_t s);
 cudaError_t launch_correct_reduce(const InstDev* I, InstState* S, const double* part, int ninst,

@@ -34,12 +34,15 @@ struct PersistPlan {
     int ntsm[kMaxLevels];
     int ntre[kMaxLevels];
     int pred_pairs, ppe_bodies, nsteps;
+    long long* trace;   // optional: SM clock of block 0 after every barrier
+    int trace_cap;
+    int sub_bytes;      // dynamic shared memory of the sub-cycle (largest instance)
 };
 
 template <typename T>
 cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s);
 template <typename T>
-cudaError_t persist_occupancy(int* blocks_per_sm);
+cudaError_t persist_occupancy(int* blocks_per_sm, int smem_bytes);
 cudaError_t launch_barrier_bench(GridBar* bar, int grid, int reps, cudaStream_t s);
 
 }  // namespace ifx

@@ -74,10 +74,11 @@ template <typename T>
 __global__ void k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
-__global__ void k_subcycle(const Tile* __restrict__ tall, const int* __restrict__ sub, const LevelDev* __restrict__ LV,
+__global__ void k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                           const GhostDev* __restrict__ G, int pre, int post) {
-    b_subcycle<T>(tall, sub, LV, I, S, G, pre, post, blockIdx.x);
+                           int pre, int post) {
+    extern __shared__ __align__(16) unsigned char sub_smem[];
+    b_subcycle<T>(sub, LV, I, S, pre, post, sub_smem, false, blockIdx.x);
 }
 __global__ void k_p_finalize(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                              const InstState* __restrict__ S) { b_p_finalize(tiles, I, S, blockIdx.x); }
@@ -193,10 +194,14 @@ cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const Inst
     return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_subcycle(const Tile* tall, const int* sub, int ninst, const LevelDev* LV, const InstDev* I,
-                            const InstState* S, const GhostDev* G, int pre, int post, cudaStream_t s) {
+cudaError_t subcycle_smem_limit(int bytes) {
+    return cudaFuncSetAttribute(k_subcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+template <typename T>
+cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
+                            int pre, int post, int smem_bytes, cudaStream_t s) {
     if (ninst == 0) return cudaSuccess;
-    k_subcycle<T><<<ninst, TILE_THREADS, 0, s>>>(tall, sub, LV, I, S, G, pre, post);
+    k_subcycle<T><<<ninst, TILE_THREADS, smem_bytes, s>>>(sub, LV, I, S, pre, post);
     return cudaGetLastError();
 }
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {
@@ -231,9 +236,11 @@ template cudaError_t launch_prolong<double>(const Tile*, int, const LevelDev*, c
                                             cudaStream_t);
 template cudaError_t launch_prolong<float>(const Tile*, int, const LevelDev*, const InstState*, int, int,
                                            cudaStream_t);
-template cudaError_t launch_subcycle<double>(const Tile*, const int*, int, const LevelDev*, const InstDev*,
-                                             const InstState*, const GhostDev*, int, int, cudaStream_t);
-template cudaError_t launch_subcycle<float>(const Tile*, const int*, int, const LevelDev*, const InstDev*,
-                                            const InstState*, const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_subcycle<double>(const int*, int, const LevelDev*, const InstDev*, const InstState*,
+                                             int, int, int, cudaStream_t);
+template cudaError_t launch_subcycle<float>(const int*, int, const LevelDev*, const InstDev*, const InstState*,
+                                            int, int, int, cudaStream_t);
+template cudaError_t subcycle_smem_limit<double>(int);
+template cudaError_t subcycle_smem_limit<float>(int);
 
 }  // namespace ifx

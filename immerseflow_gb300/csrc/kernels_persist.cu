@@ -32,7 +32,8 @@ __device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(
 // gridDim.x * k.  Arrival is a release add, the wait an acquire poll, so the
 // critical path is one atomic and one poll; the counter never needs a reset
 // inside the launch (the host zeroes it before each launch).
-__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epoch) {
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epoch, long long* trace = nullptr,
+                                             int cap = 0) {
     __syncthreads();
     epoch += 1;
     if (threadIdx.x == 0) {
@@ -49,6 +50,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epo
             }
             __nanosleep(32);
         }
+        if (trace && blockIdx.x == 0 && epoch < (unsigned long long)cap) trace[epoch] = clock64();
     }
     __syncthreads();
     return vload(&b->err) == 0u;
@@ -69,7 +71,7 @@ __device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
 
 #define BAR()                                          \
     do {                                               \
-        if (!grid_barrier(P.bar, ep)) return false;    \
+        if (!grid_barrier(P.bar, ep, P.trace, P.trace_cap)) return false; \
     } while (0)
 #define FOR_VB(n) for (int vb = blockIdx.x; vb < (n); vb += gridDim.x)
 
@@ -99,6 +101,7 @@ __device__ bool vcycle(const PersistPlan& P, int* res, unsigned long long& ep) {
         if (P.ntre[l] == 0) break;
         FOR_VB(P.ntre[l]) b_restrict<T>(P.tre[l], P.LV, P.I, P.S, P.G, parity_after_pre(l - 1, P.mg_pre), vb);
         BAR();
+        if (P.ntsm[l] == 0) continue;  // only first small levels (sub-cycle) at this depth
         int cur = 0;
         for (int k = 1; k < P.mg_pre; k++) {
             FOR_VB(P.ntsm[l]) b_smooth<T>(P.tsm[l], P.LV, P.I, P.S, P.G, 0, cur, vb);
@@ -106,7 +109,11 @@ __device__ bool vcycle(const PersistPlan& P, int* res, unsigned long long& ep) {
             cur ^= 1;
         }
     }
-    FOR_VB(P.ninst) b_subcycle<T>(P.tall, P.sub, P.LV, P.I, P.S, P.G, P.mg_pre, P.mg_post, vb);
+    {
+        extern __shared__ __align__(16) unsigned char sub_smem[];
+        const bool resident = P.ninst <= (int)gridDim.x;  // geometry staged at kernel start
+        FOR_VB(P.ninst) b_subcycle<T>(P.sub, P.LV, P.I, P.S, P.mg_pre, P.mg_post, sub_smem, resident, vb);
+    }
     BAR();
     for (int l = P.lmax - 2; l >= 0; l--) {
         const Tile* tl = l == 0 ? P.t0 : P.tsm[l];
@@ -196,6 +203,12 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
 template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS) k_persist_step(PersistPlan P) {
     unsigned long long ep = 0;
+    if ((int)blockIdx.x < P.ninst && P.ninst <= (int)gridDim.x) {
+        // block k runs instance k's small levels all launch long: stage their geometry once
+        extern __shared__ __align__(16) unsigned char sub_smem[];
+        sub_stage_geometry<T>(P.sub, P.LV, P.I, blockIdx.x, sub_smem);
+    }
+    if (P.trace && blockIdx.x == 0 && threadIdx.x == 0 && P.trace_cap > 0) P.trace[0] = clock64();
     for (int s = 0; s < P.nsteps; s++)
         if (!one_step<T>(P, ep)) return;
 }
@@ -221,17 +234,21 @@ cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) 
     cudaError_t e = cudaMemsetAsync(&P.bar->count, 0, sizeof(P.bar->count), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&P};
-    return cudaLaunchCooperativeKernel((const void*)k_persist_step<T>, dim3(grid), dim3(TILE_THREADS), args, 0, s);
+    return cudaLaunchCooperativeKernel((const void*)k_persist_step<T>, dim3(grid), dim3(TILE_THREADS), args,
+                                       (size_t)P.sub_bytes, s);
 }
 
 template <typename T>
-cudaError_t persist_occupancy(int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_persist_step<T>, TILE_THREADS, 0);
+cudaError_t persist_occupancy(int* blocks_per_sm, int smem_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(k_persist_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_persist_step<T>, TILE_THREADS,
+                                                         (size_t)smem_bytes);
 }
 
 template cudaError_t launch_persist_step<double>(const PersistPlan&, int, cudaStream_t);
 template cudaError_t launch_persist_step<float>(const PersistPlan&, int, cudaStream_t);
-template cudaError_t persist_occupancy<double>(int*);
-template cudaError_t persist_occupancy<float>(int*);
+template cudaError_t persist_occupancy<double>(int*, int);
+template cudaError_t persist_occupancy<float>(int*, int);
 
 }  // namespace ifx

@@ -1,5 +1,12 @@
-// kernels_method.cu -- sm_103a kernels of the fractional step with ghost-cell
-// IBM, batched over instances.
+// method_body.cuh -- device bodies of the fractional-step kernels with
+// ghost-cell IBM, batched over instances.
+//
+// Each phase of the time step is a __device__ function b_*(..., vb) that
+// processes one "virtual block" vb: a tile (32x8 cells of one level of one
+// instance), a chunk of ghost relations, or one instance.  The same bodies
+// run as ordinary kernels (one launch per phase, kernels_method.cu; used by
+// the CUDA-graph and host-loop paths) and inside the persistent per-step
+// kernel (kernels_persist.cu), so all paths compute bit-identical results.
 //
 // The method (written because the reference leaves it unimplemented:
 // src/include/AD_PPE_Correction.cu:1-12, src/include/PPESolver.cu:73-135):
@@ -13,19 +20,8 @@
 //   projection u = u* - dt grad p (cells), U = U* - dt dp/dn (faces).
 // Coefficients follow the reference's 2/(dx_i (dx_i + dx_nb)) form
 // (src/include/ADSolver.cu:34-39).  Every phase has a CPU twin in the
-// oracle (oracle/oracle.cpp, method_step).
-//
-// Precision: state in FP64; multigrid corrections in T (double for the plain
-// path, float for the mixed path).
-
-// method_body.cuh -- device bodies of the fractional-step kernels.
-//
-// Each phase of the time step is a __device__ function b_*(..., vb) that
-// processes one "virtual block" vb: a tile (32x8 cells of one level of one
-// instance), a chunk of ghost relations, or one instance.  The same bodies
-// run as ordinary kernels (one launch per phase, kernels_method.cu; used by
-// the CUDA-graph path) and inside the persistent per-step kernel
-// (kernels_persist.cu), so both paths compute bit-identical results.
+// oracle (oracle/oracle.cpp, method_step).  State in FP64; multigrid
+// corrections in T (double for the plain path, float for the mixed path).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -36,8 +32,9 @@
 namespace ifx {
 
 // Read-only data (tile lists, level / instance / ghost tables, stencil bytes,
-// metric arrays) does not change during a time step: load it through the
-// read-only data path.  Structs are 16-byte aligned and loaded by value.
+// metric arrays) does not change during a time step: small structs that are
+// used whole (tiles, force samples) and the metric / stencil arrays are
+// loaded through the read-only data path.
 template <typename S>
 __device__ __forceinline__ S ldg_struct(const S* p) {
     static_assert(sizeof(S) % 16 == 0, "16-byte multiple");
@@ -159,7 +156,7 @@ __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* q
 // cells only, so this is an exact linear function of the fluid values.
 template <typename TC, typename TE>
 __device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
-    const GhostDev g = ldg_struct(&G[gid]);
+    const GhostDev& g = G[gid];
     TC acc = (TC)0;
     ws = (TC)0;
 #pragma unroll
@@ -171,14 +168,14 @@ __device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e
     return acc;
 }
 
-// Pressure-type Laplacian at live cell (i,j): Le = sum c (e_nb - e) with
-// closed faces dropped, Dirichlet sides adding 2c to the diagonal, and (finest
-// level) faces to IBM ghosts using the ghost's image-point value (ghost
-// unknowns eliminated).  D is the diagonal of that operator.  Coefficients
-// and arithmetic in TC, field values of type TE.
-template <typename TC, typename TE, bool LVL0>
-__device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id,
-                                    uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+// Face coefficients of cell (i,j) with closed faces dropped, and the
+// diagonal with Dirichlet sides adding 2c.
+template <typename TC>
+struct LapCoef {
+    TC ce, cw, cn, cs, dd;
+};
+template <typename TC>
+__device__ __forceinline__ LapCoef<TC> lap_coef(const LevelDev& L, int i, int j, uint8_t bt) {
     const TC* kx = LvA<TC>::kx(L);
     const TC* ky = LvA<TC>::ky(L);
     const TC* ix = LvA<TC>::ix(L);
@@ -186,27 +183,55 @@ __device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e,
     const TC ixi = __ldg(&ix[i]), iyj = __ldg(&iy[j]);
     const TC cE = __ldg(&kx[i]) * ixi, cW = __ldg(&kx[i - 1]) * ixi;
     const TC cN = __ldg(&ky[j]) * iyj, cS = __ldg(&ky[j - 1]) * iyj;
-    const TC ce = (bt & B_E) ? cE : (TC)0, cw = (bt & B_W) ? cW : (TC)0;
-    const TC cn = (bt & B_N) ? cN : (TC)0, cs = (bt & B_S) ? cS : (TC)0;
-    TC dd = ce + cw + cn + cs;
+    LapCoef<TC> c;
+    c.ce = (bt & B_E) ? cE : (TC)0;
+    c.cw = (bt & B_W) ? cW : (TC)0;
+    c.cn = (bt & B_N) ? cN : (TC)0;
+    c.cs = (bt & B_S) ? cS : (TC)0;
+    TC dd = c.ce + c.cw + c.cn + c.cs;
     if (L.dirmask) {
         if (i == L.NX && (L.dirmask & (1 << 1))) dd += (TC)2 * cE;
         if (i == 1 && (L.dirmask & (1 << 0))) dd += (TC)2 * cW;
         if (j == L.NY && (L.dirmask & (1 << 3))) dd += (TC)2 * cN;
         if (j == 1 && (L.dirmask & (1 << 2))) dd += (TC)2 * cS;
     }
-    const int P = L.pitch;
+    c.dd = dd;
+    return c;
+}
+
+// Pressure-type Laplacian at live cell (i,j): Le = sum c (e_nb - e) with
+// closed faces dropped, Dirichlet sides adding 2c to the diagonal, and (finest
+// level) faces to IBM ghosts using the ghost's image-point value (ghost
+// unknowns eliminated).  D is the diagonal of that operator.  Coefficients
+// and arithmetic in TC, field values of type TE; P is the row pitch of e
+// (L.pitch in global memory, L.nx for a level staged in shared memory).
+template <typename TC, typename TE, bool LVL0>
+__device__ __forceinline__ void lap_p(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id, int P,
+                                      uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+    const LapCoef<TC> c = lap_coef<TC>(L, i, j, bt);
     TC eE = (TC)e[id + 1], eW = (TC)e[id - 1], eN = (TC)e[id + P], eS = (TC)e[id - P];
-    TC dm = dd;
+    TC dm = c.dd;
     if (LVL0 && (bt & 0xF0)) {
         TC ws;
-        if (bt & G_E) { eE = ghost_eval<TC, TE>(G, gidx[id + 1], e, id, ws); dm -= ce * ws; }
-        if (bt & G_W) { eW = ghost_eval<TC, TE>(G, gidx[id - 1], e, id, ws); dm -= cw * ws; }
-        if (bt & G_N) { eN = ghost_eval<TC, TE>(G, gidx[id + P], e, id, ws); dm -= cn * ws; }
-        if (bt & G_S) { eS = ghost_eval<TC, TE>(G, gidx[id - P], e, id, ws); dm -= cs * ws; }
+        if (bt & G_E) { eE = ghost_eval<TC, TE>(G, gidx[id + 1], e, id, ws); dm -= c.ce * ws; }
+        if (bt & G_W) { eW = ghost_eval<TC, TE>(G, gidx[id - 1], e, id, ws); dm -= c.cw * ws; }
+        if (bt & G_N) { eN = ghost_eval<TC, TE>(G, gidx[id + P], e, id, ws); dm -= c.cn * ws; }
+        if (bt & G_S) { eS = ghost_eval<TC, TE>(G, gidx[id - P], e, id, ws); dm -= c.cs * ws; }
     }
-    Le = ce * eE + cw * eW + cn * eN + cs * eS - dd * (TC)e[id];
+    Le = c.ce * eE + c.cw * eW + c.cn * eN + c.cs * eS - c.dd * (TC)e[id];
     D = dm;
+}
+
+template <typename TC, typename TE, bool LVL0>
+__device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id,
+                                    uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+    lap_p<TC, TE, LVL0>(L, e, i, j, id, L.pitch, bt, G, gidx, Le, D);
+}
+
+// Diagonal of a coarse-level operator (no IBM ghosts below the finest level).
+template <typename TC>
+__device__ __forceinline__ TC lap_diag(const LevelDev& L, int i, int j, uint8_t bt) {
+    return lap_coef<TC>(L, i, j, bt).dd;
 }
 
 // ------------------------------------------------------ step bookkeeping
@@ -225,9 +250,9 @@ __device__ __forceinline__ void b_step_begin(InstState* S, int n, int vb) {
 __device__ __forceinline__ void b_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev gh = ldg_struct(&G[g]);
+    const GhostDev& gh = G[g];
     if (gh.qown < 0) return;
-    const InstDev in = ldg_struct(&I[gh.inst]);
+    const InstDev& in = I[gh.inst];
     double fac = in.dt * in.uc * 2.0 / gh.qh;
     in.qbu[gh.qown] = in.qbu[gh.qown] - fac * (in.qbu[gh.qown] - in.u[gh.adj]);
     in.qbv[gh.qown] = in.qbv[gh.qown] - fac * (in.qbv[gh.qown] - in.v[gh.adj]);
@@ -240,8 +265,8 @@ __device__ __forceinline__ void b_ghost_gather(const GhostDev* __restrict__ G, i
                                int comps, double* __restrict__ gval, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev gh = ldg_struct(&G[g]);
-    const InstDev in = ldg_struct(&I[gh.inst]);
+    const GhostDev& gh = G[g];
+    const InstDev& in = I[gh.inst];
     if (comps & 1) {
         double a = ghost_const(gh, in.qbu, gh.cu);
 #pragma unroll
@@ -266,8 +291,8 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
                                 int comps, const double* __restrict__ gval, int vb) {
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
-    const GhostDev gh = ldg_struct(&G[g]);
-    const InstDev in = ldg_struct(&I[gh.inst]);
+    const GhostDev& gh = G[g];
+    const InstDev& in = I[gh.inst];
     if (comps & 1) in.u[gh.cell] = gval[3 * (size_t)g];
     if (comps & 2) in.v[gh.cell] = gval[3 * (size_t)g + 1];
     if (comps & 4) in.p[gh.cell] = gval[3 * (size_t)g + 2];
@@ -279,7 +304,7 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
 __device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     int i, j;
     tile_ij(t, i, j);
     if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
@@ -319,7 +344,7 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
                              double* __restrict__ part, int parity, int vb) {
     if ((int)vb < ntiles) {
         const Tile t = ldg_struct(&tiles[vb]);
-        const InstDev in = ldg_struct(&I[t.inst]);
+        const InstDev& in = I[t.inst];
         const int st = S[t.inst].pred_state;
         if (st == ST_DONE) return;
         const double* su = parity ? in.u2 : in.u;
@@ -359,8 +384,8 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
     } else {
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
-        const GhostDev gh = ldg_struct(&G[g]);
-        const InstDev in = ldg_struct(&I[gh.inst]);
+        const GhostDev& gh = G[g];
+        const InstDev& in = I[gh.inst];
         const int st = S[gh.inst].pred_state;
         if (st == ST_DONE) return;
         const double* su = parity ? in.u2 : in.u;
@@ -387,7 +412,7 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     const int st = S[k].pred_state;
     bool active = false;
     if (st == ST_ACTIVE) {
@@ -424,7 +449,7 @@ __device__ __forceinline__ double face_v(const InstDev& in, const double* v, int
 __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            double* __restrict__ part, int to_final, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -453,7 +478,7 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
 __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     double r[1];
     inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
     if (threadIdx.x == 0) S[k].bmean = in.singular ? r[0] / in.area : 0.0;
@@ -478,10 +503,10 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev L = ldg_struct(&LV[in.lev0]);
+    const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -510,7 +535,7 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
                                 const double* __restrict__ part, int start, LoopCtl* ctl,
                                 unsigned long long handle, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     bool active = false;
     if (S[k].ppe_state == ST_ACTIVE) {
         double r[4];
@@ -545,10 +570,10 @@ template <typename T>
 __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev L = ldg_struct(&LV[in.lev0]);
+    const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -565,10 +590,10 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev L = ldg_struct(&LV[in.lev0]);
+    const LevelDev& L = LV[in.lev0];
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
     double* zo = which == 0 ? in.kph : in.ksh;
     double* y = which == 0 ? in.kv : in.kt;
@@ -597,7 +622,7 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
 __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int which, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     if (S[k].ppe_state != ST_ACTIVE) return;
     double r[2];
     inst_sum<2>(part, in.tile_beg, in.tile_cnt, r);
@@ -612,10 +637,10 @@ template <typename T>
 __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev L = ldg_struct(&LV[in.lev0]);
+    const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -631,10 +656,10 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev L = ldg_struct(&LV[in.lev0]);
+    const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -660,7 +685,7 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev L = ldg_struct(&LV[t.lev]);
+    const LevelDev& L = LV[t.lev];
     if (S[L.inst].ppe_state != ST_ACTIVE) return;
     int i, j, id;
     uint8_t bt;
@@ -683,9 +708,9 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev C = ldg_struct(&LV[t.lev]);
+    const LevelDev& C = LV[t.lev];
     if (S[C.inst].ppe_state != ST_ACTIVE) return;
-    const LevelDev F = ldg_struct(&LV[C.parent]);
+    const LevelDev& F = LV[C.parent];
     int I0, J0;
     tile_ij(t, I0, J0);
     if (I0 < 1 || I0 > C.NX || J0 < 1 || J0 > C.NY) return;
@@ -729,9 +754,9 @@ template <typename T>
 __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev F = ldg_struct(&LV[t.lev]);
+    const LevelDev& F = LV[t.lev];
     if (S[F.inst].ppe_state != ST_ACTIVE) return;
-    const LevelDev C = ldg_struct(&LV[F.child]);
+    const LevelDev& C = LV[F.child];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -754,129 +779,362 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
     fe[id] += val;
 }
 
-// Coarsest level: e = 0, then red-black SOR sweeps.  Levels that fit are
-// staged in shared memory (same arithmetic, in the same order, as the
-// global-memory form below).
+// ------------------------------------------------- small levels (sub-cycle)
+//
+// The coarse levels of one instance with at most SUB_MAX_CELLS cells are run
+// by one block in shared memory.  The restriction into the first of them
+// (with its zero-start sweep) is an ordinary tile phase; the block then
+// stages, for every small level, e, e2, r and the stencil bytes (compact rows
+// of nx cells, ghost ring included), the 1-D metric arrays and the
+// prolongation tables, and runs the rest of the V-cycle on them.  The
+// per-cell arithmetic is that of b_restrict / b_smooth / b_prolong.
+
+// View of a staged level; the pointers are formed from the dynamic shared
+// memory base and the offsets of its SubHdr, so accesses compile to
+// shared-memory loads and stores.
 template <typename T>
-__device__ void coarse_solve_level(const LevelDev& L) {
-    T* e = (T*)L.e;
-    const T* r = (const T*)L.r;
-    const T om = (T)COARSE_OMEGA;
-    const int NXY = L.NX * L.NY;
-    const int nx = L.nx, ncell = L.nx * L.ny;
-    if (ncell <= COARSE_SMEM_CELLS && L.nx <= 256 && L.ny <= 256) {
-        __shared__ T se[COARSE_SMEM_CELLS], sr[COARSE_SMEM_CELLS];
-        __shared__ uint8_t sb[COARSE_SMEM_CELLS];
-        __shared__ T skx[256], sky[256], six[256], siy[256];
-        const T* kx = LvA<T>::kx(L);
-        const T* ky = LvA<T>::ky(L);
-        const T* ix = LvA<T>::ix(L);
-        const T* iy = LvA<T>::iy(L);
-        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-            const int i = q % nx, j = q / nx, id = i + j * L.pitch;
-            se[q] = (T)0;
-            sr[q] = r[id];
-            sb[q] = __ldg(&L.bits[id]);
-        }
-        for (int q = threadIdx.x; q < L.nx; q += blockDim.x) { skx[q] = kx[q]; six[q] = ix[q]; }
-        for (int q = threadIdx.x; q < L.ny; q += blockDim.x) { sky[q] = ky[q]; siy[q] = iy[q]; }
-        __syncthreads();
-        for (int it = 0; it < COARSE_SWEEPS; it++) {
-            for (int col = 0; col < 2; col++) {
-                for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
-                    const int i = 1 + q % L.NX, j = 1 + q / L.NX;
-                    if (((i + j) & 1) != col) continue;
-                    const int id = i + j * nx;
-                    const uint8_t bt = sb[id];
-                    if (!(bt & 0x0F)) continue;
-                    const T cE = skx[i] * six[i], cW = skx[i - 1] * six[i];
-                    const T cN = sky[j] * siy[j], cS = sky[j - 1] * siy[j];
-                    const T ce = (bt & B_E) ? cE : (T)0, cw = (bt & B_W) ? cW : (T)0;
-                    const T cn = (bt & B_N) ? cN : (T)0, cs = (bt & B_S) ? cS : (T)0;
-                    T dd = ce + cw + cn + cs;
-                    if (L.dirmask) {
-                        if (i == L.NX && (L.dirmask & (1 << 1))) dd += (T)2 * cE;
-                        if (i == 1 && (L.dirmask & (1 << 0))) dd += (T)2 * cW;
-                        if (j == L.NY && (L.dirmask & (1 << 3))) dd += (T)2 * cN;
-                        if (j == 1 && (L.dirmask & (1 << 2))) dd += (T)2 * cS;
-                    }
-                    const T Le = ce * se[id + 1] + cw * se[id - 1] + cn * se[id + nx] + cs * se[id - nx] - dd * se[id];
-                    se[id] = se[id] + om * (Le - sr[id]) * rcpa(dd);
-                }
-                __syncthreads();
+struct SubGeo {
+    T *e, *e2, *r, *kx, *ix, *dw, *pwx, *ky, *iy, *dh, *pwy;
+    int *pI, *pIn, *pJ, *pJn;
+    uint8_t* b;
+    signed char *psx, *psy;
+    int NX, NY, nx, ny, dirmask, child, depth;
+};
+
+template <typename T>
+__device__ __forceinline__ SubGeo<T> sub_geo(unsigned char* sm, const SubHdr& h) {
+    unsigned char* p = sm + h.base;
+    const SubLayout& o = h.o;
+    SubGeo<T> g;
+    g.e = (T*)(p + o.e); g.e2 = (T*)(p + o.e2); g.r = (T*)(p + o.r);
+    g.kx = (T*)(p + o.kx); g.ix = (T*)(p + o.ix); g.dw = (T*)(p + o.dw); g.pwx = (T*)(p + o.pwx);
+    g.ky = (T*)(p + o.ky); g.iy = (T*)(p + o.iy); g.dh = (T*)(p + o.dh); g.pwy = (T*)(p + o.pwy);
+    g.pI = (int*)(p + o.pI); g.pIn = (int*)(p + o.pIn); g.pJ = (int*)(p + o.pJ); g.pJn = (int*)(p + o.pJn);
+    g.b = p + o.b;
+    g.psx = (signed char*)(p + o.psx); g.psy = (signed char*)(p + o.psy);
+    g.NX = h.NX; g.NY = h.NY; g.nx = h.nx; g.ny = h.ny;
+    g.dirmask = h.dirmask; g.child = h.child; g.depth = h.depth;
+    return g;
+}
+
+// dst[q] = src[row-major q with row pitch `pitch`], q < n, rows of nx; eight
+// loads in flight per thread.
+template <typename U>
+__device__ __forceinline__ void sub_load_rows(U* dst, const U* src, int nx, int n, int pitch) {
+    for (int base = threadIdx.x; base < n; base += 8 * blockDim.x) {
+        U v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int q = base + k * (int)blockDim.x;
+            if (q < n) {
+                const int j = q / nx;
+                v[k] = src[q + j * (pitch - nx)];
             }
         }
-        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-            const int i = q % nx, j = q / nx;
-            e[i + j * L.pitch] = se[q];
-        }
-        __syncthreads();
-        return;
-    }
-    const int n = L.pitch * L.ny;
-    for (int id = threadIdx.x; id < n; id += blockDim.x) e[id] = (T)0;
-    __syncthreads();
-    for (int it = 0; it < COARSE_SWEEPS; it++) {
-        for (int col = 0; col < 2; col++) {
-            for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
-                const int i = 1 + q % L.NX, j = 1 + q / L.NX;
-                if (((i + j) & 1) != col) continue;
-                const int id = i + j * L.pitch;
-                const uint8_t bt = __ldg(&L.bits[id]);
-                if (!(bt & 0x0F)) continue;
-                T Le, D;
-                lap<T, T, false>(L, e, i, j, id, bt, nullptr, nullptr, Le, D);
-                e[id] = e[id] + om * (Le - r[id]) * rcpa(D);
-            }
-            __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int q = base + k * (int)blockDim.x;
+            if (q < n) dst[q] = v[k];
         }
     }
 }
 
-// Small coarse levels of one instance (vb = instance) in one block: the
-// restriction into the first small level, its smoothing, every coarser level
-// down to the RB-SOR solve and back up.  Same per-cell bodies and order as
-// the tile phases; tiles of a level are processed one after another.
+template <typename U>
+__device__ __forceinline__ void sub_load_ro(U* dst, const U* src, int n) {
+    for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = __ldg(&src[q]);
+}
+
 template <typename T>
-__device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const int* __restrict__ sub,
-                                           const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
-                                           const InstState* __restrict__ S, const GhostDev* __restrict__ G,
-                                           int pre, int post, int vb) {
+__device__ __forceinline__ LapCoef<T> sub_coef(const SubGeo<T>& g, int i, int j, uint8_t bt) {
+    const T ixi = g.ix[i], iyj = g.iy[j];
+    const T cE = g.kx[i] * ixi, cW = g.kx[i - 1] * ixi;
+    const T cN = g.ky[j] * iyj, cS = g.ky[j - 1] * iyj;
+    LapCoef<T> c;
+    c.ce = (bt & B_E) ? cE : (T)0;
+    c.cw = (bt & B_W) ? cW : (T)0;
+    c.cn = (bt & B_N) ? cN : (T)0;
+    c.cs = (bt & B_S) ? cS : (T)0;
+    T dd = c.ce + c.cw + c.cn + c.cs;
+    if (g.dirmask) {
+        if (i == g.NX && (g.dirmask & (1 << 1))) dd += (T)2 * cE;
+        if (i == 1 && (g.dirmask & (1 << 0))) dd += (T)2 * cW;
+        if (j == g.NY && (g.dirmask & (1 << 3))) dd += (T)2 * cN;
+        if (j == 1 && (g.dirmask & (1 << 2))) dd += (T)2 * cS;
+    }
+    c.dd = dd;
+    return c;
+}
+
+template <typename T>
+__device__ __forceinline__ T sub_lap(const SubGeo<T>& g, const T* e, int i, int j, int id, uint8_t bt, T& D) {
+    const LapCoef<T> c = sub_coef<T>(g, i, j, bt);
+    const int P = g.nx;
+    D = c.dd;
+    return c.ce * e[id + 1] + c.cw * e[id - 1] + c.cn * e[id + P] + c.cs * e[id - P] - c.dd * e[id];
+}
+
+// Weighted-Jacobi sweep of a staged level (src -> dst by parity).
+template <typename T>
+__device__ __forceinline__ void sub_smooth(const SubGeo<T>& g, int src_alt, T om) {
+    const T* src = src_alt ? g.e2 : g.e;
+    T* dst = src_alt ? g.e : g.e2;
+    const int NX = g.NX, nx = g.nx, NXY = g.NX * g.NY;
+    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
+        const int j = 1 + q / NX, i = 1 + q - (j - 1) * NX, id = i + j * nx;
+        const uint8_t bt = g.b[id];
+        if (!(bt & 0x0F)) continue;
+        T D;
+        const T Le = sub_lap<T>(g, src, i, j, id, bt, D);
+        dst[id] = src[id] + om * (Le - g.r[id]) * rcpa(D);
+    }
+}
+
+// Area-weighted restriction of the fine residual r - L e (buffer fine_alt of
+// staged level f) onto staged level c; a middle level also takes its first
+// sweep from zero (e = -om r / D).
+template <typename T>
+__device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>& f, int fine_alt, T om) {
+    const T* fe = fine_alt ? f.e2 : f.e;
+    const int NX = c.NX, NXY = c.NX * c.NY;
+    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
+        const int J0 = 1 + q / NX, I0 = 1 + q - (J0 - 1) * NX, cid = I0 + J0 * c.nx;
+        const uint8_t cb = c.b[cid];
+        if (!(cb & 0x0F)) {
+            c.r[cid] = (T)0;
+            continue;
+        }
+        T acc = (T)0;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int i = 2 * I0 - 1 + di, j = 2 * J0 - 1 + dj;
+                if (i > f.NX || j > f.NY) continue;
+                const int id = i + j * f.nx;
+                const uint8_t bt = f.b[id];
+                if (!(bt & 0x0F)) continue;
+                T D;
+                const T Le = sub_lap<T>(f, fe, i, j, id, bt, D);
+                acc += (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
+            }
+        const T rv = acc / (c.dw[I0] * c.dh[J0]);
+        c.r[cid] = rv;
+        if (c.child >= 0) c.e[cid] = -om * rv * rcpa(sub_coef<T>(c, I0, J0, cb).dd);
+    }
+}
+
+// Bilinear prolongation of staged level c's correction onto staged level f.
+template <typename T>
+__device__ __forceinline__ void sub_prolong(const SubGeo<T>& f, const SubGeo<T>& c, int fine_alt, int coarse_alt) {
+    const T* ce = (coarse_alt && c.child >= 0) ? c.e2 : c.e;
+    T* fe = fine_alt ? f.e2 : f.e;
+    const int NX = f.NX, nx = f.nx, NXY = f.NX * f.NY, CP = c.nx;
+    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
+        const int j = 1 + q / NX, i = 1 + q - (j - 1) * NX, id = i + j * nx;
+        if (!(f.b[id] & 0x0F)) continue;
+        const int I0 = f.pI[i], In = f.pIn[i], J0 = f.pJ[j], Jn = f.pJn[j];
+        const T wx = f.pwx[i], wy = f.pwy[j];
+        const T sx = (T)f.psx[i], sy = (T)f.psy[j];
+        T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
+        const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
+        w00 = (c.b[c00] & 0x0F) ? w00 : (T)0;
+        w10 = (c.b[c10] & 0x0F) ? w10 : (T)0;
+        w01 = (c.b[c01] & 0x0F) ? w01 : (T)0;
+        w11 = (c.b[c11] & 0x0F) ? w11 : (T)0;
+        const T sw = w00 + w10 + w01 + w11;
+        const T val = (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
+        fe[id] += val;
+    }
+}
+
+// Synchronises the first n threads of the block (n a multiple of 32).
+__device__ __forceinline__ void sub_sync(int n) {
+    if (n == 32) __syncwarp();
+    else if (n == (int)blockDim.x) __syncthreads();
+    else asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
+}
+
+// Coarsest level: e = 0, then red-black SOR sweeps.  Each thread keeps the
+// operator of its cells (at most SUB_COARSE_PER_THREAD) in registers; only
+// the warps that own cells take part.
+template <typename T>
+__device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g) {
+    const T om = (T)COARSE_OMEGA;
+    const int NX = g.NX, nx = g.nx, NXY = g.NX * g.NY;
+    const int nthr = min((int)blockDim.x, (NXY + 31) & ~31);
+    for (int q = threadIdx.x; q < nx * g.ny; q += blockDim.x) g.e[q] = (T)0;
+    __syncthreads();
+    if ((int)threadIdx.x < nthr) {
+        int id[SUB_COARSE_PER_THREAD], col[SUB_COARSE_PER_THREAD];
+        T ce[SUB_COARSE_PER_THREAD], cw[SUB_COARSE_PER_THREAD], cn[SUB_COARSE_PER_THREAD],
+            cs[SUB_COARSE_PER_THREAD], dd[SUB_COARSE_PER_THREAD], rd[SUB_COARSE_PER_THREAD],
+            rr[SUB_COARSE_PER_THREAD];
+#pragma unroll
+        for (int k = 0; k < SUB_COARSE_PER_THREAD; k++) {
+            const int q = threadIdx.x + k * nthr;
+            id[k] = -1;
+            col[k] = 2;
+            ce[k] = cw[k] = cn[k] = cs[k] = dd[k] = rd[k] = rr[k] = (T)0;
+            if (q < NXY) {
+                const int j = 1 + q / NX, i = 1 + q - (j - 1) * NX, c = i + j * nx;
+                const uint8_t bt = g.b[c];
+                if (bt & 0x0F) {
+                    const LapCoef<T> lc = sub_coef<T>(g, i, j, bt);
+                    id[k] = c;
+                    col[k] = (i + j) & 1;
+                    ce[k] = lc.ce; cw[k] = lc.cw; cn[k] = lc.cn; cs[k] = lc.cs; dd[k] = lc.dd;
+                    rd[k] = rcpa(lc.dd);
+                    rr[k] = g.r[c];
+                }
+            }
+        }
+        T* e = g.e;
+        for (int it = 0; it < COARSE_SWEEPS; it++) {
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+#pragma unroll
+                for (int k = 0; k < SUB_COARSE_PER_THREAD; k++) {
+                    if (col[k] != cc) continue;
+                    const int c = id[k];
+                    const T ec = e[c];
+                    const T Le = ce[k] * e[c + 1] + cw[k] * e[c - 1] + cn[k] * e[c + nx] + cs[k] * e[c - nx] - dd[k] * ec;
+                    e[c] = ec + om * (Le - rr[k]) * rd[k];
+                }
+                sub_sync(nthr);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Stages the geometry of instance k's small levels (headers, metric arrays,
+// prolongation tables, stencil bytes) in the block's dynamic shared memory.
+template <typename T>
+__device__ __forceinline__ void sub_stage_geometry(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
+                                                   const InstDev* __restrict__ I, int k, unsigned char* sm) {
+    SubHdr* hdr = (SubHdr*)sm;
+    const InstDev& in = I[k];
+    const int lb = sub[k];
+    const int ns = in.lev0 + in.nlev - lb;
+    if ((int)threadIdx.x < ns) {
+        size_t off = SUB_HDR_BYTES;
+        for (int q = 0; q < (int)threadIdx.x; q++) off += sub_level_bytes(LV[lb + q].nx, LV[lb + q].ny, (int)sizeof(T));
+        const LevelDev& L = LV[lb + threadIdx.x];
+        SubHdr h;
+        h.o = sub_layout(L.nx, L.ny, (int)sizeof(T));
+        h.base = (unsigned)off;
+        h.NX = L.NX; h.NY = L.NY; h.nx = L.nx; h.ny = L.ny;
+        h.dirmask = L.dirmask; h.child = L.child; h.depth = L.depth;
+        h.ns = ns;
+        hdr[threadIdx.x] = h;
+    }
+    __syncthreads();
+    for (int s = 0; s < ns; s++) {
+        const LevelDev& L = LV[lb + s];
+        const SubGeo<T> g = sub_geo<T>(sm, hdr[s]);
+        const int n = g.nx * g.ny;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int j = q / g.nx;
+            g.b[q] = __ldg(&L.bits[q + j * (L.pitch - g.nx)]);
+        }
+        sub_load_ro<T>(g.kx, LvA<T>::kx(L), g.nx);
+        sub_load_ro<T>(g.ix, LvA<T>::ix(L), g.nx);
+        sub_load_ro<T>(g.dw, LvA<T>::dw(L), g.nx);
+        sub_load_ro<T>(g.ky, LvA<T>::ky(L), g.ny);
+        sub_load_ro<T>(g.iy, LvA<T>::iy(L), g.ny);
+        sub_load_ro<T>(g.dh, LvA<T>::dh(L), g.ny);
+        if (g.child >= 0) {
+            sub_load_ro<T>(g.pwx, LvA<T>::pwx(L), g.nx);
+            sub_load_ro<T>(g.pwy, LvA<T>::pwy(L), g.ny);
+            sub_load_ro<int>(g.pI, L.pI, g.nx);
+            sub_load_ro<int>(g.pIn, L.pIn, g.nx);
+            sub_load_ro<int>(g.pJ, L.pJ, g.ny);
+            sub_load_ro<int>(g.pJn, L.pJn, g.ny);
+            sub_load_ro<signed char>(g.psx, L.psx, g.nx);
+            sub_load_ro<signed char>(g.psy, L.psy, g.ny);
+        }
+    }
+    __syncthreads();
+}
+
+// Small coarse levels of one instance (vb = instance) in one block, from the
+// first small level (restricted by the tile phase before) down to the RB-SOR
+// solve and back up; the first small level's correction is written back to
+// its global buffer for the prolongation above it.  sm: dynamic shared
+// memory of at least the instance's staged bytes; geometry_staged: the block
+// staged this instance's geometry there before (persistent kernel).
+template <typename T>
+__device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
+                                           const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                           int pre, int post, unsigned char* sm, bool geometry_staged, int vb) {
     const int k = vb;
     if (S[k].ppe_state != ST_ACTIVE) return;
-    const InstDev in = ldg_struct(&I[k]);
-    const int lb = sub[k];
-    const int top = in.lev0 + in.nlev - 1;
-    // descend: restriction into each small level, then its pre-smoothing
-    for (int lv = lb; lv <= top; lv++) {
-        const LevelDev C = ldg_struct(&LV[lv]);
-        const int fa = parity_after_pre(C.depth - 1, pre);
-        for (int t = C.tbeg; t < C.tbeg + C.tcnt; t++) b_restrict<T>(tall, LV, I, S, G, fa, t);
-        __syncthreads();
-        if (lv == top) {
-            coarse_solve_level<T>(C);
+    if (!geometry_staged) sub_stage_geometry<T>(sub, LV, I, k, sm);
+    const SubHdr* hdr = (const SubHdr*)sm;
+    const int ns = hdr[0].ns;
+    const T om = (T)I[k].omega;
+    const LevelDev& L0 = LV[sub[k]];
+    {
+        const SubGeo<T> g = sub_geo<T>(sm, hdr[0]);
+        const int n = g.nx * g.ny;
+        if (g.child >= 0) sub_load_rows<T>(g.e, (const T*)L0.e, g.nx, n, L0.pitch);  // zero-start sweep of the tile phase
+        else
+            for (int q = threadIdx.x; q < n; q += blockDim.x) g.e[q] = (T)0;
+        sub_load_rows<T>(g.r, (const T*)L0.r, g.nx, n, L0.pitch);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) g.e2[q] = (T)0;
+        for (int s = 1; s < ns; s++) {
+            const SubGeo<T> c = sub_geo<T>(sm, hdr[s]);
+            const int m = c.nx * c.ny;
+            for (int q = threadIdx.x; q < m; q += blockDim.x) {
+                c.e[q] = (T)0;
+                c.e2[q] = (T)0;
+            }
+        }
+    }
+    __syncthreads();
+    // descend
+    for (int s = 0; s < ns; s++) {
+        const SubGeo<T> g = sub_geo<T>(sm, hdr[s]);
+        if (s > 0) {
+            const SubGeo<T> f = sub_geo<T>(sm, hdr[s - 1]);
+            sub_restrict<T>(g, f, parity_after_pre(f.depth, pre), om);
+            __syncthreads();
+        }
+        if (g.child < 0) {
+            sub_coarse_solve<T>(g);
             break;
         }
         int cur = 0;
         for (int q = 1; q < pre; q++) {
-            for (int t = C.tbeg; t < C.tbeg + C.tcnt; t++) b_smooth<T>(tall, LV, I, S, G, 0, cur, t);
+            sub_smooth<T>(g, cur, om);
             __syncthreads();
             cur ^= 1;
         }
     }
-    // ascend: prolongation into each small middle level, then its post-smoothing
-    for (int lv = top - 1; lv >= lb; lv--) {
-        const LevelDev F = ldg_struct(&LV[lv]);
-        int cur = parity_after_pre(F.depth, pre);
-        for (int t = F.tbeg; t < F.tbeg + F.tcnt; t++)
-            b_prolong<T>(tall, LV, S, cur, parity_after_post(F.depth + 1, pre, post), t);
+    // ascend
+    for (int s = ns - 2; s >= 0; s--) {
+        const SubGeo<T> f = sub_geo<T>(sm, hdr[s]);
+        const SubGeo<T> c = sub_geo<T>(sm, hdr[s + 1]);
+        int cur = parity_after_pre(f.depth, pre);
+        sub_prolong<T>(f, c, cur, parity_after_post(f.depth + 1, pre, post));
         __syncthreads();
         for (int q = 0; q < post; q++) {
-            for (int t = F.tbeg; t < F.tbeg + F.tcnt; t++) b_smooth<T>(tall, LV, I, S, G, 0, cur, t);
+            sub_smooth<T>(f, cur, om);
             __syncthreads();
             cur ^= 1;
         }
     }
+    // write back the first small level's correction (the buffer its last sweep ended on)
+    const SubGeo<T> g = sub_geo<T>(sm, hdr[0]);
+    const int res = (g.child < 0) ? 0 : parity_after_post(g.depth, pre, post);
+    const T* src = res ? g.e2 : g.e;
+    T* dst = (T*)(res ? L0.e2 : L0.e);
+    const int n = g.nx * g.ny;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int j = q / g.nx;
+        dst[q + j * (L0.pitch - g.nx)] = src[q];
+    }
+    __syncthreads();  // the block may stage another instance in the same memory
 }
 
 // ------------------------------------------------------------ projection
@@ -884,7 +1142,7 @@ __device__ __forceinline__ void b_subcycle(const Tile* __restrict__ tall, const 
 __device__ __forceinline__ void b_p_finalize(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                              const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     if (!in.singular) return;
     int i, j;
     tile_ij(t, i, j);
@@ -914,7 +1172,7 @@ __device__ __forceinline__ double corr_v(const InstDev& in, int j, int id) {
 __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                           double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
-    const InstDev in = ldg_struct(&I[t.inst]);
+    const InstDev& in = I[t.inst];
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -962,7 +1220,7 @@ __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const 
 __device__ __forceinline__ void b_correct_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                  const double* __restrict__ part, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     double m = 0.0, a[2] = {0.0, 0.0};
     for (int t = threadIdx.x; t < in.tile_cnt; t += blockDim.x) {
         const double* q = part + (size_t)(in.tile_beg + t) * NPART;
@@ -1015,7 +1273,7 @@ __device__ __forceinline__ double bil(const double* q, int c, int P, double xi, 
 
 __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
     const int k = vb;
-    const InstDev in = ldg_struct(&I[k]);
+    const InstDev& in = I[k];
     if (!in.body) {
         if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
         return;

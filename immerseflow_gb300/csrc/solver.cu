@@ -466,8 +466,8 @@ ifx_status setup_persistent(ifx_solver* S) {
     CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, S->device));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device));
     if (!coop) return IFX_OK;
-    if (S->prec == IFX_PREC_FP64) CUDA_TRY(persist_occupancy<double>(&bps));
-    else CUDA_TRY(persist_occupancy<float>(&bps));
+    if (S->prec == IFX_PREC_FP64) CUDA_TRY(persist_occupancy<double>(&bps, S->sub_bytes));
+    else CUDA_TRY(persist_occupancy<float>(&bps, S->sub_bytes));
     if (bps < 1) return IFX_OK;
     S->persist_grid = sms * std::min(bps, 4);
     if (S->persist_grid > 64 * 32) S->persist_grid = 64 * 32;
@@ -496,6 +496,7 @@ ifx_status setup_persistent(ifx_solver* S) {
     P.lmax = S->lmax;
     P.mg_pre = S->mg_pre;
     P.mg_post = S->mg_post;
+    P.sub_bytes = S->sub_bytes;
     P.pred_pairs = max_pred_pairs(S);
     P.ppe_bodies = max_ppe_bodies(S);
     CUDA_TRY(cudaStreamSynchronize(S->stream));
@@ -639,10 +640,25 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dupload(S, &gidx_d, gidx));
         d.gidx = gidx_d;
         const int nl = (int)I.lev.size();
-        // first level handled inside one block per instance (>= 1, <= coarsest)
+        // first level handled inside one block per instance (>= 1, <= coarsest): at
+        // most SUB_MAX_CELLS cells, and it and every coarser level staged in
+        // shared memory within SUB_SMEM_MAX bytes
+        const int tsz = S->prec == IFX_PREC_FP64 ? 8 : 4;
+        auto staged = [&](int from) {
+            size_t b = SUB_HDR_BYTES;
+            for (int l = from; l < nl; l++) b += sub_level_bytes(I.lev[l].nx, I.lev[l].ny, tsz);
+            return b;
+        };
         int lb = nl - 1;
         for (int l = 1; l < nl; l++)
-            if ((long long)I.lev[l].NX * I.lev[l].NY <= SUB_MAX_CELLS) { lb = l; break; }
+            if ((long long)I.lev[l].NX * I.lev[l].NY <= SUB_MAX_CELLS && staged(l) <= (size_t)SUB_SMEM_MAX) {
+                lb = l;
+                break;
+            }
+        if (nl < 2 || nl - lb > kSubLevels || staged(lb) > (size_t)SUB_SMEM_MAX ||
+            (long long)I.lev[nl - 1].NX * I.lev[nl - 1].NY > (long long)TILE_THREADS * SUB_COARSE_PER_THREAD)
+            return set_error(IFX_ERR_ARG, "grid too small or too elongated for the multigrid hierarchy");
+        S->sub_bytes = std::max(S->sub_bytes, (int)staged(lb));
         for (int l = 0; l < nl; l++) {
             HostLevel& L = I.lev[l];
             IFX_TRY(dupload(S, &L.d_kx, L.kx)); IFX_TRY(dupload(S, &L.d_ky, L.ky));
@@ -689,9 +705,11 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
                 I.tile_beg = (int)hT0.size();
                 I.tile_cnt = (int)tl.size();
                 hT0.insert(hT0.end(), tl.begin(), tl.end());
-            } else if (l < lb) {
-                tre[l].insert(tre[l].end(), tl.begin(), tl.end());
-                tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
+            } else {
+                // tile phases: restriction into every level down to the first
+                // small one, smoothing and prolongation above it
+                if (l <= lb) tre[l].insert(tre[l].end(), tl.begin(), tl.end());
+                if (l < lb) tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
             }
         }
         hSub.push_back(I.lev_base + lb);
@@ -728,6 +746,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     }
     IFX_TRY(dupload(S, &S->dTall, hTall));
     IFX_TRY(dupload(S, &S->dSub, hSub));
+    if (S->prec == IFX_PREC_FP64) CUDA_TRY(subcycle_smem_limit<double>(S->sub_bytes));
+    else CUDA_TRY(subcycle_smem_limit<float>(S->sub_bytes));
     IFX_TRY(dalloc(S, &S->dPart, (size_t)S->nt0 * NPART));
     IFX_TRY(dalloc(S, &S->dS, n));
     IFX_TRY(dalloc(S, &S->dCtl, 1));
@@ -795,6 +815,7 @@ int seq_vcycle(Seq& q) {
     for (int l = 1; l < L; l++) {
         if (S->ntre[l] == 0) break;
         q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, parity_after_pre(l - 1, pre), st));
+        if (S->ntsm[l] == 0) continue;
         int cur = 0;
         for (int k = 1; k < pre; k++) {
             q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, 0, cur, st));
@@ -802,7 +823,7 @@ int seq_vcycle(Seq& q) {
         }
     }
     // small levels of every instance: one block each
-    q.add(launch_subcycle<T>(S->dTall, S->dSub, (int)S->inst.size(), S->dLV, S->dI, S->dS, S->dG, pre, post, st));
+    q.add(launch_subcycle<T>(S->dSub, (int)S->inst.size(), S->dLV, S->dI, S->dS, pre, post, S->sub_bytes, st));
     for (int l = L - 2; l >= 0; l--) {
         const Tile* tl = l == 0 ? S->dT0 : S->dTsm[l];
         const int nt = l == 0 ? S->nt0 : S->ntsm[l];
@@ -1539,6 +1560,37 @@ extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, do
     if (cells) *cells = c;
     if (S->prec == IFX_PREC_FP64) return profile_kernel<double>(S, kernel, reps, ms_per_launch);
     return profile_kernel<float>(S, kernel, reps, ms_per_launch);
+}
+
+extern "C" ifx_status ifx_trace_step(ifx_solver* S, int cap, double* us, int* n) {
+    if (!S || !us || !n || cap < 1) return set_error(IFX_ERR_ARG, "ifx_trace_step: bad argument");
+    if (S->mode != IFX_MODE_METHOD || S->persist_grid == 0) return set_error(IFX_ERR_STATE, "ifx_trace_step needs the persistent kernel");
+    CUDA_TRY(cudaSetDevice(S->device));
+    long long* d = nullptr;
+    IFX_TRY(dalloc(S, &d, (size_t)cap + 1));
+    CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(long long) * (cap + 1), S->stream));
+    S->plan.trace = d;
+    S->plan.trace_cap = cap + 1;
+    S->plan.nsteps = 1;
+    cudaError_t e = S->prec == IFX_PREC_FP64 ? launch_persist_step<double>(S->plan, S->persist_grid, S->stream)
+                                             : launch_persist_step<float>(S->plan, S->persist_grid, S->stream);
+    S->plan.trace = nullptr;
+    S->plan.trace_cap = 0;
+    if (e != cudaSuccess) return cuerr(e, "ifx_trace_step");
+    std::vector<long long> h(cap + 1);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(long long) * (cap + 1), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    int khz = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S->device));
+    int k = 0;
+    while (k < cap && h[k + 1] != 0) {
+        us[k] = (double)(h[k + 1] - h[k]) / (khz * 1e-3);
+        k++;
+    }
+    *n = k;
+    S->steps_done += 1;
+    S->launches += 1;
+    return check_states(S);
 }
 
 extern "C" ifx_status ifx_synchronize(ifx_solver* S) {

@@ -226,6 +226,11 @@ ifx_status ifx_synchronize(ifx_solver* s);
  * *cells receives the interior cells one launch covers.  Scratch buffers and
  * the per-step iteration state are overwritten; the flow state is not. */
 ifx_status ifx_profile_kernel(ifx_solver* s, int kernel, int reps, double* ms_per_launch, long long* cells);
+/* Measurement hook (no reference counterpart): runs one time step with the
+ * persistent per-step kernel and records the SM clock of block 0 after every
+ * grid barrier; us[k] receives the time between barrier k and k+1 in
+ * microseconds (SM clock rate), *n the number of intervals (<= cap). */
+ifx_status ifx_trace_step(ifx_solver* s, int cap, double* us, int* n);
 void       ifx_destroy(ifx_solver* s);
 
 #ifdef __cplusplus
