@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
+                    help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
     return ap.parse_args()
 
 
@@ -117,7 +119,7 @@ def measured_peak():
 
 def committed_traffic():
     """DRAM bytes per launch of the roofline kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "smooth_l0_cylinder_384x256.md")
+    p = os.path.join(ROOT, "profiles", "persist_step_cylinder_384x256.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -193,6 +195,18 @@ def main():
         torch.cuda.synchronize()
 
     import immerseflow_gb300 as ifx
+
+    if args.profile:
+        prec = capi.PREC_MIXED if args.profile == "mixed" else capi.PREC_FP64
+        cfg, _, _ = cases.cylinder(precision=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.step(args.warmup)
+        s.synchronize()
+        torch.cuda.nvtx.range_push("step")
+        s.step(args.steps)
+        s.synchronize()
+        torch.cuda.nvtx.range_pop()
+        return 0
 
     flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
