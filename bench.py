@@ -24,10 +24,19 @@ roofline  : the dominant kernel is the persistent per-step kernel (one launch
               (coarse levels) + 2 applies x (s + 25) + updates 33 + s + 25 +
               s + 65;
             phase_roofline times the finest-level smoothing sweep alone;
-cpu_baseline: the CPU oracle (same scheme, FP64, all host threads).
+cpu_baseline: the CPU oracle (same scheme, FP64, all host threads);
+batched   : the batched sweep (256 seeded instances of uneven grid, Re and
+            ellipse, one batched solver each for mixed and plain FP64,
+            execution mode picked by the autotuner), Mcell-updates/s, solves/s
+            of 500-step runs, error of mixed vs FP64 per instance;
+served    : a seeded Poisson request stream through the continuous-batching
+            server (real-time arrivals, cohorts admitted by device memory),
+            solves/s, Mcell-updates/s and p50/p99 latency, the two smallest
+            requests re-run alone in FP64 for the error.
 
 --impl reference times the CPU restatement of the reference scheme (the
-reference's own code is CUDA-only) on the same workload.
+reference's pressure solver does not compile and it has no projection or
+immersed boundary) on the same workload.
 Under torchrun with N>1 every rank advances its own replica (weak scaling,
 no collective on the data path).
 """
@@ -39,6 +48,8 @@ import subprocess
 import sys
 import tempfile
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -55,6 +66,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch", type=int, default=256, help="instances of the batched sweep (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--serve", type=int, default=48, help="requests of the served stream (0: skip)")
+    ap.add_argument("--rate", type=float, default=16.0, help="served stream arrival rate [1/s]")
     ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
     return ap.parse_args()
@@ -127,6 +142,107 @@ def committed_traffic():
     except Exception:
         pass
     return None
+
+
+def rel_l2(a, b):
+    return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
+
+
+def copy_cfg(cfg, precision):
+    c = type(cfg).from_buffer_copy(cfg)
+    c.precision = precision
+    return c
+
+
+def batched_sweep(ifx, capi, cases, n_inst, steps, warm):
+    """Batched sweep: n_inst uneven instances (seeded), mixed vs plain FP64, each
+    advanced in one batch; execution mode chosen by the autotuner."""
+    res, fields = {}, {}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        specs = cases.batch_sample(count=n_inst, seed=0, precision=prec)
+        ncell = sum(c.nx * c.ny for c, _, _ in specs)
+        s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+        s.step(max(1, warm - 2))
+        mode, _ = s.autotune(steps=1)
+        s.step(2)
+        l0 = s.stats().kernel_launches
+        s.step(steps)
+        ms = s.last_step_ms()
+        launches = s.stats().kernel_launches - l0
+        its = [s.stats(k).last_ppe_iters for k in range(n_inst)]
+        ads = [s.stats(k).last_ad_iters for k in range(n_inst)]
+        fields[name] = [(s.get(capi.FIELD_U, inst=k), s.get(capi.FIELD_V, inst=k), s.stats(k).cd) for k in range(n_inst)]
+        res[name] = {"value": ncell * steps / (ms * 1e-3) / 1e6, "unit": METRIC, "ms_per_step": ms / steps,
+                     "exec": {0: "persistent", 1: "graph"}.get(mode, str(mode)), "gpu_launches": launches,
+                     "ppe_iters_mean": float(np.mean(its)), "ppe_iters_max": int(max(its)),
+                     "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes()}
+        res["cells"] = ncell
+        s.close()
+    errs = [rel_l2(np.concatenate([um.ravel(), vm.ravel()]), np.concatenate([u6.ravel(), v6.ravel()]))
+            for (um, vm, _), (u6, v6, _) in zip(fields["mixed"], fields["fp64"])]
+    cds = [abs(cm - c6) / max(abs(c6), 1e-12) for (_, _, cm), (_, _, c6) in zip(fields["mixed"], fields["fp64"])]
+    res.update({"workload": f"batched sweep: {n_inst} instances (seed 0), grids log-uniform 64x64..512x384, "
+                            "Re U[50,300], ellipse aspect U[0.1,1], angle U[-30,30] deg",
+                "instances": n_inst, "timed_steps": steps,
+                "speedup_mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+                "solves_per_s_500_steps": n_inst / (res["mixed"]["ms_per_step"] * 1e-3 * 500),
+                "accuracy_vs_fp64": {"rel_l2_velocity_max": max(errs), "rel_l2_velocity_median": float(np.median(errs)),
+                                     "cd_rel_err_max": max(cds)},
+                "l2": "inputs larger than L2 (device_bytes)"})
+    return res
+
+
+def served_stream(ifx, capi, cases, nreq, rate, budget):
+    """Served stream through the continuous-batching server: seeded Poisson
+    arrivals in real time; latency = completion - arrival."""
+    stream = cases.served_stream(nreq, rate, seed=0, precision=capi.PREC_MIXED, nmin=64, nmax=512, smin=20, smax=200)
+    srv = ifx.Server(budget, max_cohort=32)
+    arr, done, work, spec_of = {}, {}, 0, {}
+    t0 = time.perf_counter()
+    i = 0
+    ticks = 0
+    peak_cohorts = 0
+    while len(done) < nreq:
+        now = time.perf_counter() - t0
+        while i < nreq and stream[i][0] <= now:
+            t_arr, cfg, xf, yf, n = stream[i]
+            rid = srv.submit(cfg, xf, yf, n)
+            arr[rid] = t_arr
+            spec_of[rid] = (cfg, xf, yf, n)
+            work += cfg.nx * cfg.ny * n
+            i += 1
+        info = srv.info()
+        if info["running"] == 0 and info["waiting"] == 0:
+            if i < nreq:
+                time.sleep(max(0.0, stream[i][0] - (time.perf_counter() - t0)))
+            continue
+        srv.tick()
+        ticks += 1
+        peak_cohorts = max(peak_cohorts, srv.info()["cohorts"])
+        tnow = time.perf_counter() - t0
+        for rid in srv.poll():
+            done[rid] = tnow
+    lat = np.array([done[r] - arr[r] for r in arr]) * 1e3
+    span = max(done.values()) - stream[0][0]
+    # accuracy: the two smallest requests re-run alone in plain FP64
+    small = sorted(arr, key=lambda r: spec_of[r][0].nx * spec_of[r][0].ny)[:2]
+    errs = []
+    for r in small:
+        cfg, xf, yf, n = spec_of[r]
+        s = ifx.Solver.create(copy_cfg(cfg, capi.PREC_FP64), xf, yf)
+        s.step(n)
+        a = np.concatenate([srv.result(r, capi.FIELD_U).ravel(), srv.result(r, capi.FIELD_V).ravel()])
+        b = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+        errs.append(rel_l2(a, b))
+        s.close()
+    srv.close()
+    return {"workload": f"served stream: {nreq} requests (seed 0), Poisson arrivals at {rate}/s, cylinder or ellipse, "
+                        "grids log-uniform 64^2..512^2, Re U[50,1000], 20..200 steps each",
+            "requests": nreq, "solves_per_s": nreq / span, "value": work / span / 1e6, "unit": METRIC,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max())},
+            "ticks": ticks, "peak_cohorts": peak_cohorts, "hbm_budget_bytes": budget, "precision": "mixed",
+            "accuracy_vs_fp64": {"rel_l2_velocity_max": max(errs), "requests_checked": len(errs)}}
 
 
 def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
@@ -318,6 +434,10 @@ def main():
                        "ppe_mean_fp64": sum(pits64) / len(pits64)},
         "clocks": clocks,
     }
+    if args.batch > 0:
+        line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup)
+    if args.serve > 0:
+        line["served"] = served_stream(ifx, capi, cases, args.serve, args.rate, 64 << 30)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
         n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)

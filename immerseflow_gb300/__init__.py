@@ -51,7 +51,31 @@ _SIGS = {
     "ifx_trace_step": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int)]),
     "ifx_profile_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "ifx_destroy": (None, [C.c_void_p]),
+    "ifx_step_async": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
+    "ifx_step_wait": (C.c_int, [C.c_void_p]),
+    "ifx_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_get_exec_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_set_instance_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "ifx_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "ifx_estimate_bytes": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_size_t)]),
+    "ifx_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "ifx_server_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Config), _dp, _dp, C.c_int, C.POINTER(C.c_longlong)]),
+    "ifx_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_server_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int, C.POINTER(C.c_int)]),
+    "ifx_server_request_state": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ifx_server_result": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, _dp, C.c_size_t]),
+    "ifx_server_request_stats": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(Stats)]),
+    "ifx_server_release": (C.c_int, [C.c_void_p, C.c_longlong]),
+    "ifx_server_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_size_t)]),
+    "ifx_server_destroy": (None, [C.c_void_p]),
 }
+
+EXEC_DEFAULT, EXEC_PERSISTENT, EXEC_GRAPH, EXEC_HOST = -1, 0, 1, 2
+REQ_WAITING, REQ_RUNNING, REQ_FINISHED, REQ_FAILED = 0, 1, 2, 3
 
 
 class IFXError(RuntimeError):
@@ -218,6 +242,34 @@ class Solver:
     def synchronize(self):
         _check(lib().ifx_synchronize(self._h))
 
+    def step_async(self, n=1):
+        _check(lib().ifx_step_async(self._h, int(n)))
+
+    def step_wait(self):
+        _check(lib().ifx_step_wait(self._h))
+
+    def set_exec_mode(self, mode):
+        _check(lib().ifx_set_exec_mode(self._h, int(mode)))
+
+    def exec_mode(self):
+        m = C.c_int()
+        _check(lib().ifx_get_exec_mode(self._h, C.byref(m)))
+        return m.value
+
+    def autotune(self, steps=2):
+        """Pick the fastest execution mode by timing; state is restored.  Returns (mode, ms/step)."""
+        m, ms = C.c_int(), C.c_double()
+        _check(lib().ifx_autotune(self._h, int(steps), C.byref(m), C.byref(ms)))
+        return m.value, ms.value
+
+    def set_active(self, inst, active):
+        _check(lib().ifx_set_instance_active(self._h, int(inst), 1 if active else 0))
+
+    def device_bytes(self):
+        b = C.c_size_t()
+        _check(lib().ifx_device_bytes(self._h, C.byref(b)))
+        return b.value
+
     def close(self):
         if self._h:
             lib().ifx_destroy(self._h)
@@ -230,7 +282,76 @@ class Solver:
             pass
 
 
+def estimate_bytes(cfg):
+    b = C.c_size_t()
+    _check(lib().ifx_estimate_bytes(C.byref(cfg), C.byref(b)))
+    return b.value
+
+
+class Server:
+    """Continuous-batching solve server (ifx_server_* in the C ABI)."""
+
+    def __init__(self, hbm_budget_bytes, max_cohort=64, exec_mode=None):
+        self._h = C.c_void_p()
+        _check(lib().ifx_server_create(int(hbm_budget_bytes), int(max_cohort), C.byref(self._h)))
+        if exec_mode is not None:
+            _check(lib().ifx_server_set_exec_mode(self._h, int(exec_mode)))
+
+    def submit(self, cfg, xf, yf, nsteps):
+        xf = np.ascontiguousarray(xf, dtype=np.float64)
+        yf = np.ascontiguousarray(yf, dtype=np.float64)
+        rid = C.c_longlong()
+        _check(lib().ifx_server_submit(self._h, C.byref(cfg), _dptr(xf), _dptr(yf), int(nsteps), C.byref(rid)))
+        return rid.value
+
+    def tick(self):
+        n = C.c_int()
+        _check(lib().ifx_server_tick(self._h, C.byref(n)))
+        return n.value
+
+    def poll(self, cap=1024):
+        ids = (C.c_longlong * cap)()
+        n = C.c_int()
+        _check(lib().ifx_server_poll(self._h, ids, cap, C.byref(n)))
+        return list(ids[:n.value])
+
+    def state(self, rid):
+        st, done, nx, ny = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib().ifx_server_request_state(self._h, int(rid), C.byref(st), C.byref(done), C.byref(nx), C.byref(ny)))
+        return st.value, done.value, nx.value, ny.value
+
+    def result(self, rid, field):
+        _, _, nx, ny = self.state(rid)
+        out = np.empty(nx * ny)
+        _check(lib().ifx_server_result(self._h, int(rid), int(field), _dptr(out), out.size))
+        return out.reshape(ny, nx)
+
+    def stats(self, rid):
+        s = Stats()
+        _check(lib().ifx_server_request_stats(self._h, int(rid), C.byref(s)))
+        return s
+
+    def release(self, rid):
+        _check(lib().ifx_server_release(self._h, int(rid)))
+
+    def info(self):
+        w, r, c, b = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(lib().ifx_server_info(self._h, C.byref(w), C.byref(r), C.byref(c), C.byref(b)))
+        return {"waiting": w.value, "running": r.value, "cohorts": c.value, "used_bytes": b.value}
+
+    def close(self):
+        if self._h:
+            lib().ifx_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 from .interface import ImmerseFlow  # noqa: E402  (mirror of the reference object)
 
-__all__ = ["Config", "Stats", "default_config", "Solver", "ImmerseFlow", "IFXError", "config_read",
-           "grid_read", "write_tecplot", "lib", "capi"]
+__all__ = ["Config", "Stats", "default_config", "Solver", "Server", "ImmerseFlow", "IFXError", "config_read",
+           "grid_read", "write_tecplot", "estimate_bytes", "lib", "capi"]

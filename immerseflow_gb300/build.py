@@ -28,6 +28,7 @@ SOURCES = [
     ("solver.cu", []),
     ("io.cpp", ["-x", "cu"]),
     ("noalloc.cu", []),
+    ("server.cpp", ["-x", "cu"]),
 ]
 
 

@@ -145,6 +145,7 @@ struct alignas(16) InstDev {
     int singular, dirmask, body, lev0, nlev;
     int tile_beg, tile_cnt;      // level-0 tiles (for per-instance partial sums)
     int ghost_beg, ghost_cnt;
+    int retired;                 // set between steps: a step leaves the instance unchanged
     double dt, re, dtre, idt, omega;
     double ad_lim, ppe_tol;
     int ad_itermax, ppe_itermax, n_fluid, mixed_inner;

@@ -61,6 +61,9 @@ struct ifx_solver {
     double last_ms = 0.0;
     long long launches = 0;
     std::vector<void*> allocs;       // every device allocation, freed at destroy
+    size_t device_bytes = 0;         // their total size
+    int exec_override = -1;          // IFX_EXEC_*; -1: environment / default
+    int pending_mode = 0, pending_steps = 0;  // steps issued and not yet waited for
     std::vector<ifx::Instance> inst;
 
     // batched device tables

@@ -7,7 +7,7 @@
 namespace ifx {
 
 // ---- method path (kernels_method.cu)
-cudaError_t launch_step_begin(InstState* S, int n, cudaStream_t s);
+cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, cudaStream_t s);
 cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStream_t s);
 cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int comps, double* gval,
                               cudaStream_t s);

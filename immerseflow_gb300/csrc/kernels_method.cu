@@ -19,11 +19,13 @@
 // path, float for the mixed path).
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "method_body.cuh"
 
 namespace ifx {
 
-__global__ void k_step_begin(InstState* S, int n) { b_step_begin(S, n, blockIdx.x); }
+__global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n) { b_step_begin(I, S, n, blockIdx.x); }
 __global__ void k_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I) { b_outflow(G, ng, I, blockIdx.x); }
 __global__ void k_ghost_gather(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
                                int comps, double* __restrict__ gval) { b_ghost_gather(G, ng, I, comps, gval, blockIdx.x); }
@@ -94,8 +96,8 @@ __global__ void k_forces(const InstDev* __restrict__ I, InstState* __restrict__ 
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
-cudaError_t launch_step_begin(InstState* S, int n, cudaStream_t s) {
-    k_step_begin<<<nblk(n, 128), 128, 0, s>>>(S, n);
+cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, cudaStream_t s) {
+    k_step_begin<<<nblk(n, 128), 128, 0, s>>>(I, S, n);
     return cudaGetLastError();
 }
 cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStream_t s) {
@@ -195,7 +197,17 @@ cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const Inst
 }
 template <typename T>
 cudaError_t subcycle_smem_limit(int bytes) {
-    return cudaFuncSetAttribute(k_subcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    // the attribute belongs to the kernel, shared by every solver on the device: only raise it
+    static std::mutex mu;
+    static int cur[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = dev >= 0 && dev < 64 ? dev : 0;
+    std::lock_guard<std::mutex> g(mu);
+    if (bytes <= cur[dev]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_subcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur[dev] = bytes;
+    return e;
 }
 template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,

@@ -16,6 +16,8 @@
 // next barrier, and the host reports the failure (the GPU is left usable).
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "ifx_persist.h"
 #include "method_body.cuh"
 
@@ -136,7 +138,7 @@ __device__ bool vcycle(const PersistPlan& P, int* res, unsigned long long& ep) {
 template <typename T>
 __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     const int n = P.ninst;
-    FOR_VB(nchunks(n)) b_step_begin(P.S, n, vb);
+    FOR_VB(nchunks(n)) b_step_begin(P.I, P.S, n, vb);
     FOR_VB(nchunks(P.ng)) b_outflow(P.G, P.ng, P.I, vb);
     BAR();
     if (!ghost_fill(P, 3, ep)) return false;
@@ -240,8 +242,21 @@ cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) 
 
 template <typename T>
 cudaError_t persist_occupancy(int* blocks_per_sm, int smem_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(k_persist_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-    if (e != cudaSuccess) return e;
+    {
+        // the attribute belongs to the kernel, shared by every solver on the device: only raise it
+        static std::mutex mu;
+        static int cur[64] = {0};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        dev = dev >= 0 && dev < 64 ? dev : 0;
+        std::lock_guard<std::mutex> g(mu);
+        if (smem_bytes > cur[dev]) {
+            cudaError_t e = cudaFuncSetAttribute(k_persist_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 smem_bytes);
+            if (e != cudaSuccess) return e;
+            cur[dev] = smem_bytes;
+        }
+    }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_persist_step<T>, TILE_THREADS,
                                                          (size_t)smem_bytes);
 }

@@ -236,12 +236,13 @@ __device__ __forceinline__ TC lap_diag(const LevelDev& L, int i, int j, uint8_t 
 
 // ------------------------------------------------------ step bookkeeping
 
-__device__ __forceinline__ void b_step_begin(InstState* S, int n, int vb) {
+__device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, InstState* S, int n, int vb) {
     int k = vb * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    S[k].pred_state = ST_ACTIVE;
+    const int st = I[k].retired ? ST_DONE : ST_ACTIVE;
+    S[k].pred_state = st;
     S[k].pred_iters = 0;
-    S[k].ppe_state = ST_ACTIVE;
+    S[k].ppe_state = st;
     S[k].ppe_iters = 0;
 }
 
@@ -253,6 +254,7 @@ __device__ __forceinline__ void b_outflow(const GhostDev* __restrict__ G, int ng
     const GhostDev& gh = G[g];
     if (gh.qown < 0) return;
     const InstDev& in = I[gh.inst];
+    if (in.retired) return;
     double fac = in.dt * in.uc * 2.0 / gh.qh;
     in.qbu[gh.qown] = in.qbu[gh.qown] - fac * (in.qbu[gh.qown] - in.u[gh.adj]);
     in.qbv[gh.qown] = in.qbv[gh.qown] - fac * (in.qbv[gh.qown] - in.v[gh.adj]);
@@ -267,6 +269,7 @@ __device__ __forceinline__ void b_ghost_gather(const GhostDev* __restrict__ G, i
     if (g >= ng) return;
     const GhostDev& gh = G[g];
     const InstDev& in = I[gh.inst];
+    if (in.retired) return;
     if (comps & 1) {
         double a = ghost_const(gh, in.qbu, gh.cu);
 #pragma unroll
@@ -293,6 +296,7 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
     if (g >= ng) return;
     const GhostDev& gh = G[g];
     const InstDev& in = I[gh.inst];
+    if (in.retired) return;
     if (comps & 1) in.u[gh.cell] = gval[3 * (size_t)g];
     if (comps & 2) in.v[gh.cell] = gval[3 * (size_t)g + 1];
     if (comps & 4) in.p[gh.cell] = gval[3 * (size_t)g + 2];
@@ -305,6 +309,7 @@ __device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const
                            const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
+    if (in.retired) return;
     int i, j;
     tile_ij(t, i, j);
     if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
@@ -450,6 +455,7 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
                            double* __restrict__ part, int to_final, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
+    if (in.retired) return;
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -479,6 +485,7 @@ __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, Inst
                              const double* __restrict__ part, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
+    if (in.retired) return;
     double r[1];
     inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
     if (threadIdx.x == 0) S[k].bmean = in.singular ? r[0] / in.area : 0.0;
@@ -1143,6 +1150,7 @@ __device__ __forceinline__ void b_p_finalize(const Tile* __restrict__ tiles, con
                              const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
+    if (in.retired) return;
     if (!in.singular) return;
     int i, j;
     tile_ij(t, i, j);
@@ -1173,6 +1181,7 @@ __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const 
                           double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
+    if (in.retired) return;
     int i, j;
     tile_ij(t, i, j);
     const int P = in.pitch, id = i + j * P;
@@ -1221,6 +1230,7 @@ __device__ __forceinline__ void b_correct_reduce(const InstDev* __restrict__ I, 
                                  const double* __restrict__ part, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
+    if (in.retired) return;
     double m = 0.0, a[2] = {0.0, 0.0};
     for (int t = threadIdx.x; t < in.tile_cnt; t += blockDim.x) {
         const double* q = part + (size_t)(in.tile_beg + t) * NPART;
@@ -1274,6 +1284,7 @@ __device__ __forceinline__ double bil(const double* q, int c, int P, double xi, 
 __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
+    if (in.retired) return;
     if (!in.body) {
         if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
         return;

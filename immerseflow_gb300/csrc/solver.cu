@@ -51,6 +51,7 @@ ifx_status dalloc(ifx_solver* S, T** out, size_t n) {
     size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
     CUDA_TRY(cudaMalloc(&p, bytes));
     S->allocs.push_back(p);
+    S->device_bytes += bytes;
     CUDA_TRY(cudaMemsetAsync(p, 0, bytes, S->stream));
     *out = (T*)p;
     return IFX_OK;
@@ -843,7 +844,7 @@ void seq_pre(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    q.add(launch_step_begin(S->dS, n, st));
+    q.add(launch_step_begin(S->dI, S->dS, n, st));
     q.add(launch_outflow(S->dG, S->ng, S->dI, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;  // ghost fill is two kernels
@@ -1035,6 +1036,8 @@ ifx_status check_states(ifx_solver* S) {
 // Execution mode from IFX_EXEC: "persistent" (default when cooperative
 // launch is available), "graph", or "host" (IFX_NO_GRAPH=1 also selects host).
 int exec_mode(const ifx_solver* S) {
+    if (S->exec_override == 0 && S->persist_grid > 0) return 0;
+    if (S->exec_override == 1 || S->exec_override == 2) return S->exec_override;
     const char* e = std::getenv("IFX_EXEC");
     const char* ng = std::getenv("IFX_NO_GRAPH");
     if (ng && ng[0] == '1') return 2;
@@ -1043,11 +1046,15 @@ int exec_mode(const ifx_solver* S) {
     return S->persist_grid > 0 ? 0 : 1;
 }
 
+// Issues nsteps time steps on the solver's stream.  The host-loop mode reads
+// the convergence state after every loop body, so it completes the steps here.
 template <typename T>
-ifx_status step_method(ifx_solver* S, int nsteps) {
+ifx_status step_launch(ifx_solver* S, int nsteps) {
     if (S->poisoned) return set_error(IFX_ERR_STATE, "a grid barrier timed out earlier; recreate the solver");
     const int mode = exec_mode(S);
     S->use_graph = mode == 1;
+    S->pending_mode = mode;
+    S->pending_steps = nsteps;
     CUDA_TRY(cudaEventRecord(S->ev0, S->stream));
     if (mode == 0) {
         S->plan.nsteps = nsteps;
@@ -1060,6 +1067,14 @@ ifx_status step_method(ifx_solver* S, int nsteps) {
         for (int s = 0; s < nsteps; s++) IFX_TRY(step_method_host<T>(S));
     }
     CUDA_TRY(cudaEventRecord(S->ev1, S->stream));
+    return IFX_OK;
+}
+
+// Waits for the steps issued by step_launch and checks the solver state.
+ifx_status step_finish(ifx_solver* S) {
+    const int nsteps = S->pending_steps, mode = S->pending_mode;
+    if (nsteps == 0) return IFX_OK;
+    S->pending_steps = 0;
     CUDA_TRY(cudaEventSynchronize(S->ev1));
     float ms = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
@@ -1074,7 +1089,7 @@ ifx_status step_method(ifx_solver* S, int nsteps) {
         }
     }
     ifx_status st = check_states(S);
-    if (S->use_graph) {
+    if (mode == 1) {
         // kernels executed by the graph: fixed segments plus loop bodies
         int pairs = 0, bodies = 0;
         for (size_t k = 0; k < S->inst.size(); k++) {
@@ -1340,8 +1355,136 @@ extern "C" ifx_status ifx_step(ifx_solver* S, int nsteps) {
     if (nsteps == 0) return IFX_OK;
     CUDA_TRY(cudaSetDevice(S->device));
     if (S->mode == IFX_MODE_REFERENCE) return step_reference(S, nsteps);
-    if (S->prec == IFX_PREC_FP64) return step_method<double>(S, nsteps);
-    return step_method<float>(S, nsteps);
+    IFX_TRY(step_finish(S));
+    if (S->prec == IFX_PREC_FP64) IFX_TRY(step_launch<double>(S, nsteps));
+    else IFX_TRY(step_launch<float>(S, nsteps));
+    return step_finish(S);
+}
+
+extern "C" ifx_status ifx_step_async(ifx_solver* S, int nsteps) {
+    if (!S || nsteps < 0) return set_error(IFX_ERR_ARG, "ifx_step_async: bad argument");
+    if (nsteps == 0) return IFX_OK;
+    CUDA_TRY(cudaSetDevice(S->device));
+    if (S->mode == IFX_MODE_REFERENCE) return step_reference(S, nsteps);
+    IFX_TRY(step_finish(S));
+    if (S->prec == IFX_PREC_FP64) return step_launch<double>(S, nsteps);
+    return step_launch<float>(S, nsteps);
+}
+
+extern "C" ifx_status ifx_step_wait(ifx_solver* S) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_step_wait: null solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    return step_finish(S);
+}
+
+extern "C" ifx_status ifx_set_exec_mode(ifx_solver* S, int mode) {
+    if (!S || mode < IFX_EXEC_DEFAULT || mode > IFX_EXEC_HOST) return set_error(IFX_ERR_ARG, "ifx_set_exec_mode: bad argument");
+    if (mode == IFX_EXEC_PERSISTENT && S->persist_grid == 0)
+        return set_error(IFX_ERR_STATE, "persistent execution is not available for this solver");
+    IFX_TRY(step_finish(S));
+    S->exec_override = mode;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_exec_mode(ifx_solver* S, int* mode) {
+    if (!S || !mode) return set_error(IFX_ERR_ARG, "ifx_get_exec_mode: bad argument");
+    *mode = S->mode == IFX_MODE_METHOD ? exec_mode(S) : IFX_EXEC_HOST;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_set_instance_active(ifx_solver* S, int inst, int active) {
+    if (!S || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_set_instance_active: bad argument");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_set_instance_active needs a METHOD-mode solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    Instance& I = S->inst[inst];
+    I.dev.retired = active ? 0 : 1;
+    CUDA_TRY(cudaMemcpyAsync(&S->dI[inst].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+namespace {
+// Device copy of the state a time step carries to the next one (cell and
+// face velocities, convection history, pressure, outflow boundary values and
+// the per-instance iteration state).
+struct StateSnapshot {
+    std::vector<std::pair<void*, size_t>> items;  // (source, bytes)
+    std::vector<void*> copies;
+    ifx_status take(ifx_solver* S) {
+        for (const Instance& I : S->inst) {
+            const InstDev& d = I.dev;
+            const size_t nc = I.ncell * sizeof(double), nq = 4 * (size_t)I.qstride * sizeof(double);
+            for (void* p : {(void*)d.u, (void*)d.v, (void*)d.U, (void*)d.V, (void*)d.Nu, (void*)d.Nv, (void*)d.p})
+                items.push_back({p, nc});
+            items.push_back({(void*)d.qbu, nq});
+            items.push_back({(void*)d.qbv, nq});
+        }
+        items.push_back({(void*)S->dS, S->inst.size() * sizeof(InstState)});
+        for (auto& it : items) {
+            void* c = nullptr;
+            CUDA_TRY(cudaMalloc(&c, it.second));
+            copies.push_back(c);
+            CUDA_TRY(cudaMemcpyAsync(c, it.first, it.second, cudaMemcpyDeviceToDevice, S->stream));
+        }
+        CUDA_TRY(cudaStreamSynchronize(S->stream));
+        return IFX_OK;
+    }
+    ifx_status restore(ifx_solver* S) {
+        for (size_t k = 0; k < items.size(); k++)
+            CUDA_TRY(cudaMemcpyAsync(items[k].first, copies[k], items[k].second, cudaMemcpyDeviceToDevice, S->stream));
+        CUDA_TRY(cudaStreamSynchronize(S->stream));
+        return IFX_OK;
+    }
+    ~StateSnapshot() {
+        for (void* c : copies) cudaFree(c);
+    }
+};
+}  // namespace
+
+extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double* ms_per_step) {
+    if (!S || steps < 1) return set_error(IFX_ERR_ARG, "ifx_autotune: bad argument");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_autotune needs a METHOD-mode solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    StateSnapshot snap;
+    IFX_TRY(snap.take(S));
+    const long long steps0 = S->steps_done;
+    const int saved = S->exec_override;
+    std::vector<int> cand;
+    if (S->persist_grid > 0) cand.push_back(IFX_EXEC_PERSISTENT);
+    cand.push_back(IFX_EXEC_GRAPH);
+    int best = cand[0];
+    double best_ms = 1e300;
+    ifx_status st = IFX_OK;
+    for (int m : cand) {
+        S->exec_override = m;
+        st = ifx_step(S, 1);  // warm-up (builds the graph on first use)
+        if (st == IFX_OK) st = ifx_step(S, steps);
+        if (st == IFX_OK) st = snap.restore(S);
+        if (st != IFX_OK) break;
+        const double ms = S->last_ms / steps;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = m;
+        }
+    }
+    S->steps_done = steps0;
+    if (st != IFX_OK) {
+        S->exec_override = saved;
+        snap.restore(S);
+        return st;
+    }
+    S->exec_override = best;
+    if (chosen) *chosen = best;
+    if (ms_per_step) *ms_per_step = best_ms;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_device_bytes(const ifx_solver* S, size_t* bytes) {
+    if (!S || !bytes) return set_error(IFX_ERR_ARG, "ifx_device_bytes: bad argument");
+    *bytes = S->device_bytes;
+    return IFX_OK;
 }
 
 extern "C" ifx_status ifx_ppe_reference(ifx_solver* S, int* iters) {
@@ -1353,6 +1496,7 @@ extern "C" ifx_status ifx_ppe_reference(ifx_solver* S, int* iters) {
 
 extern "C" ifx_status ifx_get_field_i(ifx_solver* S, int inst, int field, double* host, size_t n) {
     if (!S || !host || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_field: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     const Instance& I = S->inst[inst];
     size_t need;
     IFX_TRY(field_size(I, field, &need));
@@ -1408,6 +1552,7 @@ extern "C" ifx_status ifx_get_field(ifx_solver* S, int field, double* host, size
 
 extern "C" ifx_status ifx_set_field_i(ifx_solver* S, int inst, int field, const double* host, size_t n) {
     if (!S || !host || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_set_field: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     const Instance& I = S->inst[inst];
     if (field != IFX_FIELD_U && field != IFX_FIELD_V && field != IFX_FIELD_P)
         return set_error(IFX_ERR_ARG, "ifx_set_field: only u, v, p can be set");
@@ -1431,6 +1576,7 @@ extern "C" ifx_status ifx_set_field(ifx_solver* S, int field, const double* host
 
 extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
     if (!S || !dir) return set_error(IFX_ERR_ARG, "ifx_write_results: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     const Instance& I = S->inst[0];
     const size_t n = (size_t)I.nx * I.ny;
     std::vector<double> q(n);
@@ -1446,6 +1592,7 @@ extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
 
 extern "C" ifx_status ifx_get_stats(ifx_solver* S, int inst, ifx_stats* out) {
     if (!S || !out || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_stats: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     std::memset(out, 0, sizeof(*out));
     out->steps = S->steps_done;
     out->kernel_launches = S->launches;
@@ -1487,6 +1634,7 @@ extern "C" ifx_status ifx_forces(ifx_solver* S, double* cd, double* cl) {
 extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* cells, int* nb, double* wu,
                                          double* wp, double* bi_ip, int* count) {
     if (!S || !count || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_ibm_ghosts: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     const Instance& I = S->inst[inst];
     *count = (S->mode == IFX_MODE_METHOD) ? I.n_ibm : 0;
     if (*count == 0 || cap <= 0) return IFX_OK;
@@ -1519,6 +1667,7 @@ extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* 
 
 extern "C" ifx_status ifx_last_step_ms(ifx_solver* S, double* ms) {
     if (!S || !ms) return set_error(IFX_ERR_ARG, "ifx_last_step_ms: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     *ms = S->last_ms;
     return IFX_OK;
 }
@@ -1527,7 +1676,7 @@ template <typename T>
 static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms) {
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    CUDA_TRY(launch_step_begin(S->dS, n, st));
+    CUDA_TRY(launch_step_begin(S->dI, S->dS, n, st));
     auto one = [&]() -> cudaError_t {
         switch (kernel) {
             case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, st);
@@ -1552,6 +1701,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
 extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, double* ms_per_launch,
                                          long long* cells) {
     if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 4) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     if (kernel == 4 && S->persist_grid == 0) return set_error(IFX_ERR_STATE, "cooperative launch unavailable");
     if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_profile_kernel needs a METHOD-mode solver");
     CUDA_TRY(cudaSetDevice(S->device));
@@ -1564,6 +1714,7 @@ extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, do
 
 extern "C" ifx_status ifx_trace_step(ifx_solver* S, int cap, double* us, int* n) {
     if (!S || !us || !n || cap < 1) return set_error(IFX_ERR_ARG, "ifx_trace_step: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     if (S->mode != IFX_MODE_METHOD || S->persist_grid == 0) return set_error(IFX_ERR_STATE, "ifx_trace_step needs the persistent kernel");
     CUDA_TRY(cudaSetDevice(S->device));
     long long* d = nullptr;
@@ -1595,6 +1746,7 @@ extern "C" ifx_status ifx_trace_step(ifx_solver* S, int cap, double* us, int* n)
 
 extern "C" ifx_status ifx_synchronize(ifx_solver* S) {
     if (!S) return set_error(IFX_ERR_ARG, "ifx_synchronize: null solver");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     return IFX_OK;
 }

@@ -168,6 +168,35 @@ ifx_status ifx_get_dims(const ifx_solver* s, int inst, int* nx, int* ny);
 /* One reference time step is ImmerseFlow::ADsolver (src/include/ADSolver.cu:268-395)
  * in REFERENCE mode; in METHOD mode it is predictor -> PPE -> projection. */
 ifx_status ifx_step(ifx_solver* s, int nsteps);
+
+/* Asynchronous form (no reference counterpart): ifx_step_async issues nsteps
+ * steps on the solver's own stream and returns; ifx_step_wait waits for them
+ * and checks the state (every other call on the handle waits first).  Handles
+ * on different streams overlap on the device.  The host-loop execution mode
+ * completes the steps inside ifx_step_async. */
+ifx_status ifx_step_async(ifx_solver* s, int nsteps);
+ifx_status ifx_step_wait(ifx_solver* s);
+
+/* Execution of a METHOD-mode step; all modes give bit-identical results. */
+#define IFX_EXEC_DEFAULT    (-1) /* IFX_EXEC environment variable, else persistent */
+#define IFX_EXEC_PERSISTENT 0    /* one cooperative launch per ifx_step call        */
+#define IFX_EXEC_GRAPH      1    /* one CUDA-graph launch per step (device loops)   */
+#define IFX_EXEC_HOST       2    /* one launch per phase, loops driven by the host  */
+ifx_status ifx_set_exec_mode(ifx_solver* s, int mode);
+ifx_status ifx_get_exec_mode(ifx_solver* s, int* mode);
+
+/* Autotuner (no reference counterpart): times `steps` steps in each available
+ * execution mode (after one warm-up step each), restores the solver state
+ * afterwards, and keeps the fastest mode.  The modes give bit-identical
+ * results, so tuning never changes an answer. */
+ifx_status ifx_autotune(ifx_solver* s, int steps, int* chosen_mode, double* ms_per_step);
+
+/* Batch membership (no reference counterpart): an inactive instance is left
+ * unchanged by later steps while the others advance. */
+ifx_status ifx_set_instance_active(ifx_solver* s, int inst, int active);
+/* Device memory held by the handle, bytes. */
+ifx_status ifx_device_bytes(const ifx_solver* s, size_t* bytes);
+
 /* ImmerseFlow::PPESolver (src/include/PPESolver.cu:137-205): Jacobi Laplace with
  * p = 100 on the i=0 and j=0 ghosts, stopped on the signed residual sum. */
 ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
@@ -217,6 +246,41 @@ ifx_status ifx_get_stats(ifx_solver* s, int inst, ifx_stats* out);
  * the solver's own stream. */
 ifx_status ifx_last_step_ms(ifx_solver* s, double* ms);
 ifx_status ifx_synchronize(ifx_solver* s);
+
+/* ------------------------------------------------------------------ server */
+/* Continuous-batching solve server (no reference counterpart; the reference
+ * runs one case per process, src/main.cu:75-102).  Submitted METHOD-mode cases
+ * wait in FIFO order; each ifx_server_tick admits the waiting requests that
+ * fit in the device-memory budget as one batched cohort with its own stream
+ * and state kept on the device, then advances every live cohort by one time
+ * step (all cohorts issued before any is waited for, so they overlap on the
+ * GPU).  A request that completed its steps is copied out (u, v, p, stats)
+ * and stops computing; a cohort whose requests all finished frees its memory.
+ * Results do not depend on the cohort a request ran in.  One host thread per
+ * server. */
+typedef struct ifx_server ifx_server;
+#define IFX_REQ_WAITING  0
+#define IFX_REQ_RUNNING  1
+#define IFX_REQ_FINISHED 2
+#define IFX_REQ_FAILED   3
+/* Device bytes one METHOD-mode instance of this configuration needs (estimate). */
+ifx_status ifx_estimate_bytes(const ifx_config* cfg, size_t* bytes);
+ifx_status ifx_server_create(size_t hbm_budget_bytes, int max_cohort, ifx_server** out);
+/* Execution mode of the cohorts (IFX_EXEC_*, default IFX_EXEC_GRAPH). */
+ifx_status ifx_server_set_exec_mode(ifx_server* v, int mode);
+ifx_status ifx_server_submit(ifx_server* v, const ifx_config* cfg, const double* xf, const double* yf,
+                             int nsteps, long long* id);
+ifx_status ifx_server_tick(ifx_server* v, int* n_finished);
+/* Finished (or failed) request ids, oldest first; each is returned once. */
+ifx_status ifx_server_poll(ifx_server* v, long long* ids, int cap, int* n);
+ifx_status ifx_server_request_state(ifx_server* v, long long id, int* state, int* steps_done, int* nx, int* ny);
+/* Field IFX_FIELD_U, _V or _P of a finished request (nx*ny values). */
+ifx_status ifx_server_result(ifx_server* v, long long id, int field, double* host, size_t n);
+ifx_status ifx_server_request_stats(ifx_server* v, long long id, ifx_stats* out);
+/* Forgets a finished request and its results. */
+ifx_status ifx_server_release(ifx_server* v, long long id);
+ifx_status ifx_server_info(ifx_server* v, int* waiting, int* running, int* cohorts, size_t* used_bytes);
+void       ifx_server_destroy(ifx_server* v);
 /* Measurement hook (no reference counterpart): launches one kernel of the
  * time step `reps` times back to back on the solver's stream and returns the
  * mean device time per launch (CUDA events).  kernel: 0 finest-level

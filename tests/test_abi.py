@@ -24,7 +24,7 @@ def declared_functions():
 def test_every_declared_symbol_is_exported():
     lib = C.CDLL(ifx.LIB_PATH)
     names = declared_functions()
-    assert len(names) >= 24
+    assert len(names) >= 45
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
 

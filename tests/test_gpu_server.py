@@ -1,0 +1,113 @@
+"""Batch membership, asynchronous steps and the continuous-batching server on
+the GPU.  A request's result must not depend on the cohort it ran in: every
+finished request is compared bit for bit with the same case run alone."""
+import numpy as np
+import pytest
+
+import immerseflow_gb300 as ifx
+from immerseflow_gb300 import _capi as capi
+from immerseflow_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def case(nx, ny, re=100.0, b=0.5, angle=0.0, prec=capi.PREC_MIXED):
+    return cases.external(nx, ny, 12.0, 8.0, 4.0, 4.0, 0.5, b, angle, re, 1e-2, prec, ratio=4.0, width=1.0)
+
+
+def alone(cfg, xf, yf, nsteps):
+    s = ifx.Solver.create(cfg, xf, yf)
+    s.step(nsteps)
+    return {f: s.get(f) for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P)}
+
+
+def test_async_step_equals_step():
+    spec = case(64, 48)
+    a = ifx.Solver.create(*spec)
+    b = ifx.Solver.create(*spec)
+    a.step(3)
+    for _ in range(3):
+        b.step_async(1)
+        b.step_wait()
+    for f in (capi.FIELD_U, capi.FIELD_P):
+        assert np.array_equal(a.get(f), b.get(f))
+
+
+def test_inactive_instance_is_left_unchanged():
+    specs = [case(64, 48), case(56, 40, re=150.0, b=0.25, angle=15.0)]
+    s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+    s.step(2)
+    frozen = {f: s.get(f, inst=0) for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF)}
+    s.set_active(0, False)
+    s.step(2)
+    for f, a in frozen.items():
+        assert np.array_equal(s.get(f, inst=0), a), f
+    ref = alone(*specs[1], 4)
+    for f, a in ref.items():
+        assert np.array_equal(s.get(f, inst=1), a), f
+    s.set_active(0, True)
+    s.step(1)
+    assert not np.array_equal(s.get(capi.FIELD_U, inst=0), frozen[capi.FIELD_U])
+
+
+def test_server_results_equal_alone_runs():
+    stream = [(case(64, 48), 4), (case(48, 40, re=80.0, b=0.2, angle=-20.0), 2),
+              (case(72, 40, re=200.0, b=0.35, angle=10.0), 3), (case(40, 40, re=60.0), 5),
+              (case(56, 48, re=120.0, b=0.5), 1)]
+    srv = ifx.Server(1 << 33, max_cohort=8)
+    ids = {}
+    done = []
+    # arrivals interleaved with ticks: later requests join while earlier ones run
+    for t in range(40):
+        if t < len(stream):
+            spec, n = stream[t]
+            ids[srv.submit(*spec, nsteps=n)] = (spec, n)
+        srv.tick()
+        done += srv.poll()
+        if len(done) == len(stream):
+            break
+    assert sorted(done) == sorted(ids)
+    assert srv.info()["cohorts"] == 0 and srv.info()["used_bytes"] == 0
+    for rid, (spec, n) in ids.items():
+        st, steps, _, _ = srv.state(rid)
+        assert st == ifx.REQ_FINISHED and steps == n
+        ref = alone(*spec, n)
+        for f, a in ref.items():
+            assert np.array_equal(srv.result(rid, f), a), (rid, f)
+        srv.release(rid)
+    srv.close()
+
+
+def test_server_admits_by_memory_budget():
+    stream = [(case(64, 48), 2), (case(64, 48, re=150.0), 2), (case(64, 48, re=60.0), 2)]
+    one = ifx.estimate_bytes(stream[0][0][0])
+    srv = ifx.Server(int(one * 1.5), max_cohort=8)
+    ids = [srv.submit(*spec, nsteps=n) for spec, n in stream]
+    srv.tick()
+    info = srv.info()
+    assert info["running"] == 1 and info["waiting"] == 2
+    done = []
+    for _ in range(20):
+        srv.tick()
+        done += srv.poll()
+        if len(done) == 3:
+            break
+    assert sorted(done) == ids
+    for rid, (spec, n) in zip(ids, stream):
+        ref = alone(*spec, n)
+        assert np.array_equal(srv.result(rid, capi.FIELD_U), ref[capi.FIELD_U])
+    srv.close()
+
+
+def test_autotune_keeps_results():
+    spec = case(64, 48)
+    a = ifx.Solver.create(*spec)
+    a.step(1)
+    mode, ms = a.autotune(steps=2)
+    assert mode in (ifx.EXEC_PERSISTENT, ifx.EXEC_GRAPH) and ms > 0
+    assert a.exec_mode() == mode
+    a.step(2)
+    b = ifx.Solver.create(*spec)
+    b.step(3)
+    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+        assert np.array_equal(a.get(f), b.get(f)), f
