@@ -87,7 +87,7 @@ IFX_HD inline size_t sub_level_bytes(int nx, int ny, int tsize) { return sub_lay
 struct SubHdr {
     SubLayout o;
     unsigned base;  // byte offset of the level's arrays
-    int NX, NY, nx, ny, dirmask, child, depth, ns;
+    int NX, NY, nx, ny, dirmask, child, depth, ns, cx, cy;
 };
 constexpr size_t SUB_HDR_BYTES = (kSubLevels * sizeof(SubHdr) + 15) & ~(size_t)15;
 
@@ -130,6 +130,7 @@ struct alignas(16) LevelDev {
     int child;   // LevelDev index of the next coarser level, -1 at the coarsest
     int parent;  // LevelDev index of the next finer level, -1 at the finest
     int tbeg, tcnt;  // this level's tiles in the all-levels tile table
+    int cx, cy;      // cells of the parent level per cell of this one, in x and y (1 or 2)
 };
 
 // One body-surface sample for drag/lift (stationary body: built once).

@@ -17,6 +17,7 @@ ifx_status set_error(ifx_status st, const std::string& msg);
 // One multigrid level of one instance, host copy.
 struct HostLevel {
     int NX = 0, NY = 0, nx = 0, ny = 0, pitch = 0;
+    int cx = 1, cy = 1;  // cells of the next finer level per cell of this one, in x and y
     std::vector<double> dw, dh, xc, yc, kx, ky, ix, iy;
     std::vector<uint8_t> act, bits;  // pitched
     std::vector<int> pI, pIn, pJ, pJn;

@@ -733,12 +733,13 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     const T* fdw = LvA<T>::dw(F);
     const T* fdh = LvA<T>::dh(F);  // read through __ldg below
     T acc = (T)0;
+    const int cx = C.cx, cy = C.cy;
 #pragma unroll
     for (int dj = 0; dj < 2; dj++)
 #pragma unroll
         for (int di = 0; di < 2; di++) {
-            const int i = 2 * I0 - 1 + di, j = 2 * J0 - 1 + dj;
-            if (i > F.NX || j > F.NY) continue;
+            const int i = cx * (I0 - 1) + 1 + di, j = cy * (J0 - 1) + 1 + dj;
+            if (di >= cx || dj >= cy || i > F.NX || j > F.NY) continue;
             const int id = i + j * F.pitch;
             const uint8_t bt = __ldg(&F.bits[id]);
             if (!(bt & 0x0F)) continue;
@@ -805,7 +806,7 @@ struct SubGeo {
     int *pI, *pIn, *pJ, *pJn;
     uint8_t* b;
     signed char *psx, *psy;
-    int NX, NY, nx, ny, dirmask, child, depth;
+    int NX, NY, nx, ny, dirmask, child, depth, cx, cy;
 };
 
 template <typename T>
@@ -821,6 +822,7 @@ __device__ __forceinline__ SubGeo<T> sub_geo(unsigned char* sm, const SubHdr& h)
     g.psx = (signed char*)(p + o.psx); g.psy = (signed char*)(p + o.psy);
     g.NX = h.NX; g.NY = h.NY; g.nx = h.nx; g.ny = h.ny;
     g.dirmask = h.dirmask; g.child = h.child; g.depth = h.depth;
+    g.cx = h.cx; g.cy = h.cy;
     return g;
 }
 
@@ -915,8 +917,8 @@ __device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>
         for (int dj = 0; dj < 2; dj++)
 #pragma unroll
             for (int di = 0; di < 2; di++) {
-                const int i = 2 * I0 - 1 + di, j = 2 * J0 - 1 + dj;
-                if (i > f.NX || j > f.NY) continue;
+                const int i = c.cx * (I0 - 1) + 1 + di, j = c.cy * (J0 - 1) + 1 + dj;
+                if (di >= c.cx || dj >= c.cy || i > f.NX || j > f.NY) continue;
                 const int id = i + j * f.nx;
                 const uint8_t bt = f.b[id];
                 if (!(bt & 0x0F)) continue;
@@ -1033,6 +1035,7 @@ __device__ __forceinline__ void sub_stage_geometry(const int* __restrict__ sub, 
         h.NX = L.NX; h.NY = L.NY; h.nx = L.nx; h.ny = L.ny;
         h.dirmask = L.dirmask; h.child = L.child; h.depth = L.depth;
         h.ns = ns;
+        h.cx = L.cx; h.cy = L.cy;
         hdr[threadIdx.x] = h;
     }
     __syncthreads();

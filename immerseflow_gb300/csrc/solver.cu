@@ -112,6 +112,22 @@ void build_grid(Instance& I, const double* xf, const double* yf) {
 
 // Multigrid hierarchy from the tagged finest level.  Coarse cells merge 2x2
 // children (ceil at odd sizes); a coarse cell is active when any child is.
+// Coarsening of a multigrid level with NX x NY cells on an lx x ly domain: by
+// 2 in a direction that has at least 4 cells, except that while the mean
+// spacings differ by more than sqrt(2) only the finer direction is coarsened
+// (semi-coarsening: point smoothing leaves errors that are rough along the
+// weakly coupled, coarsely spaced direction).  The finest level is always
+// coarsened when possible; coarser ones while they have more than 64 cells.
+// Returns false for the coarsest level.  The oracle uses the same rule.
+bool mg_coarsening(int NX, int NY, double lx, double ly, bool finest, int* cx, int* cy) {
+    if (!finest && NX * NY <= 64) return false;
+    const double hx = lx / NX, hy = ly / NY, r = 1.4142135623730951;
+    const bool x_coarse = hx > r * hy, y_coarse = hy > r * hx;  // that direction is already coarser
+    *cx = (NX >= 4 && !x_coarse) ? 2 : 1;
+    *cy = (NY >= 4 && !y_coarse) ? 2 : 1;
+    return *cx == 2 || *cy == 2;
+}
+
 void build_levels(Instance& I) {
     I.lev.clear();
     HostLevel l0;
@@ -131,24 +147,28 @@ void build_levels(Instance& I) {
     l0.yc[0] = I.yf[0] - 0.5 * l0.dh[0];
     l0.yc[I.ny - 1] = I.yf[I.NY] + 0.5 * l0.dh[I.ny - 1];
     I.lev.push_back(l0);
+    const double lx = I.xf[I.NX] - I.xf[0], ly = I.yf[I.NY] - I.yf[0];
     while (true) {
         const HostLevel& f = I.lev.back();
-        if (!(f.NX >= 4 && f.NY >= 4 && (I.lev.size() == 1 || f.NX * f.NY > 64))) break;
+        int cx, cy;
+        if (!mg_coarsening(f.NX, f.NY, lx, ly, I.lev.size() == 1, &cx, &cy)) break;
         HostLevel c;
-        c.NX = (f.NX + 1) / 2;
-        c.NY = (f.NY + 1) / 2;
+        c.cx = cx;
+        c.cy = cy;
+        c.NX = cx == 2 ? (f.NX + 1) / 2 : f.NX;
+        c.NY = cy == 2 ? (f.NY + 1) / 2 : f.NY;
         c.nx = c.NX + 2;
         c.ny = c.NY + 2;
         c.pitch = round_up(c.nx, 32);
         c.dw.assign(c.nx, 0.0);
         c.dh.assign(c.ny, 0.0);
         for (int Ic = 1; Ic <= c.NX; Ic++) {
-            int i = 2 * Ic - 1;
-            c.dw[Ic] = f.dw[i] + (i + 1 <= f.NX ? f.dw[i + 1] : 0.0);
+            int i = cx * (Ic - 1) + 1;
+            c.dw[Ic] = f.dw[i] + (cx == 2 && i + 1 <= f.NX ? f.dw[i + 1] : 0.0);
         }
         for (int Jc = 1; Jc <= c.NY; Jc++) {
-            int j = 2 * Jc - 1;
-            c.dh[Jc] = f.dh[j] + (j + 1 <= f.NY ? f.dh[j + 1] : 0.0);
+            int j = cy * (Jc - 1) + 1;
+            c.dh[Jc] = f.dh[j] + (cy == 2 && j + 1 <= f.NY ? f.dh[j + 1] : 0.0);
         }
         c.dw[0] = c.dw[1];
         c.dw[c.nx - 1] = c.dw[c.nx - 2];
@@ -193,9 +213,9 @@ void build_levels(Instance& I) {
             for (int J = 1; J <= v.NY; J++)
                 for (int Ic = 1; Ic <= v.NX; Ic++) {
                     uint8_t a = 0;
-                    for (int dj = 0; dj < 2; dj++)
-                        for (int di = 0; di < 2; di++) {
-                            int i = 2 * Ic - 1 + di, j = 2 * J - 1 + dj;
+                    for (int dj = 0; dj < v.cy; dj++)
+                        for (int di = 0; di < v.cx; di++) {
+                            int i = v.cx * (Ic - 1) + 1 + di, j = v.cy * (J - 1) + 1 + dj;
                             if (i <= f.NX && j <= f.NY) a |= f.act[i + j * f.pitch];
                         }
                     v.act[Ic + J * v.pitch] = a;
@@ -237,6 +257,13 @@ void build_levels(Instance& I) {
             // centres: the neighbour beyond a domain side is the cell itself
             // with sign +1 (Neumann) or -1 (Dirichlet)
             for (int i = 1; i <= f.NX; i++) {
+                if (v.cx == 1) {  // not coarsened in x: the coarse column of the same index
+                    f.pI[i] = i;
+                    f.pIn[i] = i;
+                    f.pwx[i] = 0.0;
+                    f.psx[i] = 1;
+                    continue;
+                }
                 int Ic = (i + 1) / 2;
                 int In = f.xc[i] < v.xc[Ic] ? Ic - 1 : Ic + 1;
                 double w = (f.xc[i] - v.xc[Ic]) / (v.xc[In] - v.xc[Ic]);
@@ -249,6 +276,13 @@ void build_levels(Instance& I) {
                 f.psx[i] = sg;
             }
             for (int j = 1; j <= f.NY; j++) {
+                if (v.cy == 1) {
+                    f.pJ[j] = j;
+                    f.pJn[j] = j;
+                    f.pwy[j] = 0.0;
+                    f.psy[j] = 1;
+                    continue;
+                }
                 int Jc = (j + 1) / 2;
                 int Jn = f.yc[j] < v.yc[Jc] ? Jc - 1 : Jc + 1;
                 double w = (f.yc[j] - v.yc[Jc]) / (v.yc[Jn] - v.yc[Jc]);
@@ -691,6 +725,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ld.pI = L.d_pI; ld.pIn = L.d_pIn; ld.pJ = L.d_pJ; ld.pJn = L.d_pJn;
             ld.pwx = L.d_pwx; ld.pwy = L.d_pwy; ld.pwxf = L.d_pwxf; ld.pwyf = L.d_pwyf;
             ld.psx = L.d_psx; ld.psy = L.d_psy;
+            ld.cx = L.cx;
+            ld.cy = L.cy;
             ld.child = (l + 1 < nl) ? I.lev_base + l + 1 : -1;
             ld.parent = (l > 0) ? I.lev_base + l - 1 : -1;
             // tiles

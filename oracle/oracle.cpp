@@ -418,6 +418,7 @@ struct Ghost {
 
 struct Level {
     int NX, NY, nx, ny;
+    int cx = 1, cy = 1;  // cells of the next finer level per cell of this one, in x and y
     std::vector<double> dw, dh, xc, yc, kx, ky, ix, iy;  // widths, centres, face coeffs, 1/width
     std::vector<uint8_t> act, bits;
     std::vector<double> e, e2, r;
@@ -620,6 +621,21 @@ void build_ghosts(orc_solver* S) {
     for (auto& g : S->ghosts) if (g.side < 0) S->n_ibm++;
 }
 
+// Coarsening of a multigrid level with NX x NY cells on an lx x ly domain
+// (method rule; the CUDA path's host code uses the same one): by 2 in a
+// direction that has at least 4 cells, except that while the mean spacings
+// differ by more than sqrt(2) only the finer direction is coarsened.  The
+// finest level is always coarsened when possible; coarser ones while they
+// have more than 64 cells.  Returns false when the level is the coarsest.
+bool mg_coarsening(int NX, int NY, double lx, double ly, bool finest, int* cx, int* cy) {
+    if (!finest && NX * NY <= 64) return false;
+    const double hx = lx / NX, hy = ly / NY, r = 1.4142135623730951;
+    const bool x_coarse = hx > r * hy, y_coarse = hy > r * hx;  // that direction is already coarser
+    *cx = (NX >= 4 && !x_coarse) ? 2 : 1;
+    *cy = (NY >= 4 && !y_coarse) ? 2 : 1;
+    return *cx == 2 || *cy == 2;
+}
+
 void build_levels(orc_solver* S) {
     S->L.clear();
     Level l0;
@@ -631,22 +647,27 @@ void build_levels(orc_solver* S) {
     l0.xc[0] = S->xf[0] - 0.5 * l0.dw[0]; l0.xc[S->nx - 1] = S->xf[S->NX] + 0.5 * l0.dw[S->nx - 1];
     l0.yc[0] = S->yf[0] - 0.5 * l0.dh[0]; l0.yc[S->ny - 1] = S->yf[S->NY] + 0.5 * l0.dh[S->ny - 1];
     S->L.push_back(l0);
-    // coarsen while the level is large and both sides can halve
+    // coarsen while the level is large: by 2 in each direction, or only in the
+    // direction of the finer mean spacing while the cells are anisotropic
+    // (semi-coarsening: point smoothing does not damp errors that are rough
+    // along the weakly coupled, coarsely spaced direction)
+    const double lx = S->xf[S->NX] - S->xf[0], ly = S->yf[S->NY] - S->yf[0];
     while (true) {
         const Level& f = S->L.back();
-        // the finest level is always coarsened once (method mode needs NX, NY >= 4)
-        if (!(f.NX >= 4 && f.NY >= 4 && (S->L.size() == 1 || f.NX * f.NY > 64))) break;
+        int cx, cy;
+        if (!mg_coarsening(f.NX, f.NY, lx, ly, S->L.size() == 1, &cx, &cy)) break;
         Level c;
-        c.NX = (f.NX + 1) / 2; c.NY = (f.NY + 1) / 2;
+        c.cx = cx; c.cy = cy;
+        c.NX = cx == 2 ? (f.NX + 1) / 2 : f.NX; c.NY = cy == 2 ? (f.NY + 1) / 2 : f.NY;
         c.nx = c.NX + 2; c.ny = c.NY + 2;
         c.dw.assign(c.nx, 0.0); c.dh.assign(c.ny, 0.0);
         for (int I = 1; I <= c.NX; I++) {
-            int i = 2 * I - 1;
-            c.dw[I] = f.dw[i] + (i + 1 <= f.NX ? f.dw[i + 1] : 0.0);
+            int i = cx * (I - 1) + 1;
+            c.dw[I] = f.dw[i] + (cx == 2 && i + 1 <= f.NX ? f.dw[i + 1] : 0.0);
         }
         for (int J = 1; J <= c.NY; J++) {
-            int j = 2 * J - 1;
-            c.dh[J] = f.dh[j] + (j + 1 <= f.NY ? f.dh[j + 1] : 0.0);
+            int j = cy * (J - 1) + 1;
+            c.dh[J] = f.dh[j] + (cy == 2 && j + 1 <= f.NY ? f.dh[j + 1] : 0.0);
         }
         c.dw[0] = c.dw[1]; c.dw[c.nx - 1] = c.dw[c.nx - 2];
         c.dh[0] = c.dh[1]; c.dh[c.ny - 1] = c.dh[c.ny - 2];
@@ -677,9 +698,9 @@ void build_levels(orc_solver* S) {
             for (int J = 1; J <= v.NY; J++)
                 for (int I = 1; I <= v.NX; I++) {
                     uint8_t a = 0;
-                    for (int dj = 0; dj < 2; dj++)
-                        for (int di = 0; di < 2; di++) {
-                            int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+                    for (int dj = 0; dj < v.cy; dj++)
+                        for (int di = 0; di < v.cx; di++) {
+                            int i = v.cx * (I - 1) + 1 + di, j = v.cy * (J - 1) + 1 + dj;
                             if (i <= f.NX && j <= f.NY) a |= f.act[IDX(i, j, f.nx)];
                         }
                     v.act[IDX(I, J, v.nx)] = a;
@@ -708,6 +729,10 @@ void build_levels(orc_solver* S) {
             f.pI.assign(f.nx, 0); f.pIn.assign(f.nx, 0); f.pwx.assign(f.nx, 0.0); f.psx.assign(f.nx, 1.0);
             f.pJ.assign(f.ny, 0); f.pJn.assign(f.ny, 0); f.pwy.assign(f.ny, 0.0); f.psy.assign(f.ny, 1.0);
             for (int i = 1; i <= f.NX; i++) {
+                if (v.cx == 1) {  // not coarsened in x: the coarse column of the same index
+                    f.pI[i] = i; f.pIn[i] = i; f.pwx[i] = 0.0; f.psx[i] = 1.0;
+                    continue;
+                }
                 int I = (i + 1) / 2;
                 int In = f.xc[i] < v.xc[I] ? I - 1 : I + 1;
                 // ring centres are the mirror images of the first/last interior centres
@@ -718,6 +743,10 @@ void build_levels(orc_solver* S) {
                 f.pI[i] = I; f.pIn[i] = In; f.pwx[i] = w; f.psx[i] = sg;
             }
             for (int j = 1; j <= f.NY; j++) {
+                if (v.cy == 1) {
+                    f.pJ[j] = j; f.pJn[j] = j; f.pwy[j] = 0.0; f.psy[j] = 1.0;
+                    continue;
+                }
                 int J = (j + 1) / 2;
                 int Jn = f.yc[j] < v.yc[J] ? J - 1 : J + 1;
                 double w = (f.yc[j] - v.yc[J]) / (v.yc[Jn] - v.yc[J]);
@@ -816,9 +845,9 @@ void restrict_res(orc_solver* S, int l) {
         for (int I = 1; I <= c.NX; I++) {
             int cid = IDX(I, J, c.nx);
             double acc = 0.0;
-            for (int dj = 0; dj < 2; dj++)
-                for (int di = 0; di < 2; di++) {
-                    int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+            for (int dj = 0; dj < c.cy; dj++)
+                for (int di = 0; di < c.cx; di++) {
+                    int i = c.cx * (I - 1) + 1 + di, j = c.cy * (J - 1) + 1 + dj;
                     if (i > f.NX || j > f.NY) continue;
                     int id = IDX(i, j, f.nx);
                     if (!live(f, id)) continue;

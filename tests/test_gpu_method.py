@@ -152,3 +152,19 @@ def test_mixed_precision_close_to_fp64():
         assert np.linalg.norm(ub - ua) / np.linalg.norm(ua) <= 1e-6, f
     cda, cdb = a.stats().cd, b.stats().cd
     assert abs(cda - cdb) <= 1e-3 * abs(cda)
+
+
+@pytest.mark.parametrize("nx,ny", [(48, 200), (240, 40)])
+def test_anisotropic_grid_semicoarsening_vs_oracle(oracle, nx, ny):
+    """Cells up to ~6:1 use semi-coarsened multigrid levels; same hierarchy,
+    iterations and fields as the oracle."""
+    cfg, xf, yf = cases.external(nx, ny, 12.0, 8.0, 4.0, 4.0, 0.5, 0.3, 10.0, 120.0, 5e-3, capi.PREC_FP64,
+                                 ratio=4.0, width=1.0)
+    s = ifx.Solver.create(cfg, xf, yf)
+    o = oracle.method(cfg, xf, yf)
+    for _ in range(2):
+        s.step(1)
+        o.step(1)
+        assert abs(s.stats().last_ppe_iters - o.stats().last_ppe_iters) <= 1
+        assert s.stats().last_ppe_iters <= 16
+    _compare(s, o, tol=1e-9)
