@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=16.0, help="served stream arrival rate [1/s]")
     ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
+    ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch"],
+                    help="workload of --profile: the cylinder, or the batched sweep of --batch instances")
     return ap.parse_args()
 
 
@@ -314,8 +316,12 @@ def main():
 
     if args.profile:
         prec = capi.PREC_MIXED if args.profile == "mixed" else capi.PREC_FP64
-        cfg, _, _ = cases.cylinder(precision=prec)
-        s = ifx.Solver.create(cfg, xf, yf)
+        if args.profile_workload == "batch":
+            specs = cases.batch_sample(count=args.batch, seed=0, precision=prec)
+            s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+        else:
+            cfg, _, _ = cases.cylinder(precision=prec)
+            s = ifx.Solver.create(cfg, xf, yf)
         s.step(args.warmup)
         s.synchronize()
         torch.cuda.nvtx.range_push("step")
