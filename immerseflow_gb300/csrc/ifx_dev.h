@@ -29,6 +29,11 @@ constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one
 constexpr int SUB_SMEM_MAX = 96 * 1024;  // shared memory for those levels (fields, metrics, tables)
 constexpr int kSubLevels = 16;           // at most this many levels per instance
 constexpr int SUB_COARSE_PER_THREAD = 4;  // coarsest-level cells per thread in the RB-SOR solve
+// Mixed path: the FP32 BiCGSTAB restarts from the FP64 true residual once its
+// recursive residual fell by this factor since the last restart, or after
+// this many iterations.
+constexpr double PPE_RESTART_DROP = 1e-4;
+constexpr int PPE_RESTART_EVERY = 25;
 
 enum CellType : uint8_t { T_SOLID = 0, T_FLUID = 1, T_GHOST = 2, T_DOMAIN = 3 };
 // per-cell stencil bits: open faces, and (finest level) faces to an IBM ghost
@@ -158,8 +163,8 @@ struct alignas(16) InstDev {
     const uint8_t* type;
     const int* gidx;             // cell -> global ghost index (IBM ghosts), -1 otherwise
     double *qbu, *qbv;
-    // BiCGSTAB vectors of the pressure solve (FP64)
-    double *kr, *krh, *kp, *kv, *ks, *kt, *kph, *ksh;
+    // BiCGSTAB vectors of the pressure solve, in T (FP64 plain path, FP32 mixed path)
+    void *kr, *krh, *kp, *kv, *ks, *kt, *kph, *ksh;
     // mixed-precision predictor corrections
     float *du, *dv, *du2, *dv2, *rfu, *rfv;
     // body (ellipse), bit-exact predicate constants
@@ -170,10 +175,12 @@ struct alignas(16) InstDev {
 // Device-resident per-instance iteration state and diagnostics.
 struct InstState {
     int pred_state, pred_iters, ppe_state, ppe_iters;
-    int status, have_nold, pad1, pad2;
+    int status, have_nold;
+    int restart, restart_it;                  // mixed path: FP64 residual due next body; iteration of the last one
     double pred_metric, ppe_rel, bmean, bnorm, pmean;
     double rho, alpha, omega, beta;           // BiCGSTAB scalars
-    double max_div, cd, cl, flux_in, flux_out, spare;
+    double max_div, cd, cl, flux_in, flux_out;
+    double rel_restart;                       // mixed path: true relative residual at the last restart
 };
 
 // Loop control for device-side convergence: reduce kernels vote, the last

@@ -14,15 +14,22 @@ cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int c
 cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
 cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I,
                               const InstState* S, double* part, int parity, cudaStream_t s);
+// Mixed path: FP32 sweep on the correction, and the FP64 refresh (stage 0:
+// absorb the correction, stage 1: defect; finalize: absorb after the loop).
+cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng, const LevelDev* LV, const InstDev* I,
+                                const InstState* S, double* part, int parity, cudaStream_t s);
+cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
+                                int stage, int finalize, cudaStream_t s);
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
                                LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
                             cudaStream_t s);
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
+template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, cudaStream_t s);
+                              const GhostDev* G, double* part, int restart_only, cudaStream_t s);
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
-                                 LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
+                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           cudaStream_t s);
@@ -34,6 +41,7 @@ cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* par
 template <typename T>
 cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           cudaStream_t s);
+template <typename T>
 cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           double* part, cudaStream_t s);
 template <typename T>

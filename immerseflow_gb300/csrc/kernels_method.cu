@@ -36,6 +36,16 @@ __global__ void k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __rest
 __global__ void k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              double* __restrict__ part, int parity) { b_pred_sweep(tiles, ntiles, G, ng, I, S, part, parity, blockIdx.x); }
+__global__ void k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
+                               const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
+                               const InstState* __restrict__ S, double* __restrict__ part, int parity) {
+    b_pred_sweep32(tiles, ntiles, G, ng, LV, I, S, part, parity, blockIdx.x);
+}
+__global__ void k_pred_refresh(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
+                               const InstDev* __restrict__ I, const InstState* __restrict__ S, int stage,
+                               int finalize) {
+    b_pred_refresh(tiles, ntiles, G, ng, I, S, stage, finalize, blockIdx.x);
+}
 __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle) { b_pred_reduce(I, S, part, parity, ctl, handle, blockIdx.x); }
@@ -43,12 +53,15 @@ __global__ void k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __rest
                            double* __restrict__ part, int to_final) { b_face_rhs(tiles, I, part, to_final, blockIdx.x); }
 __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part) { b_rhs_reduce(I, S, part, blockIdx.x); }
+template <typename T>
 __global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                             const GhostDev* __restrict__ G, double* __restrict__ part) { b_bicg_start(tiles, LV, I, S, G, part, blockIdx.x); }
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only) {
+    b_bicg_start<T>(tiles, LV, I, S, G, part, restart_only, blockIdx.x);
+}
 __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
-                                const double* __restrict__ part, int start, LoopCtl* ctl,
-                                unsigned long long handle) { b_bicg_reduce_r(I, S, part, start, ctl, handle, blockIdx.x); }
+                                const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
+                                unsigned long long handle) { b_bicg_reduce_r(I, S, part, start, mixed, ctl, handle, blockIdx.x); }
 template <typename T>
 __global__ void k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T>(tiles, LV, I, S, blockIdx.x); }
@@ -61,9 +74,10 @@ __global__ void k_bicg_scalar(const InstDev* __restrict__ I, InstState* __restri
 template <typename T>
 __global__ void k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_s<T>(tiles, LV, I, S, blockIdx.x); }
+template <typename T>
 __global__ void k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         double* __restrict__ part) { b_bicg_x(tiles, LV, I, S, part, blockIdx.x); }
+                         double* __restrict__ part) { b_bicg_x<T>(tiles, LV, I, S, part, blockIdx.x); }
 template <typename T>
 __global__ void k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
@@ -122,6 +136,16 @@ cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, 
     k_pred_sweep<<<nt + nblk(ng, TILE_THREADS), TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, part, parity);
     return cudaGetLastError();
 }
+cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng, const LevelDev* LV, const InstDev* I,
+                                const InstState* S, double* part, int parity, cudaStream_t s) {
+    k_pred_sweep32<<<nt + nblk(ng, TILE_THREADS), TILE_THREADS, 0, s>>>(t, nt, G, ng, LV, I, S, part, parity);
+    return cudaGetLastError();
+}
+cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
+                                int stage, int finalize, cudaStream_t s) {
+    k_pred_refresh<<<nt + nblk(ng, TILE_THREADS), TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize);
+    return cudaGetLastError();
+}
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
                                LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
     k_pred_reduce<<<ninst, 256, 0, s>>>(I, S, part, parity, ctl, handle);
@@ -136,14 +160,15 @@ cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part
     k_rhs_reduce<<<ninst, 256, 0, s>>>(I, S, part);
     return cudaGetLastError();
 }
+template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, cudaStream_t s) {
-    k_bicg_start<<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part);
+                              const GhostDev* G, double* part, int restart_only, cudaStream_t s) {
+    k_bicg_start<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only);
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
-                                 LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
-    k_bicg_reduce_r<<<ninst, 256, 0, s>>>(I, S, part, start, ctl, handle);
+                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
+    k_bicg_reduce_r<<<ninst, 256, 0, s>>>(I, S, part, start, mixed, ctl, handle);
     return cudaGetLastError();
 }
 template <typename T>
@@ -169,9 +194,10 @@ cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstD
     k_bicg_s<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
     return cudaGetLastError();
 }
+template <typename T>
 cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           double* part, cudaStream_t s) {
-    k_bicg_x<<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
+    k_bicg_x<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
     return cudaGetLastError();
 }
 template <typename T>
@@ -254,5 +280,14 @@ template cudaError_t launch_subcycle<float>(const int*, int, const LevelDev*, co
                                             int, int, int, cudaStream_t);
 template cudaError_t subcycle_smem_limit<double>(int);
 template cudaError_t subcycle_smem_limit<float>(int);
+
+template cudaError_t launch_bicg_start<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+                                               const GhostDev*, double*, int, cudaStream_t);
+template cudaError_t launch_bicg_start<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+                                              const GhostDev*, double*, int, cudaStream_t);
+template cudaError_t launch_bicg_x<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
+                                           cudaStream_t);
+template cudaError_t launch_bicg_x<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
+                                          cudaStream_t);
 
 }  // namespace ifx

@@ -65,6 +65,16 @@ __device__ __forceinline__ bool any_pred_active(const InstState* S, int n) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].pred_state == ST_ACTIVE);
     return __syncthreads_or(a) != 0;
 }
+__device__ __forceinline__ bool any_pred_refresh_due(const InstDev* I, const InstState* S, int n) {
+    int a = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        InstState s;
+        s.pred_state = *(const volatile int*)&S[k].pred_state;
+        s.pred_iters = *(const volatile int*)&S[k].pred_iters;
+        a |= pred_refresh_due(I[k], s);
+    }
+    return __syncthreads_or(a) != 0;
+}
 __device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
     int a = 0;
     for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].ppe_state == ST_ACTIVE);
@@ -146,29 +156,56 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     BAR();
     // predictor: pairs of Jacobi sweeps until every instance converged
     const int npred = P.nt0 + nchunks(P.ng);
+    constexpr bool mixed32 = sizeof(T) == 4;
     for (int pair = 0; pair < P.pred_pairs; pair++) {
-        FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 0, vb);
-        BAR();
-        FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 0, nullptr, 0ull, vb);
-        BAR();
-        FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 1, vb);
-        BAR();
-        FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 1, nullptr, 0ull, vb);
-        BAR();
+        if (mixed32) {
+            if (any_pred_refresh_due(P.I, P.S, n)) {
+                FOR_VB(npred) b_pred_refresh(P.t0, P.nt0, P.G, P.ng, P.I, P.S, 0, 0, vb);
+                BAR();
+                FOR_VB(npred) b_pred_refresh(P.t0, P.nt0, P.G, P.ng, P.I, P.S, 1, 0, vb);
+                BAR();
+            }
+            for (int par = 0; par < 2; par++) {
+                FOR_VB(npred) b_pred_sweep32(P.t0, P.nt0, P.G, P.ng, P.LV, P.I, P.S, P.part, par, vb);
+                BAR();
+                FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, par, nullptr, 0ull, vb);
+                BAR();
+            }
+        } else {
+            FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 0, vb);
+            BAR();
+            FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 0, nullptr, 0ull, vb);
+            BAR();
+            FOR_VB(npred) b_pred_sweep(P.t0, P.nt0, P.G, P.ng, P.I, P.S, P.part, 1, vb);
+            BAR();
+            FOR_VB(n) b_pred_reduce(P.I, P.S, P.part, 1, nullptr, 0ull, vb);
+            BAR();
+        }
         if (!any_pred_active(P.S, n)) break;
+    }
+    if (mixed32) {
+        FOR_VB(npred) b_pred_refresh(P.t0, P.nt0, P.G, P.ng, P.I, P.S, 0, 1, vb);
+        BAR();
     }
     if (!ghost_fill(P, 3, ep)) return false;
     FOR_VB(P.nt0) b_face_rhs(P.t0, P.I, P.part, 0, vb);
     BAR();
     FOR_VB(n) b_rhs_reduce(P.I, P.S, P.part, vb);
     BAR();
-    FOR_VB(P.nt0) b_bicg_start(P.t0, P.LV, P.I, P.S, P.G, P.part, vb);
+    constexpr int mixed = sizeof(T) == 4 ? 1 : 0;
+    FOR_VB(P.nt0) b_bicg_start<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, 0, vb);
     BAR();
-    FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 1, nullptr, 0ull, vb);
+    FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 1, mixed, nullptr, 0ull, vb);
     BAR();
     // pressure: BiCGSTAB iterations until every instance converged
     for (int it = 0; it < P.ppe_bodies; it++) {
         if (!any_ppe_active(P.S, n)) break;
+        if (mixed) {  // FP64 true residual and restart where the FP32 recursion ran its course
+            FOR_VB(P.nt0) b_bicg_start<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, 1, vb);
+            BAR();
+            FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 2, 1, nullptr, 0ull, vb);
+            BAR();
+        }
         FOR_VB(P.nt0) b_bicg_p<T>(P.t0, P.LV, P.I, P.S, vb);
         BAR();
         int e1 = 0, e2 = 0;
@@ -184,9 +221,9 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
         BAR();
         FOR_VB(n) b_bicg_scalar(P.I, P.S, P.part, 1, vb);
         BAR();
-        FOR_VB(P.nt0) b_bicg_x(P.t0, P.LV, P.I, P.S, P.part, vb);
+        FOR_VB(P.nt0) b_bicg_x<T>(P.t0, P.LV, P.I, P.S, P.part, vb);
         BAR();
-        FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 0, nullptr, 0ull, vb);
+        FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 0, mixed, nullptr, 0ull, vb);
         BAR();
     }
     FOR_VB(P.nt0) b_p_finalize(P.t0, P.I, P.S, vb);

@@ -437,6 +437,154 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
     if (threadIdx.x == 0) loop_vote(ctl, active, handle);
 }
 
+// ------------------------------------------- mixed-path predictor (FP32)
+//
+// FP32 Jacobi sweeps on the correction d = q - q0, q0 = (u, v) in FP64:
+//   d <- d + D~^-1 (r0 - M d),   r0 = rhs - M q0 (FP64 defect, stored FP32);
+// the ghost relations likewise (d_g <- r0_g + sum w d_nb).  M is linear, so this
+// is the FP64 Jacobi iteration up to FP32 rounding of d, and every
+// mixed_inner sweeps q0 absorbs d and r0 is recomputed in FP64 (defect
+// correction): rounding never accumulates into the state.  The sweep metric
+// (sum |update|) and the stop rule are those of the FP64 path.
+
+__device__ __forceinline__ bool pred_refresh_due(const InstDev& in, const InstState& s) {
+    return s.pred_state == ST_ACTIVE && s.pred_iters % (in.mixed_inner > 0 ? in.mixed_inner : 8) == 0;
+}
+
+// stage 0: q0 += d, d = 0 ; stage 1: r0 = rhs - M q0 (cells), r0_g (ghosts).
+// finalize: q = q0 + d, d = 0 after the loop (every instance not retired).
+// vb: level-0 tiles, then ghost chunks (as b_pred_sweep).
+__device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, int ntiles,
+                                               const GhostDev* __restrict__ G, int ng,
+                                               const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                               int stage, int finalize, int vb) {
+    int inst, cell;
+    bool fluid = false;
+    const GhostDev* gh = nullptr;
+    if ((int)vb < ntiles) {
+        const Tile t = ldg_struct(&tiles[vb]);
+        inst = t.inst;
+        const InstDev& in = I[inst];
+        int i, j;
+        tile_ij(t, i, j);
+        if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
+        cell = i + j * in.pitch;
+        if (__ldg(&in.type[cell]) != T_FLUID) return;
+        fluid = true;
+    } else {
+        const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
+        if (g >= ng) return;
+        gh = &G[g];
+        inst = gh->inst;
+        cell = gh->cell;
+    }
+    const InstDev& in = I[inst];
+    if (in.retired) return;
+    if (!finalize && !pred_refresh_due(in, S[inst])) return;
+    if (finalize || stage == 0) {
+        in.u[cell] += (double)in.du[cell];
+        in.v[cell] += (double)in.dv[cell];
+        in.du[cell] = 0.0f;
+        in.dv[cell] = 0.0f;
+        return;
+    }
+    const double* u = in.u;
+    const double* v = in.v;
+    if (fluid) {
+        const int P = in.pitch, id = cell, j = cell / P, i = cell - j * P;
+        const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
+        const double aE = in.dtre * (__ldg(&in.kx[i]) * ixi), aW = in.dtre * (__ldg(&in.kx[i - 1]) * ixi);
+        const double aN = in.dtre * (__ldg(&in.ky[j]) * iyj), aS = in.dtre * (__ldg(&in.ky[j - 1]) * iyj);
+        const double aP = 1.0 + aE + aW + aN + aS;
+        in.rfu[id] = (float)(in.ru[id] + aE * u[id + 1] + aW * u[id - 1] + aN * u[id + P] + aS * u[id - P] - aP * u[id]);
+        in.rfv[id] = (float)(in.rv[id] + aE * v[id + 1] + aW * v[id - 1] + aN * v[id + P] + aS * v[id - P] - aP * v[id]);
+    } else {
+        double au = ghost_const(*gh, in.qbu, gh->cu), av = ghost_const(*gh, in.qbv, gh->cv);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            au += gh->wu[k] * u[gh->nb[k]];
+            av += gh->wv[k] * v[gh->nb[k]];
+        }
+        in.rfu[cell] = (float)(au - u[cell]);
+        in.rfv[cell] = (float)(av - v[cell]);
+    }
+}
+
+// One FP32 sweep on the correction; parity 0 reads (du, dv), writes (du2,
+// dv2), parity 1 the reverse.  Partials as b_pred_sweep.
+__device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, int ntiles,
+                                               const GhostDev* __restrict__ G, int ng,
+                                               const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
+                                               const InstState* __restrict__ S, double* __restrict__ part,
+                                               int parity, int vb) {
+    if ((int)vb < ntiles) {
+        const Tile t = ldg_struct(&tiles[vb]);
+        const InstDev& in = I[t.inst];
+        const int st = S[t.inst].pred_state;
+        if (st == ST_DONE) return;
+        const float* su = parity ? in.du2 : in.du;
+        const float* sv = parity ? in.dv2 : in.dv;
+        float* du = parity ? in.du : in.du2;
+        float* dv = parity ? in.dv : in.dv2;
+        int i, j;
+        tile_ij(t, i, j);
+        const bool ok = i >= 1 && i <= in.NX && j >= 1 && j <= in.NY;
+        const int P = in.pitch, id = i + j * P;
+        const bool fl = ok && __ldg(&in.type[id]) == T_FLUID;
+        if (st == ST_FINAL_IN_ALT) {
+            if (fl) {
+                du[id] = su[id];
+                dv[id] = sv[id];
+            }
+            return;
+        }
+        double m[1] = {0.0};
+        if (fl) {
+            const LevelDev& L = LV[in.lev0];
+            const float dtre = (float)in.dtre;
+            const float ixi = __ldg(&L.ixf[i]), iyj = __ldg(&L.iyf[j]);
+            const float aE = dtre * (__ldg(&L.kxf[i]) * ixi), aW = dtre * (__ldg(&L.kxf[i - 1]) * ixi);
+            const float aN = dtre * (__ldg(&L.kyf[j]) * iyj), aS = dtre * (__ldg(&L.kyf[j - 1]) * iyj);
+            const float aP = 1.0f + aE + aW + aN + aS;
+            const float di = rcpa(aP);
+            const float dU = (in.rfu[id] + aE * su[id + 1] + aW * su[id - 1] + aN * su[id + P] + aS * su[id - P] -
+                              aP * su[id]) * di;
+            const float dV = (in.rfv[id] + aE * sv[id + 1] + aW * sv[id - 1] + aN * sv[id + P] + aS * sv[id - P] -
+                              aP * sv[id]) * di;
+            du[id] = su[id] + dU;
+            dv[id] = sv[id] + dV;
+            m[0] = (double)fabsf(dU) + (double)fabsf(dV);
+        }
+        __shared__ double out[1];
+        block_sum<1>(m, out);
+        if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
+    } else {
+        const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
+        if (g >= ng) return;
+        const GhostDev& gh = G[g];
+        const InstDev& in = I[gh.inst];
+        const int st = S[gh.inst].pred_state;
+        if (st == ST_DONE) return;
+        const float* su = parity ? in.du2 : in.du;
+        const float* sv = parity ? in.dv2 : in.dv;
+        float* du = parity ? in.du : in.du2;
+        float* dv = parity ? in.dv : in.dv2;
+        if (st == ST_FINAL_IN_ALT) {
+            du[gh.cell] = su[gh.cell];
+            dv[gh.cell] = sv[gh.cell];
+            return;
+        }
+        float au = in.rfu[gh.cell], av = in.rfv[gh.cell];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            au += (float)gh.wu[k] * su[gh.nb[k]];
+            av += (float)gh.wv[k] * sv[gh.nb[k]];
+        }
+        du[gh.cell] = au;
+        dv[gh.cell] = av;
+    }
+}
+
 // -------------------------------------------------- faces and PPE source
 
 __device__ __forceinline__ double face_u(const InstDev& in, const double* u, int i, int id) {
@@ -504,15 +652,26 @@ __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, 
     return (bt & 0x0F) != 0;
 }
 
-// r = (b - mean b) - L p, rh = r, p_dir = v = 0.
+// BiCGSTAB of the pressure solve.  The Krylov vectors (r, rh, p_dir, v, s,
+// t and the preconditioned p_dir, s) are of type T: FP64 in the plain path,
+// FP32 in the mixed path, where the iterate p stays FP64 and the FP32
+// iteration restarts from the FP64 true residual b - L p ("defect
+// correction": convergence is only accepted on the true residual).  Dot
+// products are accumulated in FP64 in both paths.
+
+// r = (b - mean b) - L p in FP64, rh = r, p_dir = v = 0.  restart_only: only
+// the instances whose mixed-path restart is due.
 // partials: 0 (r,r)  1 (b,b)  2 (rh,r)  3 (p,area)
+template <typename T>
 __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                             const GhostDev* __restrict__ G, double* __restrict__ part, int vb) {
+                                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                             const GhostDev* __restrict__ G, double* __restrict__ part,
+                                             int restart_only, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
+    if (restart_only && !st.restart) return;
     const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
@@ -523,13 +682,14 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
         lap<double, double, true>(L, in.p, i, j, id, bt, G, in.gidx, Lp, D);
         const double bb = in.b[id] - st.bmean;
         const double r = bb - Lp;
-        in.kr[id] = r;
-        in.krh[id] = r;
-        in.kp[id] = 0.0;
-        in.kv[id] = 0.0;
+        const T rt = (T)r;
+        ((T*)in.kr)[id] = rt;
+        ((T*)in.krh)[id] = rt;
+        ((T*)in.kp)[id] = (T)0;
+        ((T*)in.kv)[id] = (T)0;
         acc[0] = r * r;
         acc[1] = bb * bb;
-        acc[2] = r * r;
+        acc[2] = (double)rt * (double)rt;
         acc[3] = in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];
@@ -537,30 +697,48 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
     if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
-// Convergence test on ||r||, then rho, beta for the next direction.  Votes.
+// Convergence test on ||r||, then rho, beta for the next direction.  Votes
+// (start == 0 only).  start: 1 after the initial residual, 2 after a mixed-path
+// restart (instances without one are skipped), 0 after an iteration.  mixed:
+// the recursive FP32 residual is never accepted; a restart is scheduled when
+// it fell by PPE_RESTART_DROP (or below the tolerance) since the last one, or
+// after PPE_RESTART_EVERY iterations.
 __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
-                                const double* __restrict__ part, int start, LoopCtl* ctl,
-                                unsigned long long handle, int vb) {
+                                                const double* __restrict__ part, int start, int mixed,
+                                                LoopCtl* ctl, unsigned long long handle, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
     bool active = false;
-    if (S[k].ppe_state == ST_ACTIVE) {
+    const bool run = S[k].ppe_state == ST_ACTIVE && (start != 2 || S[k].restart);
+    if (run) {
         double r[4];
         inst_sum<4>(part, in.tile_beg, in.tile_cnt, r);
         if (threadIdx.x == 0) {
             InstState& st = S[k];
-            if (start) {
+            if (start == 1) {
                 st.bnorm = sqrt(r[1]);
                 st.rho = st.alpha = st.omega = 1.0;
                 st.ppe_iters = 0;
+                st.restart = 0;
+                st.restart_it = 0;
+            } else if (start == 2) {
+                st.rho = st.alpha = st.omega = 1.0;
+                st.restart = 0;
+                st.restart_it = st.ppe_iters;
             } else {
                 st.ppe_iters += 1;
             }
             const double rel = sqrt(r[0]) / (st.bnorm > 1e-300 ? st.bnorm : 1e-300);
             st.ppe_rel = rel;
             st.pmean = r[3] / in.area;
-            if (rel <= in.ppe_tol || st.ppe_iters >= in.ppe_itermax) {
+            if (start != 0) st.rel_restart = rel;
+            const bool true_res = start != 0 || !mixed;
+            if ((true_res && rel <= in.ppe_tol) || st.ppe_iters >= in.ppe_itermax) {
                 st.ppe_state = ST_DONE;
+            } else if (!true_res && (rel <= in.ppe_tol || rel <= PPE_RESTART_DROP * st.rel_restart ||
+                                     st.ppe_iters - st.restart_it >= PPE_RESTART_EVERY)) {
+                st.restart = 1;
+                active = true;
             } else {
                 const double rho1 = r[2];
                 st.beta = (rho1 / st.rho) * (st.alpha / st.omega);
@@ -569,13 +747,13 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
             }
         }
     }
-    if (threadIdx.x == 0) loop_vote(ctl, active, handle);
+    if (threadIdx.x == 0 && start != 2) loop_vote(ctl, active, handle);
 }
 
 // p_dir = r + beta (p_dir - omega v); preconditioner input.
 template <typename T>
 __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
+                                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
@@ -585,39 +763,41 @@ __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const L
     uint8_t bt;
     tile_ij(t, i, j);
     if (!live0(L, i, j, id, bt)) return;
-    const double pd = in.kr[id] + st.beta * (in.kp[id] - st.omega * in.kv[id]);
-    in.kp[id] = pd;
-    ((T*)L.r)[id] = (T)pd;
+    T* kp = (T*)in.kp;
+    const T pd = ((const T*)in.kr)[id] + (T)st.beta * (kp[id] - (T)st.omega * ((const T*)in.kv)[id]);
+    kp[id] = pd;
+    ((T*)L.r)[id] = pd;
 }
 
-// y = L z with z the preconditioned vector (V-cycle result in T), stored in
-// FP64 as zo; partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
+// y = L z with z the preconditioned vector (V-cycle result), operator and z
+// in T; z is kept as zo.  partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
 template <typename T>
 __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which, int vb) {
+                                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt,
+                                             int which, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
     if (st.ppe_state != ST_ACTIVE) return;
     const LevelDev& L = LV[in.lev0];
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
-    double* zo = which == 0 ? in.kph : in.ksh;
-    double* y = which == 0 ? in.kv : in.kt;
+    T* zo = (T*)(which == 0 ? in.kph : in.ksh);
+    T* y = (T*)(which == 0 ? in.kv : in.kt);
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
     double acc[2] = {0.0, 0.0};
     if (live0(L, i, j, id, bt)) {
-        double Lz, D;
-        lap<double, T, true>(L, z, i, j, id, bt, G, in.gidx, Lz, D);
-        zo[id] = (double)z[id];
+        T Lz, D;
+        lap<T, T, true>(L, z, i, j, id, bt, G, in.gidx, Lz, D);
+        zo[id] = z[id];
         y[id] = Lz;
         if (which == 0) {
-            acc[0] = in.krh[id] * Lz;
+            acc[0] = (double)((const T*)in.krh)[id] * (double)Lz;
         } else {
-            acc[0] = Lz * in.ks[id];
-            acc[1] = Lz * Lz;
+            acc[0] = (double)Lz * (double)((const T*)in.ks)[id];
+            acc[1] = (double)Lz * (double)Lz;
         }
     }
     __shared__ double out[2];
@@ -642,7 +822,7 @@ __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, Ins
 // s = r - alpha v; preconditioner input.
 template <typename T>
 __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
+                                         const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
@@ -652,16 +832,17 @@ __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const L
     uint8_t bt;
     tile_ij(t, i, j);
     if (!live0(L, i, j, id, bt)) return;
-    const double sv = in.kr[id] - st.alpha * in.kv[id];
-    in.ks[id] = sv;
-    ((T*)L.r)[id] = (T)sv;
+    const T sv = ((const T*)in.kr)[id] - (T)st.alpha * ((const T*)in.kv)[id];
+    ((T*)in.ks)[id] = sv;
+    ((T*)L.r)[id] = sv;
 }
 
-// p += alpha ph + omega sh ; r = s - omega t.
+// p += alpha ph + omega sh (FP64) ; r = s - omega t (T).
 // partials: 0 (r,r)  1 unused  2 (rh,r)  3 (p,area)
+template <typename T>
 __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         double* __restrict__ part, int vb) {
+                                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                         double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
@@ -672,12 +853,12 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
     tile_ij(t, i, j);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     if (live0(L, i, j, id, bt)) {
-        const double pn = in.p[id] + st.alpha * in.kph[id] + st.omega * in.ksh[id];
+        const double pn = in.p[id] + st.alpha * (double)((const T*)in.kph)[id] + st.omega * (double)((const T*)in.ksh)[id];
         in.p[id] = pn;
-        const double r = in.ks[id] - st.omega * in.kt[id];
-        in.kr[id] = r;
-        acc[0] = r * r;
-        acc[2] = in.krh[id] * r;
+        const T r = ((const T*)in.ks)[id] - (T)st.omega * ((const T*)in.kt)[id];
+        ((T*)in.kr)[id] = r;
+        acc[0] = (double)r * (double)r;
+        acc[2] = (double)((const T*)in.krh)[id] * (double)r;
         acc[3] = pn * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];

@@ -601,10 +601,19 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
         IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
         IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
-        IFX_TRY(dalloc(S, &d.kr, nc)); IFX_TRY(dalloc(S, &d.krh, nc));
-        IFX_TRY(dalloc(S, &d.kp, nc)); IFX_TRY(dalloc(S, &d.kv, nc));
-        IFX_TRY(dalloc(S, &d.ks, nc)); IFX_TRY(dalloc(S, &d.kt, nc));
-        IFX_TRY(dalloc(S, &d.kph, nc)); IFX_TRY(dalloc(S, &d.ksh, nc));
+        if (S->prec == IFX_PREC_MIXED)
+            for (float** a : {&d.du, &d.dv, &d.du2, &d.dv2, &d.rfu, &d.rfv}) IFX_TRY(dalloc(S, a, nc));
+        for (void** kv : {&d.kr, &d.krh, &d.kp, &d.kv, &d.ks, &d.kt, &d.kph, &d.ksh}) {
+            if (S->prec == IFX_PREC_FP64) {
+                double* a = nullptr;
+                IFX_TRY(dalloc(S, &a, nc));
+                *kv = a;
+            } else {
+                float* a = nullptr;
+                IFX_TRY(dalloc(S, &a, nc));
+                *kv = a;
+            }
+        }
         double *xf_d = nullptr, *yf_d = nullptr, *xc_d = nullptr, *yc_d = nullptr, *dx_d = nullptr,
                *dy_d = nullptr, *fx_d = nullptr, *gx_d = nullptr, *fy_d = nullptr, *gy_d = nullptr;
         IFX_TRY(dupload(S, &xf_d, I.xf)); IFX_TRY(dupload(S, &yf_d, I.yf));
@@ -836,6 +845,10 @@ struct Seq {
 
 // One V-cycle on the correction equation; returns which buffer (0: e,
 // 1: e2) holds the finest-level result.
+// The FP32 (mixed) path restarts its Krylov recursion from FP64 true residuals.
+template <typename T>
+constexpr int mixed_of() { return sizeof(T) == 4 ? 1 : 0; }
+
 template <typename T>
 int seq_vcycle(Seq& q) {
     ifx_solver* S = q.S;
@@ -887,10 +900,20 @@ void seq_pre(Seq& q) {
     q.add(launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st));
 }
 
+template <typename T>
 void seq_pred_body(Seq& q, unsigned long long h) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
+    if (mixed_of<T>()) {
+        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, st));
+        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, st));
+        for (int par = 0; par < 2; par++) {
+            q.add(launch_pred_sweep32(S->dT0, S->nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, st));
+            q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st));
+        }
+        return;
+    }
     q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st));
     q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st));
     q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 1, st));
@@ -902,12 +925,13 @@ void seq_mid(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
+    if (mixed_of<T>()) q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 1, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
     q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
-    q.add(launch_bicg_start(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, st));
-    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, S->dCtl, 0ull, st));
+    q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st));
 }
 
 // One BiCGSTAB iteration with two V-cycle preconditioner applications.
@@ -916,6 +940,11 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
+    if (mixed_of<T>()) {
+        // FP64 true residual and restart for the instances whose FP32 recursion ran its course
+        q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, st));
+        q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, nullptr, 0ull, st));
+    }
     q.add(launch_bicg_p<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
     int e1 = seq_vcycle<T>(q);
     q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, st));
@@ -924,8 +953,8 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     int e2 = seq_vcycle<T>(q);
     q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, st));
     q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st));
-    q.add(launch_bicg_x(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dPart, st));
-    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st));
+    q.add(launch_bicg_x<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dPart, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, mixed_of<T>(), S->dCtl, h, st));
 }
 
 void seq_post(Seq& q) {
@@ -970,7 +999,7 @@ template <typename T>
 ifx_status step_method_host(ifx_solver* S) {
     Seq q{S};
     seq_pre(q);
-    IFX_TRY(host_loop(S, q, max_pred_pairs(S), [](Seq& qq, unsigned long long h) { seq_pred_body(qq, h); }));
+    IFX_TRY(host_loop(S, q, max_pred_pairs(S), [](Seq& qq, unsigned long long h) { seq_pred_body<T>(qq, h); }));
     seq_mid<T>(q);
     CUDA_TRY(cudaMemcpyAsync(S->hCtl, S->dCtl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, S->stream));
     CUDA_TRY(cudaStreamSynchronize(S->stream));
@@ -1047,7 +1076,7 @@ ifx_status build_graph(ifx_solver* S) {
     CUDA_TRY(cudaGraphCreate(&b.g, 0));
     S->graph = b.g;
     S->graph_nodes_pre = b.segment([](Seq& q) { seq_pre(q); });
-    S->graph_nodes_pred = b.loop([](Seq& q, unsigned long long h) { seq_pred_body(q, h); });
+    S->graph_nodes_pred = b.loop([](Seq& q, unsigned long long h) { seq_pred_body<T>(q, h); });
     S->graph_nodes_mid = b.segment([](Seq& q) { seq_mid<T>(q); });
     S->graph_nodes_ppe = b.loop([](Seq& q, unsigned long long h) { seq_ppe_body<T>(q, h); });
     S->graph_nodes_post = b.segment([](Seq& q) { seq_post(q); });
