@@ -74,6 +74,8 @@ def parse():
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
     ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch"],
                     help="workload of --profile: the cylinder, or the batched sweep of --batch instances")
+    ap.add_argument("--profile-rows", type=int, default=1, choices=[1, 4],
+                    help="rows per thread of the multigrid tile phases under --profile")
     return ap.parse_args()
 
 
@@ -175,7 +177,8 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm):
         ads = [s.stats(k).last_ad_iters for k in range(n_inst)]
         fields[name] = [(s.get(capi.FIELD_U, inst=k), s.get(capi.FIELD_V, inst=k), s.stats(k).cd) for k in range(n_inst)]
         res[name] = {"value": ncell * steps / (ms * 1e-3) / 1e6, "unit": METRIC, "ms_per_step": ms / steps,
-                     "exec": {0: "persistent", 1: "graph"}.get(mode, str(mode)), "gpu_launches": launches,
+                     "exec": {0: "persistent", 1: "graph"}.get(mode, str(mode)), "mg_tile_rows": s.mg_tile_rows(),
+                     "gpu_launches": launches,
                      "ppe_iters_mean": float(np.mean(its)), "ppe_iters_max": int(max(its)),
                      "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes()}
         res["cells"] = ncell
@@ -322,6 +325,7 @@ def main():
         else:
             cfg, _, _ = cases.cylinder(precision=prec)
             s = ifx.Solver.create(cfg, xf, yf)
+        s.set_mg_tile_rows(args.profile_rows)
         s.step(args.warmup)
         s.synchronize()
         torch.cuda.nvtx.range_push("step")

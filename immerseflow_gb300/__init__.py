@@ -53,6 +53,8 @@ _SIGS = {
     "ifx_destroy": (None, [C.c_void_p]),
     "ifx_step_async": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
+    "ifx_set_mg_tile_rows": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_get_mg_tile_rows": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_step_wait": (C.c_int, [C.c_void_p]),
     "ifx_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_get_exec_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -261,6 +263,14 @@ class Solver:
         m, ms = C.c_int(), C.c_double()
         _check(lib().ifx_autotune(self._h, int(steps), C.byref(m), C.byref(ms)))
         return m.value, ms.value
+
+    def set_mg_tile_rows(self, rows):
+        _check(lib().ifx_set_mg_tile_rows(self._h, int(rows)))
+
+    def mg_tile_rows(self):
+        r = C.c_int()
+        _check(lib().ifx_get_mg_tile_rows(self._h, C.byref(r)))
+        return r.value
 
     def set_active(self, inst, active):
         _check(lib().ifx_set_instance_active(self._h, int(inst), 1 if active else 0))

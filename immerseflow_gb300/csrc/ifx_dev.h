@@ -20,6 +20,7 @@ namespace ifx {
 constexpr int TILE_X = 32;
 constexpr int TILE_Y = 8;
 constexpr int TILE_THREADS = TILE_X * TILE_Y;
+constexpr int MG_ROWS_WIDE = 4;  // rows per thread of the wide multigrid tiles (32 x 32 cells)
 constexpr int GHOST_BLOCK = 256;
 constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift

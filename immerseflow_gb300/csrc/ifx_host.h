@@ -83,6 +83,12 @@ struct ifx_solver {
     std::vector<int> ntsm;
     std::vector<ifx::Tile*> dTre;    // per level >= 1: tiles of instances that have the level
     std::vector<int> ntre;
+    // the same lists with wide tiles (32 x 8*MG_ROWS_WIDE cells) for the multigrid phases
+    ifx::Tile* dT0W = nullptr;
+    int nt0W = 0;
+    std::vector<ifx::Tile*> dTsmW, dTreW;
+    std::vector<int> ntsmW, ntreW;
+    int mg_rows = 1;                 // rows per thread of the multigrid tile phases: 1 or MG_ROWS_WIDE
     ifx::Tile* dTall = nullptr;      // tiles of every level of every instance
     int* dSub = nullptr;             // LevelDev index of each instance's first small level
     int lmax = 0;

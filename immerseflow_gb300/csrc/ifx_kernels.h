@@ -46,13 +46,13 @@ cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstD
                           double* part, cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          const GhostDev* G, int flags, int src_alt, cudaStream_t s);
+                          const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                            const GhostDev* G, int fine_alt, cudaStream_t s);
+                            const GhostDev* G, int fine_alt, int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
-                           int coarse_alt, cudaStream_t s);
+                           int coarse_alt, int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s);

@@ -78,17 +78,17 @@ template <typename T>
 __global__ void k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          double* __restrict__ part) { b_bicg_x<T>(tiles, LV, I, S, part, blockIdx.x); }
-template <typename T>
+template <typename T, int R>
 __global__ void k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
-template <typename T>
+                         const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T, R>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
+template <typename T, int R>
 __global__ void k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                           const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
-template <typename T>
+                           const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
+template <typename T, int R>
 __global__ void k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                          const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
+                          const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
 __global__ void k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
@@ -202,23 +202,26 @@ cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstD
 }
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          const GhostDev* G, int flags, int src_alt, cudaStream_t s) {
+                          const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_smooth<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
+    if (rows == MG_ROWS_WIDE) k_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
+    else k_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                            const GhostDev* G, int fine_alt, cudaStream_t s) {
+                            const GhostDev* G, int fine_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_restrict<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
+    if (rows == MG_ROWS_WIDE) k_restrict<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
+    else k_restrict<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
-                           int coarse_alt, cudaStream_t s) {
+                           int coarse_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_prolong<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
+    if (rows == MG_ROWS_WIDE) k_prolong<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
+    else k_prolong<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
     return cudaGetLastError();
 }
 template <typename T>
@@ -263,17 +266,17 @@ cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_
 template cudaError_t launch_bicg_p<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
 template cudaError_t launch_bicg_s<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
 template cudaError_t launch_bicg_apply<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
-template cudaError_t launch_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
-template cudaError_t launch_restrict<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, cudaStream_t);
+template cudaError_t launch_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, int, cudaStream_t);
+template cudaError_t launch_restrict<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
 template cudaError_t launch_bicg_p<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
 template cudaError_t launch_bicg_s<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
 template cudaError_t launch_bicg_apply<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
-template cudaError_t launch_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
-template cudaError_t launch_restrict<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, cudaStream_t);
-template cudaError_t launch_prolong<double>(const Tile*, int, const LevelDev*, const InstState*, int, int,
+template cudaError_t launch_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, int, cudaStream_t);
+template cudaError_t launch_restrict<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_prolong<double>(const Tile*, int, const LevelDev*, const InstState*, int, int, int,
                                             cudaStream_t);
-template cudaError_t launch_prolong<float>(const Tile*, int, const LevelDev*, const InstState*, int, int,
-                                           cudaStream_t);
+template cudaError_t launch_prolong<float>(const Tile*, int, const LevelDev*, const InstState*, int, int, int,
+                                            cudaStream_t);
 template cudaError_t launch_subcycle<double>(const int*, int, const LevelDev*, const InstDev*, const InstState*,
                                              int, int, int, cudaStream_t);
 template cudaError_t launch_subcycle<float>(const int*, int, const LevelDev*, const InstDev*, const InstState*,

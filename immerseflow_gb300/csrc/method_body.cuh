@@ -866,106 +866,159 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
     if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
-// Weighted-Jacobi sweep on one multigrid level (tiles of that level for all
-// instances).  flags: 1 = start from e = 0.
-template <typename T>
+// Multigrid tile phases.  A tile is 32 columns by 8R rows of one level of
+// one instance; thread (w, lane) handles column i0+lane of rows j0+w+8r,
+// r < R.  Every load uses indices clamped into the level's interior, so all
+// of a thread's loads issue together (no load waits on the stencil byte);
+// results are stored for live cells only.  The arithmetic per cell does not
+// depend on R.
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
+                                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                         const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& L = LV[t.lev];
     if (S[L.inst].ppe_state != ST_ACTIVE) return;
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    if (!live0(L, i, j, id, bt)) return;
     const T* src = (const T*)(src_alt ? L.e2 : L.e);
     T* dst = (T*)(src_alt ? L.e : L.e2);
+    const T* rr = (const T*)L.r;
     const T om = (T)I[L.inst].omega;
-    const T r = ((const T*)L.r)[id];
-    T Le, D;
-    if (L.depth == 0) lap<T, T, true>(L, src, i, j, id, bt, G, I[L.inst].gidx, Le, D);
-    else lap<T, T, false>(L, src, i, j, id, bt, G, nullptr, Le, D);
-    dst[id] = (flags & 1) ? -om * r * rcpa(D) : src[id] + om * (Le - r) * rcpa(D);
+    const int* gidx = L.depth == 0 ? I[L.inst].gidx : nullptr;
+    const int P = L.pitch;
+    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    const int ic = clampi(i, 1, L.NX);
+    int id[R];
+    uint8_t bt[R];
+    T val[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = jb + 8 * r, jc = clampi(j, 1, L.NY);
+        id[r] = ic + jc * P;
+        bt[r] = (i == ic && j == jc) ? __ldg(&L.bits[id[r]]) : (uint8_t)0;
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int jc = id[r] / P;
+        T Le, D;
+        if (L.depth == 0) lap_p<T, T, true>(L, src, ic, jc, id[r], P, bt[r], G, gidx, Le, D);
+        else lap_p<T, T, false>(L, src, ic, jc, id[r], P, bt[r], G, nullptr, Le, D);
+        val[r] = (flags & 1) ? -om * rr[id[r]] * rcpa(D) : src[id[r]] + om * (Le - rr[id[r]]) * rcpa(D);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (bt[r] & 0x0F) dst[id[r]] = val[r];
 }
 
 // Restriction of the fine residual (area weighted) onto coarse tiles, fused
 // with the first (zero-start) smoothing sweep of a middle coarse level.
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                           const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                           const GhostDev* __restrict__ G, int fine_alt, int vb) {
+                                           const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                           const GhostDev* __restrict__ G, int fine_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& C = LV[t.lev];
     if (S[C.inst].ppe_state != ST_ACTIVE) return;
     const LevelDev& F = LV[C.parent];
-    int I0, J0;
-    tile_ij(t, I0, J0);
-    if (I0 < 1 || I0 > C.NX || J0 < 1 || J0 > C.NY) return;
-    const int cid = I0 + J0 * C.pitch;
-    const uint8_t cb = __ldg(&C.bits[cid]);
-    T* rc = (T*)C.r;
-    if (!(cb & 0x0F)) {
-        rc[cid] = (T)0;
-        return;
-    }
     const T* fe = (const T*)(fine_alt ? F.e2 : F.e);
     const T* fr = (const T*)F.r;
     const T* fdw = LvA<T>::dw(F);
-    const T* fdh = LvA<T>::dh(F);  // read through __ldg below
-    T acc = (T)0;
-    const int cx = C.cx, cy = C.cy;
+    const T* fdh = LvA<T>::dh(F);
+    const int* gidx = F.depth == 0 ? I[C.inst].gidx : nullptr;
+    T* rc = (T*)C.r;
+    const T om = (T)I[C.inst].omega;
+    const int cx = C.cx, cy = C.cy, CP = C.pitch, FP = F.pitch;
+    const int I0 = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    const int I0c = clampi(I0, 1, C.NX);
+    int cid[R];
+    bool in[R];
+    uint8_t cb[R];
+    T rv[R], ev[R];
 #pragma unroll
-    for (int dj = 0; dj < 2; dj++)
+    for (int r = 0; r < R; r++) {
+        const int J0 = jb + 8 * r, J0c = clampi(J0, 1, C.NY);
+        in[r] = I0 == I0c && J0 == J0c;
+        cid[r] = I0c + J0c * CP;
+        cb[r] = in[r] ? __ldg(&C.bits[cid[r]]) : (uint8_t)0;
+    }
 #pragma unroll
-        for (int di = 0; di < 2; di++) {
-            const int i = cx * (I0 - 1) + 1 + di, j = cy * (J0 - 1) + 1 + dj;
-            if (di >= cx || dj >= cy || i > F.NX || j > F.NY) continue;
-            const int id = i + j * F.pitch;
-            const uint8_t bt = __ldg(&F.bits[id]);
-            if (!(bt & 0x0F)) continue;
-            T Le, D;
-            if (F.depth == 0) lap<T, T, true>(F, fe, i, j, id, bt, G, I[C.inst].gidx, Le, D);
-            else lap<T, T, false>(F, fe, i, j, id, bt, G, nullptr, Le, D);
-            acc += (fr[id] - Le) * (__ldg(&fdw[i]) * __ldg(&fdh[j]));
+    for (int r = 0; r < R; r++) {
+        const int J0c = cid[r] / CP;
+        T acc = (T)0;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int fi = cx * (I0c - 1) + 1 + di, fj = cy * (J0c - 1) + 1 + dj;
+                const bool child = di < cx && dj < cy && fi <= F.NX && fj <= F.NY;
+                const int fic = child ? fi : 1, fjc = child ? fj : 1, fid = fic + fjc * FP;
+                const uint8_t fb = child ? __ldg(&F.bits[fid]) : (uint8_t)0;
+                T Le, D;
+                if (F.depth == 0) lap_p<T, T, true>(F, fe, fic, fjc, fid, FP, fb, G, gidx, Le, D);
+                else lap_p<T, T, false>(F, fe, fic, fjc, fid, FP, fb, G, nullptr, Le, D);
+                const T term = (fr[fid] - Le) * (__ldg(&fdw[fic]) * __ldg(&fdh[fjc]));
+                if (fb & 0x0F) acc += term;
+            }
+        rv[r] = acc / (__ldg(&LvA<T>::dw(C)[I0c]) * __ldg(&LvA<T>::dh(C)[J0c]));
+        ev[r] = -om * rv[r] * rcpa(lap_diag<T>(C, I0c, J0c, cb[r]));
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        if (!in[r]) continue;
+        if (!(cb[r] & 0x0F)) {
+            rc[cid[r]] = (T)0;
+            continue;
         }
-    const T rv = acc / (__ldg(&LvA<T>::dw(C)[I0]) * __ldg(&LvA<T>::dh(C)[J0]));
-    rc[cid] = rv;
-    if (C.child >= 0) {  // middle level: fused first sweep from zero
-        T Le, D;
-        lap<T, T, false>(C, (const T*)C.e, I0, J0, cid, cb, G, nullptr, Le, D);
-        ((T*)C.e)[cid] = -(T)I[C.inst].omega * rv * rcpa(D);
+        rc[cid[r]] = rv[r];
+        if (C.child >= 0) ((T*)C.e)[cid[r]] = ev[r];  // middle level: fused first sweep from zero
     }
 }
 
 // Bilinear prolongation of the coarse correction, added on the fine level.
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                          const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
+                                          const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
     if (S[F.inst].ppe_state != ST_ACTIVE) return;
     const LevelDev& C = LV[F.child];
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    if (!live0(F, i, j, id, bt)) return;
     // the coarsest level's solution is always in e; a middle level's in the buffer its sweeps ended on
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
     T* fe = (T*)(fine_alt ? F.e2 : F.e);
-    const int I0 = __ldg(&F.pI[i]), In = __ldg(&F.pIn[i]), J0 = __ldg(&F.pJ[j]), Jn = __ldg(&F.pJn[j]);
-    const T wx = __ldg(&LvA<T>::pwx(F)[i]), wy = __ldg(&LvA<T>::pwy(F)[j]);
-    const T sx = (T)__ldg(&F.psx[i]), sy = (T)__ldg(&F.psy[j]);
-    T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
-    const int CP = C.pitch;
-    const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
-    w00 = (__ldg(&C.bits[c00]) & 0x0F) ? w00 : (T)0;
-    w10 = (__ldg(&C.bits[c10]) & 0x0F) ? w10 : (T)0;
-    w01 = (__ldg(&C.bits[c01]) & 0x0F) ? w01 : (T)0;
-    w11 = (__ldg(&C.bits[c11]) & 0x0F) ? w11 : (T)0;
-    const T sw = w00 + w10 + w01 + w11;
-    const T val = (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
-    fe[id] += val;
+    const int P = F.pitch, CP = C.pitch;
+    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    const int ic = clampi(i, 1, F.NX);
+    const int I0 = __ldg(&F.pI[ic]), In = __ldg(&F.pIn[ic]);
+    const T wx = __ldg(&LvA<T>::pwx(F)[ic]), sx = (T)__ldg(&F.psx[ic]);
+    int id[R];
+    uint8_t bt[R];
+    T val[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = jb + 8 * r, jc = clampi(j, 1, F.NY);
+        id[r] = ic + jc * P;
+        bt[r] = (i == ic && j == jc) ? __ldg(&F.bits[id[r]]) : (uint8_t)0;
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int jc = id[r] / P;
+        const int J0 = __ldg(&F.pJ[jc]), Jn = __ldg(&F.pJn[jc]);
+        const T wy = __ldg(&LvA<T>::pwy(F)[jc]), sy = (T)__ldg(&F.psy[jc]);
+        T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
+        const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
+        w00 = (__ldg(&C.bits[c00]) & 0x0F) ? w00 : (T)0;
+        w10 = (__ldg(&C.bits[c10]) & 0x0F) ? w10 : (T)0;
+        w01 = (__ldg(&C.bits[c01]) & 0x0F) ? w01 : (T)0;
+        w11 = (__ldg(&C.bits[c11]) & 0x0F) ? w11 : (T)0;
+        const T sw = w00 + w10 + w01 + w11;
+        val[r] = fe[id[r]] + (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (bt[r] & 0x0F) fe[id[r]] = val[r];
 }
 
 // ------------------------------------------------- small levels (sub-cycle)

@@ -670,7 +670,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     IFX_TRY(dupload(S, &S->dIbm, hIbm));
     IFX_TRY(dalloc(S, &S->dGval, 3 * (size_t)std::max(1, S->ng)));
     IFX_TRY(dalloc(S, &S->dBiIp, 4 * (size_t)std::max(1, S->nibm)));
-    std::vector<std::vector<Tile>> tsm(lmax), tre(lmax);
+    std::vector<std::vector<Tile>> tsm(lmax), tre(lmax), tsmW(lmax), treW(lmax);
+    std::vector<Tile> hT0W;
     std::vector<Tile> hTall;
     std::vector<int> hSub;
     for (int k = 0; k < n; k++) {
@@ -741,8 +742,11 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             // tiles
             const int lv = I.lev_base + l;
             std::vector<Tile> tl;
+            std::vector<Tile> tw;  // wide tiles of the multigrid phases
             for (int j0 = 0; j0 < L.ny; j0 += TILE_Y)
                 for (int i0 = 0; i0 < L.nx; i0 += TILE_X) tl.push_back(Tile{k, lv, i0, j0});
+            for (int j0 = 0; j0 < L.ny; j0 += TILE_Y * MG_ROWS_WIDE)
+                for (int i0 = 0; i0 < L.nx; i0 += TILE_X) tw.push_back(Tile{k, lv, i0, j0});
             ld.tbeg = (int)hTall.size();
             ld.tcnt = (int)tl.size();
             hTall.insert(hTall.end(), tl.begin(), tl.end());
@@ -751,11 +755,14 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
                 I.tile_beg = (int)hT0.size();
                 I.tile_cnt = (int)tl.size();
                 hT0.insert(hT0.end(), tl.begin(), tl.end());
+                hT0W.insert(hT0W.end(), tw.begin(), tw.end());
             } else {
                 // tile phases: restriction into every level down to the first
                 // small one, smoothing and prolongation above it
                 if (l <= lb) tre[l].insert(tre[l].end(), tl.begin(), tl.end());
                 if (l < lb) tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
+                if (l <= lb) treW[l].insert(treW[l].end(), tw.begin(), tw.end());
+                if (l < lb) tsmW[l].insert(tsmW[l].end(), tw.begin(), tw.end());
             }
         }
         hSub.push_back(I.lev_base + lb);
@@ -789,6 +796,18 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dupload(S, &S->dTre[l], tre[l]));
         S->ntsm[l] = (int)tsm[l].size();
         S->ntre[l] = (int)tre[l].size();
+    }
+    IFX_TRY(dupload(S, &S->dT0W, hT0W));
+    S->nt0W = (int)hT0W.size();
+    S->dTsmW.assign(lmax, nullptr);
+    S->dTreW.assign(lmax, nullptr);
+    S->ntsmW.assign(lmax, 0);
+    S->ntreW.assign(lmax, 0);
+    for (int l = 1; l < lmax; l++) {
+        IFX_TRY(dupload(S, &S->dTsmW[l], tsmW[l]));
+        IFX_TRY(dupload(S, &S->dTreW[l], treW[l]));
+        S->ntsmW[l] = (int)tsmW[l].size();
+        S->ntreW[l] = (int)treW[l].size();
     }
     IFX_TRY(dupload(S, &S->dTall, hTall));
     IFX_TRY(dupload(S, &S->dSub, hSub));
@@ -854,34 +873,43 @@ int seq_vcycle(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int L = S->lmax, pre = S->mg_pre, post = S->mg_post;
+    // multigrid tile lists: 32x8 tiles, or wide tiles with MG_ROWS_WIDE rows per thread
+    const int R = S->mg_rows;
+    const bool W = R == MG_ROWS_WIDE;
+    const Tile* t0 = W ? S->dT0W : S->dT0;
+    const int nt0 = W ? S->nt0W : S->nt0;
+    auto tsm = [&](int l) { return W ? S->dTsmW[l] : S->dTsm[l]; };
+    auto ntsm = [&](int l) { return W ? S->ntsmW[l] : S->ntsm[l]; };
+    auto tre = [&](int l) { return W ? S->dTreW[l] : S->dTre[l]; };
+    auto ntre = [&](int l) { return W ? S->ntreW[l] : S->ntre[l]; };
     // finest level: first sweep from zero, then the rest of the pre-smoothing
-    q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, st));
+    q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, R, st));
     int cur0 = 1;
     for (int k = 1; k < pre; k++) {
-        q.add(launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur0, st));
+        q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur0, R, st));
         cur0 ^= 1;
     }
     // large coarse levels: one launch per phase
     for (int l = 1; l < L; l++) {
-        if (S->ntre[l] == 0) break;
-        q.add(launch_restrict<T>(S->dTre[l], S->ntre[l], S->dLV, S->dI, S->dS, S->dG, parity_after_pre(l - 1, pre), st));
-        if (S->ntsm[l] == 0) continue;
+        if (ntre(l) == 0) break;
+        q.add(launch_restrict<T>(tre(l), ntre(l), S->dLV, S->dI, S->dS, S->dG, parity_after_pre(l - 1, pre), R, st));
+        if (ntsm(l) == 0) continue;
         int cur = 0;
         for (int k = 1; k < pre; k++) {
-            q.add(launch_smooth<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, S->dG, 0, cur, st));
+            q.add(launch_smooth<T>(tsm(l), ntsm(l), S->dLV, S->dI, S->dS, S->dG, 0, cur, R, st));
             cur ^= 1;
         }
     }
     // small levels of every instance: one block each
     q.add(launch_subcycle<T>(S->dSub, (int)S->inst.size(), S->dLV, S->dI, S->dS, pre, post, S->sub_bytes, st));
     for (int l = L - 2; l >= 0; l--) {
-        const Tile* tl = l == 0 ? S->dT0 : S->dTsm[l];
-        const int nt = l == 0 ? S->nt0 : S->ntsm[l];
+        const Tile* tl = l == 0 ? t0 : tsm(l);
+        const int nt = l == 0 ? nt0 : ntsm(l);
         if (nt == 0) continue;
         int cur = parity_after_pre(l, pre);
-        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), st));
+        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), R, st));
         for (int k = 0; k < post; k++) {
-            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur, st));
+            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur, R, st));
             cur ^= 1;
         }
         if (l == 0) cur0 = cur;
@@ -1469,6 +1497,16 @@ extern "C" ifx_status ifx_set_instance_active(ifx_solver* S, int inst, int activ
     return IFX_OK;
 }
 
+// Rows per thread of the multigrid tile phases; the step graph is rebuilt on change.
+static void set_mg_rows(ifx_solver* S, int rows) {
+    if (rows == S->mg_rows) return;
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    if (S->graph) cudaGraphDestroy(S->graph);
+    S->gexec = nullptr;
+    S->graph = nullptr;
+    S->mg_rows = rows;
+}
+
 namespace {
 // Device copy of the state a time step carries to the next one (cell and
 // face velocities, convection history, pressure, outflow boundary values and
@@ -1515,15 +1553,19 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
     StateSnapshot snap;
     IFX_TRY(snap.take(S));
     const long long steps0 = S->steps_done;
-    const int saved = S->exec_override;
-    std::vector<int> cand;
-    if (S->persist_grid > 0) cand.push_back(IFX_EXEC_PERSISTENT);
-    cand.push_back(IFX_EXEC_GRAPH);
-    int best = cand[0];
+    const int saved = S->exec_override, saved_rows = S->mg_rows;
+    // (execution mode, rows per thread of the multigrid tile phases); the
+    // persistent kernel always uses 32x8 tiles
+    std::vector<std::pair<int, int>> cand;
+    if (S->persist_grid > 0) cand.push_back({IFX_EXEC_PERSISTENT, 1});
+    cand.push_back({IFX_EXEC_GRAPH, 1});
+    cand.push_back({IFX_EXEC_GRAPH, MG_ROWS_WIDE});
+    std::pair<int, int> best = cand[0];
     double best_ms = 1e300;
     ifx_status st = IFX_OK;
-    for (int m : cand) {
-        S->exec_override = m;
+    for (const auto& c : cand) {
+        S->exec_override = c.first;
+        set_mg_rows(S, c.second);
         st = ifx_step(S, 1);  // warm-up (builds the graph on first use)
         if (st == IFX_OK) st = ifx_step(S, steps);
         if (st == IFX_OK) st = snap.restore(S);
@@ -1531,18 +1573,35 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
         const double ms = S->last_ms / steps;
         if (ms < best_ms) {
             best_ms = ms;
-            best = m;
+            best = c;
         }
     }
     S->steps_done = steps0;
     if (st != IFX_OK) {
         S->exec_override = saved;
+        set_mg_rows(S, saved_rows);
         snap.restore(S);
         return st;
     }
-    S->exec_override = best;
-    if (chosen) *chosen = best;
+    S->exec_override = best.first;
+    set_mg_rows(S, best.second);
+    if (chosen) *chosen = best.first;
     if (ms_per_step) *ms_per_step = best_ms;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_set_mg_tile_rows(ifx_solver* S, int rows) {
+    if (!S || (rows != 1 && rows != MG_ROWS_WIDE)) return set_error(IFX_ERR_ARG, "ifx_set_mg_tile_rows: rows must be 1 or 4");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_set_mg_tile_rows needs a METHOD-mode solver");
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    set_mg_rows(S, rows);
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_mg_tile_rows(const ifx_solver* S, int* rows) {
+    if (!S || !rows) return set_error(IFX_ERR_ARG, "ifx_get_mg_tile_rows: bad argument");
+    *rows = S->mg_rows;
     return IFX_OK;
 }
 
@@ -1744,7 +1803,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
     CUDA_TRY(launch_step_begin(S->dI, S->dS, n, st));
     auto one = [&]() -> cudaError_t {
         switch (kernel) {
-            case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, st);
+            case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, 1, st);
             case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, st);
             case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
             case 4: return launch_barrier_bench(S->dBar, S->persist_grid, 1000, st);

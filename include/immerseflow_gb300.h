@@ -186,10 +186,15 @@ ifx_status ifx_set_exec_mode(ifx_solver* s, int mode);
 ifx_status ifx_get_exec_mode(ifx_solver* s, int* mode);
 
 /* Autotuner (no reference counterpart): times `steps` steps in each available
- * execution mode (after one warm-up step each), restores the solver state
- * afterwards, and keeps the fastest mode.  The modes give bit-identical
- * results, so tuning never changes an answer. */
+ * execution mode and multigrid tile shape (after one warm-up step each),
+ * restores the solver state afterwards, and keeps the fastest.  All of them
+ * give bit-identical results, so tuning never changes an answer. */
 ifx_status ifx_autotune(ifx_solver* s, int steps, int* chosen_mode, double* ms_per_step);
+/* Multigrid tile shape of the graph and host-loop modes: 1 = 32x8 cells (one
+ * row per thread), 4 = 32x32 cells (four rows per thread, more loads in flight;
+ * suits large batches).  Results do not depend on it.  The autotuner sets it. */
+ifx_status ifx_set_mg_tile_rows(ifx_solver* s, int rows);
+ifx_status ifx_get_mg_tile_rows(const ifx_solver* s, int* rows);
 
 /* Batch membership (no reference counterpart): an inactive instance is left
  * unchanged by later steps while the others advance. */

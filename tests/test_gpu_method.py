@@ -92,13 +92,14 @@ def test_rotated_ellipse_stretched_vs_oracle(oracle):
     _compare(s, o, tol=1e-9)
 
 
-def _run_mode(mode, specs, nsteps):
+def _run_mode(mode, specs, nsteps, rows=1):
     os.environ["IFX_EXEC"] = mode
     try:
         if len(specs) == 1:
             s = ifx.Solver.create(*specs[0])
         else:
             s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+        s.set_mg_tile_rows(rows)
         s.step(nsteps)
         return s
     finally:
@@ -111,10 +112,12 @@ def test_execution_modes_bit_identical(prec):
     device bodies: the results must agree bit for bit."""
     specs = [small_cylinder(prec=prec)]
     runs = {m: _run_mode(m, specs, 3) for m in ("persistent", "graph", "host")}
+    runs["graph_wide"] = _run_mode("graph", specs, 3, rows=4)
     for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF):
         a = runs["persistent"].get(f)
         assert np.array_equal(a, runs["graph"].get(f)), f
         assert np.array_equal(a, runs["host"].get(f)), f
+        assert np.array_equal(a, runs["graph_wide"].get(f)), f
     assert runs["persistent"].stats().last_ppe_iters == runs["graph"].stats().last_ppe_iters
 
 
@@ -122,9 +125,11 @@ def test_persistent_batch_equals_graph_batch():
     specs = [small_cylinder(nx=96, ny=64), cases.cavity(n=40), small_cylinder(nx=70, ny=90, angle=25.0, b=0.25)]
     a = _run_mode("persistent", specs, 2)
     b = _run_mode("graph", specs, 2)
+    c = _run_mode("graph", specs, 2, rows=4)
     for k in range(3):
         for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
             assert np.array_equal(a.get(f, inst=k), b.get(f, inst=k)), (k, f)
+            assert np.array_equal(a.get(f, inst=k), c.get(f, inst=k)), (k, f)
 
 
 def test_batch_member_equals_alone():
