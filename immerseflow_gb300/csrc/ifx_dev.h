@@ -190,7 +190,9 @@ struct LoopCtl {
     int active;
     unsigned int ticket;
     int result;
-    int pad;
+    int due;         // instances that need the optional phases of the next loop body
+    int due_result;  // published with result: predictor refresh or Krylov restart due
+    int pad[3];
 };
 
 }  // namespace ifx

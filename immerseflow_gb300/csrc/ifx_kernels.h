@@ -7,7 +7,7 @@
 namespace ifx {
 
 // ---- method path (kernels_method.cu)
-cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, cudaStream_t s);
+cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, LoopCtl* ctl, cudaStream_t s);
 cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStream_t s);
 cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int comps, double* gval,
                               cudaStream_t s);
@@ -19,7 +19,7 @@ cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, 
 cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng, const LevelDev* LV, const InstDev* I,
                                 const InstState* S, double* part, int parity, cudaStream_t s);
 cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
-                                int stage, int finalize, cudaStream_t s);
+                                int stage, int finalize, const LoopCtl* ctl, cudaStream_t s);
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
                                LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
@@ -27,7 +27,7 @@ cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* par
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int restart_only, cudaStream_t s);
+                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, cudaStream_t s);
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
                                  int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 template <typename T>

@@ -25,7 +25,7 @@
 
 namespace ifx {
 
-__global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n) { b_step_begin(I, S, n, blockIdx.x); }
+__global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl) { b_step_begin(I, S, n, ctl, blockIdx.x); }
 __global__ void k_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I) { b_outflow(G, ng, I, blockIdx.x); }
 __global__ void k_ghost_gather(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
                                int comps, double* __restrict__ gval) { b_ghost_gather(G, ng, I, comps, gval, blockIdx.x); }
@@ -41,10 +41,15 @@ __global__ void k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const
                                const InstState* __restrict__ S, double* __restrict__ part, int parity) {
     b_pred_sweep32(tiles, ntiles, G, ng, LV, I, S, part, parity, blockIdx.x);
 }
+// Optional phases (mixed path) run as grid-stride loops on a fixed grid that
+// returns at once when the last vote found nothing due.
+constexpr int OPT_GRID = 1024;
 __global__ void k_pred_refresh(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const InstDev* __restrict__ I, const InstState* __restrict__ S, int stage,
-                               int finalize) {
-    b_pred_refresh(tiles, ntiles, G, ng, I, S, stage, finalize, blockIdx.x);
+                               int finalize, const LoopCtl* ctl) {
+    if (!finalize && none_due(ctl)) return;
+    const int nvb = ntiles + (ng + TILE_THREADS - 1) / TILE_THREADS;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) b_pred_refresh(tiles, ntiles, G, ng, I, S, stage, finalize, vb);
 }
 __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
@@ -56,8 +61,10 @@ __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restric
 template <typename T>
 __global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                             const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only) {
-    b_bicg_start<T>(tiles, LV, I, S, G, part, restart_only, blockIdx.x);
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only,
+                             const LoopCtl* ctl, int nt) {
+    if (restart_only && none_due(ctl)) return;
+    for (int vb = blockIdx.x; vb < nt; vb += gridDim.x) b_bicg_start<T>(tiles, LV, I, S, G, part, restart_only, vb);
 }
 __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                 const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
@@ -110,8 +117,8 @@ __global__ void k_forces(const InstDev* __restrict__ I, InstState* __restrict__ 
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
-cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, cudaStream_t s) {
-    k_step_begin<<<nblk(n, 128), 128, 0, s>>>(I, S, n);
+cudaError_t launch_step_begin(const InstDev* I, InstState* S, int n, LoopCtl* ctl, cudaStream_t s) {
+    k_step_begin<<<nblk(n, 128), 128, 0, s>>>(I, S, n, ctl);
     return cudaGetLastError();
 }
 cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStream_t s) {
@@ -142,8 +149,9 @@ cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng
     return cudaGetLastError();
 }
 cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
-                                int stage, int finalize, cudaStream_t s) {
-    k_pred_refresh<<<nt + nblk(ng, TILE_THREADS), TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize);
+                                int stage, int finalize, const LoopCtl* ctl, cudaStream_t s) {
+    const int nvb = nt + nblk(ng, TILE_THREADS);
+    k_pred_refresh<<<nvb < OPT_GRID ? nvb : OPT_GRID, TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize, ctl);
     return cudaGetLastError();
 }
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
@@ -162,8 +170,9 @@ cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part
 }
 template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int restart_only, cudaStream_t s) {
-    k_bicg_start<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only);
+                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, cudaStream_t s) {
+    const int grid = restart_only && nt > OPT_GRID ? OPT_GRID : nt;
+    k_bicg_start<T><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt);
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
@@ -285,9 +294,9 @@ template cudaError_t subcycle_smem_limit<double>(int);
 template cudaError_t subcycle_smem_limit<float>(int);
 
 template cudaError_t launch_bicg_start<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                               const GhostDev*, double*, int, cudaStream_t);
+                                               const GhostDev*, double*, int, const LoopCtl*, cudaStream_t);
 template cudaError_t launch_bicg_start<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                              const GhostDev*, double*, int, cudaStream_t);
+                                              const GhostDev*, double*, int, const LoopCtl*, cudaStream_t);
 template cudaError_t launch_bicg_x<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
                                            cudaStream_t);
 template cudaError_t launch_bicg_x<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,

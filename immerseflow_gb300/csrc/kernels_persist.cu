@@ -75,6 +75,12 @@ __device__ __forceinline__ bool any_pred_refresh_due(const InstDev* I, const Ins
     }
     return __syncthreads_or(a) != 0;
 }
+__device__ __forceinline__ bool any_restart_due(const InstState* S, int n) {
+    int a = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        a |= *(const volatile int*)&S[k].ppe_state == ST_ACTIVE && *(const volatile int*)&S[k].restart != 0;
+    return __syncthreads_or(a) != 0;
+}
 __device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
     int a = 0;
     for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].ppe_state == ST_ACTIVE);
@@ -148,7 +154,7 @@ __device__ bool vcycle(const PersistPlan& P, int* res, unsigned long long& ep) {
 template <typename T>
 __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     const int n = P.ninst;
-    FOR_VB(nchunks(n)) b_step_begin(P.I, P.S, n, vb);
+    FOR_VB(nchunks(n)) b_step_begin(P.I, P.S, n, nullptr, vb);
     FOR_VB(nchunks(P.ng)) b_outflow(P.G, P.ng, P.I, vb);
     BAR();
     if (!ghost_fill(P, 3, ep)) return false;
@@ -200,7 +206,7 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     // pressure: BiCGSTAB iterations until every instance converged
     for (int it = 0; it < P.ppe_bodies; it++) {
         if (!any_ppe_active(P.S, n)) break;
-        if (mixed) {  // FP64 true residual and restart where the FP32 recursion ran its course
+        if (mixed && any_restart_due(P.S, n)) {  // FP64 true residual and restart where the FP32 recursion ran its course
             FOR_VB(P.nt0) b_bicg_start<T>(P.t0, P.LV, P.I, P.S, P.G, P.part, 1, vb);
             BAR();
             FOR_VB(n) b_bicg_reduce_r(P.I, P.S, P.part, 2, 1, nullptr, 0ull, vb);

@@ -128,21 +128,33 @@ __device__ __forceinline__ void inst_sum(const double* part, int beg, int cnt, d
     for (int k = 0; k < NV; k++) res[k] = out[k];
 }
 
-__device__ __forceinline__ void loop_vote(LoopCtl* ctl, bool active, unsigned long long handle) {
+// due: the instance needs the optional phases of the next loop body (mixed
+// path: predictor refresh, Krylov restart); their kernels return at once
+// when no instance does.
+__device__ __forceinline__ void loop_vote(LoopCtl* ctl, bool active, unsigned long long handle, bool due = false) {
     // thread 0 of each voting block; no-op inside the persistent kernel (ctl == nullptr)
     if (!ctl) return;
     if (active) atomicAdd(&ctl->active, 1);
+    if (due) atomicAdd(&ctl->due, 1);
     __threadfence();
     unsigned int t = atomicAdd(&ctl->ticket, 1u);
     if (t == gridDim.x - 1) {
         __threadfence();
         int a = atomicAdd(&ctl->active, 0);
+        int d = atomicAdd(&ctl->due, 0);
         ctl->result = a;
+        ctl->due_result = d;
         ctl->active = 0;
+        ctl->due = 0;
         ctl->ticket = 0u;
         __threadfence();
         if (handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, a > 0 ? 1u : 0u);
     }
+}
+
+// Optional phases: nothing to do when the last vote found no instance due.
+__device__ __forceinline__ bool none_due(const LoopCtl* ctl) {
+    return ctl != nullptr && *(const volatile int*)&ctl->due_result == 0;
 }
 
 __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* qb, double c0) {
@@ -236,7 +248,9 @@ __device__ __forceinline__ TC lap_diag(const LevelDev& L, int i, int j, uint8_t 
 
 // ------------------------------------------------------ step bookkeeping
 
-__device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, InstState* S, int n, int vb) {
+__device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl,
+                                             int vb) {
+    if (ctl && vb == 0 && threadIdx.x == 0) ctl->due_result = 1;  // the first predictor body refreshes
     int k = vb * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int st = I[k].retired ? ST_DONE : ST_ACTIVE;
@@ -419,7 +433,7 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
     const int k = vb;
     const InstDev& in = I[k];
     const int st = S[k].pred_state;
-    bool active = false;
+    bool active = false, due = false;
     if (st == ST_ACTIVE) {
         double r[1];
         inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
@@ -430,11 +444,12 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
             const bool done = r[0] <= in.ad_lim || it >= in.ad_itermax;
             if (done) S[k].pred_state = parity == 0 ? ST_FINAL_IN_ALT : ST_DONE;
             active = !done;
+            due = active && it % (in.mixed_inner > 0 ? in.mixed_inner : 8) == 0;
         }
     } else if (st == ST_FINAL_IN_ALT) {
         if (threadIdx.x == 0) S[k].pred_state = ST_DONE;
     }
-    if (threadIdx.x == 0) loop_vote(ctl, active, handle);
+    if (threadIdx.x == 0) loop_vote(ctl, active, handle, due);
 }
 
 // ------------------------------------------- mixed-path predictor (FP32)
@@ -708,7 +723,8 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
                                                 LoopCtl* ctl, unsigned long long handle, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
-    bool active = false;
+    bool active = false, due = false;
+    if (start == 2 && none_due(ctl)) return;
     const bool run = S[k].ppe_state == ST_ACTIVE && (start != 2 || S[k].restart);
     if (run) {
         double r[4];
@@ -739,6 +755,7 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
                                      st.ppe_iters - st.restart_it >= PPE_RESTART_EVERY)) {
                 st.restart = 1;
                 active = true;
+                due = true;
             } else {
                 const double rho1 = r[2];
                 st.beta = (rho1 / st.rho) * (st.alpha / st.omega);
@@ -747,7 +764,7 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
             }
         }
     }
-    if (threadIdx.x == 0 && start != 2) loop_vote(ctl, active, handle);
+    if (threadIdx.x == 0 && start != 2) loop_vote(ctl, active, handle, due);
 }
 
 // p_dir = r + beta (p_dir - omega v); preconditioner input.

@@ -921,7 +921,7 @@ void seq_pre(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    q.add(launch_step_begin(S->dI, S->dS, n, st));
+    q.add(launch_step_begin(S->dI, S->dS, n, S->dCtl, st));
     q.add(launch_outflow(S->dG, S->ng, S->dI, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;  // ghost fill is two kernels
@@ -934,8 +934,8 @@ void seq_pred_body(Seq& q, unsigned long long h) {
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
     if (mixed_of<T>()) {
-        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, st));
-        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, st));
+        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, S->dCtl, st));
+        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, S->dCtl, st));
         for (int par = 0; par < 2; par++) {
             q.add(launch_pred_sweep32(S->dT0, S->nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, st));
             q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st));
@@ -953,12 +953,12 @@ void seq_mid(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    if (mixed_of<T>()) q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 1, st));
+    if (mixed_of<T>()) q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 1, nullptr, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
     q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
-    q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, st));
+    q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, nullptr, st));
     q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st));
 }
 
@@ -970,8 +970,8 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     const int n = (int)S->inst.size();
     if (mixed_of<T>()) {
         // FP64 true residual and restart for the instances whose FP32 recursion ran its course
-        q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, st));
-        q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, nullptr, 0ull, st));
+        q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, st));
+        q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st));
     }
     q.add(launch_bicg_p<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
     int e1 = seq_vcycle<T>(q);
@@ -1800,7 +1800,7 @@ template <typename T>
 static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms) {
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    CUDA_TRY(launch_step_begin(S->dI, S->dS, n, st));
+    CUDA_TRY(launch_step_begin(S->dI, S->dS, n, S->dCtl, st));
     auto one = [&]() -> cudaError_t {
         switch (kernel) {
             case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, 1, st);
