@@ -86,15 +86,15 @@ __global__ void k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restr
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          double* __restrict__ part) { b_bicg_x<T>(tiles, LV, I, S, part, blockIdx.x); }
 template <typename T, int R>
-__global__ void k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T, R>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
 template <typename T, int R>
-__global__ void k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, 4) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
 template <typename T, int R>
-__global__ void k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, 4) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
 __global__ void k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,

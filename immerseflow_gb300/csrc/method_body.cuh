@@ -908,18 +908,19 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
     const int P = L.pitch;
     const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
     const int ic = clampi(i, 1, L.NX);
-    int id[R];
+    int id[R], jcs[R];
     uint8_t bt[R];
     T val[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int j = jb + 8 * r, jc = clampi(j, 1, L.NY);
+        jcs[r] = jc;
         id[r] = ic + jc * P;
         bt[r] = (i == ic && j == jc) ? __ldg(&L.bits[id[r]]) : (uint8_t)0;
     }
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int jc = id[r] / P;
+        const int jc = jcs[r];
         T Le, D;
         if (L.depth == 0) lap_p<T, T, true>(L, src, ic, jc, id[r], P, bt[r], G, gidx, Le, D);
         else lap_p<T, T, false>(L, src, ic, jc, id[r], P, bt[r], G, nullptr, Le, D);
@@ -950,7 +951,7 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     const int cx = C.cx, cy = C.cy, CP = C.pitch, FP = F.pitch;
     const int I0 = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
     const int I0c = clampi(I0, 1, C.NX);
-    int cid[R];
+    int cid[R], jcs[R];
     bool in[R];
     uint8_t cb[R];
     T rv[R], ev[R];
@@ -958,12 +959,13 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     for (int r = 0; r < R; r++) {
         const int J0 = jb + 8 * r, J0c = clampi(J0, 1, C.NY);
         in[r] = I0 == I0c && J0 == J0c;
+        jcs[r] = J0c;
         cid[r] = I0c + J0c * CP;
         cb[r] = in[r] ? __ldg(&C.bits[cid[r]]) : (uint8_t)0;
     }
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int J0c = cid[r] / CP;
+        const int J0c = jcs[r];
         T acc = (T)0;
 #pragma unroll
         for (int dj = 0; dj < 2; dj++)
@@ -1010,18 +1012,19 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
     const int ic = clampi(i, 1, F.NX);
     const int I0 = __ldg(&F.pI[ic]), In = __ldg(&F.pIn[ic]);
     const T wx = __ldg(&LvA<T>::pwx(F)[ic]), sx = (T)__ldg(&F.psx[ic]);
-    int id[R];
+    int id[R], jcs[R];
     uint8_t bt[R];
     T val[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int j = jb + 8 * r, jc = clampi(j, 1, F.NY);
+        jcs[r] = jc;
         id[r] = ic + jc * P;
         bt[r] = (i == ic && j == jc) ? __ldg(&F.bits[id[r]]) : (uint8_t)0;
     }
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int jc = id[r] / P;
+        const int jc = jcs[r];
         const int J0 = __ldg(&F.pJ[jc]), Jn = __ldg(&F.pJn[jc]);
         const T wy = __ldg(&LvA<T>::pwy(F)[jc]), sy = (T)__ldg(&F.psy[jc]);
         T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
