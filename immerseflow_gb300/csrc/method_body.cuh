@@ -79,16 +79,19 @@ __device__ __forceinline__ void tile_ij(const Tile& t, int& i, int& j) {
 }
 
 // Deterministic block sum of NV values; result valid in thread 0..NV-1 as out[k].
-template <int NV>
+// RT: arithmetic of the in-warp stage (float on the mixed path, whose Krylov
+// vectors are FP32: FP64 butterfly adds on every lane are slow on GB300); the
+// warp results are summed in FP64.
+template <int NV, typename RT = double>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* out) {
     __shared__ double sh[NV][32];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        double x = v[k];
+        RT x = (RT)v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (l == 0) sh[k][w] = x;
+        if (l == 0) sh[k][w] = (double)x;
     }
     __syncthreads();
     if (threadIdx.x < NV) {
@@ -571,7 +574,7 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
             m[0] = (double)fabsf(dU) + (double)fabsf(dV);
         }
         __shared__ double out[1];
-        block_sum<1>(m, out);
+        block_sum<1, float>(m, out);
         if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
     } else {
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
@@ -708,7 +711,7 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
         acc[3] = in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];
-    block_sum<4>(acc, out);
+    block_sum<4, T>(acc, out);
     if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
@@ -818,7 +821,7 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
         }
     }
     __shared__ double out[2];
-    block_sum<2>(acc, out);
+    block_sum<2, T>(acc, out);
     if (threadIdx.x < 2) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
@@ -879,7 +882,7 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
         acc[3] = pn * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
     }
     __shared__ double out[4];
-    block_sum<4>(acc, out);
+    block_sum<4, T>(acc, out);
     if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
 }
 
