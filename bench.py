@@ -148,6 +148,27 @@ def committed_traffic():
     return None
 
 
+def cell_step_bytes(ad_iters, ppe_iters, mixed):
+    """Algorithmic bytes per interior cell of one time step (stencil byte 1 B).
+
+    s: multigrid word, k: Krylov vector word (4/4 mixed, 8/8 plain FP64); the
+    state (u, v, U, V, p, b, history) is FP64.  Convection + AB2 rhs 81,
+    faces + source 41, BiCGSTAB start 16 + 4k + 1, projection 81; predictor
+    sweep 49 (FP64) or 25 + 89/8 (FP32 sweep on the correction plus the FP64
+    refresh every 8 sweeps); per BiCGSTAB iteration 2 V-cycles x
+    (15.25 s + 6) x 4/3 (coarse levels), 2 applies x (s + 3k + 1), direction
+    4k + s + 1, s-update 3k + s + 1, iterate update 16 + 6k + 1; the mixed
+    path adds about two FP64 restarts (16 + 4k + 1 each) per step.
+    """
+    s = k = 4 if mixed else 8
+    v = 15.25 * s + 6.0
+    per_it = 2 * v * 4.0 / 3.0 + 2 * (s + 3 * k + 1) + (4 * k + s + 1) + (3 * k + s + 1) + (16 + 6 * k + 1)
+    pred = 25 + 89 / 8 if mixed else 49
+    start = 16 + 4 * k + 1
+    restarts = 2 * start if mixed else 0
+    return 81 + pred * ad_iters + 41 + start + restarts + 81 + per_it * ppe_iters
+
+
 def rel_l2(a, b):
     return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
 
@@ -158,7 +179,7 @@ def copy_cfg(cfg, precision):
     return c
 
 
-def batched_sweep(ifx, capi, cases, n_inst, steps, warm):
+def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
     """Batched sweep: n_inst uneven instances (seeded), mixed vs plain FP64, each
     advanced in one batch; execution mode chosen by the autotuner."""
     res, fields = {}, {}
@@ -175,12 +196,17 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm):
         launches = s.stats().kernel_launches - l0
         its = [s.stats(k).last_ppe_iters for k in range(n_inst)]
         ads = [s.stats(k).last_ad_iters for k in range(n_inst)]
+        # algorithmic bytes of the last timed step, per instance with its own iteration counts
+        nbytes = sum(c.nx * c.ny * cell_step_bytes(a, p, prec == capi.PREC_MIXED)
+                     for (c, _, _), a, p in zip(specs, ads, its))
         fields[name] = [(s.get(capi.FIELD_U, inst=k), s.get(capi.FIELD_V, inst=k), s.stats(k).cd) for k in range(n_inst)]
         res[name] = {"value": ncell * steps / (ms * 1e-3) / 1e6, "unit": METRIC, "ms_per_step": ms / steps,
                      "exec": {0: "persistent", 1: "graph"}.get(mode, str(mode)), "mg_tile_rows": s.mg_tile_rows(),
                      "gpu_launches": launches,
                      "ppe_iters_mean": float(np.mean(its)), "ppe_iters_max": int(max(its)),
-                     "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes()}
+                     "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes(),
+                     "roofline": {"bound": "hbm", "achieved": nbytes / (ms / steps * 1e-3) / 1e9, "unit": "GB/s",
+                                  "bytes_per_step": nbytes, "peak": peak, "frac": nbytes / (ms / steps * 1e-3) / 1e9 / peak}}
         res["cells"] = ncell
         s.close()
     errs = [rel_l2(np.concatenate([um.ravel(), vm.ravel()]), np.concatenate([u6.ravel(), v6.ravel()]))
@@ -341,9 +367,7 @@ def main():
         torch.cuda.synchronize()
 
     def step_bytes(st, sword):
-        v = 15.25 * sword + 6.0
-        per_it = 2 * v * 4.0 / 3.0 + 2 * (sword + 25) + (33 + sword) + (25 + sword) + 65
-        return cells * (81 + 49 * st.last_ad_iters + 41 + 49 + 81 + per_it * st.last_ppe_iters)
+        return cells * cell_step_bytes(st.last_ad_iters, st.last_ppe_iters, sword == 4)
 
     def timed(prec):
         cfg, _, _ = cases.cylinder(precision=prec)
@@ -445,7 +469,7 @@ def main():
         "clocks": clocks,
     }
     if args.batch > 0:
-        line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup)
+        line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup, peak)
     if args.serve > 0:
         line["served"] = served_stream(ifx, capi, cases, args.serve, args.rate, 64 << 30)
     if rank == 0 and world == 1 and not args.no_cpu:
