@@ -63,6 +63,7 @@ _SIGS = {
     "ifx_estimate_bytes": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_size_t)]),
     "ifx_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
     "ifx_server_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_server_set_steps_per_tick": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Config), _dp, _dp, C.c_int, C.POINTER(C.c_longlong)]),
     "ifx_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_server_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int, C.POINTER(C.c_int)]),
@@ -301,11 +302,13 @@ def estimate_bytes(cfg):
 class Server:
     """Continuous-batching solve server (ifx_server_* in the C ABI)."""
 
-    def __init__(self, hbm_budget_bytes, max_cohort=64, exec_mode=None):
+    def __init__(self, hbm_budget_bytes, max_cohort=64, exec_mode=None, steps_per_tick=None):
         self._h = C.c_void_p()
         _check(lib().ifx_server_create(int(hbm_budget_bytes), int(max_cohort), C.byref(self._h)))
         if exec_mode is not None:
             _check(lib().ifx_server_set_exec_mode(self._h, int(exec_mode)))
+        if steps_per_tick is not None:
+            _check(lib().ifx_server_set_steps_per_tick(self._h, int(steps_per_tick)))
 
     def submit(self, cfg, xf, yf, nsteps):
         xf = np.ascontiguousarray(xf, dtype=np.float64)

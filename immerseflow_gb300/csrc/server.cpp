@@ -5,7 +5,8 @@
 // tick the waiting requests that fit in the device-memory budget are admitted
 // together as one cohort: one batched solver on its own CUDA stream, state
 // resident on the device until the request finishes.  Every live cohort then
-// advances one time step; the steps of all cohorts are issued before any is
+// advances up to steps_per_tick time steps (never past the first of its
+// requests to finish); the steps of all cohorts are issued before any is
 // waited for, so cohorts admitted at different times overlap on the GPU.  A
 // request that has done its steps is copied out (u, v, p, statistics) and
 // made inactive in its cohort, which stops its work while the other members
@@ -57,10 +58,12 @@ struct ifx_server {
         ifx_solver* s = nullptr;
         std::vector<long long> ids;
         int live = 0;
+        int pending = 0;  // steps issued this tick
         size_t bytes = 0;
     };
     size_t budget = 0, used = 0;
     int max_cohort = 64;
+    int steps_per_tick = 1;  // a cohort advances up to this many steps per tick
     int exec_mode = IFX_EXEC_GRAPH;
     long long next_id = 1;
     std::map<long long, Request> reqs;
@@ -133,6 +136,12 @@ extern "C" ifx_status ifx_server_create(size_t hbm_budget_bytes, int max_cohort,
     return IFX_OK;
 }
 
+extern "C" ifx_status ifx_server_set_steps_per_tick(ifx_server* V, int steps) {
+    if (!V || steps < 1) return set_error(IFX_ERR_ARG, "ifx_server_set_steps_per_tick: bad argument");
+    V->steps_per_tick = steps;
+    return IFX_OK;
+}
+
 extern "C" ifx_status ifx_server_set_exec_mode(ifx_server* V, int mode) {
     if (!V || mode < IFX_EXEC_DEFAULT || mode > IFX_EXEC_HOST) return set_error(IFX_ERR_ARG, "ifx_server_set_exec_mode: bad argument");
     V->exec_mode = mode;
@@ -161,9 +170,16 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
     if (!V) return set_error(IFX_ERR_ARG, "ifx_server_tick: null server");
     const size_t before = V->finished.size();
     ifx_status worst = admit(V);
-    // issue one step on every cohort, then wait for all of them
+    // issue the steps of every cohort (up to steps_per_tick, never past the
+    // first request to finish), then wait for all of them
     for (auto& c : V->cohorts) {
-        ifx_status st = ifx_step_async(c.s, 1);
+        int k = V->steps_per_tick;
+        for (long long id : c.ids) {
+            const ifx_server::Request& r = V->reqs[id];
+            if (r.state == 1) k = std::min(k, r.nsteps - r.done);
+        }
+        c.pending = std::max(k, 1);
+        ifx_status st = ifx_step_async(c.s, c.pending);
         if (st != IFX_OK) worst = st;
     }
     for (auto it = V->cohorts.begin(); it != V->cohorts.end();) {
@@ -182,7 +198,8 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
             for (size_t k = 0; k < c.ids.size(); k++) {
                 ifx_server::Request& r = V->reqs[c.ids[k]];
                 if (r.state != 1) continue;
-                if (++r.done < r.nsteps) continue;
+                r.done += c.pending;
+                if (r.done < r.nsteps) continue;
                 const size_t n = (size_t)r.nx * r.ny;
                 r.u.resize(n);
                 r.v.resize(n);

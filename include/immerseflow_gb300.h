@@ -257,9 +257,9 @@ ifx_status ifx_synchronize(ifx_solver* s);
  * runs one case per process, src/main.cu:75-102).  Submitted METHOD-mode cases
  * wait in FIFO order; each ifx_server_tick admits the waiting requests that
  * fit in the device-memory budget as one batched cohort with its own stream
- * and state kept on the device, then advances every live cohort by one time
- * step (all cohorts issued before any is waited for, so they overlap on the
- * GPU).  A request that completed its steps is copied out (u, v, p, stats)
+ * and state kept on the device, then advances every live cohort by up to
+ * steps_per_tick time steps (all cohorts issued before any is waited for, so
+ * they overlap on the GPU).  A request that completed its steps is copied out (u, v, p, stats)
  * and stops computing; a cohort whose requests all finished frees its memory.
  * Results do not depend on the cohort a request ran in.  One host thread per
  * server. */
@@ -273,6 +273,9 @@ ifx_status ifx_estimate_bytes(const ifx_config* cfg, size_t* bytes);
 ifx_status ifx_server_create(size_t hbm_budget_bytes, int max_cohort, ifx_server** out);
 /* Execution mode of the cohorts (IFX_EXEC_*, default IFX_EXEC_GRAPH). */
 ifx_status ifx_server_set_exec_mode(ifx_server* v, int mode);
+/* Steps a cohort advances per tick at most (default 1; a cohort never runs past
+ * the step count of one of its requests, so results do not depend on it). */
+ifx_status ifx_server_set_steps_per_tick(ifx_server* v, int steps);
 ifx_status ifx_server_submit(ifx_server* v, const ifx_config* cfg, const double* xf, const double* yf,
                              int nsteps, long long* id);
 ifx_status ifx_server_tick(ifx_server* v, int* n_finished);

@@ -54,7 +54,7 @@ def test_server_results_equal_alone_runs():
     stream = [(case(64, 48), 4), (case(48, 40, re=80.0, b=0.2, angle=-20.0), 2),
               (case(72, 40, re=200.0, b=0.35, angle=10.0), 3), (case(40, 40, re=60.0), 5),
               (case(56, 48, re=120.0, b=0.5), 1)]
-    srv = ifx.Server(1 << 33, max_cohort=8)
+    srv = ifx.Server(1 << 33, max_cohort=8, steps_per_tick=3)
     ids = {}
     done = []
     # arrivals interleaved with ticks: later requests join while earlier ones run
@@ -81,7 +81,7 @@ def test_server_results_equal_alone_runs():
 def test_server_admits_by_memory_budget():
     stream = [(case(64, 48), 2), (case(64, 48, re=150.0), 2), (case(64, 48, re=60.0), 2)]
     one = ifx.estimate_bytes(stream[0][0][0])
-    srv = ifx.Server(int(one * 1.5), max_cohort=8)
+    srv = ifx.Server(int(one * 1.5), max_cohort=8, steps_per_tick=1)
     ids = [srv.submit(*spec, nsteps=n) for spec, n in stream]
     srv.tick()
     info = srv.info()
