@@ -1139,14 +1139,20 @@ __device__ __forceinline__ T sub_lap(const SubGeo<T>& g, const T* e, int i, int 
     return c.ce * e[id + 1] + c.cw * e[id - 1] + c.cn * e[id + P] + c.cs * e[id - P] - c.dd * e[id];
 }
 
+// Loops over the interior cells of a staged level: warps take rows, lanes
+// take columns (no integer division per cell).
+#define SUB_FOR_CELLS(g, i, j)                                                                   \
+    for (int j = 1 + (int)(threadIdx.x >> 5); j <= (g).NY; j += (int)(blockDim.x >> 5))          \
+        for (int i = 1 + (int)(threadIdx.x & 31); i <= (g).NX; i += 32)
+
 // Weighted-Jacobi sweep of a staged level (src -> dst by parity).
 template <typename T>
 __device__ __forceinline__ void sub_smooth(const SubGeo<T>& g, int src_alt, T om) {
     const T* src = src_alt ? g.e2 : g.e;
     T* dst = src_alt ? g.e : g.e2;
-    const int NX = g.NX, nx = g.nx, NXY = g.NX * g.NY;
-    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
-        const int j = 1 + q / NX, i = 1 + q - (j - 1) * NX, id = i + j * nx;
+    const int nx = g.nx;
+    SUB_FOR_CELLS(g, i, j) {
+        const int id = i + j * nx;
         const uint8_t bt = g.b[id];
         if (!(bt & 0x0F)) continue;
         T D;
@@ -1161,9 +1167,8 @@ __device__ __forceinline__ void sub_smooth(const SubGeo<T>& g, int src_alt, T om
 template <typename T>
 __device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>& f, int fine_alt, T om) {
     const T* fe = fine_alt ? f.e2 : f.e;
-    const int NX = c.NX, NXY = c.NX * c.NY;
-    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
-        const int J0 = 1 + q / NX, I0 = 1 + q - (J0 - 1) * NX, cid = I0 + J0 * c.nx;
+    SUB_FOR_CELLS(c, I0, J0) {
+        const int cid = I0 + J0 * c.nx;
         const uint8_t cb = c.b[cid];
         if (!(cb & 0x0F)) {
             c.r[cid] = (T)0;
@@ -1194,9 +1199,9 @@ template <typename T>
 __device__ __forceinline__ void sub_prolong(const SubGeo<T>& f, const SubGeo<T>& c, int fine_alt, int coarse_alt) {
     const T* ce = (coarse_alt && c.child >= 0) ? c.e2 : c.e;
     T* fe = fine_alt ? f.e2 : f.e;
-    const int NX = f.NX, nx = f.nx, NXY = f.NX * f.NY, CP = c.nx;
-    for (int q = threadIdx.x; q < NXY; q += blockDim.x) {
-        const int j = 1 + q / NX, i = 1 + q - (j - 1) * NX, id = i + j * nx;
+    const int nx = f.nx, CP = c.nx;
+    SUB_FOR_CELLS(f, i, j) {
+        const int id = i + j * nx;
         if (!(f.b[id] & 0x0F)) continue;
         const int I0 = f.pI[i], In = f.pIn[i], J0 = f.pJ[j], Jn = f.pJn[j];
         const T wx = f.pwx[i], wy = f.pwy[j];
@@ -1230,6 +1235,38 @@ __device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g) {
     const int nthr = min((int)blockDim.x, (NXY + 31) & ~31);
     for (int q = threadIdx.x; q < nx * g.ny; q += blockDim.x) g.e[q] = (T)0;
     __syncthreads();
+    if (NXY <= 32) {
+        // one warp, one cell per lane: neighbours by shuffle (cells beyond the
+        // interior hold e = 0, like the ghost ring)
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            const bool own = lane < NXY;
+            const int j = 1 + (own ? lane / NX : 0), i = 1 + (own ? lane - (j - 1) * NX : 0);
+            const int c = i + j * nx;
+            const uint8_t bt = own ? g.b[c] : (uint8_t)0;
+            const bool live = bt & 0x0F;
+            const LapCoef<T> lc = sub_coef<T>(g, i, j, bt);
+            const T rd = live ? rcpa(lc.dd) : (T)0, rr = own ? g.r[c] : (T)0;
+            const int col = (i + j) & 1;
+            const bool hasE = i < NX, hasW = i > 1, hasN = j < g.NY, hasS = j > 1;
+            T e = (T)0;
+            for (int it = 0; it < COARSE_SWEEPS; it++) {
+#pragma unroll
+                for (int cc = 0; cc < 2; cc++) {
+                    const T vE = __shfl_down_sync(0xffffffffu, e, 1), vW = __shfl_up_sync(0xffffffffu, e, 1);
+                    const T vN = __shfl_sync(0xffffffffu, e, min(lane + NX, 31));
+                    const T vS = __shfl_sync(0xffffffffu, e, max(lane - NX, 0));
+                    const T eE = hasE ? vE : (T)0, eW = hasW ? vW : (T)0;
+                    const T eN = hasN ? vN : (T)0, eS = hasS ? vS : (T)0;
+                    const T Le = lc.ce * eE + lc.cw * eW + lc.cn * eN + lc.cs * eS - lc.dd * e;
+                    if (live && col == cc) e = e + om * (Le - rr) * rd;
+                }
+            }
+            if (live) g.e[c] = e;
+        }
+        __syncthreads();
+        return;
+    }
     if ((int)threadIdx.x < nthr) {
         int id[SUB_COARSE_PER_THREAD], col[SUB_COARSE_PER_THREAD];
         T ce[SUB_COARSE_PER_THREAD], cw[SUB_COARSE_PER_THREAD], cn[SUB_COARSE_PER_THREAD],
