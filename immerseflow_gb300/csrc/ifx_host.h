@@ -81,7 +81,7 @@ struct ifx_solver {
     int nt0 = 0;
     std::vector<ifx::Tile*> dTsm;    // per level >= 1: tiles of instances for which it is a middle level
     std::vector<int> ntsm;
-    std::vector<ifx::Tile*> dTre;    // per level >= 1: tiles of instances that have the level
+    std::vector<ifx::Tile*> dTre;    // per level >= 1: tiles of the next finer level (from (1,1)) of instances that have the level
     std::vector<int> ntre;
     // the same lists with wide tiles (32 x 8*MG_ROWS_WIDE cells) for the multigrid phases
     ifx::Tile* dT0W = nullptr;

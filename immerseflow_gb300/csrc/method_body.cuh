@@ -934,68 +934,84 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
         if (bt[r] & 0x0F) dst[id[r]] = val[r];
 }
 
-// Restriction of the fine residual (area weighted) onto coarse tiles, fused
-// with the first (zero-start) smoothing sweep of a middle coarse level.
+// Restriction of the fine residual (area weighted) onto the coarse level,
+// fused with the first (zero-start) smoothing sweep of a middle coarse level.
+// One thread per FINE cell: tiles of the fine level start at (1, 1), so the
+// fine cells of a coarse cell share a tile (lanes 2k, 2k+1 when x is coarsened,
+// warps 2w, 2w+1 when y is); each thread forms (r - L e) dA of its cell, pairs
+// are summed in x by shuffle and then in y through shared memory (order:
+// (t00 + t10) + (t01 + t11), as the oracle), and the thread of the first child
+// writes the coarse cell.
 template <typename T, int R = 1>
 __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                            const GhostDev* __restrict__ G, int fine_alt, int vb) {
+    __shared__ T rows[R][TILE_Y][TILE_X];
     const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev& C = LV[t.lev];
-    if (S[C.inst].ppe_state != ST_ACTIVE) return;
-    const LevelDev& F = LV[C.parent];
+    const LevelDev& F = LV[t.lev];
+    if (S[F.inst].ppe_state != ST_ACTIVE) return;
+    const LevelDev& C = LV[F.child];
     const T* fe = (const T*)(fine_alt ? F.e2 : F.e);
     const T* fr = (const T*)F.r;
-    const T* fdw = LvA<T>::dw(F);
-    const T* fdh = LvA<T>::dh(F);
-    const int* gidx = F.depth == 0 ? I[C.inst].gidx : nullptr;
-    T* rc = (T*)C.r;
-    const T om = (T)I[C.inst].omega;
-    const int cx = C.cx, cy = C.cy, CP = C.pitch, FP = F.pitch;
-    const int I0 = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
-    const int I0c = clampi(I0, 1, C.NX);
-    int cid[R], jcs[R];
+    const int* gidx = F.depth == 0 ? I[F.inst].gidx : nullptr;
+    const int FP = F.pitch, cx = C.cx, cy = C.cy;
+    const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+    const int i = t.i0 + lane;
+    const bool inx = i <= F.NX;
+    const int ic = inx ? i : F.NX;
     bool in[R];
-    uint8_t cb[R];
-    T rv[R], ev[R];
+    int id[R], jcs[R];
+    uint8_t fb[R];
+    T term[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int J0 = jb + 8 * r, J0c = clampi(J0, 1, C.NY);
-        in[r] = I0 == I0c && J0 == J0c;
-        jcs[r] = J0c;
-        cid[r] = I0c + J0c * CP;
-        cb[r] = in[r] ? __ldg(&C.bits[cid[r]]) : (uint8_t)0;
+        const int j = t.j0 + w + 8 * r;
+        in[r] = inx && j <= F.NY;
+        jcs[r] = j <= F.NY ? j : F.NY;
+        id[r] = ic + jcs[r] * FP;
+        fb[r] = in[r] ? __ldg(&F.bits[id[r]]) : (uint8_t)0;
     }
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int J0c = jcs[r];
-        T acc = (T)0;
-#pragma unroll
-        for (int dj = 0; dj < 2; dj++)
-#pragma unroll
-            for (int di = 0; di < 2; di++) {
-                const int fi = cx * (I0c - 1) + 1 + di, fj = cy * (J0c - 1) + 1 + dj;
-                const bool child = di < cx && dj < cy && fi <= F.NX && fj <= F.NY;
-                const int fic = child ? fi : 1, fjc = child ? fj : 1, fid = fic + fjc * FP;
-                const uint8_t fb = child ? __ldg(&F.bits[fid]) : (uint8_t)0;
-                T Le, D;
-                if (F.depth == 0) lap_p<T, T, true>(F, fe, fic, fjc, fid, FP, fb, G, gidx, Le, D);
-                else lap_p<T, T, false>(F, fe, fic, fjc, fid, FP, fb, G, nullptr, Le, D);
-                const T term = (fr[fid] - Le) * (__ldg(&fdw[fic]) * __ldg(&fdh[fjc]));
-                if (fb & 0x0F) acc += term;
-            }
-        rv[r] = acc / (__ldg(&LvA<T>::dw(C)[I0c]) * __ldg(&LvA<T>::dh(C)[J0c]));
-        ev[r] = -om * rv[r] * rcpa(lap_diag<T>(C, I0c, J0c, cb[r]));
+        T Le, D;
+        if (F.depth == 0) lap_p<T, T, true>(F, fe, ic, jcs[r], id[r], FP, fb[r], G, gidx, Le, D);
+        else lap_p<T, T, false>(F, fe, ic, jcs[r], id[r], FP, fb[r], G, nullptr, Le, D);
+        term[r] = (fb[r] & 0x0F) ? (fr[id[r]] - Le) * (__ldg(&LvA<T>::dw(F)[ic]) * __ldg(&LvA<T>::dh(F)[jcs[r]])) : (T)0;
     }
+    // x pairs: (2I-1, 2I) are lanes (2k, 2k+1); the even lane keeps t0 + t1
+    if (cx == 2) {
+#pragma unroll
+        for (int r = 0; r < R; r++) term[r] = term[r] + __shfl_xor_sync(0xffffffffu, term[r], 1);
+    }
+    // y pairs: rows (2J-1, 2J) are warps (2m, 2m+1)
+    if (cy == 2) {
+        if (w & 1) {
+#pragma unroll
+            for (int r = 0; r < R; r++) rows[r][w][lane] = term[r];
+        }
+        __syncthreads();
+        if (!(w & 1)) {
+#pragma unroll
+            for (int r = 0; r < R; r++) term[r] = term[r] + rows[r][w + 1][lane];
+        }
+    }
+    if ((cx == 2 && (lane & 1)) || (cy == 2 && (w & 1))) return;
+    T* rc = (T*)C.r;
+    const T om = (T)I[F.inst].omega;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (!in[r]) continue;
-        if (!(cb[r] & 0x0F)) {
-            rc[cid[r]] = (T)0;
+        const int j = t.j0 + w + 8 * r;
+        const int I0 = cx == 2 ? (i + 1) >> 1 : i, J0 = cy == 2 ? (j + 1) >> 1 : j;
+        const int cid = I0 + J0 * C.pitch;
+        const uint8_t cb = __ldg(&C.bits[cid]);
+        if (!(cb & 0x0F)) {
+            rc[cid] = (T)0;
             continue;
         }
-        rc[cid[r]] = rv[r];
-        if (C.child >= 0) ((T*)C.e)[cid[r]] = ev[r];  // middle level: fused first sweep from zero
+        const T rv = term[r] / (__ldg(&LvA<T>::dw(C)[I0]) * __ldg(&LvA<T>::dh(C)[J0]));
+        rc[cid] = rv;
+        if (C.child >= 0) ((T*)C.e)[cid] = -om * rv * rcpa(lap_diag<T>(C, I0, J0, cb));
     }
 }
 
@@ -1174,7 +1190,7 @@ __device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>
             c.r[cid] = (T)0;
             continue;
         }
-        T acc = (T)0;
+        T rowsum[2] = {(T)0, (T)0};  // (t00 + t10) + (t01 + t11), as the tile phase
 #pragma unroll
         for (int dj = 0; dj < 2; dj++)
 #pragma unroll
@@ -1186,8 +1202,10 @@ __device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>
                 if (!(bt & 0x0F)) continue;
                 T D;
                 const T Le = sub_lap<T>(f, fe, i, j, id, bt, D);
-                acc += (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
+                const T term = (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
+                rowsum[dj] = di == 0 ? term : rowsum[dj] + term;
             }
+        const T acc = c.cy == 2 ? rowsum[0] + rowsum[1] : rowsum[0];
         const T rv = acc / (c.dw[I0] * c.dh[J0]);
         c.r[cid] = rv;
         if (c.child >= 0) c.e[cid] = -om * rv * rcpa(sub_coef<T>(c, I0, J0, cb).dd);

@@ -169,9 +169,12 @@ extern "C" ifx_status ifx_server_submit(ifx_server* V, const ifx_config* cfg, co
 extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
     if (!V) return set_error(IFX_ERR_ARG, "ifx_server_tick: null server");
     const size_t before = V->finished.size();
-    ifx_status worst = admit(V);
-    // issue the steps of every cohort (up to steps_per_tick, never past the
-    // first request to finish), then wait for all of them
+    ifx_status worst = IFX_OK;
+    // issue the steps of every live cohort (up to steps_per_tick, never past the
+    // first request to finish); new requests are admitted while those run (the
+    // new cohort's set-up overlaps them) and step from the next tick on; then
+    // wait for all of them
+    const size_t nold = V->cohorts.size();
     for (auto& c : V->cohorts) {
         int k = V->steps_per_tick;
         for (long long id : c.ids) {
@@ -182,7 +185,13 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
         ifx_status st = ifx_step_async(c.s, c.pending);
         if (st != IFX_OK) worst = st;
     }
-    for (auto it = V->cohorts.begin(); it != V->cohorts.end();) {
+    {
+        ifx_status st = admit(V);
+        if (st != IFX_OK) worst = st;
+    }
+    size_t idx = 0;
+    for (auto it = V->cohorts.begin(); it != V->cohorts.end(); idx++) {
+        if (idx >= nold) break;  // admitted this tick: no steps yet
         ifx_server::Cohort& c = *it;
         ifx_status st = ifx_step_wait(c.s);
         bool drop = false;

@@ -758,10 +758,17 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
                 hT0W.insert(hT0W.end(), tw.begin(), tw.end());
             } else {
                 // tile phases: restriction into every level down to the first
-                // small one, smoothing and prolongation above it
-                if (l <= lb) tre[l].insert(tre[l].end(), tl.begin(), tl.end());
+                // small one (tiles of the finer level starting at (1, 1), so that
+                // the children of a coarse cell share a tile), smoothing and
+                // prolongation above it
+                if (l <= lb) {
+                    const HostLevel& f = I.lev[l - 1];
+                    for (int j0 = 1; j0 <= f.NY; j0 += TILE_Y)
+                        for (int i0 = 1; i0 <= f.NX; i0 += TILE_X) tre[l].push_back(Tile{k, lv - 1, i0, j0});
+                    for (int j0 = 1; j0 <= f.NY; j0 += TILE_Y * MG_ROWS_WIDE)
+                        for (int i0 = 1; i0 <= f.NX; i0 += TILE_X) treW[l].push_back(Tile{k, lv - 1, i0, j0});
+                }
                 if (l < lb) tsm[l].insert(tsm[l].end(), tl.begin(), tl.end());
-                if (l <= lb) treW[l].insert(treW[l].end(), tw.begin(), tw.end());
                 if (l < lb) tsmW[l].insert(tsmW[l].end(), tw.begin(), tw.end());
             }
         }
@@ -801,13 +808,13 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     S->nt0W = (int)hT0W.size();
     S->dTsmW.assign(lmax, nullptr);
     S->dTreW.assign(lmax, nullptr);
-    S->ntsmW.assign(lmax, 0);
     S->ntreW.assign(lmax, 0);
+    S->ntsmW.assign(lmax, 0);
     for (int l = 1; l < lmax; l++) {
         IFX_TRY(dupload(S, &S->dTsmW[l], tsmW[l]));
         IFX_TRY(dupload(S, &S->dTreW[l], treW[l]));
-        S->ntsmW[l] = (int)tsmW[l].size();
         S->ntreW[l] = (int)treW[l].size();
+        S->ntsmW[l] = (int)tsmW[l].size();
     }
     IFX_TRY(dupload(S, &S->dTall, hTall));
     IFX_TRY(dupload(S, &S->dSub, hSub));

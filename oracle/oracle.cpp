@@ -847,7 +847,8 @@ void restrict_res(orc_solver* S, int l) {
     for (int J = 1; J <= c.NY; J++)
         for (int I = 1; I <= c.NX; I++) {
             int cid = IDX(I, J, c.nx);
-            double acc = 0.0;
+            // children summed in x pairs first, then the two rows: (t00 + t10) + (t01 + t11)
+            double rowsum[2] = {0.0, 0.0};
             for (int dj = 0; dj < c.cy; dj++)
                 for (int di = 0; di < c.cx; di++) {
                     int i = c.cx * (I - 1) + 1 + di, j = c.cy * (J - 1) + 1 + dj;
@@ -856,8 +857,9 @@ void restrict_res(orc_solver* S, int l) {
                     if (!live(f, id)) continue;
                     double Le, D;
                     lap(S, f, f.e.data(), i, j, &Le, &D, l == 0);
-                    acc += (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
+                    rowsum[dj] += (f.r[id] - Le) * (f.dw[i] * f.dh[j]);
                 }
+            const double acc = c.cy == 2 ? rowsum[0] + rowsum[1] : rowsum[0];
             c.r[cid] = live(c, cid) ? acc / (c.dw[I] * c.dh[J]) : 0.0;
         }
 }
