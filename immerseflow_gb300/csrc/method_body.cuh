@@ -169,18 +169,22 @@ __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* q
 // Image-point value of the IBM ghost at global entry gid, from field e;
 // ws receives the weight on cell `self`.  Pressure stencils reference fluid
 // cells only, so this is an exact linear function of the fluid values.
-template <typename TC, typename TE>
-__device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
+template <typename TC, typename Fetch>
+__device__ __forceinline__ TC ghost_eval_f(const GhostDev* G, int gid, Fetch fetch, int self, TC& ws) {
     const GhostDev& g = G[gid];
     TC acc = (TC)0;
     ws = (TC)0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const TC w = (TC)g.wp[k];
-        acc += w * (TC)e[g.nb[k]];
+        acc += w * fetch(g.nb[k]);
         if (g.nb[k] == self) ws += w;
     }
     return acc;
+}
+template <typename TC, typename TE>
+__device__ __forceinline__ TC ghost_eval(const GhostDev* G, int gid, const TE* e, int self, TC& ws) {
+    return ghost_eval_f<TC>(G, gid, [e](int q) { return (TC)e[q]; }, self, ws);
 }
 
 // Face coefficients of cell (i,j) with closed faces dropped, and the
@@ -220,22 +224,37 @@ __device__ __forceinline__ LapCoef<TC> lap_coef(const LevelDev& L, int i, int j,
 // unknowns eliminated).  D is the diagonal of that operator.  Coefficients
 // and arithmetic in TC, field values of type TE; P is the row pitch of e
 // (L.pitch in global memory, L.nx for a level staged in shared memory).
-template <typename TC, typename TE, bool LVL0>
-__device__ __forceinline__ void lap_p(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id, int P,
-                                      uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+// Same, from the values of the cell (eP) and its four neighbours; fetch(q)
+// returns the value at dense index q for the IBM ghosts' image-point stencils.
+template <typename TC, bool LVL0, typename Fetch>
+__device__ __forceinline__ void lap_vals(const LevelDev& L, int i, int j, int id, int P, uint8_t bt, const GhostDev* G,
+                                         const int* gidx, TC eE, TC eW, TC eN, TC eS, TC eP, Fetch fetch, TC& Le,
+                                         TC& D) {
     const LapCoef<TC> c = lap_coef<TC>(L, i, j, bt);
-    TC eE = (TC)e[id + 1], eW = (TC)e[id - 1], eN = (TC)e[id + P], eS = (TC)e[id - P];
     TC dm = c.dd;
     if (LVL0 && (bt & 0xF0)) {
         TC ws;
-        if (bt & G_E) { eE = ghost_eval<TC, TE>(G, gidx[id + 1], e, id, ws); dm -= c.ce * ws; }
-        if (bt & G_W) { eW = ghost_eval<TC, TE>(G, gidx[id - 1], e, id, ws); dm -= c.cw * ws; }
-        if (bt & G_N) { eN = ghost_eval<TC, TE>(G, gidx[id + P], e, id, ws); dm -= c.cn * ws; }
-        if (bt & G_S) { eS = ghost_eval<TC, TE>(G, gidx[id - P], e, id, ws); dm -= c.cs * ws; }
+        if (bt & G_E) { eE = ghost_eval_f<TC>(G, gidx[id + 1], fetch, id, ws); dm -= c.ce * ws; }
+        if (bt & G_W) { eW = ghost_eval_f<TC>(G, gidx[id - 1], fetch, id, ws); dm -= c.cw * ws; }
+        if (bt & G_N) { eN = ghost_eval_f<TC>(G, gidx[id + P], fetch, id, ws); dm -= c.cn * ws; }
+        if (bt & G_S) { eS = ghost_eval_f<TC>(G, gidx[id - P], fetch, id, ws); dm -= c.cs * ws; }
     }
-    Le = c.ce * eE + c.cw * eW + c.cn * eN + c.cs * eS - c.dd * (TC)e[id];
+    Le = c.ce * eE + c.cw * eW + c.cn * eN + c.cs * eS - c.dd * eP;
     D = dm;
 }
+
+template <typename TC, typename TE, bool LVL0>
+__device__ __forceinline__ void lap_p(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id, int P,
+                                      uint8_t bt, const GhostDev* G, const int* gidx, TC& Le, TC& D) {
+    lap_vals<TC, LVL0>(L, i, j, id, P, bt, G, gidx, (TC)e[id + 1], (TC)e[id - 1], (TC)e[id + P], (TC)e[id - P],
+                       (TC)e[id], [e](int q) { return (TC)e[q]; }, Le, D);
+}
+
+// Weighted-Jacobi update of a cell, and the first sweep from zero.
+template <typename T>
+__device__ __forceinline__ T jacobi_update(T e, T r, T Le, T D, T om) { return e + om * (Le - r) * rcpa(D); }
+template <typename T>
+__device__ __forceinline__ T jacobi_from_zero(T r, T D, T om) { return -om * r * rcpa(D); }
 
 template <typename TC, typename TE, bool LVL0>
 __device__ __forceinline__ void lap(const LevelDev& L, const TE* __restrict__ e, int i, int j, int id,
@@ -927,7 +946,7 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
         T Le, D;
         if (L.depth == 0) lap_p<T, T, true>(L, src, ic, jc, id[r], P, bt[r], G, gidx, Le, D);
         else lap_p<T, T, false>(L, src, ic, jc, id[r], P, bt[r], G, nullptr, Le, D);
-        val[r] = (flags & 1) ? -om * rr[id[r]] * rcpa(D) : src[id[r]] + om * (Le - rr[id[r]]) * rcpa(D);
+        val[r] = (flags & 1) ? jacobi_from_zero<T>(rr[id[r]], D, om) : jacobi_update<T>(src[id[r]], rr[id[r]], Le, D, om);
     }
 #pragma unroll
     for (int r = 0; r < R; r++)
@@ -1011,8 +1030,24 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
         }
         const T rv = term[r] / (__ldg(&LvA<T>::dw(C)[I0]) * __ldg(&LvA<T>::dh(C)[J0]));
         rc[cid] = rv;
-        if (C.child >= 0) ((T*)C.e)[cid] = -om * rv * rcpa(lap_diag<T>(C, I0, J0, cb));
+        if (C.child >= 0) ((T*)C.e)[cid] = jacobi_from_zero<T>(rv, lap_diag<T>(C, I0, J0, cb), om);
     }
+}
+
+// Bilinear correction at fine cell (i, j) from the next coarser level; ce(I, J)
+// returns a coarse value, cb(I, J) a coarse stencil byte.
+template <typename T, typename FE, typename FB>
+__device__ __forceinline__ T prolong_corr(const LevelDev& F, int i, int j, FE ce, FB cb) {
+    const int I0 = __ldg(&F.pI[i]), In = __ldg(&F.pIn[i]), J0 = __ldg(&F.pJ[j]), Jn = __ldg(&F.pJn[j]);
+    const T wx = __ldg(&LvA<T>::pwx(F)[i]), wy = __ldg(&LvA<T>::pwy(F)[j]);
+    const T sx = (T)__ldg(&F.psx[i]), sy = (T)__ldg(&F.psy[j]);
+    T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
+    w00 = (cb(I0, J0) & 0x0F) ? w00 : (T)0;
+    w10 = (cb(In, J0) & 0x0F) ? w10 : (T)0;
+    w01 = (cb(I0, Jn) & 0x0F) ? w01 : (T)0;
+    w11 = (cb(In, Jn) & 0x0F) ? w11 : (T)0;
+    const T sw = w00 + w10 + w01 + w11;
+    return (w00 * ce(I0, J0) + sx * w10 * ce(In, J0) + sy * w01 * ce(I0, Jn) + (sx * sy) * w11 * ce(In, Jn)) / sw;
 }
 
 // Bilinear prolongation of the coarse correction, added on the fine level.
@@ -1027,10 +1062,11 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
     T* fe = (T*)(fine_alt ? F.e2 : F.e);
     const int P = F.pitch, CP = C.pitch;
+    const uint8_t* cbits = C.bits;
+    auto fce = [ce, CP](int I, int J) { return ce[I + J * CP]; };
+    auto fcb = [cbits, CP](int I, int J) { return __ldg(&cbits[I + J * CP]); };
     const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
     const int ic = clampi(i, 1, F.NX);
-    const int I0 = __ldg(&F.pI[ic]), In = __ldg(&F.pIn[ic]);
-    const T wx = __ldg(&LvA<T>::pwx(F)[ic]), sx = (T)__ldg(&F.psx[ic]);
     int id[R], jcs[R];
     uint8_t bt[R];
     T val[R];
@@ -1042,19 +1078,7 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
         bt[r] = (i == ic && j == jc) ? __ldg(&F.bits[id[r]]) : (uint8_t)0;
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int jc = jcs[r];
-        const int J0 = __ldg(&F.pJ[jc]), Jn = __ldg(&F.pJn[jc]);
-        const T wy = __ldg(&LvA<T>::pwy(F)[jc]), sy = (T)__ldg(&F.psy[jc]);
-        T w00 = ((T)1 - wx) * ((T)1 - wy), w10 = wx * ((T)1 - wy), w01 = ((T)1 - wx) * wy, w11 = wx * wy;
-        const int c00 = I0 + J0 * CP, c10 = In + J0 * CP, c01 = I0 + Jn * CP, c11 = In + Jn * CP;
-        w00 = (__ldg(&C.bits[c00]) & 0x0F) ? w00 : (T)0;
-        w10 = (__ldg(&C.bits[c10]) & 0x0F) ? w10 : (T)0;
-        w01 = (__ldg(&C.bits[c01]) & 0x0F) ? w01 : (T)0;
-        w11 = (__ldg(&C.bits[c11]) & 0x0F) ? w11 : (T)0;
-        const T sw = w00 + w10 + w01 + w11;
-        val[r] = fe[id[r]] + (w00 * ce[c00] + sx * w10 * ce[c10] + sy * w01 * ce[c01] + (sx * sy) * w11 * ce[c11]) / sw;
-    }
+    for (int r = 0; r < R; r++) val[r] = fe[id[r]] + prolong_corr<T>(F, ic, jcs[r], fce, fcb);
 #pragma unroll
     for (int r = 0; r < R; r++)
         if (bt[r] & 0x0F) fe[id[r]] = val[r];
@@ -1173,7 +1197,7 @@ __device__ __forceinline__ void sub_smooth(const SubGeo<T>& g, int src_alt, T om
         if (!(bt & 0x0F)) continue;
         T D;
         const T Le = sub_lap<T>(g, src, i, j, id, bt, D);
-        dst[id] = src[id] + om * (Le - g.r[id]) * rcpa(D);
+        dst[id] = jacobi_update<T>(src[id], g.r[id], Le, D, om);
     }
 }
 
@@ -1208,7 +1232,7 @@ __device__ __forceinline__ void sub_restrict(const SubGeo<T>& c, const SubGeo<T>
         const T acc = c.cy == 2 ? rowsum[0] + rowsum[1] : rowsum[0];
         const T rv = acc / (c.dw[I0] * c.dh[J0]);
         c.r[cid] = rv;
-        if (c.child >= 0) c.e[cid] = -om * rv * rcpa(sub_coef<T>(c, I0, J0, cb).dd);
+        if (c.child >= 0) c.e[cid] = jacobi_from_zero<T>(rv, sub_coef<T>(c, I0, J0, cb).dd, om);
     }
 }
 
