@@ -136,12 +136,14 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per launch of the roofline kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "persist_step_cylinder_384x256.md")
+def committed_traffic(persistent):
+    """DRAM bytes per step of the cylinder step from the committed ncu summary:
+    the persistent kernel's launch, or the sum over the step's kernels."""
+    name = "persist_step_cylinder_384x256.md" if persistent else "launch_list_cylinder_384x256_host.md"
+    key = "traffic_bytes_per_launch:" if persistent else "traffic_bytes_per_step:"
     try:
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith(key):
                 return float(line.split(":")[1])
     except Exception:
         pass
@@ -167,6 +169,13 @@ def cell_step_bytes(ad_iters, ppe_iters, mixed):
     start = 16 + 4 * k + 1
     restarts = 2 * start if mixed else 0
     return 81 + pred * ad_iters + 41 + start + restarts + 81 + per_it * ppe_iters
+
+
+def exec_name(s):
+    mode = {0: "persistent", 1: "graph", 2: "host"}.get(s.exec_mode(), "?")
+    rows = s.mg_tile_rows()
+    cmg = s.cluster_vcycle()[1]
+    return f"{mode}, multigrid tiles 32x{8 * rows}" + (", cluster V-cycle" if cmg else "") + " (autotuned)"
 
 
 def rel_l2(a, b):
@@ -372,6 +381,8 @@ def main():
     def timed(prec):
         cfg, _, _ = cases.cylinder(precision=prec)
         s = ifx.Solver.create(cfg, xf, yf)
+        s.step(1)
+        s.autotune(steps=2)  # execution mode and tile shape; the state is restored afterwards
         for _ in range(args.warmup):
             flush()
             s.step(1)
@@ -434,7 +445,8 @@ def main():
 
     # roofline of the dominant kernel: the per-step kernel (persistent mode)
     peak, peak_kind = measured_peak()
-    traffic = committed_traffic()
+    persistent = s.exec_mode() == 0
+    traffic = committed_traffic(persistent)
     achieved = step_bytes_total / (total_ms * 1e-3) / 1e9
     # one phase alone: the finest-level smoothing sweep, FP32 in the mixed path
     k_ms, k_cells = s.profile_kernel(0, reps=200)
@@ -450,17 +462,19 @@ def main():
         "dtype": "f32 multigrid + f64 BiCGSTAB/state", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": [384, 256], "cells": cells, "parallelism": f"replicas x{world}",
                    "precision": "mixed", "ppe_tol": cfg_m.ppe_tol, "l2": "flushed before every timed step (256 MB write)",
-                   "execution": os.environ.get("IFX_EXEC", "persistent")},
+                   "execution": exec_name(s)},
         "plain_fp64": {"value": value64, "ms_per_step": total64 / args.steps, "gpu_launches": launches64,
+                       "execution": exec_name(s64),
                        "speedup_mixed_over_fp64": value / value64},
         "accuracy_vs_fp64": {"rel_l2_velocity": err_u, "cd_rel_err": err_cd, "cd": cd_m, "cd_fp64": st64.cd},
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "k_persist_step<float> (one launch per time step)",
+        "roofline": {"bound": "hbm", "kernel": ("k_persist_step<float> (one launch per time step)" if persistent else
+                                                "the step's kernels (one CUDA graph launch per time step)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic,
                      "bytes_per_launch": step_bytes_total / args.steps, "ms_per_launch": total_ms / args.steps,
-                     "note": "working set ~30 MB is L2-resident; grid-barrier/latency bound at this size"},
+                     "note": "working set ~30 MB is L2-resident; launch/barrier latency bound at this size"},
         "phase_roofline": {"kernel": "k_smooth<float> finest level, launched alone", "bytes_per_cell": 13,
                            "cells_per_launch": k_cells, "ms_per_launch": k_ms, "achieved_gbs": k_bw,
                            "frac": k_bw / peak, "grid_barrier_us": bar_us},

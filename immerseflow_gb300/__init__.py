@@ -55,6 +55,8 @@ _SIGS = {
     "ifx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
     "ifx_set_mg_tile_rows": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_get_mg_tile_rows": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_set_cluster_vcycle": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_get_cluster_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ifx_step_wait": (C.c_int, [C.c_void_p]),
     "ifx_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_get_exec_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -272,6 +274,15 @@ class Solver:
         r = C.c_int()
         _check(lib().ifx_get_mg_tile_rows(self._h, C.byref(r)))
         return r.value
+
+    def set_cluster_vcycle(self, on):
+        _check(lib().ifx_set_cluster_vcycle(self._h, 1 if on else 0))
+
+    def cluster_vcycle(self):
+        """(available, on)"""
+        a, o = C.c_int(), C.c_int()
+        _check(lib().ifx_get_cluster_vcycle(self._h, C.byref(a), C.byref(o)))
+        return bool(a.value), bool(o.value)
 
     def set_active(self, inst, active):
         _check(lib().ifx_set_instance_active(self._h, int(inst), 1 if active else 0))

@@ -23,6 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 SOURCES = [
     ("kernels_method.cu", []),
     ("kernels_persist.cu", []),
+    ("kernels_cluster.cu", []),
     ("kernels_ibm.cu", ["-fmad=false"]),
     ("kernels_ref.cu", []),
     ("solver.cu", []),

@@ -97,6 +97,54 @@ struct SubHdr {
 };
 constexpr size_t SUB_HDR_BYTES = (kSubLevels * sizeof(SubHdr) + 15) & ~(size_t)15;
 
+// Cluster V-cycle (graph and host-loop modes, instances that fit): the
+// multigrid levels above the sub-cycle are row-partitioned across the shared
+// memory of one thread-block cluster per instance.
+constexpr int CMG_CTAS = 16;        // CTAs per cluster
+constexpr int CMG_THREADS = 1024;   // threads per CTA
+constexpr int CMG_MAX_LEVELS = 8;   // distributed levels at most
+constexpr size_t CMG_SMEM_MAX = 200 * 1024;
+
+// Per-CTA shared-memory layout (byte offsets): for each distributed level the
+// CTA's m rows of e, e2, r (T) and stencil bytes, and the cluster-wide row
+// pointer tables (one generic pointer per row of the level, for e, e2, r and
+// the stencil bytes); a zero row for the ghost ring; the sub-cycle area.
+struct CmgLevel {
+    unsigned e, e2, r, b, pe, pe2, pr, pb;
+    int m;  // rows per CTA
+};
+struct CmgLayout {
+    CmgLevel lv[CMG_MAX_LEVELS];
+    unsigned zero, zerob, sub, bytes;
+    int nd;
+};
+IFX_HD inline CmgLayout cmg_layout(int nd, const int* nx, const int* ny, int tsize, size_t sub_bytes) {
+    CmgLayout L;
+    size_t o = 0, nxmax = 0;
+    const size_t ts = (size_t)tsize;
+    L.nd = nd;
+    for (int l = 0; l < nd && l < CMG_MAX_LEVELS; l++) {
+        const int m = (ny[l] - 2 + CMG_CTAS - 1) / CMG_CTAS;
+        const size_t n = (size_t)m * nx[l], rows = (size_t)ny[l];
+        CmgLevel& c = L.lv[l];
+        c.m = m;
+        c.e = (unsigned)o;   o += sub_al16(n * ts);
+        c.e2 = (unsigned)o;  o += sub_al16(n * ts);
+        c.r = (unsigned)o;   o += sub_al16(n * ts);
+        c.b = (unsigned)o;   o += sub_al16(n);
+        c.pe = (unsigned)o;  o += sub_al16(rows * 8);
+        c.pe2 = (unsigned)o; o += sub_al16(rows * 8);
+        c.pr = (unsigned)o;  o += sub_al16(rows * 8);
+        c.pb = (unsigned)o;  o += sub_al16(rows * 8);
+        if ((size_t)nx[l] > nxmax) nxmax = (size_t)nx[l];
+    }
+    L.zero = (unsigned)o;  o += sub_al16(nxmax * ts);
+    L.zerob = (unsigned)o; o += sub_al16(nxmax);
+    L.sub = (unsigned)o;   o += sub_al16(sub_bytes);
+    L.bytes = (unsigned)o;
+    return L;
+}
+
 struct alignas(16) Tile {
     int inst;  // instance index
     int lev;   // index into the LevelDev array

@@ -89,6 +89,8 @@ struct ifx_solver {
     std::vector<ifx::Tile*> dTsmW, dTreW;
     std::vector<int> ntsmW, ntreW;
     int mg_rows = 1;                 // rows per thread of the multigrid tile phases: 1 or MG_ROWS_WIDE
+    size_t cmg_bytes = 0;            // cluster V-cycle: shared memory per CTA (largest instance)
+    int cmg_ok = 0, cmg_use = 0;     // it fits / graph and host-loop modes use it
     ifx::Tile* dTall = nullptr;      // tiles of every level of every instance
     int* dSub = nullptr;             // LevelDev index of each instance's first small level
     int lmax = 0;

@@ -56,6 +56,15 @@ cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const Inst
 template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s);
+// Cluster V-cycle (kernels_cluster.cu): shared-memory bytes for one instance,
+// set-up (attributes; *ok = 1 when ninst clusters fit on the device at once),
+// launch (one cluster per instance; writes the finest level's correction).
+size_t cluster_vcycle_bytes(int nd, const int* nx, const int* ny, int tsize, size_t sub_bytes);
+template <typename T>
+cudaError_t cluster_vcycle_setup(int smem_bytes, int ninst, int* ok);
+template <typename T>
+cudaError_t launch_vcycle_cluster(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
+                                  const GhostDev* G, int pre, int post, int smem_bytes, cudaStream_t s);
 // Allows k_subcycle<T> `bytes` of dynamic shared memory (above the 48 KB default).
 template <typename T>
 cudaError_t subcycle_smem_limit(int bytes);

@@ -704,6 +704,19 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             (long long)I.lev[nl - 1].NX * I.lev[nl - 1].NY > (long long)TILE_THREADS * SUB_COARSE_PER_THREAD)
             return set_error(IFX_ERR_ARG, "grid too small or too elongated for the multigrid hierarchy");
         S->sub_bytes = std::max(S->sub_bytes, (int)staged(lb));
+        {   // cluster V-cycle: levels 0 .. lb-1 distributed, then the sub-cycle area
+            const int nd = lb;
+            size_t cb = (size_t)-1;
+            if (nd <= CMG_MAX_LEVELS) {
+                int nxs[CMG_MAX_LEVELS], nys[CMG_MAX_LEVELS];
+                for (int l = 0; l < nd; l++) {
+                    nxs[l] = I.lev[l].nx;
+                    nys[l] = I.lev[l].ny;
+                }
+                cb = cluster_vcycle_bytes(nd, nxs, nys, tsz, staged(lb));
+            }
+            S->cmg_bytes = std::max(S->cmg_bytes, cb);
+        }
         for (int l = 0; l < nl; l++) {
             HostLevel& L = I.lev[l];
             IFX_TRY(dupload(S, &L.d_kx, L.kx)); IFX_TRY(dupload(S, &L.d_ky, L.ky));
@@ -820,6 +833,14 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     IFX_TRY(dupload(S, &S->dSub, hSub));
     if (S->prec == IFX_PREC_FP64) CUDA_TRY(subcycle_smem_limit<double>(S->sub_bytes));
     else CUDA_TRY(subcycle_smem_limit<float>(S->sub_bytes));
+    S->cmg_ok = 0;
+    if (S->cmg_bytes <= CMG_SMEM_MAX) {
+        int ok = 0;
+        cudaError_t e = S->prec == IFX_PREC_FP64 ? cluster_vcycle_setup<double>((int)S->cmg_bytes, n, &ok)
+                                                 : cluster_vcycle_setup<float>((int)S->cmg_bytes, n, &ok);
+        S->cmg_ok = e == cudaSuccess && ok;
+        if (e != cudaSuccess) cudaGetLastError();  // cluster launches unavailable: tile V-cycle only
+    }
     IFX_TRY(dalloc(S, &S->dPart, (size_t)S->nt0 * NPART));
     IFX_TRY(dalloc(S, &S->dS, n));
     IFX_TRY(dalloc(S, &S->dCtl, 1));
@@ -880,6 +901,11 @@ int seq_vcycle(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int L = S->lmax, pre = S->mg_pre, post = S->mg_post;
+    if (S->cmg_use) {  // the whole V-cycle on one thread-block cluster per instance
+        q.add(launch_vcycle_cluster<T>(S->dSub, (int)S->inst.size(), S->dLV, S->dI, S->dS, S->dG, pre, post,
+                                       (int)S->cmg_bytes, st));
+        return parity_after_post(0, pre, post);
+    }
     // multigrid tile lists: 32x8 tiles, or wide tiles with MG_ROWS_WIDE rows per thread
     const int R = S->mg_rows;
     const bool W = R == MG_ROWS_WIDE;
@@ -1504,14 +1530,24 @@ extern "C" ifx_status ifx_set_instance_active(ifx_solver* S, int inst, int activ
     return IFX_OK;
 }
 
-// Rows per thread of the multigrid tile phases; the step graph is rebuilt on change.
-static void set_mg_rows(ifx_solver* S, int rows) {
-    if (rows == S->mg_rows) return;
+// Rows per thread of the multigrid tile phases, or the cluster V-cycle; the
+// step graph is rebuilt on change.
+static void drop_graph(ifx_solver* S) {
     if (S->gexec) cudaGraphExecDestroy(S->gexec);
     if (S->graph) cudaGraphDestroy(S->graph);
     S->gexec = nullptr;
     S->graph = nullptr;
+}
+static void set_mg_rows(ifx_solver* S, int rows) {
+    if (rows == S->mg_rows) return;
+    drop_graph(S);
     S->mg_rows = rows;
+}
+static void set_cluster_mg(ifx_solver* S, int on) {
+    on = on && S->cmg_ok;
+    if (on == S->cmg_use) return;
+    drop_graph(S);
+    S->cmg_use = on;
 }
 
 namespace {
@@ -1560,19 +1596,24 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
     StateSnapshot snap;
     IFX_TRY(snap.take(S));
     const long long steps0 = S->steps_done;
-    const int saved = S->exec_override, saved_rows = S->mg_rows;
-    // (execution mode, rows per thread of the multigrid tile phases); the
-    // persistent kernel always uses 32x8 tiles
-    std::vector<std::pair<int, int>> cand;
-    if (S->persist_grid > 0) cand.push_back({IFX_EXEC_PERSISTENT, 1});
-    cand.push_back({IFX_EXEC_GRAPH, 1});
-    cand.push_back({IFX_EXEC_GRAPH, MG_ROWS_WIDE});
-    std::pair<int, int> best = cand[0];
+    const int saved = S->exec_override, saved_rows = S->mg_rows, saved_cmg = S->cmg_use;
+    // (execution mode, rows per thread of the multigrid tile phases, cluster
+    // V-cycle); the persistent kernel always uses 32x8 tiles
+    struct Cand {
+        int mode, rows, cmg;
+    };
+    std::vector<Cand> cand;
+    if (S->persist_grid > 0) cand.push_back({IFX_EXEC_PERSISTENT, 1, 0});
+    cand.push_back({IFX_EXEC_GRAPH, 1, 0});
+    cand.push_back({IFX_EXEC_GRAPH, MG_ROWS_WIDE, 0});
+    if (S->cmg_ok) cand.push_back({IFX_EXEC_GRAPH, 1, 1});
+    Cand best = cand[0];
     double best_ms = 1e300;
     ifx_status st = IFX_OK;
     for (const auto& c : cand) {
-        S->exec_override = c.first;
-        set_mg_rows(S, c.second);
+        S->exec_override = c.mode;
+        set_mg_rows(S, c.rows);
+        set_cluster_mg(S, c.cmg);
         st = ifx_step(S, 1);  // warm-up (builds the graph on first use)
         if (st == IFX_OK) st = ifx_step(S, steps);
         if (st == IFX_OK) st = snap.restore(S);
@@ -1587,12 +1628,14 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
     if (st != IFX_OK) {
         S->exec_override = saved;
         set_mg_rows(S, saved_rows);
+        set_cluster_mg(S, saved_cmg);
         snap.restore(S);
         return st;
     }
-    S->exec_override = best.first;
-    set_mg_rows(S, best.second);
-    if (chosen) *chosen = best.first;
+    S->exec_override = best.mode;
+    set_mg_rows(S, best.rows);
+    set_cluster_mg(S, best.cmg);
+    if (chosen) *chosen = best.mode;
     if (ms_per_step) *ms_per_step = best_ms;
     return IFX_OK;
 }
@@ -1603,6 +1646,23 @@ extern "C" ifx_status ifx_set_mg_tile_rows(ifx_solver* S, int rows) {
     CUDA_TRY(cudaSetDevice(S->device));
     IFX_TRY(step_finish(S));
     set_mg_rows(S, rows);
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_set_cluster_vcycle(ifx_solver* S, int on) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_set_cluster_vcycle: null solver");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_set_cluster_vcycle needs a METHOD-mode solver");
+    if (on && !S->cmg_ok) return set_error(IFX_ERR_STATE, "the cluster V-cycle does not fit these instances on this device");
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    set_cluster_mg(S, on);
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_cluster_vcycle(const ifx_solver* S, int* available, int* on) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_get_cluster_vcycle: null solver");
+    if (available) *available = S->cmg_ok;
+    if (on) *on = S->cmg_use;
     return IFX_OK;
 }
 

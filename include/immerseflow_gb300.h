@@ -195,6 +195,14 @@ ifx_status ifx_autotune(ifx_solver* s, int steps, int* chosen_mode, double* ms_p
  * suits large batches).  Results do not depend on it.  The autotuner sets it. */
 ifx_status ifx_set_mg_tile_rows(ifx_solver* s, int rows);
 ifx_status ifx_get_mg_tile_rows(const ifx_solver* s, int* rows);
+/* Cluster V-cycle of the graph and host-loop modes: the multigrid levels above
+ * the small ones held in the distributed shared memory of one 16-CTA
+ * thread-block cluster per instance, phases separated by cluster barriers.
+ * Available when every instance fits (about 100k cells per instance in the
+ * mixed path) and the device runs that many clusters at once.  Results do not
+ * depend on it.  The autotuner considers it. */
+ifx_status ifx_set_cluster_vcycle(ifx_solver* s, int on);
+ifx_status ifx_get_cluster_vcycle(const ifx_solver* s, int* available, int* on);
 
 /* Batch membership (no reference counterpart): an inactive instance is left
  * unchanged by later steps while the others advance. */

@@ -173,3 +173,26 @@ def test_anisotropic_grid_semicoarsening_vs_oracle(oracle, nx, ny):
         assert abs(s.stats().last_ppe_iters - o.stats().last_ppe_iters) <= 1
         assert s.stats().last_ppe_iters <= 16
     _compare(s, o, tol=1e-9)
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+@pytest.mark.parametrize("nx,ny", [(96, 64), (256, 160)])
+def test_cluster_vcycle_bit_identical(prec, nx, ny):
+    """The V-cycle on one thread-block cluster (levels in distributed shared
+    memory) gives the tile path's result bit for bit."""
+    spec = small_cylinder(prec=prec, nx=nx, ny=ny)
+    a = _run_mode("graph", [spec], 3)
+    os.environ["IFX_EXEC"] = "graph"
+    try:
+        b = ifx.Solver.create(*spec)
+        available, _ = b.cluster_vcycle()
+        if not available:
+            pytest.skip("cluster V-cycle does not fit this case on this device")
+        b.set_cluster_vcycle(True)
+        assert b.cluster_vcycle() == (True, True)
+        b.step(3)
+    finally:
+        del os.environ["IFX_EXEC"]
+    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF):
+        assert np.array_equal(a.get(f), b.get(f)), f
+    assert a.stats().last_ppe_iters == b.stats().last_ppe_iters
