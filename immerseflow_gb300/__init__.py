@@ -62,12 +62,27 @@ _SIGS = {
     "ifx_get_exec_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_set_instance_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ifx_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "ifx_checkpoint_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
+    "ifx_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "ifx_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "ifx_checkpoint_write": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ifx_checkpoint_read": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ifx_write_snapshot_ascii": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    "ifx_read_snapshot_ascii": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    "ifx_probes_read": (C.c_int, [C.c_char_p, C.c_int, _dp, C.POINTER(C.c_int)]),
+    "ifx_set_history": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
+    "ifx_get_probe_cells": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]),
+    "ifx_get_history": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ifx_write_probe_file": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    "ifx_write_force_file": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
     "ifx_estimate_bytes": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_size_t)]),
     "ifx_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
     "ifx_server_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_server_set_steps_per_tick": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Config), _dp, _dp, C.c_int, C.POINTER(C.c_longlong)]),
     "ifx_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_server_preempt": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int]),
     "ifx_server_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int, C.POINTER(C.c_int)]),
     "ifx_server_request_state": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -124,6 +139,15 @@ def grid_read(path, n):
     out = np.zeros(n)
     _check(lib().ifx_grid_read(os.fsencode(path), n, _dptr(out)))
     return out
+
+
+def probes_read(path):
+    """probe.dat (probe_init, test/UTIL_PRE_SIM.f90:172-202) -> (n, 2) array."""
+    n = C.c_int()
+    _check(lib().ifx_probes_read(os.fsencode(path), 0, None, C.byref(n)))
+    xy = np.zeros(2 * max(n.value, 1))
+    _check(lib().ifx_probes_read(os.fsencode(path), n.value, _dptr(xy), C.byref(n)))
+    return xy[:2 * n.value].reshape(n.value, 2)
 
 
 def write_tecplot(path, x, y, q):
@@ -284,6 +308,61 @@ class Solver:
         _check(lib().ifx_get_cluster_vcycle(self._h, C.byref(a), C.byref(o)))
         return bool(a.value), bool(o.value)
 
+    # ---- restart / checkpoint
+    def checkpoint(self, inst=0):
+        """Binary checkpoint of one instance (bytes)."""
+        n = C.c_size_t()
+        _check(lib().ifx_checkpoint_bytes(self._h, int(inst), C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(lib().ifx_checkpoint_save(self._h, int(inst), buf, n.value))
+        return buf.raw
+
+    def restore(self, blob, inst=0):
+        """Loads a checkpoint made by checkpoint() into instance inst."""
+        buf = C.create_string_buffer(bytes(blob), len(blob))
+        _check(lib().ifx_checkpoint_load(self._h, int(inst), buf, len(blob)))
+
+    def checkpoint_write(self, path):
+        _check(lib().ifx_checkpoint_write(self._h, os.fsencode(path)))
+
+    def checkpoint_read(self, path):
+        _check(lib().ifx_checkpoint_read(self._h, os.fsencode(path)))
+
+    def write_snapshot_ascii(self, path, inst=0):
+        _check(lib().ifx_write_snapshot_ascii(self._h, int(inst), os.fsencode(path)))
+
+    def read_snapshot_ascii(self, path, inst=0):
+        _check(lib().ifx_read_snapshot_ascii(self._h, int(inst), os.fsencode(path)))
+
+    # ---- time history
+    def set_history(self, capacity, probes=(), inst=0):
+        """Records step, cd, cl and u, v, p at each probe (x, y) every step."""
+        xy = np.ascontiguousarray(np.asarray(probes, np.float64).reshape(-1))
+        n = xy.size // 2
+        _check(lib().ifx_set_history(self._h, int(inst), int(capacity), n, _dptr(xy) if n else None))
+
+    def probe_cells(self, inst=0):
+        n = C.c_int()
+        _check(lib().ifx_get_probe_cells(self._h, int(inst), 0, None, None, C.byref(n)))
+        i = (C.c_int * max(n.value, 1))()
+        j = (C.c_int * max(n.value, 1))()
+        _check(lib().ifx_get_probe_cells(self._h, int(inst), n.value, i, j, C.byref(n)))
+        return [(i[k], j[k]) for k in range(n.value)]
+
+    def history(self, cap=1 << 20, inst=0):
+        """(records, 3 + 3*nprobes) array: step, cd, cl, then u, v, p per probe."""
+        n, w = C.c_int(), C.c_int()
+        _check(lib().ifx_get_history(self._h, int(inst), 0, None, C.byref(n), C.byref(w)))
+        rows = np.zeros(max(cap, 1) * max(w.value, 1))
+        _check(lib().ifx_get_history(self._h, int(inst), int(cap), _dptr(rows), C.byref(n), C.byref(w)))
+        return rows[:n.value * w.value].reshape(n.value, w.value)
+
+    def write_probe_file(self, path, inst=0):
+        _check(lib().ifx_write_probe_file(self._h, int(inst), os.fsencode(path)))
+
+    def write_force_file(self, path, inst=0):
+        _check(lib().ifx_write_force_file(self._h, int(inst), os.fsencode(path)))
+
     def set_active(self, inst, active):
         _check(lib().ifx_set_instance_active(self._h, int(inst), 1 if active else 0))
 
@@ -333,6 +412,10 @@ class Server:
         _check(lib().ifx_server_tick(self._h, C.byref(n)))
         return n.value
 
+    def preempt(self, rid, front=True):
+        """Takes a running request off the device (checkpoint in host memory)."""
+        _check(lib().ifx_server_preempt(self._h, int(rid), 1 if front else 0))
+
     def poll(self, cap=1024):
         ids = (C.c_longlong * cap)()
         n = C.c_int()
@@ -378,4 +461,4 @@ class Server:
 from .interface import ImmerseFlow  # noqa: E402  (mirror of the reference object)
 
 __all__ = ["Config", "Stats", "default_config", "Solver", "Server", "ImmerseFlow", "IFXError", "config_read",
-           "grid_read", "write_tecplot", "estimate_bytes", "lib", "capi"]
+           "grid_read", "write_tecplot", "probes_read", "estimate_bytes", "lib", "capi"]

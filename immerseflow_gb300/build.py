@@ -30,6 +30,7 @@ SOURCES = [
     ("io.cpp", ["-x", "cu"]),
     ("noalloc.cu", []),
     ("server.cpp", ["-x", "cu"]),
+    ("state_io.cpp", ["-x", "cu"]),
 ]
 
 

@@ -219,6 +219,11 @@ struct alignas(16) InstDev {
     // body (ellipse), bit-exact predicate constants
     double bcx, bcy, ba, bb, bcs, bsn, bia2, bib2, fref;
     const ForceSample* fs;       // FORCE_SAMPLES entries when body != 0
+    // time history: a ring of hist_cap records of hist_w doubles (step, cd, cl,
+    // then u, v, p at each probe cell), written at the end of every step
+    double* hist;
+    const int* probe_cell;       // pitched cell index of each probe
+    int hist_cap, hist_w, nprobe;
 };
 
 // Device-resident per-instance iteration state and diagnostics.
@@ -230,6 +235,8 @@ struct InstState {
     double rho, alpha, omega, beta;           // BiCGSTAB scalars
     double max_div, cd, cl, flux_in, flux_out;
     double rel_restart;                       // mixed path: true relative residual at the last restart
+    long long nstep;                          // time steps this instance has done
+    long long hist_n;                         // time-history records written
 };
 
 // Loop control for device-side convergence: reduce kernels vote, the last

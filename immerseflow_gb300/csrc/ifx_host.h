@@ -50,6 +50,9 @@ struct Instance {
     InstDev dev{};                   // device pointers (host copy of the InstDev entry)
 };
 
+// Waits for steps issued by ifx_step_async and checks their state.
+ifx_status finish_pending(ifx_solver* S);
+
 }  // namespace ifx
 
 // The opaque handle of the C ABI.

@@ -276,6 +276,7 @@ __device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, Inst
     int k = vb * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int st = I[k].retired ? ST_DONE : ST_ACTIVE;
+    if (st == ST_ACTIVE) S[k].nstep++;
     S[k].pred_state = st;
     S[k].pred_iters = 0;
     S[k].ppe_state = st;
@@ -1687,26 +1688,47 @@ __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstStat
     const int k = vb;
     const InstDev& in = I[k];
     if (in.retired) return;
-    if (!in.body) {
-        if (threadIdx.x == 0) { S[k].cd = 0.0; S[k].cl = 0.0; }
-        return;
+    double cd = 0.0, cl = 0.0;  // valid in thread 0
+    if (in.body) {
+        const double mu = 1.0 / in.re;
+        const int P = in.pitch;
+        double F[2] = {0.0, 0.0};
+        for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
+            const ForceSample f = ldg_struct(&in.fs[q]);
+            const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
+            const double up = bil(in.u, f.c1, P, f.xi1, f.et1);
+            const double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
+            F[0] += (-ps * f.nx + mu * up / f.del) * f.ds;
+            F[1] += (-ps * f.ny + mu * vp / f.del) * f.ds;
+        }
+        __shared__ double out[2];
+        block_sum<2>(F, out);
+        if (threadIdx.x == 0) {
+            cd = out[0] / in.fref;
+            cl = out[1] / in.fref;
+        }
     }
-    const double mu = 1.0 / in.re;
-    const int P = in.pitch;
-    double F[2] = {0.0, 0.0};
-    for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
-        const ForceSample f = ldg_struct(&in.fs[q]);
-        const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
-        const double up = bil(in.u, f.c1, P, f.xi1, f.et1);
-        const double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
-        F[0] += (-ps * f.nx + mu * up / f.del) * f.ds;
-        F[1] += (-ps * f.ny + mu * vp / f.del) * f.ds;
-    }
-    __shared__ double out[2];
-    block_sum<2>(F, out);
     if (threadIdx.x == 0) {
-        S[k].cd = out[0] / in.fref;
-        S[k].cl = out[1] / in.fref;
+        S[k].cd = cd;
+        S[k].cl = cl;
+    }
+    // time-history record of this step: step count, forces, probe values
+    if (in.hist_cap > 0) {
+        const long long hn = S[k].hist_n;
+        double* rec = in.hist + (size_t)(hn % in.hist_cap) * in.hist_w;
+        if (threadIdx.x == 0) {
+            rec[0] = (double)S[k].nstep;
+            rec[1] = cd;
+            rec[2] = cl;
+        }
+        for (int q = threadIdx.x; q < in.nprobe; q += blockDim.x) {
+            const int c = in.probe_cell[q];
+            rec[3 + 3 * q] = in.u[c];
+            rec[4 + 3 * q] = in.v[c];
+            rec[5 + 3 * q] = in.p[c];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) S[k].hist_n = hn + 1;
     }
 }
 

@@ -13,6 +13,12 @@
 // go on; a cohort whose members have all finished frees its memory, and the
 // next tick admits more requests.  A request's result does not depend on the
 // cohort it ran in: instances in a batch share no arithmetic.
+//
+// Pre-emption: a running request can be taken off the device between ticks.
+// Its state is kept as a binary checkpoint in host memory (ifx_checkpoint_save),
+// its instance is made inactive, and it waits again; when it is admitted
+// again, its new instance loads the checkpoint and the request continues bit
+// for bit.
 #include <algorithm>
 #include <cstring>
 #include <deque>
@@ -53,10 +59,11 @@ struct ifx_server {
         int nx = 0, ny = 0;
         std::vector<double> u, v, p;
         ifx_stats st;
+        std::vector<char> resume;  // checkpoint of a pre-empted request
     };
     struct Cohort {
         ifx_solver* s = nullptr;
-        std::vector<long long> ids;
+        std::vector<long long> ids;  // per instance; -1 once its request was pre-empted
         int live = 0;
         int pending = 0;  // steps issued this tick
         size_t bytes = 0;
@@ -108,17 +115,30 @@ static ifx_status admit(ifx_server* V) {
         }
         return st;
     }
-    ifx_device_bytes(c.s, &c.bytes);
     c.ids = take;
     c.live = (int)take.size();
+    ifx_status worst = IFX_OK;
     for (size_t k = 0; k < take.size(); k++) {
         ifx_server::Request& r = V->reqs[take[k]];
         r.state = 1;
         ifx_get_dims(c.s, (int)k, &r.nx, &r.ny);
+        if (!r.resume.empty()) {
+            const ifx_status e = ifx_checkpoint_load(c.s, (int)k, r.resume.data(), r.resume.size());
+            if (e != IFX_OK) {
+                ifx_set_instance_active(c.s, (int)k, 0);
+                r.state = 3;
+                V->finished.push_back(r.id);
+                c.live--;
+                worst = e;
+            }
+            r.resume.clear();
+            r.resume.shrink_to_fit();
+        }
     }
+    ifx_device_bytes(c.s, &c.bytes);
     V->used += c.bytes;
     V->cohorts.push_back(c);
-    return IFX_OK;
+    return worst;
 }
 
 extern "C" ifx_status ifx_estimate_bytes(const ifx_config* cfg, size_t* bytes) {
@@ -178,6 +198,7 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
     for (auto& c : V->cohorts) {
         int k = V->steps_per_tick;
         for (long long id : c.ids) {
+            if (id < 0) continue;
             const ifx_server::Request& r = V->reqs[id];
             if (r.state == 1) k = std::min(k, r.nsteps - r.done);
         }
@@ -198,13 +219,14 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
         if (st != IFX_OK) {
             worst = st;
             for (long long id : c.ids)
-                if (V->reqs[id].state == 1) {
+                if (id >= 0 && V->reqs[id].state == 1) {
                     V->reqs[id].state = 3;
                     V->finished.push_back(id);
                 }
             drop = true;
         } else {
             for (size_t k = 0; k < c.ids.size(); k++) {
+                if (c.ids[k] < 0) continue;
                 ifx_server::Request& r = V->reqs[c.ids[k]];
                 if (r.state != 1) continue;
                 r.done += c.pending;
@@ -235,6 +257,41 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
     }
     if (n_finished) *n_finished = (int)(V->finished.size() - before);
     return worst;
+}
+
+extern "C" ifx_status ifx_server_preempt(ifx_server* V, long long id, int front) {
+    if (!V) return set_error(IFX_ERR_ARG, "ifx_server_preempt: null server");
+    auto it = V->reqs.find(id);
+    if (it == V->reqs.end()) return set_error(IFX_ERR_ARG, "ifx_server_preempt: unknown request");
+    ifx_server::Request& r = it->second;
+    if (r.state != 1) return set_error(IFX_ERR_STATE, "ifx_server_preempt: request is not running");
+    for (auto ci = V->cohorts.begin(); ci != V->cohorts.end(); ++ci) {
+        ifx_server::Cohort& c = *ci;
+        const auto pos = std::find(c.ids.begin(), c.ids.end(), id);
+        if (pos == c.ids.end()) continue;
+        const int k = (int)(pos - c.ids.begin());
+        size_t nb = 0;
+        ifx_status st = ifx_checkpoint_bytes(c.s, k, &nb);
+        if (st != IFX_OK) return st;
+        r.resume.resize(nb);
+        st = ifx_checkpoint_save(c.s, k, r.resume.data(), nb);
+        if (st == IFX_OK) st = ifx_set_instance_active(c.s, k, 0);
+        if (st != IFX_OK) {
+            r.resume.clear();
+            return st;
+        }
+        r.state = 0;
+        *pos = -1;  // the slot no longer belongs to the request
+        if (front) V->waiting.push_front(id);
+        else V->waiting.push_back(id);
+        if (--c.live == 0) {
+            ifx_destroy(c.s);
+            V->used -= std::min(V->used, c.bytes);
+            V->cohorts.erase(ci);
+        }
+        return IFX_OK;
+    }
+    return set_error(IFX_ERR_STATE, "ifx_server_preempt: request has no cohort");
 }
 
 extern "C" ifx_status ifx_server_poll(ifx_server* V, long long* ids, int cap, int* n) {

@@ -1423,6 +1423,10 @@ ifx_status get_pitched(ifx_solver* S, const Instance& I, const double* src, doub
 
 // ================================================================== C ABI
 
+namespace ifx {
+ifx_status finish_pending(ifx_solver* S) { return S->pending_steps ? step_finish(S) : IFX_OK; }
+}  // namespace ifx
+
 static ifx_status new_solver(ifx_solver** out) {
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -1570,6 +1574,7 @@ struct StateSnapshot {
                 items.push_back({p, nc});
             items.push_back({(void*)d.qbu, nq});
             items.push_back({(void*)d.qbv, nq});
+            if (d.hist_cap > 0) items.push_back({(void*)d.hist, (size_t)d.hist_cap * d.hist_w * sizeof(double)});
         }
         items.push_back({(void*)S->dS, S->inst.size() * sizeof(InstState)});
         for (auto& it : items) {

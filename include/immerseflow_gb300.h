@@ -260,6 +260,54 @@ ifx_status ifx_get_stats(ifx_solver* s, int inst, ifx_stats* out);
 ifx_status ifx_last_step_ms(ifx_solver* s, double* ms);
 ifx_status ifx_synchronize(ifx_solver* s);
 
+/* ------------------------------------------------------- restart / checkpoint */
+/* The reference parses `Restart Restart_Time` and `Write Interval`
+ * (src/main.cu:27-30,50-53) without using them; its Fortran predecessor
+ * restarts from an ASCII snapshot (test/UTIL_PRE_SIM.f90:120-149).
+ * Binary checkpoint of one instance: every array a step carries into the next
+ * (METHOD: cell and face velocities, convection history, pressure, outflow
+ * boundary values, iteration state; REFERENCE: u, v, p), so that a run
+ * restarted from it continues bit for bit.  A checkpoint loads into an
+ * instance of the same mode, grid, body and boundary types (any precision,
+ * any batch position); a header and a checksum are checked.  Loading into a
+ * one-instance handle also sets its step count. */
+ifx_status ifx_checkpoint_bytes(const ifx_solver* s, int inst, size_t* bytes);
+ifx_status ifx_checkpoint_save(ifx_solver* s, int inst, void* buf, size_t n);
+ifx_status ifx_checkpoint_load(ifx_solver* s, int inst, const void* buf, size_t n);
+/* Every instance of the handle to / from one file (written atomically). */
+ifx_status ifx_checkpoint_write(ifx_solver* s, const char* path);
+ifx_status ifx_checkpoint_read(ifx_solver* s, const char* path);
+/* ASCII snapshot in the predecessor's layout: three header lines (the third
+ * names the step), then one row per cell including ghosts, j outer, i inner:
+ * x y u v p uf vf iblank (uf / vf: east / north face velocity of the cell).
+ * It holds no convection history: the first step after reading it starts the
+ * Adams-Bashforth history again (forward-Euler convection, as at t = 0). */
+ifx_status ifx_write_snapshot_ascii(ifx_solver* s, int inst, const char* path);
+ifx_status ifx_read_snapshot_ascii(ifx_solver* s, int inst, const char* path);
+
+/* ------------------------------------------------------------ time history */
+/* probe_init (test/UTIL_PRE_SIM.f90:172-202): probe.dat holds the probe count,
+ * a skipped line, then one "x y" line per probe.  *n receives the count; up to
+ * cap probes are stored in xy (x0, y0, x1, y1, ...). */
+ifx_status ifx_probes_read(const char* path, int cap, double* xy, int* n);
+/* METHOD mode: record, at the end of every step, the step count, cd, cl and
+ * u, v, p at each probe into a device ring buffer of `capacity` records (0
+ * switches recording off).  A probe samples the cell whose centre is nearest
+ * in x and in y (first minimum over the cell centres, ghosts included, as
+ * probe_init's minloc).  Resets the record count. */
+ifx_status ifx_set_history(ifx_solver* s, int inst, int capacity, int nprobes, const double* xy);
+/* Cell indices (0-based, ghost cell 0) of the probes; *n = probe count. */
+ifx_status ifx_get_probe_cells(ifx_solver* s, int inst, int cap, int* i, int* j, int* n);
+/* The newest min(records, capacity, cap) records, oldest first; each row has
+ * *width = 3 + 3*nprobes doubles: step, cd, cl, then u, v, p per probe. */
+ifx_status ifx_get_history(ifx_solver* s, int inst, int cap, double* rows, int* n, int* width);
+/* probe_output.dat: a header line (count, probe cell centres x then y, cell
+ * indices i then j), a blank line, " Time  U   V  P", then one row per
+ * recorded step: time, and u v p of each probe. */
+ifx_status ifx_write_probe_file(ifx_solver* s, int inst, const char* path);
+/* Force history: " Time  Cd  Cl", then one row per recorded step. */
+ifx_status ifx_write_force_file(ifx_solver* s, int inst, const char* path);
+
 /* ------------------------------------------------------------------ server */
 /* Continuous-batching solve server (no reference counterpart; the reference
  * runs one case per process, src/main.cu:75-102).  Submitted METHOD-mode cases
@@ -287,6 +335,12 @@ ifx_status ifx_server_set_steps_per_tick(ifx_server* v, int steps);
 ifx_status ifx_server_submit(ifx_server* v, const ifx_config* cfg, const double* xf, const double* yf,
                              int nsteps, long long* id);
 ifx_status ifx_server_tick(ifx_server* v, int* n_finished);
+/* Pre-emption between ticks: a running request's state is saved as a binary
+ * checkpoint in host memory, its instance stops, and it waits again (at the
+ * front of the queue if front != 0, else at the back).  When admitted again
+ * it continues from the checkpoint; its result is the same as if it had not
+ * been interrupted. */
+ifx_status ifx_server_preempt(ifx_server* v, long long id, int front);
 /* Finished (or failed) request ids, oldest first; each is returned once. */
 ifx_status ifx_server_poll(ifx_server* v, long long* ids, int cap, int* n);
 ifx_status ifx_server_request_state(ifx_server* v, long long id, int* state, int* steps_done, int* nx, int* ny);
