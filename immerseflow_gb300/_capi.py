@@ -16,6 +16,7 @@ IFX_ERR_DIVERGED = 7
 IFX_ERR_BUDGET = 8
 IFX_ERR_STATE = 9
 IFX_ERR_NODEVICE = 10
+PPE_JACOBI, PPE_POINT_GS, PPE_LINE_SOR = 0, 1, 2
 
 MODE_REFERENCE = 0
 MODE_METHOD = 1
@@ -64,6 +65,7 @@ class Config(C.Structure):
         ("mg_omega", C.c_double),
         ("mixed_inner", C.c_int),
         ("force_ref_u", C.c_double), ("force_ref_len", C.c_double),
+        ("ppe_method", C.c_int), ("relax_ad", C.c_double), ("relax_ppe", C.c_double),
         ("xgrid", C.c_char * PATH_MAX), ("ygrid", C.c_char * PATH_MAX),
     ]
 
@@ -106,6 +108,7 @@ def default_config():
     c.mg_omega = 0.8
     c.mixed_inner = 8
     c.force_ref_u, c.force_ref_len = 1.0, 1.0
+    c.ppe_method, c.relax_ad, c.relax_ppe = PPE_JACOBI, 1.0, 1.0
     c.xgrid = b"xgrid.dat2"
     c.ygrid = b"ygrid.dat2"
     return c

@@ -121,6 +121,7 @@ struct ifx_solver {
     double *r_dx = nullptr, *r_dy = nullptr, *r_xc = nullptr, *r_yc = nullptr, *r_ib = nullptr;
     double *r_coef = nullptr, *r_sx = nullptr, *r_sy = nullptr, *r_uf = nullptr, *r_vf = nullptr, *r_res = nullptr;
     double* r_out = nullptr;         // device reduction results (+ ticket)
+    double* r_line = nullptr;        // line-SOR elimination scratch
     double* h_out = nullptr;         // pinned
     int r_cur = 0;                   // 0: state in r_u/r_v, 1: in r_ut/r_vt
     std::vector<int> r_iters;

@@ -88,6 +88,7 @@ cudaError_t launch_ghost_weights(GhostDev* G, const int* ibm, int nibm, const In
 struct RefDev {
     int nx, ny;
     double dt, re;
+    double w_ad;  // relaxation of the velocity Jacobi update (1: none)
     const double *dx, *dy, *iblank;
     double *aP, *aE, *aW, *aN, *aS, *sx, *sy, *uf, *vf, *res;
 };
@@ -106,5 +107,13 @@ cudaError_t launch_ref_init(int nx, int ny, const double* xc, const double* yc, 
 cudaError_t launch_ref_ppe_coeffs(const RefDev& R, cudaStream_t s);
 cudaError_t launch_ref_ppe_bc(const RefDev& R, double* p, cudaStream_t s);
 cudaError_t launch_ref_ppe_sweep(const RefDev& R, const double* p, double* pn, double* out, cudaStream_t s);
+// One red-black point Gauss-Seidel / SOR iteration in place (red (i+j even)
+// cells, then black), then the signed residual sum -> out[0].
+cudaError_t launch_ref_ppe_rbgs(const RefDev& R, double* p, double w, double* out, cudaStream_t s);
+// One zebra x-line SOR iteration in place (odd rows, then even rows; each row
+// solved exactly along x with the Thomas algorithm, scratch cp/dp of nx*ny),
+// then the signed residual sum -> out[0].
+cudaError_t launch_ref_ppe_lines(const RefDev& R, double* p, double* cp, double* dp, double w, double* out,
+                                 cudaStream_t s);
 
 }  // namespace ifx

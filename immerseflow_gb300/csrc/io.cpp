@@ -91,6 +91,9 @@ extern "C" void ifx_config_default(ifx_config* c) {
     c->mixed_inner = 8;
     c->force_ref_u = 1.0;
     c->force_ref_len = 1.0;
+    c->ppe_method = IFX_PPE_JACOBI;
+    c->relax_ad = 1.0;
+    c->relax_ppe = 1.0;
     std::snprintf(c->xgrid, IFX_PATH_MAX, "xgrid.dat2");
     std::snprintf(c->ygrid, IFX_PATH_MAX, "ygrid.dat2");
 }
@@ -142,9 +145,15 @@ extern "C" ifx_status ifx_config_read(const char* path, ifx_config* c) {
         } else if (line.find("Lx") != std::string::npos) {
             if (!next() || !(iss >> c->lx >> c->ly)) return bad("Lx");
         } else if (line.find("w-AD") != std::string::npos) {
-            if (!next() || !(iss >> c->w_ad >> c->w_ppe >> c->ad_itermax >> c->ppe_itermax >> c->ad_solver >>
-                             c->ppe_solver))
+            // w-AD and w-PPE are ints in the reference (src/header/globalVariables.cuh:26);
+            // read as numbers so that a relaxation factor such as 0.8 is kept
+            double wa = 1.0, wp = 1.0;
+            if (!next() || !(iss >> wa >> wp >> c->ad_itermax >> c->ppe_itermax >> c->ad_solver >> c->ppe_solver))
                 return bad("w-AD");
+            c->w_ad = (int)wa;
+            c->w_ppe = (int)wp;
+            c->relax_ad = wa;
+            c->relax_ppe = wp;
         } else if (line.find("ErrorMax") != std::string::npos) {
             if (!next() || !(iss >> c->error_max >> c->tmax >> c->dt >> c->re >> c->mu)) return bad("ErrorMax");
         } else if (line.find("Write Interval") != std::string::npos) {
@@ -206,6 +215,13 @@ extern "C" ifx_status ifx_config_read(const char* path, ifx_config* c) {
             if (!next() || !(iss >> c->mixed_inner)) return bad("Mixed-Inner");
         } else if (line.find("Force-Reference") != std::string::npos) {
             if (!next() || !(iss >> c->force_ref_u >> c->force_ref_len)) return bad("Force-Reference");
+        } else if (line.find("PPE-Method") != std::string::npos) {
+            std::string w;
+            if (!next() || !(iss >> w)) return bad("PPE-Method");
+            if (w == "jacobi" || w == "0") c->ppe_method = IFX_PPE_JACOBI;
+            else if (w == "point-gs" || w == "1") c->ppe_method = IFX_PPE_POINT_GS;
+            else if (w == "line-sor" || w == "2") c->ppe_method = IFX_PPE_LINE_SOR;
+            else return bad("PPE-Method");
         } else if (line.find("Grid-Files") != std::string::npos) {
             if (!next() || !(iss >> xg >> yg)) return bad("Grid-Files");
         }

@@ -120,6 +120,11 @@ __global__ void k_ref_jacobi(RefDev R, const double* __restrict__ u, const doubl
     const double b = R.sy[id] + R.aE[id] * v[id + 1] + R.aW[id] * v[id - 1] + R.aN[id] * v[id + nx] +
                      R.aS[id] * v[id - nx];
     vn[id] = R.iblank[id] * b / R.aP[id];
+    // under-relaxation, the reference's commented-out lines (src/include/ADSolver.cu:95,116)
+    if (R.w_ad != 1.0) {
+        un[id] = (1.0 - R.w_ad) * u[id] + R.w_ad * un[id];
+        vn[id] = (1.0 - R.w_ad) * v[id] + R.w_ad * vn[id];
+    }
 }
 
 // Fixed-order two-level sum: each block writes its partial, the last block
@@ -243,6 +248,50 @@ __global__ void k_ref_ppe_resid(RefDev R, const double* __restrict__ p, double* 
     blocks_sum<1>(r, R.res, ticket, out);
 }
 
+// Point Gauss-Seidel / SOR on one colour of the red-black ordering, in place:
+// the jacobiIteration update (src/include/PPESolver.cu:21-25) of the cells
+// with (i + j) % 2 == colour, relaxed as (1 - w) p + w p_new when w != 1.
+// Cells of one colour only read the other colour, so a launch is race-free.
+__global__ void k_ref_ppe_rb(RefDev R, double* __restrict__ p, int colour, double w) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = R.nx, ny = R.ny;
+    if (id >= nx * ny) return;
+    const int i = id % nx, j = id / nx;
+    if (!(i > 0 && i < nx - 1 && j > 0 && j < ny - 1) || ((i + j) & 1) != colour) return;
+    const double g =
+        -(p[id + 1] * R.aE[id] + p[id - 1] * R.aW[id] + p[id + nx] * R.aN[id] + p[id - nx] * R.aS[id]) / R.aP[id];
+    p[id] = w == 1.0 ? g : (1.0 - w) * p[id] + w * g;
+}
+
+// Line SOR along x for the rows j = first, first + 2, ... (one thread per row):
+//   aW p[i-1] + aP p[i] + aE p[i+1] = -(aN p[i,j+1] + aS p[i,j-1])
+// for i = 1..nx-2, ghost values at i = 0 and nx-1 moved to the right-hand
+// side, solved by the Thomas algorithm (forward elimination into cp, dp, back
+// substitution), then relaxed as (1 - w) p + w x when w != 1.  Rows of one
+// parity only read rows of the other, so a launch is race-free.
+__global__ void k_ref_ppe_line(RefDev R, double* __restrict__ p, double* __restrict__ cp, double* __restrict__ dp,
+                               int first, double w) {
+    const int j = first + 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int nx = R.nx, ny = R.ny;
+    if (j > ny - 2) return;
+    const int b = j * nx, last = nx - 2;
+    for (int i = 1; i <= last; i++) {
+        const int id = b + i;
+        double rhs = -(R.aN[id] * p[id + nx] + R.aS[id] * p[id - nx]);
+        if (i == 1) rhs -= R.aW[id] * p[id - 1];
+        if (i == last) rhs -= R.aE[id] * p[id + 1];
+        const double m = i == 1 ? R.aP[id] : R.aP[id] - R.aW[id] * cp[id - 1];
+        cp[id] = i == last ? 0.0 : R.aE[id] / m;
+        dp[id] = i == 1 ? rhs / m : (rhs - R.aW[id] * dp[id - 1]) / m;
+    }
+    double x = 0.0;
+    for (int i = last; i >= 1; i--) {
+        const int id = b + i;
+        x = i == last ? dp[id] : dp[id] - cp[id] * x;
+        p[id] = w == 1.0 ? x : (1.0 - w) * p[id] + w * x;
+    }
+}
+
 static inline int nb256(int n) { return (n + 255) / 256; }
 
 cudaError_t launch_ref_coeffs(const RefDev& R, cudaStream_t s) {
@@ -284,6 +333,26 @@ cudaError_t launch_ref_ppe_coeffs(const RefDev& R, cudaStream_t s) {
 }
 cudaError_t launch_ref_ppe_bc(const RefDev& R, double* p, cudaStream_t s) {
     k_ref_ppe_bc<<<nb256(R.nx * R.ny), 256, 0, s>>>(R, p);
+    return cudaGetLastError();
+}
+cudaError_t launch_ref_ppe_rbgs(const RefDev& R, double* p, double w, double* out, cudaStream_t s) {
+    for (int colour = 0; colour < 2; colour++) {
+        k_ref_ppe_rb<<<nb256(R.nx * R.ny), 256, 0, s>>>(R, p, colour, w);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    k_ref_ppe_resid<<<nb256(R.nx * R.ny), 256, 0, s>>>(R, p, out, (unsigned int*)(out + 2));
+    return cudaGetLastError();
+}
+cudaError_t launch_ref_ppe_lines(const RefDev& R, double* p, double* cp, double* dp, double w, double* out,
+                                 cudaStream_t s) {
+    const int rows = (R.ny - 2 + 1) / 2;  // rows of the larger parity
+    for (int first = 1; first <= 2; first++) {
+        k_ref_ppe_line<<<(rows + 63) / 64, 64, 0, s>>>(R, p, cp, dp, first, w);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    k_ref_ppe_resid<<<nb256(R.nx * R.ny), 256, 0, s>>>(R, p, out, (unsigned int*)(out + 2));
     return cudaGetLastError();
 }
 cudaError_t launch_ref_ppe_sweep(const RefDev& R, const double* p, double* pn, double* out, cudaStream_t s) {

@@ -473,6 +473,9 @@ ifx_status validate(const ifx_config* c) {
         return set_error(IFX_ERR_ARG, "body semi-axes must be positive");
     for (int s = 0; s < 4; s++)
         if (c->bc_type[s] < 0 || c->bc_type[s] > 3) return set_error(IFX_ERR_ARG, "bad boundary type");
+    if (c->ppe_method != IFX_PPE_JACOBI)
+        return set_error(IFX_ERR_ARG, "PPE-Method point-gs / line-sor selects the REFERENCE-mode pressure solve; "
+                                      "method mode solves the pressure with multigrid-preconditioned BiCGSTAB");
     return IFX_OK;
 }
 
@@ -1251,6 +1254,8 @@ ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf
     I.ny = I.NY + 2;
     I.pitch = I.nx;
     I.ncell = (size_t)I.nx * I.ny;
+    if (c->ppe_method < IFX_PPE_JACOBI || c->ppe_method > IFX_PPE_LINE_SOR) return set_error(IFX_ERR_ARG, "bad PPE-Method");
+    if (!(c->relax_ad < 2.0) || !(c->relax_ppe < 2.0)) return set_error(IFX_ERR_ARG, "relaxation factors must be below 2");
     if (I.NX < 2 || I.NY < 2) return set_error(IFX_ERR_ARG, "reference mode needs nx, ny >= 2");
     build_grid(I, xf, yf);
     const int nx = I.nx, ny = I.ny;
@@ -1287,6 +1292,7 @@ ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf
     IFX_TRY(dalloc(S, &S->r_vf, (size_t)(nx - 1) * (ny - 1)));
     IFX_TRY(dalloc(S, &S->r_res, 2 * ((n + 255) / 256) + 2));
     IFX_TRY(dalloc(S, &S->r_out, 4));
+    if (c->ppe_method == IFX_PPE_LINE_SOR) IFX_TRY(dalloc(S, &S->r_line, n));
     CUDA_TRY(cudaMallocHost((void**)&S->h_out, 4 * sizeof(double)));
     // initializeData (src/include/preSim.cu:201-217)
     CUDA_TRY(launch_ref_init(nx, ny, S->r_xc, S->r_yc, S->r_u, S->r_v, S->r_p, S->stream));
@@ -1296,6 +1302,9 @@ ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     return IFX_OK;
 }
+
+// A relaxation factor as read from w-AD / w-PPE: 0 (unset) and 1 mean none.
+double relax_factor(double w) { return w > 0.0 ? w : 1.0; }
 
 RefDev refdev(ifx_solver* S) {
     const Instance& I = S->inst[0];
@@ -1318,6 +1327,7 @@ RefDev refdev(ifx_solver* S) {
     R.uf = S->r_uf;
     R.vf = S->r_vf;
     R.res = S->r_res;
+    R.w_ad = relax_factor(I.cfg.relax_ad);
     return R;
 }
 
@@ -1379,11 +1389,21 @@ ifx_status ppe_reference(ifx_solver* S, int* iters) {
     double* tmp = S->r_pt;
     double residual = 1.0;
     int it = 0;
+    const int method = I.cfg.ppe_method;
+    const double w = relax_factor(I.cfg.relax_ppe);
     // pow(10.0, -6.0) at src/include/PPESolver.cu:172
     while (residual > 1e-6 && it < I.cfg.ppe_itermax) {
-        CUDA_TRY(launch_ref_ppe_sweep(R, cur, tmp, S->r_out, st));
-        S->launches += 2;
-        std::swap(cur, tmp);
+        if (method == IFX_PPE_POINT_GS) {
+            CUDA_TRY(launch_ref_ppe_rbgs(R, cur, w, S->r_out, st));
+            S->launches += 3;
+        } else if (method == IFX_PPE_LINE_SOR) {
+            CUDA_TRY(launch_ref_ppe_lines(R, cur, S->r_pt, S->r_line, w, S->r_out, st));
+            S->launches += 3;
+        } else {
+            CUDA_TRY(launch_ref_ppe_sweep(R, cur, tmp, S->r_out, st));
+            S->launches += 2;
+            std::swap(cur, tmp);
+        }
         CUDA_TRY(cudaMemcpyAsync(S->h_out, S->r_out, sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         residual = S->h_out[0];

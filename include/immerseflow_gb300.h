@@ -76,6 +76,15 @@ typedef int ifx_status;
 #define IFX_FIELD_XC       8  /* cell centres x, nx                             */
 #define IFX_FIELD_YC       9  /* cell centres y, ny                             */
 
+/* Pressure-solve method of ifx_ppe_reference (extension keyword PPE-Method).
+ * The reference parses PPE_Solver (inputs/inputs.txt:14: 1 point GS, 2 line
+ * SOR) but always runs Jacobi (src/include/PPESolver.cu:13-31), also for its
+ * own PPE_Solver = 1 inputs; PPE_Solver is therefore kept as read and this
+ * field selects, with the same numbering.  METHOD mode accepts only 0. */
+#define IFX_PPE_JACOBI   0    /* the reference's Jacobi sweep                   */
+#define IFX_PPE_POINT_GS 1    /* red-black point Gauss-Seidel / SOR (w-PPE)     */
+#define IFX_PPE_LINE_SOR 2    /* zebra x-line SOR, tridiagonal row solves (w-PPE) */
+
 #define IFX_PATH_MAX 512
 
 /* --------------------------------------------------------------- config */
@@ -107,6 +116,8 @@ typedef struct ifx_config {
     double mg_omega;               /* weighted-Jacobi factor                    */
     int    mixed_inner;            /* FP32 predictor sweeps per FP64 residual   */
     double force_ref_u, force_ref_len;   /* drag/lift normalisation          */
+    int    ppe_method;             /* IFX_PPE_*: REFERENCE-mode pressure solve  */
+    double relax_ad, relax_ppe;    /* w-AD, w-PPE as read (0 or 1: none)        */
     char   xgrid[IFX_PATH_MAX];    /* face-coordinate files (<idx> <coord>)     */
     char   ygrid[IFX_PATH_MAX];
 } ifx_config;

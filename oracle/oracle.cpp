@@ -139,10 +139,10 @@ static void ref_bc(int nx, int ny, double* u, double* v) {
 }
 
 // nsteps x ImmerseFlow::ADsolver, src/include/ADSolver.cu:268-395.
-extern "C" int orc_ref_ad_steps(int nx, int ny, const double* dx, const double* dy,
-                                const double* iblank, double dt, double re, int itermax,
-                                double tol, int nsteps, double* u, double* v, double* ut,
-                                double* vt, double* uf, double* vf, int* iters) {
+extern "C" int orc_ref_ad_steps_w(int nx, int ny, const double* dx, const double* dy,
+                                  const double* iblank, double dt, double re, int itermax,
+                                  double tol, double w_ad, int nsteps, double* u, double* v, double* ut,
+                                  double* vt, double* uf, double* vf, int* iters) {
     const int n = nx * ny;
     // calculateADCoefficients, src/include/ADSolver.cu:12-44
     std::vector<double> aP(n, 1), aW(n, 1), aE(n, 1), aS(n, 1), aN(n, 1), sx(n), sy(n);
@@ -196,6 +196,11 @@ extern "C" int orc_ref_ad_steps(int nx, int ny, const double* dx, const double* 
                     tu[id] = iblank[id] * a / aP[id];
                     double b = sy[id] + aE[id] * cv[id + 1] + aW[id] * cv[id - 1] + aN[id] * cv[id + nx] + aS[id] * cv[id - nx];
                     tv[id] = iblank[id] * b / aP[id];
+                    // under-relaxation as commented out at src/include/ADSolver.cu:95,116
+                    if (w_ad != 1.0) {
+                        tu[id] = (1.0 - w_ad) * cu[id] + w_ad * tu[id];
+                        tv[id] = (1.0 - w_ad) * cv[id] + w_ad * tv[id];
+                    }
                 }
             ref_bc(nx, ny, cu, cv);
             std::swap(cu, tu);
@@ -226,10 +231,29 @@ extern "C" int orc_ref_ad_steps(int nx, int ny, const double* dx, const double* 
     return 0;
 }
 
+extern "C" int orc_ref_ad_steps(int nx, int ny, const double* dx, const double* dy,
+                                const double* iblank, double dt, double re, int itermax,
+                                double tol, int nsteps, double* u, double* v, double* ut,
+                                double* vt, double* uf, double* vf, int* iters) {
+    return orc_ref_ad_steps_w(nx, ny, dx, dy, iblank, dt, re, itermax, tol, 1.0, nsteps, u, v, ut, vt, uf, vf, iters);
+}
+
 // PPESolver with the coefficients calculatePPECoefficients intends
-// (src/include/PPESolver.cu:13-71,73-104,137-205).
-extern "C" int orc_ref_ppe(int nx, int ny, const double* dx, const double* dy, int itermax,
-                           double tol, double* p, int* iters) {
+// (src/include/PPESolver.cu:13-71,73-104,137-205).  method 0 is its Jacobi
+// sweep; 1 and 2 are the solvers inputs/inputs.txt:14 advertises (PPE_Solver
+// 1 point GS, 2 line SOR), parsed at src/main.cu:42 but not implemented
+// there, restated here in their textbook forms:
+//  1: red-black point Gauss-Seidel, red cells ((i + j) even) first, each the
+//     Jacobi update of src/include/PPESolver.cu:21-25 from the current values,
+//     relaxed as (1 - w) p + w p_new when w != 1;
+//  2: zebra line SOR along x, odd rows (j = 1, 3, ...) first: each row solved
+//     exactly for its unknowns with the neighbouring rows fixed (Thomas
+//     algorithm, ghosts at i = 0 and nx-1 on the right-hand side), relaxed
+//     the same way.
+// The stop rule is the reference's for every method: the signed residual sum
+// over the interior after a full iteration.
+extern "C" int orc_ref_ppe_opt(int nx, int ny, const double* dx, const double* dy, int itermax,
+                               double tol, int method, double w, double* p, int* iters) {
     const int n = nx * ny;
     std::vector<double> aP(n, 1), aW(n, 1), aE(n, 1), aS(n, 1), aN(n, 1), pt(n), res(n, 0.0);
     for (int j = 1; j < ny - 1; j++)
@@ -254,15 +278,48 @@ extern "C" int orc_ref_ppe(int nx, int ny, const double* dx, const double* dy, i
     double* tmp = pt.data();
     double residual = 1.0;
     int it = 0;
+    std::vector<double> cp(nx), dp(nx);
     while (residual > tol && it < itermax) {
-        for (int id = 0; id < n; id++) tmp[id] = cur[id];
-        for (int j = 1; j < ny - 1; j++)
-            for (int i = 1; i < nx - 1; i++) {
-                int id = IDX(i, j, nx);
-                tmp[id] = -(cur[id + 1] * aE[id] + cur[id - 1] * aW[id] + cur[id + nx] * aN[id] +
-                            cur[id - nx] * aS[id]) / aP[id];
-            }
-        std::swap(cur, tmp);
+        if (method == 1) {
+            for (int colour = 0; colour < 2; colour++)
+                for (int j = 1; j < ny - 1; j++)
+                    for (int i = 1; i < nx - 1; i++) {
+                        if (((i + j) & 1) != colour) continue;
+                        int id = IDX(i, j, nx);
+                        double g = -(cur[id + 1] * aE[id] + cur[id - 1] * aW[id] + cur[id + nx] * aN[id] +
+                                     cur[id - nx] * aS[id]) / aP[id];
+                        cur[id] = w == 1.0 ? g : (1.0 - w) * cur[id] + w * g;
+                    }
+        } else if (method == 2) {
+            const int last = nx - 2;
+            for (int first = 1; first <= 2; first++)
+                for (int j = first; j <= ny - 2; j += 2) {
+                    for (int i = 1; i <= last; i++) {
+                        int id = IDX(i, j, nx);
+                        double rhs = -(aN[id] * cur[id + nx] + aS[id] * cur[id - nx]);
+                        if (i == 1) rhs -= aW[id] * cur[id - 1];
+                        if (i == last) rhs -= aE[id] * cur[id + 1];
+                        double m = i == 1 ? aP[id] : aP[id] - aW[id] * cp[i - 1];
+                        cp[i] = i == last ? 0.0 : aE[id] / m;
+                        dp[i] = i == 1 ? rhs / m : (rhs - aW[id] * dp[i - 1]) / m;
+                    }
+                    double x = 0.0;
+                    for (int i = last; i >= 1; i--) {
+                        int id = IDX(i, j, nx);
+                        x = i == last ? dp[i] : dp[i] - cp[i] * x;
+                        cur[id] = w == 1.0 ? x : (1.0 - w) * cur[id] + w * x;
+                    }
+                }
+        } else {
+            for (int id = 0; id < n; id++) tmp[id] = cur[id];
+            for (int j = 1; j < ny - 1; j++)
+                for (int i = 1; i < nx - 1; i++) {
+                    int id = IDX(i, j, nx);
+                    tmp[id] = -(cur[id + 1] * aE[id] + cur[id - 1] * aW[id] + cur[id + nx] * aN[id] +
+                                cur[id - nx] * aS[id]) / aP[id];
+                }
+            std::swap(cur, tmp);
+        }
         residual = 0.0;
         for (int j = 1; j < ny - 1; j++)
             for (int i = 1; i < nx - 1; i++) {
@@ -276,6 +333,11 @@ extern "C" int orc_ref_ppe(int nx, int ny, const double* dx, const double* dy, i
     if (cur != p) std::memcpy(p, cur, sizeof(double) * n);
     if (iters) *iters = it;
     return 0;
+}
+
+extern "C" int orc_ref_ppe(int nx, int ny, const double* dx, const double* dy, int itermax,
+                           double tol, double* p, int* iters) {
+    return orc_ref_ppe_opt(nx, ny, dx, dy, itermax, tol, 0, 1.0, p, iters);
 }
 
 // Body predicate, evaluated without FMA contraction (file built with

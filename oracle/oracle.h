@@ -53,6 +53,16 @@ int orc_ref_ad_steps(int nx, int ny, const double* dx, const double* dy,
  * stopped when the signed residual sum over the interior drops below tol. */
 int orc_ref_ppe(int nx, int ny, const double* dx, const double* dy, int itermax,
                 double tol, double* p, int* iters);
+/* The same with the solver inputs/inputs.txt:14 advertises: method 0 Jacobi,
+ * 1 red-black point Gauss-Seidel / SOR, 2 zebra x-line SOR; w = relaxation. */
+int orc_ref_ppe_opt(int nx, int ny, const double* dx, const double* dy, int itermax,
+                    double tol, int method, double w, double* p, int* iters);
+/* orc_ref_ad_steps with the Jacobi update relaxed by w_ad (1: none), the
+ * reference's commented-out lines src/include/ADSolver.cu:95,116. */
+int orc_ref_ad_steps_w(int nx, int ny, const double* dx, const double* dy,
+                       const double* iblank, double dt, double re, int itermax,
+                       double tol, double w_ad, int nsteps, double* u, double* v, double* ut,
+                       double* vt, double* uf, double* vf, int* iters);
 
 /* Bit-exact body predicate used for iBlank tagging: 1 = inside the ellipse. */
 int orc_inside(double x, double y, double cx, double cy, double c, double s,

@@ -19,6 +19,10 @@ class Oracle:
         L.orc_ref_ad_steps.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int,
                                        C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         L.orc_ref_ppe.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_double, _dp, C.POINTER(C.c_int)]
+        L.orc_ref_ppe_opt.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_double, _dp,
+                                      C.POINTER(C.c_int)]
+        L.orc_ref_ad_steps_w.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int,
+                                         C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         L.orc_inside.argtypes = [C.c_double] * 8
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(capi.Config), _dp, _dp, C.c_int]
@@ -37,7 +41,7 @@ class Oracle:
         self.lib.orc_grid(nx, ny, np.ascontiguousarray(xf), np.ascontiguousarray(yf), xc, yc, dx, dy)
         return xc, yc, dx, dy
 
-    def ref_ad(self, xf, yf, dt, re, itermax, nsteps, iblank=None):
+    def ref_ad(self, xf, yf, dt, re, itermax, nsteps, iblank=None, w_ad=1.0):
         nx, ny = len(xf) + 1, len(yf) + 1
         xc, yc, dx, dy = self.grid(nx, ny, xf, yf)
         u, v, p = np.zeros(nx * ny), np.zeros(nx * ny), np.zeros(nx * ny)
@@ -46,15 +50,16 @@ class Oracle:
         uf, vf = np.zeros((nx - 1) * (ny - 2)), np.zeros((nx - 2) * (ny - 1))
         ib = np.ones(nx * ny) if iblank is None else np.ascontiguousarray(iblank, np.float64)
         iters = np.zeros(max(1, nsteps), np.int32)
-        self.lib.orc_ref_ad_steps(nx, ny, dx, dy, ib, dt, re, itermax, 1e-6, nsteps, u, v, ut, vt, uf, vf, iters)
+        self.lib.orc_ref_ad_steps_w(nx, ny, dx, dy, ib, dt, re, itermax, 1e-6, w_ad, nsteps, u, v, ut, vt, uf, vf,
+                                    iters)
         return u.reshape(ny, nx), v.reshape(ny, nx), iters[:nsteps], uf, vf
 
-    def ref_ppe(self, xf, yf, itermax=100000, tol=1e-6):
+    def ref_ppe(self, xf, yf, itermax=100000, tol=1e-6, method=0, w=1.0):
         nx, ny = len(xf) + 1, len(yf) + 1
         _, _, dx, dy = self.grid(nx, ny, xf, yf)
         p = np.zeros(nx * ny)
         it = C.c_int(0)
-        self.lib.orc_ref_ppe(nx, ny, dx, dy, itermax, tol, p, C.byref(it))
+        self.lib.orc_ref_ppe_opt(nx, ny, dx, dy, itermax, tol, method, w, p, C.byref(it))
         return p.reshape(ny, nx), it.value
 
     # ---- method solver

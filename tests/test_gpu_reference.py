@@ -96,3 +96,52 @@ def test_interface_mirror_runs_reference_main(golden, golden_dir, tmp_path):
     lines = (tmp_path / "uc.dat").read_text().splitlines()[3:]
     u = np.array([float(l.split(",")[2]) for l in lines]).reshape(52, 52)
     assert np.abs(u - golden["uc"]).max() <= 2 * PRINT_TOL
+
+
+@pytest.mark.parametrize("method,w", [(capi.PPE_POINT_GS, 1.0), (capi.PPE_POINT_GS, 1.8), (capi.PPE_LINE_SOR, 1.0),
+                                      (capi.PPE_LINE_SOR, 1.6)])
+def test_ppe_solver_options_vs_oracle(golden_dir, oracle, method, w):
+    """PPE_Solver 1 (point GS) and 2 (line SOR) of inputs/inputs.txt:14, with
+    w-PPE relaxation: a fixed number of iterations agrees with the oracle to
+    1e-12, and the solve under the reference's stop rule to 1e-9 with the same
+    iteration count (within 2: the signed residual sum is compared to 1e-6)."""
+    c = ifx.config_read(os.path.join(golden_dir, "inputs", "inputs.txt"))
+    c.ppe_method, c.relax_ppe = method, w
+    xf = ifx.grid_read(c.xgrid.decode(), c.nx + 1)
+    yf = ifx.grid_read(c.ygrid.decode(), c.ny + 1)
+    c.ppe_itermax = 40
+    s = ifx.Solver.create(c, xf, yf)
+    assert s.ppe_reference() == 40
+    po, ito = oracle.ref_ppe(xf, yf, itermax=40, method=method, w=w)
+    assert ito == 40
+    assert np.abs(s.get(capi.FIELD_P) - po).max() <= FP_RTOL * 100.0
+    c.ppe_itermax = 100000
+    s = ifx.Solver.create(c, xf, yf)
+    it = s.ppe_reference()
+    po, ito = oracle.ref_ppe(xf, yf, method=method, w=w)
+    assert abs(it - ito) <= 2 and it < 14000
+    assert np.abs(s.get(capi.FIELD_P) - po).max() <= 1e-9
+
+
+def test_ad_relaxation_vs_oracle(golden_dir, oracle):
+    """w-AD under-relaxation (the reference's commented-out src/include/ADSolver.cu:95,116)."""
+    c = ifx.config_read(os.path.join(golden_dir, "inputs", "inputs.txt"))
+    c.relax_ad = 0.8
+    xf = ifx.grid_read(c.xgrid.decode(), c.nx + 1)
+    yf = ifx.grid_read(c.ygrid.decode(), c.ny + 1)
+    s = ifx.Solver.create(c, xf, yf)
+    s.step(5)
+    uo, vo, iters, _, _ = oracle.ref_ad(xf, yf, 1e-3, 150.0, 25, 5, w_ad=0.8)
+    assert np.abs(s.get(capi.FIELD_U) - uo).max() <= FP_RTOL * np.abs(uo).max()
+    assert np.abs(s.get(capi.FIELD_V) - vo).max() <= FP_RTOL * max(np.abs(vo).max(), 1.0)
+    assert s.stats().ad_iters_total == int(iters.sum())
+
+
+def test_method_mode_rejects_reference_ppe_options():
+    from immerseflow_gb300 import cases
+
+    cfg, xf, yf = cases.cavity(n=32)
+    cfg.ppe_method = capi.PPE_LINE_SOR
+    with pytest.raises(ifx.IFXError) as e:
+        ifx.Solver.create(cfg, xf, yf)
+    assert e.value.status == capi.IFX_ERR_ARG

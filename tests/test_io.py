@@ -99,6 +99,25 @@ def test_malformed_inputs_are_parse_errors(tmp_path, bad):
     assert e.value.status == capi.IFX_ERR_PARSE
 
 
+def test_relaxation_factors_and_ppe_method(golden_dir, tmp_path):
+    """w-AD / w-PPE are ints in the reference (src/header/globalVariables.cuh:26):
+    kept as ints, and as read in relax_ad / relax_ppe; PPE-Method selects the
+    solver the PPE_Solver column names (1 point GS, 2 line SOR)."""
+    src = open(os.path.join(golden_dir, "inputs", "inputs.txt")).read()
+    c = ifx.config_read(os.path.join(golden_dir, "inputs", "inputs.txt"))
+    assert (c.relax_ad, c.relax_ppe, c.ppe_method) == (1.0, 1.0, capi.PPE_JACOBI)
+    p = tmp_path / "inputs.txt"
+    p.write_text(src.replace("1       1       25          100000          1         1",
+                             "0.8     1.5     25          100000          1         2") + "PPE-Method\nline-sor\n")
+    c = ifx.config_read(str(p))
+    assert (c.w_ad, c.w_ppe, c.relax_ad, c.relax_ppe) == (0, 1, 0.8, 1.5)
+    assert (c.ppe_solver, c.ppe_method) == (2, capi.PPE_LINE_SOR)
+    p.write_text(src + "PPE-Method\nmultigrid\n")
+    with pytest.raises(ifx.IFXError) as e:
+        ifx.config_read(str(p))
+    assert e.value.status == capi.IFX_ERR_PARSE
+
+
 def test_missing_inputs_is_io_error(tmp_path):
     with pytest.raises(ifx.IFXError) as e:
         ifx.config_read(str(tmp_path / "nope.txt"))
