@@ -915,6 +915,15 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// True when the tile's instance is still solving.  The state is indexed by
+// the tile's own instance (not the level's), and the test also reads the
+// level's first field (NX, never negative), so the two loads are in flight
+// together instead of one after the other.
+__device__ __forceinline__ bool tile_live(const Tile& t, const LevelDev& L, const InstState* __restrict__ S) {
+    const int state = S[t.inst].ppe_state, nx = L.NX;
+    return (state == ST_ACTIVE) & (nx >= 0);
+}
+
 // Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
 template <typename T, int R = 1>
 __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
@@ -922,12 +931,12 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
                                          const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& L = LV[t.lev];
-    if (S[L.inst].ppe_state != ST_ACTIVE) return;
+    if (!tile_live(t, L, S)) return;
     const T* src = (const T*)(src_alt ? L.e2 : L.e);
     T* dst = (T*)(src_alt ? L.e : L.e2);
     const T* rr = (const T*)L.r;
-    const T om = (T)I[L.inst].omega;
-    const int* gidx = L.depth == 0 ? I[L.inst].gidx : nullptr;
+    const T om = (T)I[t.inst].omega;
+    const int* gidx = L.depth == 0 ? I[t.inst].gidx : nullptr;
     const int P = L.pitch;
     const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
     const int ic = clampi(i, 1, L.NX);
@@ -969,11 +978,11 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     __shared__ T rows[R][TILE_Y][TILE_X];
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
-    if (S[F.inst].ppe_state != ST_ACTIVE) return;
+    if (!tile_live(t, F, S)) return;
     const LevelDev& C = LV[F.child];
     const T* fe = (const T*)(fine_alt ? F.e2 : F.e);
     const T* fr = (const T*)F.r;
-    const int* gidx = F.depth == 0 ? I[F.inst].gidx : nullptr;
+    const int* gidx = F.depth == 0 ? I[t.inst].gidx : nullptr;
     const int FP = F.pitch, cx = C.cx, cy = C.cy;
     const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
     const int i = t.i0 + lane;
@@ -1017,7 +1026,7 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     }
     if ((cx == 2 && (lane & 1)) || (cy == 2 && (w & 1))) return;
     T* rc = (T*)C.r;
-    const T om = (T)I[F.inst].omega;
+    const T om = (T)I[t.inst].omega;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (!in[r]) continue;
@@ -1057,7 +1066,7 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
                                           const InstState* __restrict__ S, int fine_alt, int coarse_alt, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
-    if (S[F.inst].ppe_state != ST_ACTIVE) return;
+    if (!tile_live(t, F, S)) return;
     const LevelDev& C = LV[F.child];
     // the coarsest level's solution is always in e; a middle level's in the buffer its sweeps ended on
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
@@ -1103,12 +1112,12 @@ __device__ __forceinline__ void b_prolong_post2(const Tile* __restrict__ tiles, 
     __shared__ uint8_t bs[PP_N];
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
-    if (S[F.inst].ppe_state != ST_ACTIVE) return;
+    if (!tile_live(t, F, S)) return;
     const LevelDev& C = LV[F.child];
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
     T* fe = (T*)(fine_alt ? F.e2 : F.e);
     const T* fr = (const T*)F.r;
-    const T om = (T)I[F.inst].omega;
+    const T om = (T)I[t.inst].omega;
     const int P = F.pitch, CP = C.pitch, ib = t.i0 - 2, jb = t.j0 - 2;
     const uint8_t* cbits = C.bits;
     auto fce = [ce, CP](int I0, int J0) { return ce[I0 + J0 * CP]; };
