@@ -387,8 +387,8 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
     if ((int)vb < ntiles) {
         const Tile t = ldg_struct(&tiles[vb]);
         const InstDev& in = I[t.inst];
-        const int st = S[t.inst].pred_state;
-        if (st == ST_DONE) return;
+        const int st = S[t.inst].pred_state, nxi = in.NX;  // loads in flight together
+        if ((st == ST_DONE) | (nxi < 0)) return;
         const double* su = parity ? in.u2 : in.u;
         const double* sv = parity ? in.v2 : in.v;
         double* du = parity ? in.u : in.u2;
@@ -558,8 +558,8 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
     if ((int)vb < ntiles) {
         const Tile t = ldg_struct(&tiles[vb]);
         const InstDev& in = I[t.inst];
-        const int st = S[t.inst].pred_state;
-        if (st == ST_DONE) return;
+        const int st = S[t.inst].pred_state, nxi = in.NX;  // loads in flight together
+        if ((st == ST_DONE) | (nxi < 0)) return;
         const float* su = parity ? in.du2 : in.du;
         const float* sv = parity ? in.dv2 : in.dv;
         float* du = parity ? in.du : in.du2;
@@ -697,6 +697,21 @@ __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, 
 // correction": convergence is only accepted on the true residual).  Dot
 // products are accumulated in FP64 in both paths.
 
+// True when the tile's instance is still solving.  The state is indexed by
+// the tile's own instance (not the level's), and the test also reads the
+// level's first field (NX, never negative), so the two loads are in flight
+// together instead of one after the other.
+__device__ __forceinline__ bool tile_live(const Tile& t, const LevelDev& L, const InstState* __restrict__ S) {
+    const int state = S[t.inst].ppe_state, nx = L.NX;
+    return (state == ST_ACTIVE) & (nx >= 0);
+}
+// The same for a finest-level tile, also touching the instance's fields.
+__device__ __forceinline__ bool tile_live0(const Tile& t, const LevelDev& L, const InstDev& in,
+                                           const InstState* __restrict__ S) {
+    const int state = S[t.inst].ppe_state, nx = L.NX, nxi = in.NX;
+    return (state == ST_ACTIVE) & (nx >= 0) & (nxi >= 0);
+}
+
 // r = (b - mean b) - L p in FP64, rh = r, p_dir = v = 0.  restart_only: only
 // the instances whose mixed-path restart is due.
 // partials: 0 (r,r)  1 (b,b)  2 (rh,r)  3 (p,area)
@@ -708,9 +723,9 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
     if (restart_only && !st.restart) return;
-    const LevelDev& L = LV[in.lev0];
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -797,8 +812,8 @@ __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const L
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -819,8 +834,8 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
     T* zo = (T*)(which == 0 ? in.kph : in.ksh);
     T* y = (T*)(which == 0 ? in.kv : in.kt);
@@ -866,8 +881,8 @@ __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const L
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -886,8 +901,8 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     const InstState& st = S[t.inst];
-    if (st.ppe_state != ST_ACTIVE) return;
-    const LevelDev& L = LV[in.lev0];
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
@@ -914,15 +929,6 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
 // depend on R.
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
-// True when the tile's instance is still solving.  The state is indexed by
-// the tile's own instance (not the level's), and the test also reads the
-// level's first field (NX, never negative), so the two loads are in flight
-// together instead of one after the other.
-__device__ __forceinline__ bool tile_live(const Tile& t, const LevelDev& L, const InstState* __restrict__ S) {
-    const int state = S[t.inst].ppe_state, nx = L.NX;
-    return (state == ST_ACTIVE) & (nx >= 0);
-}
 
 // Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
 template <typename T, int R = 1>
