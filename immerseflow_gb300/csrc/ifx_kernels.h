@@ -27,7 +27,8 @@ cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* par
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, cudaStream_t s);
+                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, int ninst,
+                              cudaStream_t s);
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
                                  int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 template <typename T>

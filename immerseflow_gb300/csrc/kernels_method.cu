@@ -58,13 +58,53 @@ __global__ void k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __rest
                            double* __restrict__ part, int to_final) { b_face_rhs(tiles, I, part, to_final, blockIdx.x); }
 __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part) { b_rhs_reduce(I, S, part, blockIdx.x); }
+// restart_only: for a chunk of blockDim instances at a time, every block forms
+// the exclusive prefix sum of the finest-level tile counts of the instances
+// whose restart is due (others count 0; each instance's tiles are contiguous
+// in the list), and the grid strides over the concatenated due tiles: the pass
+// costs in proportion to the tiles restarting, spread over the whole grid.
 template <typename T>
 __global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only,
-                             const LoopCtl* ctl, int nt) {
-    if (restart_only && none_due(ctl)) return;
-    for (int vb = blockIdx.x; vb < nt; vb += gridDim.x) b_bicg_start<T>(tiles, LV, I, S, G, part, restart_only, vb);
+                             const LoopCtl* ctl, int nt, int ninst) {
+    if (!restart_only) {
+        for (int vb = blockIdx.x; vb < nt; vb += gridDim.x) b_bicg_start<T>(tiles, LV, I, S, G, part, 0, vb);
+        return;
+    }
+    if (none_due(ctl)) return;
+    __shared__ int dbeg[TILE_THREADS], doff[TILE_THREADS + 1], wtot[TILE_THREADS / 32];
+    const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+    for (int k0 = 0; k0 < ninst; k0 += blockDim.x) {
+        const int k = k0 + (int)threadIdx.x;
+        const bool d = k < ninst && S[k].ppe_state == ST_ACTIVE && S[k].restart;
+        const int cnt = d ? I[k].tile_cnt : 0;
+        int inc = cnt;  // inclusive scan within the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wtot[w] = inc;
+        __syncthreads();
+        int base = 0;
+        for (int q = 0; q < w; q++) base += wtot[q];
+        dbeg[threadIdx.x] = d ? I[k].tile_beg : 0;
+        doff[threadIdx.x] = base + inc - cnt;
+        if ((int)threadIdx.x == (int)blockDim.x - 1) doff[blockDim.x] = base + inc;
+        __syncthreads();
+        const int total = doff[blockDim.x];
+        for (int v = blockIdx.x; v < total; v += gridDim.x) {
+            int lo = 0, hi = (int)blockDim.x;  // last entry with doff <= v
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (doff[mid] <= v) lo = mid;
+                else hi = mid;
+            }
+            b_bicg_start<T>(tiles, LV, I, S, G, part, 1, dbeg[lo] + (v - doff[lo]));
+        }
+        __syncthreads();
+    }
 }
 __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                 const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
@@ -176,9 +216,10 @@ cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part
 }
 template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, cudaStream_t s) {
+                              const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, int ninst,
+                              cudaStream_t s) {
     const int grid = restart_only && nt > OPT_GRID ? OPT_GRID : nt;
-    k_bicg_start<T><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt);
+    k_bicg_start<T><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt, ninst);
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
@@ -311,9 +352,9 @@ template cudaError_t subcycle_smem_limit<double>(int);
 template cudaError_t subcycle_smem_limit<float>(int);
 
 template cudaError_t launch_bicg_start<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                               const GhostDev*, double*, int, const LoopCtl*, cudaStream_t);
+                                               const GhostDev*, double*, int, const LoopCtl*, int, cudaStream_t);
 template cudaError_t launch_bicg_start<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
-                                              const GhostDev*, double*, int, const LoopCtl*, cudaStream_t);
+                                              const GhostDev*, double*, int, const LoopCtl*, int, cudaStream_t);
 template cudaError_t launch_bicg_x<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
                                            cudaStream_t);
 template cudaError_t launch_bicg_x<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,

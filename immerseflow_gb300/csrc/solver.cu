@@ -999,7 +999,7 @@ void seq_mid(Seq& q) {
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
     q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
-    q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, nullptr, st));
+    q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, nullptr, n, st));
     q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st));
 }
 
@@ -1011,7 +1011,7 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     const int n = (int)S->inst.size();
     if (mixed_of<T>()) {
         // FP64 true residual and restart for the instances whose FP32 recursion ran its course
-        q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, st));
+        q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, n, st));
         q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st));
     }
     q.add(launch_bicg_p<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
