@@ -833,7 +833,6 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
                                              int which, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
-    const InstState& st = S[t.inst];
     const LevelDev& L = LV[t.lev];  // finest-level tiles
     if (!tile_live0(t, L, in, S)) return;
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
