@@ -31,20 +31,21 @@ cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const I
                               cudaStream_t s);
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
                                  int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
+// Finest-level Krylov phases take rows = 1 (32x8 tiles) or MG_ROWS_WIDE (32x32 tiles).
 template <typename T>
 cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          cudaStream_t s);
+                          int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int e_alt, int which, cudaStream_t s);
+                              const GhostDev* G, double* part, int e_alt, int which, int rows, cudaStream_t s);
 cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
                                cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          cudaStream_t s);
+                          int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          double* part, cudaStream_t s);
+                          double* part, int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s);

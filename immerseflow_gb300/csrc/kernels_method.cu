@@ -109,22 +109,22 @@ __global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __r
 __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                 const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
                                 unsigned long long handle) { b_bicg_reduce_r(I, S, part, start, mixed, ctl, handle, blockIdx.x); }
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T>(tiles, LV, I, S, blockIdx.x); }
-template <typename T>
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T, R>(tiles, LV, I, S, blockIdx.x); }
+template <typename T, int R>
 __global__ void k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) { b_bicg_apply<T>(tiles, LV, I, S, G, part, e_alt, which, blockIdx.x); }
+                             const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) { b_bicg_apply<T, R>(tiles, LV, I, S, G, part, e_alt, which, blockIdx.x); }
 __global__ void k_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int which) { b_bicg_scalar(I, S, part, which, blockIdx.x); }
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                         const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_s<T>(tiles, LV, I, S, blockIdx.x); }
-template <typename T>
+                         const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_s<T, R>(tiles, LV, I, S, blockIdx.x); }
+template <typename T, int R>
 __global__ void k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                         double* __restrict__ part) { b_bicg_x<T>(tiles, LV, I, S, part, blockIdx.x); }
+                         double* __restrict__ part) { b_bicg_x<T, R>(tiles, LV, I, S, part, blockIdx.x); }
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
@@ -227,16 +227,19 @@ cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* p
     k_bicg_reduce_r<<<ninst, 256, 0, s>>>(I, S, part, start, mixed, ctl, handle);
     return cudaGetLastError();
 }
+// Finest-level Krylov phases: rows = 1 on 32x8 tiles, MG_ROWS_WIDE on 32x32 tiles.
 template <typename T>
 cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          cudaStream_t s) {
-    k_bicg_p<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+                          int rows, cudaStream_t s) {
+    if (rows == MG_ROWS_WIDE) k_bicg_p<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+    else k_bicg_p<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                              const GhostDev* G, double* part, int e_alt, int which, cudaStream_t s) {
-    k_bicg_apply<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
+                              const GhostDev* G, double* part, int e_alt, int which, int rows, cudaStream_t s) {
+    if (rows == MG_ROWS_WIDE) k_bicg_apply<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
+    else k_bicg_apply<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
@@ -246,14 +249,16 @@ cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* par
 }
 template <typename T>
 cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          cudaStream_t s) {
-    k_bicg_s<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+                          int rows, cudaStream_t s) {
+    if (rows == MG_ROWS_WIDE) k_bicg_s<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
+    else k_bicg_s<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
     return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                          double* part, cudaStream_t s) {
-    k_bicg_x<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
+                          double* part, int rows, cudaStream_t s) {
+    if (rows == MG_ROWS_WIDE) k_bicg_x<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
+    else k_bicg_x<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, part);
     return cudaGetLastError();
 }
 template <typename T>
@@ -330,14 +335,14 @@ cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_
     return cudaGetLastError();
 }
 
-template cudaError_t launch_bicg_p<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
-template cudaError_t launch_bicg_s<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
-template cudaError_t launch_bicg_apply<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
+template cudaError_t launch_bicg_p<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, int, cudaStream_t);
+template cudaError_t launch_bicg_s<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, int, cudaStream_t);
+template cudaError_t launch_bicg_apply<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, int, cudaStream_t);
 template cudaError_t launch_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, int, cudaStream_t);
 template cudaError_t launch_restrict<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
-template cudaError_t launch_bicg_p<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
-template cudaError_t launch_bicg_s<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, cudaStream_t);
-template cudaError_t launch_bicg_apply<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, cudaStream_t);
+template cudaError_t launch_bicg_p<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, int, cudaStream_t);
+template cudaError_t launch_bicg_s<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, int, cudaStream_t);
+template cudaError_t launch_bicg_apply<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, double*, int, int, int, cudaStream_t);
 template cudaError_t launch_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, int, cudaStream_t);
 template cudaError_t launch_restrict<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, const GhostDev*, int, int, cudaStream_t);
 template cudaError_t launch_prolong<double>(const Tile*, int, const LevelDev*, const InstState*, int, int, int,
@@ -356,8 +361,8 @@ template cudaError_t launch_bicg_start<double>(const Tile*, int, const LevelDev*
 template cudaError_t launch_bicg_start<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
                                               const GhostDev*, double*, int, const LoopCtl*, int, cudaStream_t);
 template cudaError_t launch_bicg_x<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
-                                           cudaStream_t);
+                                           int, cudaStream_t);
 template cudaError_t launch_bicg_x<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*, double*,
-                                          cudaStream_t);
+                                          int, cudaStream_t);
 
 }  // namespace ifx

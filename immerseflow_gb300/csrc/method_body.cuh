@@ -683,6 +683,8 @@ __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, Inst
 // preconditioned by one multigrid V-cycle in T.  Per-instance scalars live
 // in InstState; every reduction is per instance over its tiles, fixed order.
 
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
 __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, uint8_t& bt) {
     if (i < 1 || i > L.NX || j < 1 || j > L.NY) return false;
     id = i + j * L.pitch;
@@ -805,8 +807,53 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
     if (threadIdx.x == 0 && start != 2) loop_vote(ctl, active, handle, due);
 }
 
+// Finest-level Krylov tiles: 32 columns by 8R rows; thread (w, lane) handles
+// column i0+lane of rows j0+w+8r.  Loads use indices clamped into the level's
+// interior so that they issue together; stores are for live cells only.  A
+// tile of R > 1 rows writes the partial sums of each of its 32x8 sub-tiles,
+// formed by the same block reduction over the same threads as a 32x8 tile,
+// into that sub-tile's slot: results do not depend on R.
+template <int R>
+struct Rows0 {
+    int ic, id[R], jc[R];
+    uint8_t bt[R];
+    bool in_i;
+};
+template <int R>
+__device__ __forceinline__ void rows0(const LevelDev& L, const Tile& t, Rows0<R>& q) {
+    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    q.ic = clampi(i, 1, L.NX);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = jb + 8 * r;
+        q.jc[r] = clampi(j, 1, L.NY);
+        q.id[r] = q.ic + q.jc[r] * L.pitch;
+        q.bt[r] = (i == q.ic && j == q.jc[r]) ? __ldg(&L.bits[q.id[r]]) : (uint8_t)0;
+    }
+}
+// Slot of the partial sums of 32x8 sub-tile r of finest-level tile t: its
+// index in the instance's list of 32x8 tiles (rows of tiles outer); ok is
+// false below the level's last row of tiles.
+__device__ __forceinline__ size_t sub_slot(const InstDev& in, const LevelDev& L, const Tile& t, int r, bool& ok) {
+    const int ntx = (L.nx + TILE_X - 1) / TILE_X, nty = (L.ny + TILE_Y - 1) / TILE_Y, row = t.j0 / TILE_Y + r;
+    ok = row < nty;
+    return (size_t)in.tile_beg + (size_t)row * ntx + t.i0 / TILE_X;
+}
+template <int NV, typename RT, int R>
+__device__ __forceinline__ void write_sub_partials(const InstDev& in, const LevelDev& L, const Tile& t,
+                                                   double (&acc)[R][NV], double* __restrict__ part) {
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        __shared__ double out[NV];
+        block_sum<NV, RT>(acc[r], out);
+        bool ok;
+        const size_t q = sub_slot(in, L, t, r, ok);
+        if (ok && threadIdx.x < NV) part[q * NPART + threadIdx.x] = out[threadIdx.x];
+    }
+}
+
 // p_dir = r + beta (p_dir - omega v); preconditioner input.
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
@@ -814,19 +861,24 @@ __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const L
     const InstState& st = S[t.inst];
     const LevelDev& L = LV[t.lev];  // finest-level tiles
     if (!tile_live0(t, L, in, S)) return;
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    if (!live0(L, i, j, id, bt)) return;
+    Rows0<R> q;
+    rows0<R>(L, t, q);
     T* kp = (T*)in.kp;
-    const T pd = ((const T*)in.kr)[id] + (T)st.beta * (kp[id] - (T)st.omega * ((const T*)in.kv)[id]);
-    kp[id] = pd;
-    ((T*)L.r)[id] = pd;
+    const T beta = (T)st.beta, om = (T)st.omega;
+    T pd[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) pd[r] = ((const T*)in.kr)[q.id[r]] + beta * (kp[q.id[r]] - om * ((const T*)in.kv)[q.id[r]]);
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (q.bt[r] & 0x0F) {
+            kp[q.id[r]] = pd[r];
+            ((T*)L.r)[q.id[r]] = pd[r];
+        }
 }
 
 // y = L z with z the preconditioned vector (V-cycle result), operator and z
 // in T; z is kept as zo.  partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt,
@@ -838,25 +890,28 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
     const T* z = (const T*)(e_alt ? L.e2 : L.e);
     T* zo = (T*)(which == 0 ? in.kph : in.ksh);
     T* y = (T*)(which == 0 ? in.kv : in.kt);
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    double acc[2] = {0.0, 0.0};
-    if (live0(L, i, j, id, bt)) {
+    const T* w2 = (const T*)(which == 0 ? in.krh : in.ks);
+    Rows0<R> q;
+    rows0<R>(L, t, q);
+    double acc[R][2];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
         T Lz, D;
-        lap<T, T, true>(L, z, i, j, id, bt, G, in.gidx, Lz, D);
-        zo[id] = z[id];
-        y[id] = Lz;
-        if (which == 0) {
-            acc[0] = (double)((const T*)in.krh)[id] * (double)Lz;
-        } else {
-            acc[0] = (double)Lz * (double)((const T*)in.ks)[id];
-            acc[1] = (double)Lz * (double)Lz;
+        lap_p<T, T, true>(L, z, q.ic, q.jc[r], q.id[r], L.pitch, q.bt[r], G, in.gidx, Lz, D);
+        const T zc = z[q.id[r]], wv = w2[q.id[r]];
+        acc[r][0] = acc[r][1] = 0.0;
+        if (q.bt[r] & 0x0F) {
+            zo[q.id[r]] = zc;
+            y[q.id[r]] = Lz;
+            if (which == 0) {
+                acc[r][0] = (double)wv * (double)Lz;
+            } else {
+                acc[r][0] = (double)Lz * (double)wv;
+                acc[r][1] = (double)Lz * (double)Lz;
+            }
         }
     }
-    __shared__ double out[2];
-    block_sum<2, T>(acc, out);
-    if (threadIdx.x < 2) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
+    write_sub_partials<2, T, R>(in, L, t, acc, part);
 }
 
 // alpha = rho / (rh, v)   (which = 0)   or   omega = (t, s) / (t, t)   (which = 1)
@@ -874,7 +929,7 @@ __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, Ins
 }
 
 // s = r - alpha v; preconditioner input.
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                          const InstDev* __restrict__ I, const InstState* __restrict__ S, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
@@ -882,18 +937,23 @@ __device__ __forceinline__ void b_bicg_s(const Tile* __restrict__ tiles, const L
     const InstState& st = S[t.inst];
     const LevelDev& L = LV[t.lev];  // finest-level tiles
     if (!tile_live0(t, L, in, S)) return;
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    if (!live0(L, i, j, id, bt)) return;
-    const T sv = ((const T*)in.kr)[id] - (T)st.alpha * ((const T*)in.kv)[id];
-    ((T*)in.ks)[id] = sv;
-    ((T*)L.r)[id] = sv;
+    Rows0<R> q;
+    rows0<R>(L, t, q);
+    const T alpha = (T)st.alpha;
+    T sv[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) sv[r] = ((const T*)in.kr)[q.id[r]] - alpha * ((const T*)in.kv)[q.id[r]];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (q.bt[r] & 0x0F) {
+            ((T*)in.ks)[q.id[r]] = sv[r];
+            ((T*)L.r)[q.id[r]] = sv[r];
+        }
 }
 
 // p += alpha ph + omega sh (FP64) ; r = s - omega t (T).
 // partials: 0 (r,r)  1 unused  2 (rh,r)  3 (p,area)
-template <typename T>
+template <typename T, int R = 1>
 __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                          double* __restrict__ part, int vb) {
@@ -902,22 +962,28 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
     const InstState& st = S[t.inst];
     const LevelDev& L = LV[t.lev];  // finest-level tiles
     if (!tile_live0(t, L, in, S)) return;
-    int i, j, id;
-    uint8_t bt;
-    tile_ij(t, i, j);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    if (live0(L, i, j, id, bt)) {
-        const double pn = in.p[id] + st.alpha * (double)((const T*)in.kph)[id] + st.omega * (double)((const T*)in.ksh)[id];
-        in.p[id] = pn;
-        const T r = ((const T*)in.ks)[id] - (T)st.omega * ((const T*)in.kt)[id];
-        ((T*)in.kr)[id] = r;
-        acc[0] = (double)r * (double)r;
-        acc[2] = (double)((const T*)in.krh)[id] * (double)r;
-        acc[3] = pn * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
+    Rows0<R> q;
+    rows0<R>(L, t, q);
+    const double alpha = st.alpha, omega = st.omega;
+    const double dxi = __ldg(&in.dx[q.ic]);
+    double acc[R][4];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int id = q.id[r];
+        const double pn = in.p[id] + alpha * (double)((const T*)in.kph)[id] + omega * (double)((const T*)in.ksh)[id];
+        const T rv = ((const T*)in.ks)[id] - (T)omega * ((const T*)in.kt)[id];
+        const T rh = ((const T*)in.krh)[id];
+        const double dyj = __ldg(&in.dy[q.jc[r]]);
+        acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = 0.0;
+        if (q.bt[r] & 0x0F) {
+            in.p[id] = pn;
+            ((T*)in.kr)[id] = rv;
+            acc[r][0] = (double)rv * (double)rv;
+            acc[r][2] = (double)rh * (double)rv;
+            acc[r][3] = pn * (dxi * dyj);
+        }
     }
-    __shared__ double out[4];
-    block_sum<4, T>(acc, out);
-    if (threadIdx.x < 4) part[(size_t)vb * NPART + threadIdx.x] = out[threadIdx.x];
+    write_sub_partials<4, T, R>(in, L, t, acc, part);
 }
 
 // Multigrid tile phases.  A tile is 32 columns by 8R rows of one level of
@@ -926,8 +992,6 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
 // of a thread's loads issue together (no load waits on the stencil byte);
 // results are stored for live cells only.  The arithmetic per cell does not
 // depend on R.
-
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
 template <typename T, int R = 1>

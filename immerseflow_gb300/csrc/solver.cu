@@ -1009,20 +1009,24 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
+    // finest-level Krylov phases on the multigrid tile shape
+    const int R = S->mg_rows;
+    const Tile* t0 = R == MG_ROWS_WIDE ? S->dT0W : S->dT0;
+    const int nt0 = R == MG_ROWS_WIDE ? S->nt0W : S->nt0;
     if (mixed_of<T>()) {
         // FP64 true residual and restart for the instances whose FP32 recursion ran its course
         q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, n, st));
         q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st));
     }
-    q.add(launch_bicg_p<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
+    q.add(launch_bicg_p<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
     int e1 = seq_vcycle<T>(q);
-    q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, st));
+    q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, R, st));
     q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 0, st));
-    q.add(launch_bicg_s<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, st));
+    q.add(launch_bicg_s<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
     int e2 = seq_vcycle<T>(q);
-    q.add(launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, st));
+    q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, R, st));
     q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st));
-    q.add(launch_bicg_x<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dPart, st));
+    q.add(launch_bicg_x<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dPart, R, st));
     q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, mixed_of<T>(), S->dCtl, h, st));
 }
 
@@ -1901,7 +1905,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
     auto one = [&]() -> cudaError_t {
         switch (kernel) {
             case 0: return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, 1, st);
-            case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, st);
+            case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, 1, st);
             case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
             case 4: return launch_barrier_bench(S->dBar, S->persist_grid, 1000, st);
             default: return launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st);
