@@ -16,10 +16,11 @@ cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, 
                               const InstState* S, double* part, int parity, cudaStream_t s);
 // Mixed path: FP32 sweep on the correction, and the FP64 refresh (stage 0:
 // absorb the correction, stage 1: defect; finalize: absorb after the loop).
+// rows: 1 on 32x8 tiles, MG_ROWS_WIDE on 32x32 tiles.
 cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng, const LevelDev* LV, const InstDev* I,
-                                const InstState* S, double* part, int parity, cudaStream_t s);
+                                const InstState* S, double* part, int parity, int rows, cudaStream_t s);
 cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
-                                int stage, int finalize, const LoopCtl* ctl, cudaStream_t s);
+                                int stage, int finalize, const LoopCtl* ctl, int rows, cudaStream_t s);
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
                                LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,

@@ -36,20 +36,22 @@ __global__ void k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __rest
 __global__ void k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              double* __restrict__ part, int parity) { b_pred_sweep(tiles, ntiles, G, ng, I, S, part, parity, blockIdx.x); }
+template <int R>
 __global__ void k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
                                const InstState* __restrict__ S, double* __restrict__ part, int parity) {
-    b_pred_sweep32(tiles, ntiles, G, ng, LV, I, S, part, parity, blockIdx.x);
+    b_pred_sweep32<R>(tiles, ntiles, G, ng, LV, I, S, part, parity, blockIdx.x);
 }
 // Optional phases (mixed path) run as grid-stride loops on a fixed grid that
 // returns at once when the last vote found nothing due.
 constexpr int OPT_GRID = 1024;
+template <int R>
 __global__ void k_pred_refresh(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const InstDev* __restrict__ I, const InstState* __restrict__ S, int stage,
                                int finalize, const LoopCtl* ctl) {
     if (!finalize && none_due(ctl)) return;
     const int nvb = ntiles + (ng + TILE_THREADS - 1) / TILE_THREADS;
-    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) b_pred_refresh(tiles, ntiles, G, ng, I, S, stage, finalize, vb);
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) b_pred_refresh<R>(tiles, ntiles, G, ng, I, S, stage, finalize, vb);
 }
 __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
@@ -190,14 +192,17 @@ cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, 
     return cudaGetLastError();
 }
 cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng, const LevelDev* LV, const InstDev* I,
-                                const InstState* S, double* part, int parity, cudaStream_t s) {
-    k_pred_sweep32<<<nt + nblk(ng, TILE_THREADS), TILE_THREADS, 0, s>>>(t, nt, G, ng, LV, I, S, part, parity);
+                                const InstState* S, double* part, int parity, int rows, cudaStream_t s) {
+    const int g = nt + nblk(ng, TILE_THREADS);
+    if (rows == MG_ROWS_WIDE) k_pred_sweep32<MG_ROWS_WIDE><<<g, TILE_THREADS, 0, s>>>(t, nt, G, ng, LV, I, S, part, parity);
+    else k_pred_sweep32<1><<<g, TILE_THREADS, 0, s>>>(t, nt, G, ng, LV, I, S, part, parity);
     return cudaGetLastError();
 }
 cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
-                                int stage, int finalize, const LoopCtl* ctl, cudaStream_t s) {
-    const int nvb = nt + nblk(ng, TILE_THREADS);
-    k_pred_refresh<<<nvb < OPT_GRID ? nvb : OPT_GRID, TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize, ctl);
+                                int stage, int finalize, const LoopCtl* ctl, int rows, cudaStream_t s) {
+    const int nvb = nt + nblk(ng, TILE_THREADS), g = nvb < OPT_GRID ? nvb : OPT_GRID;
+    if (rows == MG_ROWS_WIDE) k_pred_refresh<MG_ROWS_WIDE><<<g, TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize, ctl);
+    else k_pred_refresh<1><<<g, TILE_THREADS, 0, s>>>(t, nt, G, ng, I, S, stage, finalize, ctl);
     return cudaGetLastError();
 }
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,

@@ -268,6 +268,53 @@ __device__ __forceinline__ TC lap_diag(const LevelDev& L, int i, int j, uint8_t 
     return lap_coef<TC>(L, i, j, bt).dd;
 }
 
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Finest-level Krylov tiles: 32 columns by 8R rows; thread (w, lane) handles
+// column i0+lane of rows j0+w+8r.  Loads use indices clamped into the level's
+// interior so that they issue together; stores are for live cells only.  A
+// tile of R > 1 rows writes the partial sums of each of its 32x8 sub-tiles,
+// formed by the same block reduction over the same threads as a 32x8 tile,
+// into that sub-tile's slot: results do not depend on R.
+template <int R>
+struct Rows0 {
+    int ic, id[R], jc[R];
+    uint8_t bt[R];
+    bool in_i;
+};
+template <int R>
+__device__ __forceinline__ void rows0(const LevelDev& L, const Tile& t, Rows0<R>& q) {
+    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    q.ic = clampi(i, 1, L.NX);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = jb + 8 * r;
+        q.jc[r] = clampi(j, 1, L.NY);
+        q.id[r] = q.ic + q.jc[r] * L.pitch;
+        q.bt[r] = (i == q.ic && j == q.jc[r]) ? __ldg(&L.bits[q.id[r]]) : (uint8_t)0;
+    }
+}
+// Slot of the partial sums of 32x8 sub-tile r of finest-level tile t: its
+// index in the instance's list of 32x8 tiles (rows of tiles outer); ok is
+// false below the level's last row of tiles.
+__device__ __forceinline__ size_t sub_slot(const InstDev& in, const LevelDev& L, const Tile& t, int r, bool& ok) {
+    const int ntx = (L.nx + TILE_X - 1) / TILE_X, nty = (L.ny + TILE_Y - 1) / TILE_Y, row = t.j0 / TILE_Y + r;
+    ok = row < nty;
+    return (size_t)in.tile_beg + (size_t)row * ntx + t.i0 / TILE_X;
+}
+template <int NV, typename RT, int R>
+__device__ __forceinline__ void write_sub_partials(const InstDev& in, const LevelDev& L, const Tile& t,
+                                                   double (&acc)[R][NV], double* __restrict__ part) {
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        __shared__ double out[NV];
+        block_sum<NV, RT>(acc[r], out);
+        bool ok;
+        const size_t q = sub_slot(in, L, t, r, ok);
+        if (ok && threadIdx.x < NV) part[q * NPART + threadIdx.x] = out[threadIdx.x];
+    }
+}
+
 // ------------------------------------------------------ step bookkeeping
 
 __device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl,
@@ -491,34 +538,8 @@ __device__ __forceinline__ bool pred_refresh_due(const InstDev& in, const InstSt
 
 // stage 0: q0 += d, d = 0 ; stage 1: r0 = rhs - M q0 (cells), r0_g (ghosts).
 // finalize: q = q0 + d, d = 0 after the loop (every instance not retired).
-// vb: level-0 tiles, then ghost chunks (as b_pred_sweep).
-__device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, int ntiles,
-                                               const GhostDev* __restrict__ G, int ng,
-                                               const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                                               int stage, int finalize, int vb) {
-    int inst, cell;
-    bool fluid = false;
-    const GhostDev* gh = nullptr;
-    if ((int)vb < ntiles) {
-        const Tile t = ldg_struct(&tiles[vb]);
-        inst = t.inst;
-        const InstDev& in = I[inst];
-        int i, j;
-        tile_ij(t, i, j);
-        if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
-        cell = i + j * in.pitch;
-        if (__ldg(&in.type[cell]) != T_FLUID) return;
-        fluid = true;
-    } else {
-        const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
-        if (g >= ng) return;
-        gh = &G[g];
-        inst = gh->inst;
-        cell = gh->cell;
-    }
-    const InstDev& in = I[inst];
-    if (in.retired) return;
-    if (!finalize && !pred_refresh_due(in, S[inst])) return;
+__device__ __forceinline__ void pred_refresh_cell(const InstDev& in, int cell, const GhostDev* gh, int stage,
+                                                  int finalize) {
     if (finalize || stage == 0) {
         in.u[cell] += (double)in.du[cell];
         in.v[cell] += (double)in.dv[cell];
@@ -528,7 +549,7 @@ __device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, i
     }
     const double* u = in.u;
     const double* v = in.v;
-    if (fluid) {
+    if (!gh) {
         const int P = in.pitch, id = cell, j = cell / P, i = cell - j * P;
         const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
         const double aE = in.dtre * (__ldg(&in.kx[i]) * ixi), aW = in.dtre * (__ldg(&in.kx[i - 1]) * ixi);
@@ -548,8 +569,43 @@ __device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, i
     }
 }
 
+// vb: level-0 tiles of 32 x 8R cells, then ghost chunks (as b_pred_sweep).
+template <int R = 1>
+__device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, int ntiles,
+                                               const GhostDev* __restrict__ G, int ng,
+                                               const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                               int stage, int finalize, int vb) {
+    if ((int)vb < ntiles) {
+        const Tile t = ldg_struct(&tiles[vb]);
+        const InstDev& in = I[t.inst];
+        if (in.retired) return;
+        if (!finalize && !pred_refresh_due(in, S[t.inst])) return;
+        const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+        if (i < 1 || i > in.NX) return;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = jb + 8 * r;
+            if (j < 1 || j > in.NY) continue;
+            const int cell = i + j * in.pitch;
+            if (__ldg(&in.type[cell]) != T_FLUID) continue;
+            pred_refresh_cell(in, cell, nullptr, stage, finalize);
+        }
+    } else {
+        const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
+        if (g >= ng) return;
+        const GhostDev* gh = &G[g];
+        const InstDev& in = I[gh->inst];
+        if (in.retired) return;
+        if (!finalize && !pred_refresh_due(in, S[gh->inst])) return;
+        pred_refresh_cell(in, gh->cell, gh, stage, finalize);
+    }
+}
+
 // One FP32 sweep on the correction; parity 0 reads (du, dv), writes (du2,
-// dv2), parity 1 the reverse.  Partials as b_pred_sweep.
+// dv2), parity 1 the reverse.  Tiles of 32 x 8R cells with loads at indices
+// clamped into the interior; partials as b_pred_sweep, one per 32x8 sub-tile
+// (the same reduction as a 32x8 tile: results do not depend on R).
+template <int R = 1>
 __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, int ntiles,
                                                const GhostDev* __restrict__ G, int ng,
                                                const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
@@ -558,44 +614,56 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
     if ((int)vb < ntiles) {
         const Tile t = ldg_struct(&tiles[vb]);
         const InstDev& in = I[t.inst];
-        const int st = S[t.inst].pred_state, nxi = in.NX;  // loads in flight together
-        if ((st == ST_DONE) | (nxi < 0)) return;
+        const LevelDev& L = LV[t.lev];  // finest-level tiles
+        const int st = S[t.inst].pred_state, nxi = in.NX, nxl = L.NX;  // loads in flight together
+        if ((st == ST_DONE) | (nxi < 0) | (nxl < 0)) return;
         const float* su = parity ? in.du2 : in.du;
         const float* sv = parity ? in.dv2 : in.dv;
         float* du = parity ? in.du : in.du2;
         float* dv = parity ? in.dv : in.dv2;
-        int i, j;
-        tile_ij(t, i, j);
-        const bool ok = i >= 1 && i <= in.NX && j >= 1 && j <= in.NY;
-        const int P = in.pitch, id = i + j * P;
-        const bool fl = ok && __ldg(&in.type[id]) == T_FLUID;
+        const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+        const int ic = clampi(i, 1, in.NX), P = in.pitch;
+        int id[R], jc[R];
+        bool fl[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = jb + 8 * r;
+            jc[r] = clampi(j, 1, in.NY);
+            id[r] = ic + jc[r] * P;
+            fl[r] = i == ic && j == jc[r] && __ldg(&in.type[id[r]]) == T_FLUID;
+        }
         if (st == ST_FINAL_IN_ALT) {
-            if (fl) {
-                du[id] = su[id];
-                dv[id] = sv[id];
-            }
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                if (fl[r]) {
+                    du[id[r]] = su[id[r]];
+                    dv[id[r]] = sv[id[r]];
+                }
             return;
         }
-        double m[1] = {0.0};
-        if (fl) {
-            const LevelDev& L = LV[in.lev0];
-            const float dtre = (float)in.dtre;
-            const float ixi = __ldg(&L.ixf[i]), iyj = __ldg(&L.iyf[j]);
-            const float aE = dtre * (__ldg(&L.kxf[i]) * ixi), aW = dtre * (__ldg(&L.kxf[i - 1]) * ixi);
-            const float aN = dtre * (__ldg(&L.kyf[j]) * iyj), aS = dtre * (__ldg(&L.kyf[j - 1]) * iyj);
+        const float dtre = (float)in.dtre;
+        const float ixi = __ldg(&L.ixf[ic]);
+        const float aE = dtre * (__ldg(&L.kxf[ic]) * ixi), aW = dtre * (__ldg(&L.kxf[ic - 1]) * ixi);
+        double m[R][1];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int q = id[r];
+            const float iyj = __ldg(&L.iyf[jc[r]]);
+            const float aN = dtre * (__ldg(&L.kyf[jc[r]]) * iyj), aS = dtre * (__ldg(&L.kyf[jc[r] - 1]) * iyj);
             const float aP = 1.0f + aE + aW + aN + aS;
             const float di = rcpa(aP);
-            const float dU = (in.rfu[id] + aE * su[id + 1] + aW * su[id - 1] + aN * su[id + P] + aS * su[id - P] -
-                              aP * su[id]) * di;
-            const float dV = (in.rfv[id] + aE * sv[id + 1] + aW * sv[id - 1] + aN * sv[id + P] + aS * sv[id - P] -
-                              aP * sv[id]) * di;
-            du[id] = su[id] + dU;
-            dv[id] = sv[id] + dV;
-            m[0] = (double)fabsf(dU) + (double)fabsf(dV);
+            const float dU = (in.rfu[q] + aE * su[q + 1] + aW * su[q - 1] + aN * su[q + P] + aS * su[q - P] -
+                              aP * su[q]) * di;
+            const float dV = (in.rfv[q] + aE * sv[q + 1] + aW * sv[q - 1] + aN * sv[q + P] + aS * sv[q - P] -
+                              aP * sv[q]) * di;
+            m[r][0] = 0.0;
+            if (fl[r]) {
+                du[q] = su[q] + dU;
+                dv[q] = sv[q] + dV;
+                m[r][0] = (double)fabsf(dU) + (double)fabsf(dV);
+            }
         }
-        __shared__ double out[1];
-        block_sum<1, float>(m, out);
-        if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
+        write_sub_partials<1, float, R>(in, L, t, m, part);
     } else {
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
@@ -682,8 +750,6 @@ __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, Inst
 // BiCGSTAB in FP64 on L p = b (ghost-eliminated finest-level operator),
 // preconditioned by one multigrid V-cycle in T.  Per-instance scalars live
 // in InstState; every reduction is per instance over its tiles, fixed order.
-
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 __device__ __forceinline__ bool live0(const LevelDev& L, int i, int j, int& id, uint8_t& bt) {
     if (i < 1 || i > L.NX || j < 1 || j > L.NY) return false;
@@ -805,51 +871,6 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
         }
     }
     if (threadIdx.x == 0 && start != 2) loop_vote(ctl, active, handle, due);
-}
-
-// Finest-level Krylov tiles: 32 columns by 8R rows; thread (w, lane) handles
-// column i0+lane of rows j0+w+8r.  Loads use indices clamped into the level's
-// interior so that they issue together; stores are for live cells only.  A
-// tile of R > 1 rows writes the partial sums of each of its 32x8 sub-tiles,
-// formed by the same block reduction over the same threads as a 32x8 tile,
-// into that sub-tile's slot: results do not depend on R.
-template <int R>
-struct Rows0 {
-    int ic, id[R], jc[R];
-    uint8_t bt[R];
-    bool in_i;
-};
-template <int R>
-__device__ __forceinline__ void rows0(const LevelDev& L, const Tile& t, Rows0<R>& q) {
-    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
-    q.ic = clampi(i, 1, L.NX);
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int j = jb + 8 * r;
-        q.jc[r] = clampi(j, 1, L.NY);
-        q.id[r] = q.ic + q.jc[r] * L.pitch;
-        q.bt[r] = (i == q.ic && j == q.jc[r]) ? __ldg(&L.bits[q.id[r]]) : (uint8_t)0;
-    }
-}
-// Slot of the partial sums of 32x8 sub-tile r of finest-level tile t: its
-// index in the instance's list of 32x8 tiles (rows of tiles outer); ok is
-// false below the level's last row of tiles.
-__device__ __forceinline__ size_t sub_slot(const InstDev& in, const LevelDev& L, const Tile& t, int r, bool& ok) {
-    const int ntx = (L.nx + TILE_X - 1) / TILE_X, nty = (L.ny + TILE_Y - 1) / TILE_Y, row = t.j0 / TILE_Y + r;
-    ok = row < nty;
-    return (size_t)in.tile_beg + (size_t)row * ntx + t.i0 / TILE_X;
-}
-template <int NV, typename RT, int R>
-__device__ __forceinline__ void write_sub_partials(const InstDev& in, const LevelDev& L, const Tile& t,
-                                                   double (&acc)[R][NV], double* __restrict__ part) {
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-        __shared__ double out[NV];
-        block_sum<NV, RT>(acc[r], out);
-        bool ok;
-        const size_t q = sub_slot(in, L, t, r, ok);
-        if (ok && threadIdx.x < NV) part[q * NPART + threadIdx.x] = out[threadIdx.x];
-    }
 }
 
 // p_dir = r + beta (p_dir - omega v); preconditioner input.

@@ -975,10 +975,14 @@ void seq_pred_body(Seq& q, unsigned long long h) {
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
     if (mixed_of<T>()) {
-        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, S->dCtl, st));
-        q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, S->dCtl, st));
+        // on the multigrid tile shape
+        const int R = S->mg_rows;
+        const Tile* t0 = R == MG_ROWS_WIDE ? S->dT0W : S->dT0;
+        const int nt0 = R == MG_ROWS_WIDE ? S->nt0W : S->nt0;
+        q.add(launch_pred_refresh(t0, nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, S->dCtl, R, st));
+        q.add(launch_pred_refresh(t0, nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, S->dCtl, R, st));
         for (int par = 0; par < 2; par++) {
-            q.add(launch_pred_sweep32(S->dT0, S->nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, st));
+            q.add(launch_pred_sweep32(t0, nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, R, st));
             q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st));
         }
         return;
@@ -994,7 +998,10 @@ void seq_mid(Seq& q) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
-    if (mixed_of<T>()) q.add(launch_pred_refresh(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 1, nullptr, st));
+    if (mixed_of<T>())
+        q.add(launch_pred_refresh(S->mg_rows == MG_ROWS_WIDE ? S->dT0W : S->dT0,
+                                  S->mg_rows == MG_ROWS_WIDE ? S->nt0W : S->nt0, S->dG, S->ng, S->dI, S->dS, 0, 1,
+                                  nullptr, S->mg_rows, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
