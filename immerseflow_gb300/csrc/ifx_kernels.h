@@ -39,6 +39,10 @@ cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstD
 template <typename T>
 cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                               const GhostDev* G, double* part, int e_alt, int which, int rows, cudaStream_t s);
+// Direction update (which 0: p_dir, 1: s) fused with the first V-cycle sweep.
+template <typename T>
+cudaError_t launch_bicg_dir_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                                   const GhostDev* G, int which, int rows, cudaStream_t s);
 cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
                                cudaStream_t s);
 template <typename T>

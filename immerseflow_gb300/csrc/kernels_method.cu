@@ -115,6 +115,12 @@ template <typename T, int R>
 __global__ void k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T, R>(tiles, LV, I, S, blockIdx.x); }
 template <typename T, int R>
+__global__ void k_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                  const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                  const GhostDev* __restrict__ G, int which) {
+    b_bicg_dir_smooth<T, R>(tiles, LV, I, S, G, which, blockIdx.x);
+}
+template <typename T, int R>
 __global__ void k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) { b_bicg_apply<T, R>(tiles, LV, I, S, G, part, e_alt, which, blockIdx.x); }
@@ -240,6 +246,17 @@ cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstD
     else k_bicg_p<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S);
     return cudaGetLastError();
 }
+template <typename T>
+cudaError_t launch_bicg_dir_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                                   const GhostDev* G, int which, int rows, cudaStream_t s) {
+    if (rows == MG_ROWS_WIDE) k_bicg_dir_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, which);
+    else k_bicg_dir_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, which);
+    return cudaGetLastError();
+}
+template cudaError_t launch_bicg_dir_smooth<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+                                                    const GhostDev*, int, int, cudaStream_t);
+template cudaError_t launch_bicg_dir_smooth<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+                                                   const GhostDev*, int, int, cudaStream_t);
 template <typename T>
 cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                               const GhostDev* G, double* part, int e_alt, int which, int rows, cudaStream_t s) {

@@ -897,6 +897,51 @@ __device__ __forceinline__ void b_bicg_p(const Tile* __restrict__ tiles, const L
         }
 }
 
+// The direction update (which = 0: p_dir as b_bicg_p; 1: s as b_bicg_s)
+// fused with the V-cycle's first, zero-start smoothing sweep of the finest
+// level that follows it (as b_smooth with flags = 1, src_alt = 0): the new
+// vector is the sweep's right-hand side, so it is used from registers instead
+// of being read back.  Same arithmetic as the two phases.
+template <typename T, int R = 1>
+__device__ __forceinline__ void b_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                                  const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                                  const GhostDev* __restrict__ G, int which, int vb) {
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev& in = I[t.inst];
+    const InstState& st = S[t.inst];
+    const LevelDev& L = LV[t.lev];  // finest-level tiles
+    if (!tile_live0(t, L, in, S)) return;
+    Rows0<R> q;
+    rows0<R>(L, t, q);
+    const T* kr = (const T*)in.kr;
+    const T* kv = (const T*)in.kv;
+    T* out = (T*)(which == 0 ? in.kp : in.ks);
+    const T* src = (const T*)L.e;
+    T* dst = (T*)L.e2;
+    const T om = (T)in.omega;
+    T val[R], e1[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int id = q.id[r];
+        if (which == 0) {
+            const T beta = (T)st.beta, omg = (T)st.omega;
+            val[r] = kr[id] + beta * (((const T*)in.kp)[id] - omg * kv[id]);
+        } else {
+            val[r] = kr[id] - (T)st.alpha * kv[id];
+        }
+        T Le, D;
+        lap_p<T, T, true>(L, src, q.ic, q.jc[r], id, L.pitch, q.bt[r], G, in.gidx, Le, D);
+        e1[r] = jacobi_from_zero<T>(val[r], D, om);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (q.bt[r] & 0x0F) {
+            out[q.id[r]] = val[r];
+            ((T*)L.r)[q.id[r]] = val[r];
+            dst[q.id[r]] = e1[r];
+        }
+}
+
 // y = L z with z the preconditioned vector (V-cycle result), operator and z
 // in T; z is kept as zo.  partials: which=0 -> (rh, y) ; which=1 -> (y, s), (y, y)
 template <typename T, int R = 1>

@@ -899,8 +899,10 @@ struct Seq {
 template <typename T>
 constexpr int mixed_of() { return sizeof(T) == 4 ? 1 : 0; }
 
+// first_done: the finest level's zero-start sweep already ran (fused with
+// the Krylov direction update).
 template <typename T>
-int seq_vcycle(Seq& q) {
+int seq_vcycle(Seq& q, bool first_done = false) {
     ifx_solver* S = q.S;
     cudaStream_t st = S->stream;
     const int L = S->lmax, pre = S->mg_pre, post = S->mg_post;
@@ -919,7 +921,7 @@ int seq_vcycle(Seq& q) {
     auto tre = [&](int l) { return W ? S->dTreW[l] : S->dTre[l]; };
     auto ntre = [&](int l) { return W ? S->ntreW[l] : S->ntre[l]; };
     // finest level: first sweep from zero, then the rest of the pre-smoothing
-    q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, R, st));
+    if (!first_done) q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, R, st));
     int cur0 = 1;
     for (int k = 1; k < pre; k++) {
         q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur0, R, st));
@@ -1025,12 +1027,16 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
         q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, n, st));
         q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st));
     }
-    q.add(launch_bicg_p<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
-    int e1 = seq_vcycle<T>(q);
+    // direction updates fused with the first sweep of the tile V-cycle
+    const bool fuse = !S->cmg_use;
+    if (fuse) q.add(launch_bicg_dir_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 0, R, st));
+    else q.add(launch_bicg_p<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
+    int e1 = seq_vcycle<T>(q, fuse);
     q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, R, st));
     q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 0, st));
-    q.add(launch_bicg_s<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
-    int e2 = seq_vcycle<T>(q);
+    if (fuse) q.add(launch_bicg_dir_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, R, st));
+    else q.add(launch_bicg_s<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
+    int e2 = seq_vcycle<T>(q, fuse);
     q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, R, st));
     q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st));
     q.add(launch_bicg_x<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dPart, R, st));
