@@ -32,7 +32,10 @@ batched   : the batched sweep (256 seeded instances of uneven grid, Re and
 served    : a seeded Poisson request stream through the continuous-batching
             server (real-time arrivals, cohorts admitted by device memory),
             solves/s, Mcell-updates/s and p50/p99 latency, the two smallest
-            requests re-run alone in FP64 for the error.
+            requests re-run alone in FP64 for the error; the same stream
+            served in plain FP64 (served.fp64), and both precisions with every
+            request arriving at t = 0 (served.capacity: the server's
+            throughput, mixed over FP64).
 
 --impl reference times the CPU restatement of the reference scheme (the
 reference's pressure solver does not compile and it has no projection or
@@ -232,10 +235,13 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
     return res
 
 
-def served_stream(ifx, capi, cases, nreq, rate, budget):
-    """Served stream through the continuous-batching server: seeded Poisson
-    arrivals in real time; latency = completion - arrival."""
-    stream = cases.served_stream(nreq, rate, seed=0, precision=capi.PREC_MIXED, nmin=64, nmax=512, smin=20, smax=200)
+def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True):
+    """Served stream through the continuous-batching server: seeded arrivals
+    (Poisson at `rate` per second in real time, or all at t = 0 when rate is
+    None: the server's capacity); latency = completion - arrival."""
+    stream = cases.served_stream(nreq, rate or 1.0, seed=0, precision=prec, nmin=64, nmax=512, smin=20, smax=200)
+    if rate is None:
+        stream = [(0.0,) + tuple(r[1:]) for r in stream]
     srv = ifx.Server(budget, max_cohort=32)
     arr, done, work, spec_of = {}, {}, 0, {}
     t0 = time.perf_counter()
@@ -264,25 +270,41 @@ def served_stream(ifx, capi, cases, nreq, rate, budget):
             done[rid] = tnow
     lat = np.array([done[r] - arr[r] for r in arr]) * 1e3
     span = max(done.values()) - stream[0][0]
-    # accuracy: the two smallest requests re-run alone in plain FP64
-    small = sorted(arr, key=lambda r: spec_of[r][0].nx * spec_of[r][0].ny)[:2]
-    errs = []
-    for r in small:
-        cfg, xf, yf, n = spec_of[r]
-        s = ifx.Solver.create(copy_cfg(cfg, capi.PREC_FP64), xf, yf)
-        s.step(n)
-        a = np.concatenate([srv.result(r, capi.FIELD_U).ravel(), srv.result(r, capi.FIELD_V).ravel()])
-        b = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
-        errs.append(rel_l2(a, b))
-        s.close()
+    out = {"workload": f"served stream: {nreq} requests (seed 0), "
+                       + (f"Poisson arrivals at {rate}/s" if rate else "all arriving at t = 0 (capacity)")
+                       + ", cylinder or ellipse, grids log-uniform 64^2..512^2, Re U[50,1000], 20..200 steps each",
+           "requests": nreq, "solves_per_s": nreq / span, "value": work / span / 1e6, "unit": METRIC,
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+           "ticks": ticks, "peak_cohorts": peak_cohorts, "hbm_budget_bytes": budget,
+           "precision": "mixed" if prec == capi.PREC_MIXED else "fp64"}
+    if check:
+        # accuracy: the two smallest requests re-run alone in plain FP64
+        small = sorted(arr, key=lambda r: spec_of[r][0].nx * spec_of[r][0].ny)[:2]
+        errs = []
+        for r in small:
+            cfg, xf, yf, n = spec_of[r]
+            s = ifx.Solver.create(copy_cfg(cfg, capi.PREC_FP64), xf, yf)
+            s.step(n)
+            a = np.concatenate([srv.result(r, capi.FIELD_U).ravel(), srv.result(r, capi.FIELD_V).ravel()])
+            b = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+            errs.append(rel_l2(a, b))
+            s.close()
+        out["accuracy_vs_fp64"] = {"rel_l2_velocity_max": max(errs), "requests_checked": len(errs)}
     srv.close()
-    return {"workload": f"served stream: {nreq} requests (seed 0), Poisson arrivals at {rate}/s, cylinder or ellipse, "
-                        "grids log-uniform 64^2..512^2, Re U[50,1000], 20..200 steps each",
-            "requests": nreq, "solves_per_s": nreq / span, "value": work / span / 1e6, "unit": METRIC,
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max())},
-            "ticks": ticks, "peak_cohorts": peak_cohorts, "hbm_budget_bytes": budget, "precision": "mixed",
-            "accuracy_vs_fp64": {"rel_l2_velocity_max": max(errs), "requests_checked": len(errs)}}
+    return out
+
+
+def served_lines(ifx, capi, cases, nreq, rate, budget):
+    """The Poisson stream (latency) and the all-at-once stream (capacity), each
+    served in mixed precision and in plain FP64."""
+    res = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_MIXED)
+    res["fp64"] = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_FP64, check=False)
+    cap = {"mixed": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_MIXED, check=False),
+           "fp64": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_FP64, check=False)}
+    cap["speedup_mixed_over_fp64"] = cap["mixed"]["value"] / cap["fp64"]["value"]
+    res["capacity"] = cap
+    return res
 
 
 def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
@@ -485,7 +507,7 @@ def main():
     if args.batch > 0:
         line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup, peak)
     if args.serve > 0:
-        line["served"] = served_stream(ifx, capi, cases, args.serve, args.rate, 64 << 30)
+        line["served"] = served_lines(ifx, capi, cases, args.serve, args.rate, 64 << 30)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
         n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)

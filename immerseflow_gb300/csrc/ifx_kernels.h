@@ -60,10 +60,11 @@ cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const Ins
 template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
                            int coarse_alt, int rows, cudaStream_t s);
-// Prolongation plus two post-smoothing sweeps of a coarse level (32x8 tiles).
+// Prolongation plus the first post-smoothing sweep of a coarse level (32x8
+// tiles): reads buffer cur, writes buffer cur ^ 1.
 template <typename T>
-cudaError_t launch_prolong_post2(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                                 int fine_alt, int coarse_alt, cudaStream_t s);
+cudaError_t launch_prolong_sweep(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                                 int cur, int coarse_alt, cudaStream_t s);
 template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s);

@@ -145,10 +145,10 @@ template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, 4) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
-__global__ void k_prolong_post2(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                                const InstDev* __restrict__ I, const InstState* __restrict__ S, int fine_alt,
+__global__ void k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                const InstDev* __restrict__ I, const InstState* __restrict__ S, int cur,
                                 int coarse_alt) {
-    b_prolong_post2<T>(tiles, LV, I, S, fine_alt, coarse_alt, blockIdx.x);
+    b_prolong_sweep<T>(tiles, LV, I, S, cur, coarse_alt, blockIdx.x);
 }
 template <typename T>
 __global__ void k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
@@ -308,15 +308,15 @@ cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const Inst
     return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_prolong_post2(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
-                                 int fine_alt, int coarse_alt, cudaStream_t s) {
+cudaError_t launch_prolong_sweep(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                                 int cur, int coarse_alt, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_prolong_post2<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, fine_alt, coarse_alt);
+    k_prolong_sweep<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, cur, coarse_alt);
     return cudaGetLastError();
 }
-template cudaError_t launch_prolong_post2<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+template cudaError_t launch_prolong_sweep<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
                                                   int, int, cudaStream_t);
-template cudaError_t launch_prolong_post2<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
+template cudaError_t launch_prolong_sweep<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
                                                  int, int, cudaStream_t);
 template <typename T>
 cudaError_t subcycle_smem_limit(int bytes) {

@@ -1229,66 +1229,56 @@ __device__ __forceinline__ void b_prolong(const Tile* __restrict__ tiles, const 
         if (bt[r] & 0x0F) fe[id[r]] = val[r];
 }
 
-// Prolongation of the coarse correction followed by two weighted-Jacobi
-// sweeps, fused for a coarse level (no IBM ghosts) with 32x8 tiles (graph and
-// host-loop modes): the tile and a two-cell halo are staged in shared memory,
-// the correction is added on the whole region, the first sweep runs on the
-// tile plus a one-cell halo and the second on the tile, which is written back
-// to buffer fine_alt.  Same per-cell arithmetic as b_prolong followed by two
-// b_smooth sweeps; the level's other Jacobi buffer is not written (nothing
-// reads it before it is overwritten).
-constexpr int PP_W = TILE_X + 4, PP_H = TILE_Y + 4, PP_N = PP_W * PP_H;
+// Prolongation of the coarse correction fused with the first post-smoothing
+// sweep, for a coarse level (no IBM ghosts) with 32x8 tiles (graph and
+// host-loop modes).  The tile and a one-cell halo of buffer cur (the
+// pre-smoothed correction, which no block writes in this phase) are staged in
+// shared memory, the prolongation is added on the staged cells, and one
+// weighted-Jacobi sweep of the tile is written to buffer cur ^ 1.  Same values
+// as b_prolong (in place on cur) followed by b_smooth from cur into cur ^ 1;
+// buffer cur keeps its pre-prolongation values, which the next sweep (from
+// cur ^ 1 back into cur) overwrites on every live cell.
+constexpr int PS_W = TILE_X + 2, PS_H = TILE_Y + 2, PS_N = PS_W * PS_H;
 
 template <typename T>
-__device__ __forceinline__ void b_prolong_post2(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__device__ __forceinline__ void b_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                                 const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                                                int fine_alt, int coarse_alt, int vb) {
-    __shared__ T ea[PP_N], eb[PP_N], rs[PP_N];
-    __shared__ uint8_t bs[PP_N];
+                                                int cur, int coarse_alt, int vb) {
+    __shared__ T ea[PS_N];
+    __shared__ uint8_t bs[PS_N];
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
     if (!tile_live(t, F, S)) return;
     const LevelDev& C = LV[F.child];
     const T* ce = (const T*)((coarse_alt && C.child >= 0) ? C.e2 : C.e);
-    T* fe = (T*)(fine_alt ? F.e2 : F.e);
+    const T* fe = (const T*)(cur ? F.e2 : F.e);
+    T* fo = (T*)(cur ? F.e : F.e2);
     const T* fr = (const T*)F.r;
     const T om = (T)I[t.inst].omega;
-    const int P = F.pitch, CP = C.pitch, ib = t.i0 - 2, jb = t.j0 - 2;
+    const int P = F.pitch, CP = C.pitch, ib = t.i0 - 1, jb = t.j0 - 1;
     const uint8_t* cbits = C.bits;
     auto fce = [ce, CP](int I0, int J0) { return ce[I0 + J0 * CP]; };
     auto fcb = [cbits, CP](int I0, int J0) { return __ldg(&cbits[I0 + J0 * CP]); };
-    // stage the region; add the correction on its live cells
-    for (int q = threadIdx.x; q < PP_N; q += blockDim.x) {
-        const int rj = q / PP_W, ri = q - rj * PP_W, i = ib + ri, j = jb + rj;
+    // stage the tile and its halo; add the correction on the live cells
+    for (int q = threadIdx.x; q < PS_N; q += blockDim.x) {
+        const int rj = q / PS_W, ri = q - rj * PS_W, i = ib + ri, j = jb + rj;
         const bool inside = i >= 0 && i < F.nx && j >= 0 && j < F.ny;
         const int id = inside ? i + j * P : 0;
         const uint8_t bt = (inside && i >= 1 && i <= F.NX && j >= 1 && j <= F.NY) ? __ldg(&F.bits[id]) : (uint8_t)0;
         T v = inside ? fe[id] : (T)0;
         if (bt & 0x0F) v = v + prolong_corr<T>(F, i, j, fce, fcb);
         ea[q] = v;
-        rs[q] = inside ? fr[id] : (T)0;
         bs[q] = bt;
     }
     __syncthreads();
-    // first sweep on the tile and a one-cell halo
-    for (int q = threadIdx.x; q < PP_N; q += blockDim.x) {
-        const int rj = q / PP_W, ri = q - rj * PP_W;
-        T v = ea[q];
-        if (ri >= 1 && ri < PP_W - 1 && rj >= 1 && rj < PP_H - 1 && (bs[q] & 0x0F)) {
-            T Le, D;
-            lap_p<T, T, false>(F, ea, ib + ri, jb + rj, q, PP_W, bs[q], nullptr, nullptr, Le, D);
-            v = jacobi_update<T>(ea[q], rs[q], Le, D, om);
-        }
-        eb[q] = v;
-    }
-    __syncthreads();
-    // second sweep on the tile, written back
-    const int ri = 2 + (int)(threadIdx.x & 31), rj = 2 + (int)(threadIdx.x >> 5), q = ri + rj * PP_W;
+    // one sweep of the tile
+    const int ri = 1 + (int)(threadIdx.x & 31), rj = 1 + (int)(threadIdx.x >> 5), q = ri + rj * PS_W;
     const int i = ib + ri, j = jb + rj;
     if (bs[q] & 0x0F) {
+        const int id = i + j * P;
         T Le, D;
-        lap_p<T, T, false>(F, eb, i, j, q, PP_W, bs[q], nullptr, nullptr, Le, D);
-        fe[i + j * P] = jacobi_update<T>(eb[q], rs[q], Le, D, om);
+        lap_p<T, T, false>(F, ea, i, j, q, PS_W, bs[q], nullptr, nullptr, Le, D);
+        fo[id] = jacobi_update<T>(ea[q], fr[id], Le, D, om);
     }
 }
 

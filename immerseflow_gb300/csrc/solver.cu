@@ -945,13 +945,16 @@ int seq_vcycle(Seq& q, bool first_done = false) {
         const int nt = l == 0 ? nt0 : ntsm(l);
         if (nt == 0) continue;
         int cur = parity_after_pre(l, pre);
-        if (l >= 1 && post == 2) {  // fused, 32x8 tiles in either shape: the result stays in buffer cur
-            q.add(launch_prolong_post2<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, cur,
+        int k = 0;
+        if (l >= 1) {  // prolongation fused with the first sweep (32x8 tiles in either shape): cur -> cur ^ 1
+            q.add(launch_prolong_sweep<T>(S->dTsm[l], S->ntsm[l], S->dLV, S->dI, S->dS, cur,
                                           parity_after_post(l + 1, pre, post), st));
-            continue;
+            cur ^= 1;
+            k = 1;
+        } else {
+            q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), R, st));
         }
-        q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), R, st));
-        for (int k = 0; k < post; k++) {
+        for (; k < post; k++) {
             q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur, R, st));
             cur ^= 1;
         }
