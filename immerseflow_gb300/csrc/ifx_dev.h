@@ -26,6 +26,9 @@ constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
 constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
 constexpr double COARSE_OMEGA = 1.5;
+// Threads of the block that runs an instance's small levels in the graph and
+// host-loop modes (the persistent kernel runs them with its own blocks).
+constexpr int SUB_THREADS = 512;
 constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one block per instance
 constexpr int SUB_SMEM_MAX = 96 * 1024;  // shared memory for those levels (fields, metrics, tables)
 constexpr int kSubLevels = 16;           // at most this many levels per instance

@@ -151,7 +151,7 @@ __global__ void k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* 
     b_prolong_sweep<T>(tiles, LV, I, S, cur, coarse_alt, blockIdx.x);
 }
 template <typename T>
-__global__ void k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(SUB_THREADS) k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            int pre, int post) {
     extern __shared__ __align__(16) unsigned char sub_smem[];
@@ -336,7 +336,7 @@ template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s) {
     if (ninst == 0) return cudaSuccess;
-    k_subcycle<T><<<ninst, TILE_THREADS, smem_bytes, s>>>(sub, LV, I, S, pre, post);
+    k_subcycle<T><<<ninst, SUB_THREADS, smem_bytes, s>>>(sub, LV, I, S, pre, post);
     return cudaGetLastError();
 }
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {
