@@ -226,6 +226,11 @@ struct alignas(16) InstDev {
     // then u, v, p at each probe cell), written at the end of every step
     double* hist;
     const int* probe_cell;       // pitched cell index of each probe
+    // the sub-cycle's shared-memory image of this instance's small levels
+    // (headers, metric arrays, prolongation tables, stencil bytes; zero fields),
+    // staged by one contiguous copy; sub_img_bytes is a multiple of 16
+    const unsigned char* sub_img;
+    int sub_img_bytes;
     int hist_cap, hist_w, nprobe;
 };
 

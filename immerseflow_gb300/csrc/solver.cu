@@ -64,6 +64,59 @@ ifx_status dupload(ifx_solver* S, T** out, const std::vector<T>& h) {
     return IFX_OK;
 }
 
+// Shared-memory image of the sub-cycle's levels lb.. of instance I, laid out
+// as the device code reads it (SubHdr table, then per level the arrays of
+// sub_layout): metric arrays in T, prolongation tables (levels with a coarser
+// one), dense stencil bytes, and zero e, e2, r.
+template <typename T>
+std::vector<unsigned char> sub_image(const Instance& I, int lb) {
+    const int nl = (int)I.lev.size(), ns = nl - lb, ts = (int)sizeof(T);
+    size_t total = SUB_HDR_BYTES;
+    for (int s = 0; s < ns; s++) total += sub_level_bytes(I.lev[lb + s].nx, I.lev[lb + s].ny, ts);
+    std::vector<unsigned char> img(total, 0);
+    size_t off = SUB_HDR_BYTES;
+    for (int s = 0; s < ns; s++) {
+        const int l = lb + s;
+        const HostLevel& L = I.lev[l];
+        SubHdr h;
+        std::memset(&h, 0, sizeof(h));
+        h.o = sub_layout(L.nx, L.ny, ts);
+        h.base = (unsigned)off;
+        h.NX = L.NX; h.NY = L.NY; h.nx = L.nx; h.ny = L.ny;
+        h.dirmask = I.dirmask;
+        h.child = l + 1 < nl ? I.lev_base + l + 1 : -1;
+        h.depth = l;
+        h.ns = ns;
+        h.cx = L.cx; h.cy = L.cy;
+        std::memcpy(img.data() + s * sizeof(SubHdr), &h, sizeof(h));
+        unsigned char* b = img.data() + off;
+        auto put_t = [&](size_t o, const std::vector<double>& v, int n) {
+            T* d = (T*)(b + o);
+            for (int q = 0; q < n && q < (int)v.size(); q++) d[q] = (T)v[q];
+        };
+        auto put_i = [&](size_t o, const std::vector<int>& v, int n) {
+            int* d = (int*)(b + o);
+            for (int q = 0; q < n && q < (int)v.size(); q++) d[q] = v[q];
+        };
+        auto put_c = [&](size_t o, const std::vector<signed char>& v, int n) {
+            signed char* d = (signed char*)(b + o);
+            for (int q = 0; q < n && q < (int)v.size(); q++) d[q] = v[q];
+        };
+        put_t(h.o.kx, L.kx, L.nx); put_t(h.o.ix, L.ix, L.nx); put_t(h.o.dw, L.dw, L.nx);
+        put_t(h.o.ky, L.ky, L.ny); put_t(h.o.iy, L.iy, L.ny); put_t(h.o.dh, L.dh, L.ny);
+        if (h.child >= 0) {
+            put_t(h.o.pwx, L.pwx, L.nx); put_t(h.o.pwy, L.pwy, L.ny);
+            put_i(h.o.pI, L.pI, L.nx); put_i(h.o.pIn, L.pIn, L.nx);
+            put_i(h.o.pJ, L.pJ, L.ny); put_i(h.o.pJn, L.pJn, L.ny);
+            put_c(h.o.psx, L.psx, L.nx); put_c(h.o.psy, L.psy, L.ny);
+        }
+        for (int j = 0; j < L.ny; j++)
+            for (int i = 0; i < L.nx; i++) b[h.o.b + i + (size_t)j * L.nx] = L.bits[i + (size_t)j * L.pitch];
+        off += h.o.bytes;
+    }
+    return img;
+}
+
 std::vector<float> to_f(const std::vector<double>& v) {
     std::vector<float> r(v.size());
     for (size_t k = 0; k < v.size(); k++) r[k] = (float)v[k];
@@ -834,6 +887,25 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     }
     IFX_TRY(dupload(S, &S->dTall, hTall));
     IFX_TRY(dupload(S, &S->dSub, hSub));
+    {   // shared-memory images of the small levels, one buffer for all instances
+        std::vector<unsigned char> all;
+        std::vector<size_t> at(n);
+        for (int k = 0; k < n; k++) {
+            const Instance& I = S->inst[k];
+            const std::vector<unsigned char> img = S->prec == IFX_PREC_FP64 ? sub_image<double>(I, hSub[k] - I.lev_base)
+                                                                            : sub_image<float>(I, hSub[k] - I.lev_base);
+            at[k] = all.size();
+            all.insert(all.end(), img.begin(), img.end());
+            hI[k].sub_img_bytes = (int)img.size();
+        }
+        unsigned char* d_img = nullptr;
+        IFX_TRY(dupload(S, &d_img, all));
+        for (int k = 0; k < n; k++) {
+            hI[k].sub_img = d_img + at[k];
+            S->inst[k].dev.sub_img = hI[k].sub_img;
+            S->inst[k].dev.sub_img_bytes = hI[k].sub_img_bytes;
+        }
+    }
     if (S->prec == IFX_PREC_FP64) CUDA_TRY(subcycle_smem_limit<double>(S->sub_bytes));
     else CUDA_TRY(subcycle_smem_limit<float>(S->sub_bytes));
     S->cmg_ok = 0;
@@ -1924,6 +1996,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
             case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, 1, st);
             case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
             case 4: return launch_barrier_bench(S->dBar, S->persist_grid, 1000, st);
+            case 5: return launch_subcycle<T>(S->dSub, n, S->dLV, S->dI, S->dS, S->mg_pre, S->mg_post, S->sub_bytes, st);
             default: return launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st);
         }
     };
@@ -1941,7 +2014,7 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
 
 extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, double* ms_per_launch,
                                          long long* cells) {
-    if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 4) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
+    if (!S || !ms_per_launch || reps < 1 || kernel < 0 || kernel > 5) return set_error(IFX_ERR_ARG, "ifx_profile_kernel: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));
     if (kernel == 4 && S->persist_grid == 0) return set_error(IFX_ERR_STATE, "cooperative launch unavailable");
     if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_profile_kernel needs a METHOD-mode solver");

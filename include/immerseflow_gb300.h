@@ -367,7 +367,8 @@ void       ifx_server_destroy(ifx_server* v);
  * mean device time per launch (CUDA events).  kernel: 0 finest-level
  * multigrid smoothing sweep, 1 FP64 pressure operator apply (BiCGSTAB),
  * 2 predictor Jacobi sweep, 3 convection / predictor right-hand side,
- * 4 one grid barrier of the persistent per-step kernel (time per barrier).
+ * 4 one grid barrier of the persistent per-step kernel (time per barrier),
+ * 5 the small-level multigrid sub-cycle (one block per instance).
  * *cells receives the interior cells one launch covers.  Scratch buffers and
  * the per-step iteration state are overwritten; the flow state is not. */
 ifx_status ifx_profile_kernel(ifx_solver* s, int kernel, int reps, double* ms_per_launch, long long* cells);
