@@ -190,6 +190,27 @@ struct alignas(16) LevelDev {
     int cx, cy;      // cells of the parent level per cell of this one, in x and y (1 or 2)
 };
 
+// Tiles of one level of one instance, in row-major order from (x0, y0), each
+// TILE_X x th cells, with the level's descriptor and the instance's constants
+// by value (kernel parameters of the single-instance phases): a block finds
+// its tile and level without memory loads, and reads the instance's state
+// together with the fields, testing it before the stores (a single instance
+// that has converged ends the loop after the phase anyway).
+struct GridTiles {
+    LevelDev L;
+    const int* gidx;
+    double omega;
+    int inst, lev, x0, y0, ntx, th;
+    IFX_HD Tile tile(int vb) const {
+        Tile t;
+        t.inst = inst;
+        t.lev = lev;
+        t.i0 = x0 + (vb % ntx) * TILE_X;
+        t.j0 = y0 + (vb / ntx) * th;
+        return t;
+    }
+};
+
 // One body-surface sample for drag/lift (stationary body: built once).
 // Pressure is sampled bilinearly at the surface point (base cell c0,
 // weights xi0/et0), velocity at a probe del along the normal (c1, xi1/et1).

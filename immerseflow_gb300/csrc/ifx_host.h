@@ -75,6 +75,7 @@ struct ifx_solver {
     ifx::InstState* dS = nullptr;
     ifx::InstState* hS = nullptr;    // pinned mirror
     ifx::LevelDev* dLV = nullptr;
+    std::vector<ifx::LevelDev> hLV;  // host copy of dLV
     ifx::GhostDev* dG = nullptr;
     int ng = 0, nibm = 0;
     int* dIbm = nullptr;             // global indices of IBM ghost entries

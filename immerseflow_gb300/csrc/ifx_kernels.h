@@ -54,6 +54,10 @@ cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstD
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s);
+// Smoothing sweep of one level of a one-instance solver (tiles from the grid).
+template <typename T>
+cudaError_t launch_smooth_grid(const GridTiles& g, int nt, const InstState* S, const GhostDev* G, int flags,
+                               int src_alt, int rows, cudaStream_t s);
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                             const GhostDev* G, int fine_alt, int rows, cudaStream_t s);

@@ -138,6 +138,12 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth(const Tile* __restri
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T, R>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
 template <typename T, int R>
+__global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid(const GridTiles g, const InstState* __restrict__ S,
+                                                                const GhostDev* __restrict__ G, int flags,
+                                                                int src_alt) {
+    b_smooth_grid<T, R>(g, S, G, flags, src_alt, blockIdx.x);
+}
+template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, 4) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
@@ -291,6 +297,18 @@ cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstD
     else k_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     return cudaGetLastError();
 }
+template <typename T>
+cudaError_t launch_smooth_grid(const GridTiles& g, int nt, const InstState* S, const GhostDev* G, int flags,
+                               int src_alt, int rows, cudaStream_t s) {
+    if (nt == 0) return cudaSuccess;
+    if (rows == MG_ROWS_WIDE) k_smooth_grid<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(g, S, G, flags, src_alt);
+    else k_smooth_grid<T, 1><<<nt, TILE_THREADS, 0, s>>>(g, S, G, flags, src_alt);
+    return cudaGetLastError();
+}
+template cudaError_t launch_smooth_grid<double>(const GridTiles&, int, const InstState*, const GhostDev*, int, int,
+                                                int, cudaStream_t);
+template cudaError_t launch_smooth_grid<float>(const GridTiles&, int, const InstState*, const GhostDev*, int, int,
+                                               int, cudaStream_t);
 template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                             const GhostDev* G, int fine_alt, int rows, cudaStream_t s) {

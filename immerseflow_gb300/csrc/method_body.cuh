@@ -1061,17 +1061,11 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
 
 // Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
 template <typename T, int R = 1>
-__device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                                         const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
-    const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev& L = LV[t.lev];
-    if (!tile_live(t, L, S)) return;
+__device__ __forceinline__ void smooth_tile(const Tile& t, const LevelDev& L, const T om, const int* gidx,
+                                            const GhostDev* __restrict__ G, int flags, int src_alt, int state) {
     const T* src = (const T*)(src_alt ? L.e2 : L.e);
     T* dst = (T*)(src_alt ? L.e : L.e2);
     const T* rr = (const T*)L.r;
-    const T om = (T)I[t.inst].omega;
-    const int* gidx = L.depth == 0 ? I[t.inst].gidx : nullptr;
     const int P = L.pitch;
     const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
     const int ic = clampi(i, 1, L.NX);
@@ -1093,9 +1087,25 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
         else lap_p<T, T, false>(L, src, ic, jc, id[r], P, bt[r], G, nullptr, Le, D);
         val[r] = (flags & 1) ? jacobi_from_zero<T>(rr[id[r]], D, om) : jacobi_update<T>(src[id[r]], rr[id[r]], Le, D, om);
     }
+    if (state != ST_ACTIVE) return;
 #pragma unroll
     for (int r = 0; r < R; r++)
         if (bt[r] & 0x0F) dst[id[r]] = val[r];
+}
+template <typename T, int R = 1>
+__device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                         const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                         const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev& L = LV[t.lev];
+    if (!tile_live(t, L, S)) return;
+    smooth_tile<T, R>(t, L, (T)I[t.inst].omega, L.depth == 0 ? I[t.inst].gidx : nullptr, G, flags, src_alt, ST_ACTIVE);
+}
+template <typename T, int R = 1>
+__device__ __forceinline__ void b_smooth_grid(const GridTiles& g, const InstState* __restrict__ S,
+                                              const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {
+    const int state = S[g.inst].ppe_state;
+    smooth_tile<T, R>(g.tile(vb), g.L, (T)g.omega, g.L.depth == 0 ? g.gidx : nullptr, G, flags, src_alt, state);
 }
 
 // Restriction of the fine residual (area weighted) onto the coarse level,

@@ -861,6 +861,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         hI[k] = d;
     }
     IFX_TRY(dupload(S, &S->dLV, hLV));
+    S->hLV = hLV;
     IFX_TRY(dupload(S, &S->dT0, hT0));
     S->nt0 = (int)hT0.size();
     S->dTsm.assign(lmax, nullptr);
@@ -973,6 +974,23 @@ constexpr int mixed_of() { return sizeof(T) == 4 ? 1 : 0; }
 
 // first_done: the finest level's zero-start sweep already ran (fused with
 // the Krylov direction update).
+// Tile grid of level l of a one-instance solver (the layout of its tile
+// lists: rows of tiles of TILE_X x 8 rows cells from (0, 0)).
+GridTiles grid_of(const ifx_solver* S, int l, int rows) {
+    const Instance& I = S->inst[0];
+    GridTiles g;
+    g.L = S->hLV[I.lev_base + l];
+    g.gidx = I.dev.gidx;
+    g.omega = I.dev.omega;
+    g.inst = 0;
+    g.lev = I.lev_base + l;
+    g.x0 = 0;
+    g.y0 = 0;
+    g.th = TILE_Y * rows;
+    g.ntx = (g.L.nx + TILE_X - 1) / TILE_X;
+    return g;
+}
+
 template <typename T>
 int seq_vcycle(Seq& q, bool first_done = false) {
     ifx_solver* S = q.S;
@@ -985,6 +1003,11 @@ int seq_vcycle(Seq& q, bool first_done = false) {
     }
     // multigrid tile lists: 32x8 tiles, or wide tiles with MG_ROWS_WIDE rows per thread
     const int R = S->mg_rows;
+    const bool one = S->inst.size() == 1;  // one instance: tiles from the block index
+    auto smooth = [&](const Tile* tl, int nt, int l, int flags, int src_alt) {
+        return one ? launch_smooth_grid<T>(grid_of(S, l, R), nt, S->dS, S->dG, flags, src_alt, R, st)
+                   : launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, flags, src_alt, R, st);
+    };
     const bool W = R == MG_ROWS_WIDE;
     const Tile* t0 = W ? S->dT0W : S->dT0;
     const int nt0 = W ? S->nt0W : S->nt0;
@@ -993,10 +1016,10 @@ int seq_vcycle(Seq& q, bool first_done = false) {
     auto tre = [&](int l) { return W ? S->dTreW[l] : S->dTre[l]; };
     auto ntre = [&](int l) { return W ? S->ntreW[l] : S->ntre[l]; };
     // finest level: first sweep from zero, then the rest of the pre-smoothing
-    if (!first_done) q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, 0, R, st));
+    if (!first_done) q.add(smooth(t0, nt0, 0, 1, 0));
     int cur0 = 1;
     for (int k = 1; k < pre; k++) {
-        q.add(launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 0, cur0, R, st));
+        q.add(smooth(t0, nt0, 0, 0, cur0));
         cur0 ^= 1;
     }
     // large coarse levels: one launch per phase
@@ -1006,7 +1029,7 @@ int seq_vcycle(Seq& q, bool first_done = false) {
         if (ntsm(l) == 0) continue;
         int cur = 0;
         for (int k = 1; k < pre; k++) {
-            q.add(launch_smooth<T>(tsm(l), ntsm(l), S->dLV, S->dI, S->dS, S->dG, 0, cur, R, st));
+            q.add(smooth(tsm(l), ntsm(l), l, 0, cur));
             cur ^= 1;
         }
     }
@@ -1027,7 +1050,7 @@ int seq_vcycle(Seq& q, bool first_done = false) {
             q.add(launch_prolong<T>(tl, nt, S->dLV, S->dS, cur, parity_after_post(l + 1, pre, post), R, st));
         }
         for (; k < post; k++) {
-            q.add(launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, 0, cur, R, st));
+            q.add(smooth(tl, nt, l, 0, cur));
             cur ^= 1;
         }
         if (l == 0) cur0 = cur;
