@@ -25,12 +25,13 @@
 
 namespace ifx {
 
-// Resident blocks per SM the tile kernels are compiled for: the wide tiles
+// Resident blocks per SM the tile kernels are compiled for.  The wide tiles
 // (four rows per thread, the batched workloads, many blocks in flight) are
 // latency-bound and run fastest at eight blocks of 256 threads per SM, within
-// 32 registers a thread (a few spilled to L1); one-row tiles keep the
-// 64-register budget.
-constexpr int mg_blocks(int rows) { return rows == 1 ? 4 : 8; }
+// 32 registers a thread (a few spilled to L1); so do the FP64 one-row tiles of
+// the plain path's batches.  FP32 one-row tiles keep the 64-register budget.
+template <typename T>
+constexpr int mg_blocks(int rows) { return rows == 1 ? (sizeof(T) == 8 ? 8 : 4) : 8; }
 
 __global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl) { b_step_begin(I, S, n, ctl, blockIdx.x); }
 __global__ void k_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I) { b_outflow(G, ng, I, blockIdx.x); }
@@ -40,11 +41,11 @@ __global__ void k_ghost_scatter(const GhostDev* __restrict__ G, int ng, const In
                                 int comps, const double* __restrict__ gval) { b_ghost_scatter(G, ng, I, comps, gval, blockIdx.x); }
 __global__ void k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S) { b_conv_rhs(tiles, I, S, blockIdx.x); }
-__global__ void k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<double>(1)) k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              double* __restrict__ part, int parity) { b_pred_sweep(tiles, ntiles, G, ng, I, S, part, parity, blockIdx.x); }
 template <int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<float>(R)) k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
                                const InstState* __restrict__ S, double* __restrict__ part, int parity) {
     b_pred_sweep32<R>(tiles, ntiles, G, ng, LV, I, S, part, parity, blockIdx.x);
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_pred_sweep32(con
 // returns at once when the last vote found nothing due.
 constexpr int OPT_GRID = 1024;
 template <int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_pred_refresh(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<float>(R)) k_pred_refresh(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const InstDev* __restrict__ I, const InstState* __restrict__ S, int stage,
                                int finalize, const LoopCtl* ctl) {
     if (!finalize && none_due(ctl)) return;
@@ -119,29 +120,29 @@ __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __rest
                                 const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
                                 unsigned long long handle) { b_bicg_reduce_r(I, S, part, start, mixed, ctl, handle, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T, R>(tiles, LV, I, S, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                   const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                   const GhostDev* __restrict__ G, int which) {
     b_bicg_dir_smooth<T, R>(tiles, LV, I, S, G, which, blockIdx.x);
 }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) { b_bicg_apply<T, R>(tiles, LV, I, S, G, part, e_alt, which, blockIdx.x); }
 __global__ void k_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int which) { b_bicg_scalar(I, S, part, which, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_s<T, R>(tiles, LV, I, S, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_x(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          double* __restrict__ part) { b_bicg_x<T, R>(tiles, LV, I, S, part, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T, R>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
 template <typename T, int R>
@@ -151,11 +152,11 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid(const GridTiles
     b_smooth_grid<T, R>(g, S, G, flags, src_alt, blockIdx.x);
 }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
 template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
 __global__ void k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
