@@ -39,7 +39,7 @@ __global__ void k_ghost_gather(const GhostDev* __restrict__ G, int ng, const Ins
                                int comps, double* __restrict__ gval) { b_ghost_gather(G, ng, I, comps, gval, blockIdx.x); }
 __global__ void k_ghost_scatter(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
                                 int comps, const double* __restrict__ gval) { b_ghost_scatter(G, ng, I, comps, gval, blockIdx.x); }
-__global__ void k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S) { b_conv_rhs(tiles, I, S, blockIdx.x); }
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<double>(1)) k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<float>(R)) k_pred_refr
 __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle) { b_pred_reduce(I, S, part, parity, ctl, handle, blockIdx.x); }
-__global__ void k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            double* __restrict__ part, int to_final) { b_face_rhs(tiles, I, part, to_final, blockIdx.x); }
 __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part) { b_rhs_reduce(I, S, part, blockIdx.x); }
@@ -74,7 +74,7 @@ __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restric
 // in the list), and the grid strides over the concatenated due tiles: the pass
 // costs in proportion to the tiles restarting, spread over the whole grid.
 template <typename T>
-__global__ void k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only,
                              const LoopCtl* ctl, int nt, int ninst) {
@@ -159,7 +159,7 @@ template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T>
-__global__ void k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                 const InstDev* __restrict__ I, const InstState* __restrict__ S, int cur,
                                 int coarse_alt) {
     b_prolong_sweep<T>(tiles, LV, I, S, cur, coarse_alt, blockIdx.x);
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(SUB_THREADS) k_subcycle(const int* __restrict_
 }
 __global__ void k_p_finalize(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                              const InstState* __restrict__ S) { b_p_finalize(tiles, I, S, blockIdx.x); }
-__global__ void k_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                           double* __restrict__ part) { b_correct(tiles, I, part, blockIdx.x); }
 __global__ void k_correct_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                  const double* __restrict__ part) { b_correct_reduce(I, S, part, blockIdx.x); }
