@@ -72,6 +72,8 @@ struct ifx_server {
     int max_cohort = 64;
     int steps_per_tick = 1;  // a cohort advances up to this many steps per tick
     int exec_mode = IFX_EXEC_GRAPH;
+    int mg_rows = 0;                  // tile rows of the cohorts; 0: by precision and size
+    long long wide_cells = 1 << 18;   // mixed cohorts from this many cells use four rows
     long long next_id = 1;
     std::map<long long, Request> reqs;
     std::deque<long long> waiting;
@@ -107,6 +109,16 @@ static ifx_status admit(ifx_server* V) {
     ifx_server::Cohort c;
     ifx_status st = ifx_create_batch((int)take.size(), cfgs.data(), xs.data(), ys.data(), &c.s);
     if (st == IFX_OK && V->exec_mode != IFX_EXEC_DEFAULT) st = ifx_set_exec_mode(c.s, V->exec_mode);
+    if (st == IFX_OK) {
+        // multigrid and finest-level tile shape: four rows per thread for mixed
+        // cohorts with many cells (the latency-bound phases then keep more loads
+        // in flight), one row otherwise; results do not depend on it
+        long long cells = 0;
+        for (const ifx_config& c : cfgs) cells += (long long)c.nx * c.ny;
+        int rows = V->mg_rows;
+        if (rows == 0) rows = (cfgs[0].precision == IFX_PREC_MIXED && cells >= V->wide_cells) ? 4 : 1;
+        st = ifx_set_mg_tile_rows(c.s, rows);
+    }
     if (st != IFX_OK) {
         if (c.s) ifx_destroy(c.s);
         for (long long id : take) {

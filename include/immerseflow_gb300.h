@@ -326,7 +326,9 @@ ifx_status ifx_write_force_file(ifx_solver* s, int inst, const char* path);
  * fit in the device-memory budget as one batched cohort with its own stream
  * and state kept on the device, then advances every live cohort by up to
  * steps_per_tick time steps (all cohorts issued before any is waited for, so
- * they overlap on the GPU).  A request that completed its steps is copied out (u, v, p, stats)
+ * they overlap on the GPU).  A mixed-precision cohort of at least 2^18 cells
+ * runs its tile phases on 32x32 tiles (ifx_set_mg_tile_rows), a smaller one on
+ * 32x8 tiles.  A request that completed its steps is copied out (u, v, p, stats)
  * and stops computing; a cohort whose requests all finished frees its memory.
  * Results do not depend on the cohort a request ran in.  One host thread per
  * server. */
