@@ -14,9 +14,10 @@ value     : interior cells x steps / device time of the timed steps (CUDA
 e2e       : same metric through the C ABI with the state copied from pinned
             host buffers and the result copied back every step, wall clock;
 plain_fp64: the same steps with every kernel in FP64;
-roofline  : the dominant kernel is the persistent per-step kernel (one launch
-            per step); achieved = algorithmic bytes of the step / its event
-            time.  Algorithmic bytes per interior cell (s = 4 B FP32 multigrid
+roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
+            launch per step, or the persistent per-step kernel); achieved =
+            algorithmic bytes of the step / its event time; traffic = the DRAM
+            bytes of one warm-cache step from the committed ncu launch list.  Algorithmic bytes per interior cell (s = 4 B FP32 multigrid
             word, state words 8 B, stencil byte 1 B):
               convection+AB2 rhs 81, predictor sweep 49 (x sweeps),
               faces+source 41, BiCGSTAB start 49, projection 81,
@@ -29,6 +30,8 @@ batched   : the batched sweep (256 seeded instances of uneven grid, Re and
             ellipse, one batched solver each for mixed and plain FP64,
             execution mode picked by the autotuner), Mcell-updates/s, solves/s
             of 500-step runs, error of mixed vs FP64 per instance;
+reference_path: the REFERENCE-mode step (the reference's own scheme) at 52^2,
+            130^2 and 514^2 cells, GPU and one CPU thread;
 served    : a seeded Poisson request stream through the continuous-batching
             server (real-time arrivals, cohorts admitted by device memory),
             solves/s, Mcell-updates/s and p50/p99 latency, the two smallest
@@ -307,6 +310,44 @@ def served_lines(ifx, capi, cases, nreq, rate, budget):
     return res
 
 
+def reference_path(ifx, capi, cases, steps=20, cpu=True):
+    """The REFERENCE-mode time step (the reference's ADsolver: vortex IC,
+    explicit convection, backward-Euler diffusion by Jacobi to the L1 stop rule,
+    src/include/ADSolver.cu:268-395) on uniform unit-square grids of 52^2, 130^2
+    and 514^2 cells (ghosts included), Re 150, dt 1e-3, AD_itermax 25: GPU time
+    (CUDA events) beside the CPU restatement of the same scheme (one thread)."""
+    lines = []
+    for n in (50, 128, 512):
+        c = ifx.default_config()
+        c.nx = c.ny = n
+        c.lx = c.ly = 1.0
+        xf = cases.uniform_faces(n, 1.0)
+        s = ifx.Solver.create(c, xf, xf)
+        s.step(2)
+        s.step(steps)
+        ms = s.last_step_ms()
+        st = s.stats()
+        line = {"grid": [n + 2, n + 2], "steps": steps, "gpu_value": n * n * steps / (ms * 1e-3) / 1e6,
+                "gpu_ms_per_step": ms / steps, "jacobi_iterations_last_step": st.last_ad_iters}
+        if cpu:
+            sys.path.insert(0, os.path.join(ROOT, "tests"))
+            import _oracle
+
+            o = _oracle.Oracle()
+            k = steps if n <= 128 else 4
+            t0 = time.perf_counter()
+            o.ref_ad(xf, xf, 1e-3, 150.0, 25, k)
+            dt = time.perf_counter() - t0
+            line.update({"cpu_value": n * n * k / dt / 1e6, "cpu_steps": k, "cpu_cores": 1})
+        lines.append(line)
+        s.close()
+    return {"workload": "REFERENCE mode (the reference's ADsolver step), uniform grids on [0,1]^2, "
+                        "vortex IC, Re 150, dt 1e-3, AD_itermax 25",
+            "unit": METRIC, "lines": lines,
+            "note": "the reference's own CUDA executable builds from its sources, which do not travel to "
+                    "the GPU box; this is the drop-in REFERENCE mode on the same scheme"}
+
+
 def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
@@ -508,6 +549,8 @@ def main():
         line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup, peak)
     if args.serve > 0:
         line["served"] = served_lines(ifx, capi, cases, args.serve, args.rate, 64 << 30)
+    if rank == 0 and world == 1:
+        line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
         n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)

@@ -123,6 +123,10 @@ struct ifx_solver {
     double *r_coef = nullptr, *r_sx = nullptr, *r_sy = nullptr, *r_uf = nullptr, *r_vf = nullptr, *r_res = nullptr;
     double* r_out = nullptr;         // device reduction results (+ ticket)
     double* r_line = nullptr;        // line-SOR elimination scratch
+    ifx::GridBar* r_bar = nullptr;   // grid barrier of the one-launch step
+    int* r_iters_d = nullptr;        // Jacobi iterations per step of one launch (kRefStepsPerLaunch)
+    int* r_iters_h = nullptr;        // pinned mirror
+    int r_grid = 0;                  // blocks of the one-launch step, 0: host loop
     double* h_out = nullptr;         // pinned
     int r_cur = 0;                   // 0: state in r_u/r_v, 1: in r_ut/r_vt
     std::vector<int> r_iters;

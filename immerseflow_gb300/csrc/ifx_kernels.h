@@ -115,6 +115,14 @@ cudaError_t launch_ref_resid(const RefDev& R, const double* uo, const double* un
                              const double* vn, double* out, cudaStream_t s);
 cudaError_t launch_ref_init(int nx, int ny, const double* xc, const double* yc, double* u, double* v,
                             double* p, cudaStream_t s);
+// nsteps ADsolver steps in one cooperative launch of `grid` blocks (grid
+// barriers between the phases, stop rule evaluated on the device);
+// ref_steps_grid gives the grid (co-resident blocks, at most one per 256-cell
+// chunk), 0 when cooperative launch is unavailable.
+struct GridBar;
+int ref_steps_grid(int nx, int ny);
+cudaError_t launch_ref_steps(const RefDev& R, double* u, double* v, double* ut, double* vt, GridBar* bar,
+                             int itermax, int nsteps, int* iters, int grid, cudaStream_t s);
 // Jacobi Laplace (PPESolver intent): coefficients, BC, sweep, signed residual sum -> out[0]
 cudaError_t launch_ref_ppe_coeffs(const RefDev& R, cudaStream_t s);
 cudaError_t launch_ref_ppe_bc(const RefDev& R, double* p, cudaStream_t s);

@@ -18,45 +18,13 @@
 
 #include <mutex>
 
+#include "grid_barrier.cuh"
 #include "ifx_persist.h"
 #include "method_body.cuh"
 
 namespace ifx {
 
 namespace {
-
-constexpr long long kSpinLimit = 1ll << 23;  // x ~50-100 ns per poll: well under a second per barrier
-
-__device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(const volatile unsigned int*)p; }
-
-// Flat barrier on a monotonically increasing 64-bit arrival counter: the
-// k-th barrier of the launch is passed once the counter reaches
-// gridDim.x * k.  Arrival is a release add, the wait an acquire poll, so the
-// critical path is one atomic and one poll; the counter never needs a reset
-// inside the launch (the host zeroes it before each launch).
-__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epoch, long long* trace = nullptr,
-                                             int cap = 0) {
-    __syncthreads();
-    epoch += 1;
-    if (threadIdx.x == 0) {
-        const unsigned long long target = epoch * (unsigned long long)gridDim.x;
-        unsigned long long v;
-        asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(v) : "l"(&b->count) : "memory");
-        long long spins = 0;
-        while (true) {
-            asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(&b->count) : "memory");
-            if (v >= target) break;
-            if (++spins > kSpinLimit) {
-                atomicExch(&b->err, 1u);
-                break;
-            }
-            __nanosleep(32);
-        }
-        if (trace && blockIdx.x == 0 && epoch < (unsigned long long)cap) trace[epoch] = clock64();
-    }
-    __syncthreads();
-    return vload(&b->err) == 0u;
-}
 
 // Loop-exit tests: every block must take the same decision, so the states
 // written by other blocks before the last barrier are read with volatile loads.

@@ -9,6 +9,9 @@
 // reduced on the device in a fixed order (no per-iteration allocation).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "grid_barrier.cuh"
 #include "ifx_kernels.h"
 
 namespace ifx {
@@ -37,8 +40,8 @@ __global__ void k_ref_coeffs(RefDev R) {
 // Compute_velf with its loop structure: uf for every index, vf only for
 // indices in [(nx-1)(ny-2), (nx-2)(ny-1)) (the second grid-stride loop of
 // src/include/ADSolver.cu:179 starts from the exhausted index).
-__global__ void k_ref_velf(RefDev R, const double* __restrict__ u, const double* __restrict__ v) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void velf_cell(const RefDev& R, const double* __restrict__ u,
+                                          const double* __restrict__ v, int id) {
     const int nx = R.nx, ny = R.ny;
     const int nu = (nx - 1) * (ny - 2), nv = (nx - 2) * (ny - 1);
     if (id < nu) {
@@ -51,14 +54,16 @@ __global__ void k_ref_velf(RefDev R, const double* __restrict__ u, const double*
                    (v[idc + nx + 1] * R.dy[idc + 1] + v[idc + 1] * R.dy[idc + nx + 1]);
     }
 }
+__global__ void k_ref_velf(RefDev R, const double* __restrict__ u, const double* __restrict__ v) {
+    velf_cell(R, u, v, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // set_velocity_BC (src/include/ADSolver.cu:195-217): ghost = 2*wall - adjacent,
 // u_wall = 1, v_wall = 0.  The reference's corner cells race on a
 // neighbouring ghost; here edges use the interior neighbour and a corner
 // applies the rule twice to its diagonal interior cell (edge first, then
 // corner), which is one of the orders the reference can produce.
-__global__ void k_ref_bc(RefDev R, double* __restrict__ u, double* __restrict__ v) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void bc_cell(const RefDev& R, double* __restrict__ u, double* __restrict__ v, int q) {
     const int nx = R.nx, ny = R.ny;
     if (q >= nx * ny) return;
     const int i = q % nx, j = q / nx;
@@ -79,10 +84,13 @@ __global__ void k_ref_bc(RefDev R, double* __restrict__ u, double* __restrict__ 
         v[q] = -v[a] + 0.0 * 2.0;
     }
 }
+__global__ void k_ref_bc(RefDev R, double* __restrict__ u, double* __restrict__ v) {
+    bc_cell(R, u, v, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ADSource (src/include/ADSolver.cu:46-79), including its 0.5 factor.
-__global__ void k_ref_source(RefDev R, const double* __restrict__ u, const double* __restrict__ v) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void source_cell(const RefDev& R, const double* __restrict__ u,
+                                            const double* __restrict__ v, int id) {
     const int nx = R.nx, ny = R.ny;
     if (id >= nx * ny) return;
     const int i = id % nx, j = id / nx;
@@ -105,11 +113,14 @@ __global__ void k_ref_source(RefDev R, const double* __restrict__ u, const doubl
     R.sx[id] = sx;
     R.sy[id] = sy;
 }
+__global__ void k_ref_source(RefDev R, const double* __restrict__ u, const double* __restrict__ v) {
+    source_cell(R, u, v, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ADusolver_kernel / ADvsolver_kernel (src/include/ADSolver.cu:81-120), fused.
-__global__ void k_ref_jacobi(RefDev R, const double* __restrict__ u, const double* __restrict__ v,
-                             double* __restrict__ un, double* __restrict__ vn) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void jacobi_cell(const RefDev& R, const double* __restrict__ u,
+                                            const double* __restrict__ v, double* __restrict__ un,
+                                            double* __restrict__ vn, int id) {
     const int nx = R.nx, ny = R.ny;
     if (id >= nx * ny) return;
     const int i = id % nx, j = id / nx;
@@ -126,13 +137,18 @@ __global__ void k_ref_jacobi(RefDev R, const double* __restrict__ u, const doubl
         vn[id] = (1.0 - R.w_ad) * v[id] + R.w_ad * vn[id];
     }
 }
+__global__ void k_ref_jacobi(RefDev R, const double* __restrict__ u, const double* __restrict__ v,
+                             double* __restrict__ un, double* __restrict__ vn) {
+    jacobi_cell(R, u, v, un, vn, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Fixed-order two-level sum: each block writes its partial, the last block
 // to finish adds the partials in block order.
+// Partial sums of a block of 256 cells (warp sums, then warps in order),
+// written by thread 0 to scratch[slot * NV + k].
 template <int NV>
-__device__ void blocks_sum(double (&v)[NV], double* scratch, unsigned int* ticket, double* out) {
+__device__ __forceinline__ void block_partial(double (&v)[NV], double* scratch, int slot) {
     __shared__ double sh[NV][32];
-    __shared__ bool last;
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
@@ -146,8 +162,17 @@ __device__ void blocks_sum(double (&v)[NV], double* scratch, unsigned int* ticke
         for (int k = 0; k < NV; k++) {
             double s = 0.0;
             for (int q = 0; q < nw; q++) s += sh[k][q];
-            scratch[blockIdx.x * NV + k] = s;
+            scratch[slot * NV + k] = s;
         }
+    }
+    __syncthreads();
+}
+
+template <int NV>
+__device__ void blocks_sum(double (&v)[NV], double* scratch, unsigned int* ticket, double* out) {
+    __shared__ bool last;
+    block_partial<NV>(v, scratch, blockIdx.x);
+    if (threadIdx.x == 0) {
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
@@ -165,12 +190,11 @@ __device__ void blocks_sum(double (&v)[NV], double* scratch, unsigned int* ticke
 
 // Compute_{u,v}Residual_AD + Reduction (src/include/ADSolver.cu:122-160,
 // src/include/preSim.cu:376-445): L1 of the update over fluid interior cells.
-__global__ void k_ref_resid(RefDev R, const double* __restrict__ uo, const double* __restrict__ un,
-                            const double* __restrict__ vo, const double* __restrict__ vn, double* out,
-                            unsigned int* ticket) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void resid_cell(const RefDev& R, const double* __restrict__ uo,
+                                           const double* __restrict__ un, const double* __restrict__ vo,
+                                           const double* __restrict__ vn, int id, double (&r)[2]) {
     const int nx = R.nx, ny = R.ny;
-    double r[2] = {0.0, 0.0};
+    r[0] = r[1] = 0.0;
     if (id < nx * ny) {
         const int i = id % nx, j = id / nx;
         if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && R.iblank[id] == 1) {
@@ -178,7 +202,70 @@ __global__ void k_ref_resid(RefDev R, const double* __restrict__ uo, const doubl
             r[1] = fabs(vn[id] - vo[id]);
         }
     }
+}
+__global__ void k_ref_resid(RefDev R, const double* __restrict__ uo, const double* __restrict__ un,
+                            const double* __restrict__ vo, const double* __restrict__ vn, double* out,
+                            unsigned int* ticket) {
+    double r[2];
+    resid_cell(R, uo, un, vo, vn, blockIdx.x * blockDim.x + threadIdx.x, r);
     blocks_sum<2>(r, R.res, ticket, out);
+}
+
+// nsteps ADsolver steps in one cooperative launch: the phases of
+// launch_ref_velf / _bc / _source / _jacobi / _resid over 256-cell chunks
+// (chunk c is the block c of those launches), separated by grid barriers; the
+// L1 residual is summed chunk by chunk in the same order as blocks_sum, by
+// every block, so all blocks take the same loop decision without another
+// barrier.  iters[s] receives step s's Jacobi iterations.  The state starts
+// in (u, v) and ends in (u, v) after an even total of iterations, in
+// (ut, vt) after an odd one (the reference's buffer swaps).
+__global__ void __launch_bounds__(256) k_ref_steps(RefDev R, double* u, double* v, double* ut, double* vt,
+                                                   GridBar* bar, int itermax, int nsteps, int* iters) {
+    const int n = R.nx * R.ny, nc = (n + 255) / 256, nf = ((R.nx - 1) * (R.ny - 1) + 255) / 256;
+    unsigned long long ep = 0;
+    __shared__ double tot[2];
+    double *cu = u, *cv = v, *tu = ut, *tv = vt;
+    for (int s = 0; s < nsteps; s++) {
+        for (int c = blockIdx.x; c < nf; c += gridDim.x) velf_cell(R, cu, cv, c * 256 + threadIdx.x);
+        if (!grid_barrier(bar, ep)) return;
+        for (int c = blockIdx.x; c < nc; c += gridDim.x) bc_cell(R, cu, cv, c * 256 + threadIdx.x);
+        if (!grid_barrier(bar, ep)) return;
+        for (int c = blockIdx.x; c < nc; c += gridDim.x) source_cell(R, cu, cv, c * 256 + threadIdx.x);
+        if (!grid_barrier(bar, ep)) return;
+        double res = 1.0 + 1.0;  // ures + vres start at 1 (src/include/ADSolver.cu:313)
+        int it = 0;
+        while (res > 1e-6 && it < itermax) {
+            for (int c = blockIdx.x; c < nc; c += gridDim.x) bc_cell(R, cu, cv, c * 256 + threadIdx.x);
+            if (!grid_barrier(bar, ep)) return;
+            for (int c = blockIdx.x; c < nf; c += gridDim.x) velf_cell(R, cu, cv, c * 256 + threadIdx.x);
+            if (!grid_barrier(bar, ep)) return;
+            for (int c = blockIdx.x; c < nc; c += gridDim.x) jacobi_cell(R, cu, cv, tu, tv, c * 256 + threadIdx.x);
+            if (!grid_barrier(bar, ep)) return;
+            for (int c = blockIdx.x; c < nc; c += gridDim.x) bc_cell(R, cu, cv, c * 256 + threadIdx.x);
+            for (int c = blockIdx.x; c < nc; c += gridDim.x) {
+                double r[2];
+                resid_cell(R, cu, tu, cv, tv, c * 256 + threadIdx.x, r);
+                block_partial<2>(r, R.res, c);
+            }
+            if (!grid_barrier(bar, ep)) return;
+            if (threadIdx.x == 0) {
+                double a = 0.0, b = 0.0;
+                for (int c = 0; c < nc; c++) {
+                    a += ((volatile double*)R.res)[c * 2];
+                    b += ((volatile double*)R.res)[c * 2 + 1];
+                }
+                tot[0] = a;
+                tot[1] = b;
+            }
+            __syncthreads();
+            res = tot[0] + tot[1];
+            __syncthreads();
+            double* x = cu; cu = tu; tu = x;
+            x = cv; cv = tv; tv = x;
+            it++;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) iters[s] = it;
+    }
 }
 
 // initializeKernel (src/include/preSim.cu:57-76): vortex in uniform flow.
@@ -321,6 +408,29 @@ cudaError_t launch_ref_resid(const RefDev& R, const double* uo, const double* un
     // out[0..1]: sums; out[2] holds the block ticket (zeroed at allocation)
     k_ref_resid<<<nb256(R.nx * R.ny), 256, 0, s>>>(R, uo, un, vo, vn, out, (unsigned int*)(out + 2));
     return cudaGetLastError();
+}
+int ref_steps_grid(int nx, int ny) {
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ref_steps, 256, 0) != cudaSuccess) per_sm = 0;
+        cudaGetLastError();
+    }
+    const int nc = std::max((nx * ny + 255) / 256, ((nx - 1) * (ny - 1) + 255) / 256);
+    const int cap = per_sm * sms;
+    return cap <= 0 ? 0 : std::min(nc, cap);
+}
+cudaError_t launch_ref_steps(const RefDev& R, double* u, double* v, double* ut, double* vt, GridBar* bar,
+                             int itermax, int nsteps, int* iters, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+    if (e != cudaSuccess) return e;
+    RefDev r = R;
+    void* args[] = {&r, &u, &v, &ut, &vt, &bar, &itermax, &nsteps, &iters};
+    return cudaLaunchCooperativeKernel((const void*)k_ref_steps, dim3(grid), dim3(256), args, 0, s);
 }
 cudaError_t launch_ref_init(int nx, int ny, const double* xc, const double* yc, double* u, double* v, double* p,
                             cudaStream_t s) {

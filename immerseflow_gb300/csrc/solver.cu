@@ -1358,6 +1358,9 @@ ifx_status step_finish(ifx_solver* S) {
 
 // ---------------------------------------------------- reference mode
 
+// Steps of one cooperative REFERENCE-mode launch (the per-step iteration counts fit a fixed buffer).
+constexpr int kRefStepsPerLaunch = 1024;
+
 ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf, const double* yf) {
     S->mode = IFX_MODE_REFERENCE;
     S->inst.resize(1);
@@ -1408,6 +1411,12 @@ ifx_status create_reference(ifx_solver* S, const ifx_config* c, const double* xf
     IFX_TRY(dalloc(S, &S->r_res, 2 * ((n + 255) / 256) + 2));
     IFX_TRY(dalloc(S, &S->r_out, 4));
     if (c->ppe_method == IFX_PPE_LINE_SOR) IFX_TRY(dalloc(S, &S->r_line, n));
+    S->r_grid = ref_steps_grid(nx, ny);
+    if (S->r_grid > 0) {
+        IFX_TRY(dalloc(S, &S->r_bar, 1));
+        IFX_TRY(dalloc(S, &S->r_iters_d, kRefStepsPerLaunch));
+        CUDA_TRY(cudaMallocHost((void**)&S->r_iters_h, kRefStepsPerLaunch * sizeof(int)));
+    }
     CUDA_TRY(cudaMallocHost((void**)&S->h_out, 4 * sizeof(double)));
     // initializeData (src/include/preSim.cu:201-217)
     CUDA_TRY(launch_ref_init(nx, ny, S->r_xc, S->r_yc, S->r_u, S->r_v, S->r_p, S->stream));
@@ -1454,6 +1463,38 @@ ifx_status step_reference(ifx_solver* S, int nsteps) {
     CUDA_TRY(cudaEventRecord(S->ev0, st));
     CUDA_TRY(launch_ref_coeffs(R, st));
     S->launches++;
+    if (S->r_grid > 0 && !S->poisoned) {
+        // the whole step on the device: one cooperative launch per kRefStepsPerLaunch steps
+        for (int s0 = 0; s0 < nsteps; s0 += kRefStepsPerLaunch) {
+            const int k = std::min(kRefStepsPerLaunch, nsteps - s0);
+            double* cu = S->r_cur ? S->r_ut : S->r_u;
+            double* cv = S->r_cur ? S->r_vt : S->r_v;
+            double* tu = S->r_cur ? S->r_u : S->r_ut;
+            double* tv = S->r_cur ? S->r_v : S->r_vt;
+            CUDA_TRY(launch_ref_steps(R, cu, cv, tu, tv, S->r_bar, I.cfg.ad_itermax, k, S->r_iters_d, S->r_grid, st));
+            S->launches += 2;
+            CUDA_TRY(cudaMemcpyAsync(S->r_iters_h, S->r_iters_d, k * sizeof(int), cudaMemcpyDeviceToHost, st));
+            unsigned int err = 0;
+            CUDA_TRY(cudaMemcpyAsync(S->h_out, &S->r_bar->err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            std::memcpy(&err, S->h_out, sizeof(err));
+            if (err) {
+                S->poisoned = true;
+                return set_error(IFX_ERR_CUDA, "reference step: grid barrier timed out");
+            }
+            for (int q = 0; q < k; q++) {
+                S->r_iters.push_back(S->r_iters_h[q]);
+                S->r_cur ^= (S->r_iters_h[q] & 1);
+            }
+        }
+        CUDA_TRY(cudaEventRecord(S->ev1, st));
+        CUDA_TRY(cudaEventSynchronize(S->ev1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+        S->last_ms = ms;
+        S->steps_done += nsteps;
+        return IFX_OK;
+    }
     for (int s = 0; s < nsteps; s++) {
         double* cu = S->r_cur ? S->r_ut : S->r_u;
         double* cv = S->r_cur ? S->r_vt : S->r_v;
@@ -2098,6 +2139,7 @@ extern "C" void ifx_destroy(ifx_solver* S) {
     if (S->hS) cudaFreeHost(S->hS);
     if (S->hCtl) cudaFreeHost(S->hCtl);
     if (S->h_out) cudaFreeHost(S->h_out);
+    if (S->r_iters_h) cudaFreeHost(S->r_iters_h);
     if (S->ev0) cudaEventDestroy(S->ev0);
     if (S->ev1) cudaEventDestroy(S->ev1);
     if (S->stream) cudaStreamDestroy(S->stream);
