@@ -17,7 +17,8 @@ plain_fp64: the same steps with every kernel in FP64;
 roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
             launch per step, or the persistent per-step kernel); achieved =
             algorithmic bytes of the step / its event time; traffic = the DRAM
-            bytes of one warm-cache step from the committed ncu launch list.  Algorithmic bytes per interior cell (s = 4 B FP32 multigrid
+            bytes of one warm-cache step from the committed ncu launch list.
+            Algorithmic bytes per interior cell (s = 4 B FP32 multigrid
             word, state words 8 B, stencil byte 1 B):
               convection+AB2 rhs 81, predictor sweep 49 (x sweeps),
               faces+source 41, BiCGSTAB start 49, projection 81,
@@ -238,14 +239,14 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
     return res
 
 
-def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True):
+def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True, max_cohort=32):
     """Served stream through the continuous-batching server: seeded arrivals
     (Poisson at `rate` per second in real time, or all at t = 0 when rate is
     None: the server's capacity); latency = completion - arrival."""
     stream = cases.served_stream(nreq, rate or 1.0, seed=0, precision=prec, nmin=64, nmax=512, smin=20, smax=200)
     if rate is None:
         stream = [(0.0,) + tuple(r[1:]) for r in stream]
-    srv = ifx.Server(budget, max_cohort=32)
+    srv = ifx.Server(budget, max_cohort=max_cohort)
     arr, done, work, spec_of = {}, {}, 0, {}
     t0 = time.perf_counter()
     i = 0
