@@ -69,6 +69,7 @@ struct ifx_solver {
     int exec_override = -1;          // IFX_EXEC_*; -1: environment / default
     int pending_mode = 0, pending_steps = 0;  // steps issued and not yet waited for
     std::vector<ifx::Instance> inst;
+    std::vector<int> inst_status;    // sticky per-instance status (IFX_*), METHOD mode
 
     // batched device tables
     ifx::InstDev* dI = nullptr;

@@ -228,6 +228,22 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
         ifx_server::Cohort& c = *it;
         ifx_status st = ifx_step_wait(c.s);
         bool drop = false;
+        if (st == IFX_ERR_DIVERGED) {
+            // only the requests whose instance diverged fail (the solver retired
+            // them); the cohort's other requests go on
+            worst = st;
+            for (size_t k = 0; k < c.ids.size(); k++) {
+                if (c.ids[k] < 0) continue;
+                ifx_server::Request& r = V->reqs[c.ids[k]];
+                ifx_stats s;
+                if (r.state != 1 || ifx_get_stats(c.s, (int)k, &s) != IFX_OK || s.status != IFX_ERR_DIVERGED) continue;
+                r.state = 3;
+                r.st = s;
+                V->finished.push_back(r.id);
+                c.live--;
+            }
+            st = IFX_OK;
+        }
         if (st != IFX_OK) {
             worst = st;
             for (long long id : c.ids)

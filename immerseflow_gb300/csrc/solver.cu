@@ -1269,16 +1269,32 @@ ifx_status build_graph(ifx_solver* S) {
     return IFX_OK;
 }
 
+// Per-instance outcome of the steps just finished.  An instance whose state
+// became non-finite is marked IFX_ERR_DIVERGED and retired (later steps leave
+// it unchanged while the other instances go on); the call reports
+// IFX_ERR_DIVERGED once, when that happens.  An instance whose pressure solve
+// stopped at its iteration cap above the tolerance is marked
+// IFX_ERR_NOT_CONVERGED (a warning: its steps continue).
 ifx_status check_states(ifx_solver* S) {
     const int n = (int)S->inst.size();
+    if ((int)S->inst_status.size() != n) S->inst_status.assign(n, IFX_OK);
     CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, n * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     ifx_status worst = IFX_OK;
     for (int k = 0; k < n; k++) {
+        Instance& I = S->inst[k];
+        if (I.dev.retired) continue;
         const InstState& s = S->hS[k];
-        if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric))
+        if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric)) {
+            S->inst_status[k] = IFX_ERR_DIVERGED;
+            I.dev.retired = 1;
+            CUDA_TRY(cudaMemcpyAsync(&S->dI[k].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
             worst = IFX_ERR_DIVERGED;
+        } else if (s.ppe_iters >= I.cfg.ppe_itermax && s.ppe_rel > I.cfg.ppe_tol && S->inst_status[k] == IFX_OK) {
+            S->inst_status[k] = IFX_ERR_NOT_CONVERGED;
+        }
     }
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
     return worst;
 }
 
@@ -1349,10 +1365,7 @@ ifx_status step_finish(ifx_solver* S) {
         S->launches += (long long)nsteps * (S->graph_nodes_pre + pairs * S->graph_nodes_pred + S->graph_nodes_mid +
                                             bodies * S->graph_nodes_ppe + S->graph_nodes_post);
     }
-    for (size_t k = 0; k < S->inst.size(); k++) {
-        if (st != IFX_OK) S->hS[k].status = st;
-    }
-    if (st != IFX_OK) return set_error(st, "non-finite value in the solver state");
+    if (st != IFX_OK) return set_error(st, "non-finite value in the solver state (the instance is retired)");
     return IFX_OK;
 }
 
@@ -1996,7 +2009,7 @@ extern "C" ifx_status ifx_get_stats(ifx_solver* S, int inst, ifx_stats* out) {
     out->n_fluid = I.n_fluid;
     out->n_ibm_ghost = I.n_ibm;
     out->mg_levels = (int)I.lev.size();
-    out->status = s.status;
+    out->status = inst < (int)S->inst_status.size() ? S->inst_status[inst] : IFX_OK;
     return IFX_OK;
 }
 

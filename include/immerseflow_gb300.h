@@ -135,7 +135,11 @@ typedef struct ifx_stats {
     long long ad_iters_total, ppe_iters_total;
     long long kernel_launches;     /* kernels of this library launched so far   */
     int    n_fluid, n_ibm_ghost, mg_levels;
-    int    status;                 /* sticky per-instance status (IFX_*)         */
+    int    status;                 /* sticky per-instance status: IFX_OK,
+                                      IFX_ERR_DIVERGED (non-finite state; the
+                                      instance is retired, the others go on),
+                                      IFX_ERR_NOT_CONVERGED (a pressure solve
+                                      stopped at ppe_itermax; steps go on)     */
 } ifx_stats;
 
 /* ------------------------------------------------------ library / errors */
@@ -177,7 +181,10 @@ int        ifx_num_instances(const ifx_solver* s);
 ifx_status ifx_get_dims(const ifx_solver* s, int inst, int* nx, int* ny);
 
 /* One reference time step is ImmerseFlow::ADsolver (src/include/ADSolver.cu:268-395)
- * in REFERENCE mode; in METHOD mode it is predictor -> PPE -> projection. */
+ * in REFERENCE mode; in METHOD mode it is predictor -> PPE -> projection.
+ * METHOD mode returns IFX_ERR_DIVERGED in the call in which an instance's state
+ * becomes non-finite; that instance is retired (its stats.status says so) and
+ * the other instances of a batch are unaffected. */
 ifx_status ifx_step(ifx_solver* s, int nsteps);
 
 /* Asynchronous form (no reference counterpart): ifx_step_async issues nsteps

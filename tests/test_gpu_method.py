@@ -211,3 +211,37 @@ def test_cluster_vcycle_bit_identical(prec, nx, ny):
     for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_UF):
         assert np.array_equal(a.get(f), b.get(f)), f
     assert a.stats().last_ppe_iters == b.stats().last_ppe_iters
+
+
+def test_nan_in_one_batch_slot_leaves_the_others_unaffected():
+    """Fault injection on the host side: a NaN planted in one instance's state.
+    That instance is reported diverged and retired; the others continue and
+    equal the same instances run alone, bit for bit."""
+    specs = [small_cylinder(nx=96, ny=64), cases.cavity(n=40), small_cylinder(nx=70, ny=90, angle=25.0, b=0.25)]
+    batch = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+    batch.step(1)
+    u = batch.get(capi.FIELD_U, inst=1)
+    u[5, 7] = np.nan
+    batch.set(capi.FIELD_U, u, inst=1)
+    with pytest.raises(ifx.IFXError) as e:
+        batch.step(1)
+    assert e.value.status == capi.IFX_ERR_DIVERGED
+    assert batch.stats(1).status == capi.IFX_ERR_DIVERGED
+    assert batch.stats(0).status == capi.IFX_OK and batch.stats(2).status == capi.IFX_OK
+    batch.step(2)  # the retired instance no longer stops the batch
+    for k in (0, 2):
+        alone = ifx.Solver.create(*specs[k])
+        alone.step(4)
+        for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+            assert np.array_equal(batch.get(f, inst=k), alone.get(f)), (k, f)
+
+
+def test_pressure_iteration_cap_is_reported():
+    cfg, xf, yf = small_cylinder()
+    cfg.ppe_itermax = 1
+    s = ifx.Solver.create(cfg, xf, yf)
+    s.step(1)
+    assert s.stats().status == capi.IFX_ERR_NOT_CONVERGED
+    assert s.stats().last_ppe_iters == 1
+    s.step(1)  # a warning: the steps go on
+    assert np.all(np.isfinite(s.get(capi.FIELD_U)))

@@ -111,3 +111,32 @@ def test_autotune_keeps_results():
     b.step(3)
     for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
         assert np.array_equal(a.get(f), b.get(f)), f
+
+
+def test_server_fails_only_the_diverged_request():
+    """A request whose state becomes non-finite fails; the rest of its cohort
+    finishes with the same results as alone.  The fault is planted on the host:
+    a request whose Reynolds number (1e-300) overflows its diffusion
+    coefficients."""
+    good = [case(64, 48), case(56, 40, re=150.0, b=0.25, angle=15.0)]
+    bad = case(48, 40, re=1e-300)
+    v = ifx.Server(1 << 34, max_cohort=8, steps_per_tick=1)
+    ids = [v.submit(c, x, y, 4) for c, x, y in good]
+    bad_id = v.submit(*bad, 4)
+    diverged = False
+    for _ in range(20):
+        try:
+            v.tick()
+        except ifx.IFXError as e:
+            assert e.status == capi.IFX_ERR_DIVERGED
+            diverged = True
+        if all(v.state(i)[0] in (ifx.REQ_FINISHED, ifx.REQ_FAILED) for i in ids + [bad_id]):
+            break
+    assert diverged
+    assert v.state(bad_id)[0] == ifx.REQ_FAILED
+    for rid, (c, x, y) in zip(ids, good):
+        assert v.state(rid)[0] == ifx.REQ_FINISHED
+        ref = alone(c, x, y, 4)
+        for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+            assert np.array_equal(v.result(rid, f), ref[f]), (rid, f)
+    v.close()
