@@ -52,6 +52,8 @@ struct Instance {
 
 // Waits for steps issued by ifx_step_async and checks their state.
 ifx_status finish_pending(ifx_solver* S);
+// The checks a METHOD-mode configuration must pass at creation.
+ifx_status validate_method_config(const ifx_config* c);
 
 }  // namespace ifx
 

@@ -184,6 +184,10 @@ extern "C" ifx_status ifx_server_submit(ifx_server* V, const ifx_config* cfg, co
                                         int nsteps, long long* id) {
     if (!V || !cfg || !xf || !yf || nsteps < 1 || !id) return set_error(IFX_ERR_ARG, "ifx_server_submit: bad argument");
     if (cfg->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_ARG, "ifx_server_submit: METHOD-mode cases only");
+    {   // refused here rather than failing the cohort it would be admitted with
+        const ifx_status st = validate_method_config(cfg);
+        if (st != IFX_OK) return st;
+    }
     ifx_server::Request r;
     r.id = V->next_id++;
     r.cfg = *cfg;

@@ -1614,6 +1614,7 @@ ifx_status get_pitched(ifx_solver* S, const Instance& I, const double* src, doub
 
 namespace ifx {
 ifx_status finish_pending(ifx_solver* S) { return S->pending_steps ? step_finish(S) : IFX_OK; }
+ifx_status validate_method_config(const ifx_config* c) { return validate(c); }
 }  // namespace ifx
 
 static ifx_status new_solver(ifx_solver** out) {

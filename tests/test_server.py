@@ -45,3 +45,17 @@ def test_reference_mode_case_is_refused():
     with pytest.raises(ifx.IFXError):
         srv.submit(cfg, xf, yf, nsteps=2)
     srv.close()
+
+
+@pytest.mark.parametrize("field,value", [("re", -1.0), ("dt", 0.0), ("mg_pre", 0), ("ppe_method", capi.PPE_LINE_SOR)])
+def test_invalid_request_refused_at_submit(field, value):
+    """A configuration the solver would refuse is refused at submit, not when its
+    cohort is created (which would fail the requests admitted with it)."""
+    cfg, xf, yf = small(48, 32)
+    setattr(cfg, field, value)
+    srv = ifx.Server(1 << 30, max_cohort=4)
+    with pytest.raises(ifx.IFXError) as e:
+        srv.submit(cfg, xf, yf, nsteps=3)
+    assert e.value.status == capi.IFX_ERR_ARG
+    assert srv.info()["waiting"] == 0
+    srv.close()
