@@ -245,3 +245,28 @@ def test_pressure_iteration_cap_is_reported():
     assert s.stats().last_ppe_iters == 1
     s.step(1)  # a warning: the steps go on
     assert np.all(np.isfinite(s.get(capi.FIELD_U)))
+
+
+@pytest.mark.parametrize("nx,ny", [(17, 13), (12, 20), (33, 9)])
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_small_uneven_grids_vs_oracle(oracle, nx, ny, prec):
+    """Small uneven grids (partial tiles, two- and three-level hierarchies, the
+    coarsest level straight after the finest): every tile edge and the
+    sub-cycle bounds are exercised.  FP64 against the oracle to 1e-10; the mixed
+    path against the oracle to the mixed tolerance."""
+    cfg, xf, yf = cases.cavity(n=nx)
+    cfg.ny = ny
+    cfg.ly = 1.0 * ny / nx
+    yf = cases.uniform_faces(ny, cfg.ly)
+    cfg.precision = prec
+    s = ifx.Solver.create(cfg, xf, yf)
+    ocfg, _, _ = cases.cavity(n=nx)
+    ocfg.ny, ocfg.ly = cfg.ny, cfg.ly
+    o = oracle.method(ocfg, xf, yf)
+    s.step(4)
+    o.step(4)
+    assert np.all(np.isfinite(s.get(capi.FIELD_U)))
+    tol = FIELD_RTOL if prec == capi.PREC_FP64 else 1e-6
+    _compare(s, o, tol=tol)
+    if prec == capi.PREC_FP64:
+        assert s.stats().last_ppe_iters == o.stats().last_ppe_iters
