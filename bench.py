@@ -31,6 +31,8 @@ batched   : the batched sweep (256 seeded instances of uneven grid, Re and
             ellipse, one batched solver each for mixed and plain FP64,
             execution mode picked by the autotuner), Mcell-updates/s, solves/s
             of 500-step runs, error of mixed vs FP64 per instance;
+ellipse   : the large single-instance configuration (1024x768 ellipse,
+            Re 300), autotuned, mixed and plain FP64;
 reference_path: the REFERENCE-mode step (the reference's own scheme) at 52^2,
             130^2 and 514^2 cells, GPU and one CPU thread;
 served    : a seeded Poisson request stream through the continuous-batching
@@ -311,6 +313,32 @@ def served_lines(ifx, capi, cases, nreq, rate, budget):
     return res
 
 
+def ellipse_line(ifx, capi, cases, steps=10):
+    """The large single-instance configuration: ellipse of aspect 0.2 and chord
+    1 at 10 deg, 1024x768 cells on a 20x12 domain, Re 300, dt 2e-3; autotuned,
+    mixed and plain FP64 (device time, CUDA events)."""
+    out = {"workload": "ellipse aspect 0.2, chord 1, 10 deg, 20x12 domain, 1024x768 tanh-stretched, Re 300, dt 2e-3",
+           "unit": METRIC, "steps": steps}
+    fields = {}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        cfg, xf, yf = cases.ellipse(precision=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.step(1)
+        s.autotune(steps=1)
+        s.step(2)
+        s.step(steps)
+        ms = s.last_step_ms()
+        st = s.stats()
+        out[name] = {"value": cfg.nx * cfg.ny * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
+                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters,
+                     "predictor_iters_last": st.last_ad_iters, "cd": st.cd}
+        fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+        s.close()
+    out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["rel_l2_velocity_vs_fp64"] = rel_l2(fields["mixed"], fields["fp64"])
+    return out
+
+
 def reference_path(ifx, capi, cases, steps=20, cpu=True):
     """The REFERENCE-mode time step (the reference's ADsolver: vortex IC,
     explicit convection, backward-Euler diffusion by Jacobi to the L1 stop rule,
@@ -551,6 +579,7 @@ def main():
     if args.serve > 0:
         line["served"] = served_lines(ifx, capi, cases, args.serve, args.rate, 64 << 30)
     if rank == 0 and world == 1:
+        line["ellipse"] = ellipse_line(ifx, capi, cases)
         line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
