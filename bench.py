@@ -33,6 +33,8 @@ batched   : the batched sweep (256 seeded instances of uneven grid, Re and
             of 500-step runs, error of mixed vs FP64 per instance;
 ellipse   : the large single-instance configuration (1024x768 ellipse,
             Re 300), autotuned, mixed and plain FP64;
+long_run_accuracy: the cylinder over 1000 steps in both precisions: largest
+            drag and lift deviation of any step, velocity error at the end;
 reference_path: the REFERENCE-mode step (the reference's own scheme) at 52^2,
             130^2 and 514^2 cells, GPU and one CPU thread;
 served    : a seeded Poisson request stream through the continuous-batching
@@ -313,6 +315,28 @@ def served_lines(ifx, capi, cases, nreq, rate, budget):
     return res
 
 
+def long_run_accuracy(ifx, capi, cases, steps=1000):
+    """Mixed against plain FP64 over a long run of the cylinder (1000 steps, t = 5,
+    the impulsive start and the growth of the wake): the drag and lift of every
+    step from the device-side force history, and the velocity at the end."""
+    hist, fields = {}, {}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        cfg, xf, yf = cases.cylinder(precision=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.set_history(steps)
+        s.step(steps)
+        hist[name] = s.history(cap=steps)
+        fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+        s.close()
+    hm, h6 = hist["mixed"], hist["fp64"]
+    cd_err = float(np.max(np.abs(hm[:, 1] - h6[:, 1]) / np.maximum(np.abs(h6[:, 1]), 1e-12)))
+    cl_err = float(np.max(np.abs(hm[:, 2] - h6[:, 2])) / max(float(np.max(np.abs(h6[:, 1]))), 1e-12))
+    return {"workload": f"cylinder 384x256, Re 100, {steps} steps from the impulsive start, mixed vs plain FP64",
+            "steps": steps, "rel_l2_velocity_final": rel_l2(fields["mixed"], fields["fp64"]),
+            "cd_rel_err_max": cd_err, "cl_err_max_rel_to_cd": cl_err,
+            "cd_final": float(h6[-1, 1]), "cl_final": float(h6[-1, 2])}
+
+
 def ellipse_line(ifx, capi, cases, steps=10):
     """The large single-instance configuration: ellipse of aspect 0.2 and chord
     1 at 10 deg, 1024x768 cells on a 20x12 domain, Re 300, dt 2e-3; autotuned,
@@ -580,6 +604,7 @@ def main():
         line["served"] = served_lines(ifx, capi, cases, args.serve, args.rate, 64 << 30)
     if rank == 0 and world == 1:
         line["ellipse"] = ellipse_line(ifx, capi, cases)
+        line["long_run_accuracy"] = long_run_accuracy(ifx, capi, cases)
         line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)

@@ -174,6 +174,27 @@ def test_mixed_precision_close_to_fp64():
     assert abs(cda - cdb) <= 1e-3 * abs(cda)
 
 
+def test_mixed_precision_long_run_forces():
+    """Over 300 steps from the impulsive start, every step's drag and lift
+    (device-side force history) stay within 1e-3 of plain FP64 and the velocity
+    within 1e-6 relative L2: the FP32 sweeps' error does not accumulate."""
+    hist, vel = {}, {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        cfg, xf, yf = small_cylinder(prec=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.set_history(300)
+        s.step(300)
+        hist[prec] = s.history(cap=300)
+        vel[prec] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+    h6, hm = hist[capi.PREC_FP64], hist[capi.PREC_MIXED]
+    assert h6.shape[0] == 300 and np.array_equal(h6[:, 0], hm[:, 0])
+    scale = np.max(np.abs(h6[:, 1]))
+    assert np.max(np.abs(hm[:, 1] - h6[:, 1]) / np.abs(h6[:, 1])) <= 1e-3
+    assert np.max(np.abs(hm[:, 2] - h6[:, 2])) <= 1e-3 * scale
+    v6, vm = vel[capi.PREC_FP64], vel[capi.PREC_MIXED]
+    assert np.linalg.norm(vm - v6) / np.linalg.norm(v6) <= 1e-6
+
+
 @pytest.mark.parametrize("nx,ny", [(48, 200), (240, 40)])
 def test_anisotropic_grid_semicoarsening_vs_oracle(oracle, nx, ny):
     """Cells up to ~6:1 use semi-coarsened multigrid levels; same hierarchy,
