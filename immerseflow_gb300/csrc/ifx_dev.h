@@ -15,6 +15,8 @@
 #pragma once
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace ifx {
 
 constexpr int TILE_X = 32;
@@ -173,6 +175,11 @@ struct alignas(16) LevelDev {
     int inst, depth, dirmask;    // dirmask bit s: side s Dirichlet for pressure
     const double *kx, *ky, *ix, *iy, *dw, *dh;
     const float *kxf, *kyf, *ixf, *iyf, *dwf, *dhf;
+    // face coefficients of the pressure operator: (c_E, c_W) of column i =
+    // (kx[i] ix[i], kx[i-1] ix[i]) and (c_N, c_S) of row j = (ky[j] iy[j],
+    // ky[j-1] iy[j]), the products formed once in the level's precision
+    const double2 *cew, *cns;
+    const float2 *cewf, *cnsf;
     const uint8_t* bits;
     void* e;   // correction, T*
     void* e2;  // Jacobi partner, T*

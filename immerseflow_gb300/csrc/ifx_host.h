@@ -26,6 +26,8 @@ struct HostLevel {
     // device
     double *d_kx = nullptr, *d_ky = nullptr, *d_ix = nullptr, *d_iy = nullptr, *d_dw = nullptr, *d_dh = nullptr;
     float *d_kxf = nullptr, *d_kyf = nullptr, *d_ixf = nullptr, *d_iyf = nullptr, *d_dwf = nullptr, *d_dhf = nullptr;
+    double2 *d_cew = nullptr, *d_cns = nullptr;
+    float2 *d_cewf = nullptr, *d_cnsf = nullptr;
     uint8_t* d_bits = nullptr;
     void *d_e = nullptr, *d_e2 = nullptr, *d_r = nullptr;
     int *d_pI = nullptr, *d_pIn = nullptr, *d_pJ = nullptr, *d_pJn = nullptr;

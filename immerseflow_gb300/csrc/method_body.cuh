@@ -61,6 +61,8 @@ template <> struct LvA<double> {
     static __device__ __forceinline__ const double* dh(const LevelDev& L) { return L.dh; }
     static __device__ __forceinline__ const double* pwx(const LevelDev& L) { return L.pwx; }
     static __device__ __forceinline__ const double* pwy(const LevelDev& L) { return L.pwy; }
+    static __device__ __forceinline__ const double2* cew(const LevelDev& L) { return L.cew; }
+    static __device__ __forceinline__ const double2* cns(const LevelDev& L) { return L.cns; }
 };
 template <> struct LvA<float> {
     static __device__ __forceinline__ const float* kx(const LevelDev& L) { return L.kxf; }
@@ -71,6 +73,8 @@ template <> struct LvA<float> {
     static __device__ __forceinline__ const float* dh(const LevelDev& L) { return L.dhf; }
     static __device__ __forceinline__ const float* pwx(const LevelDev& L) { return L.pwxf; }
     static __device__ __forceinline__ const float* pwy(const LevelDev& L) { return L.pwyf; }
+    static __device__ __forceinline__ const float2* cew(const LevelDev& L) { return L.cewf; }
+    static __device__ __forceinline__ const float2* cns(const LevelDev& L) { return L.cnsf; }
 };
 
 __device__ __forceinline__ void tile_ij(const Tile& t, int& i, int& j) {
@@ -195,13 +199,9 @@ struct LapCoef {
 };
 template <typename TC>
 __device__ __forceinline__ LapCoef<TC> lap_coef(const LevelDev& L, int i, int j, uint8_t bt) {
-    const TC* kx = LvA<TC>::kx(L);
-    const TC* ky = LvA<TC>::ky(L);
-    const TC* ix = LvA<TC>::ix(L);
-    const TC* iy = LvA<TC>::iy(L);
-    const TC ixi = __ldg(&ix[i]), iyj = __ldg(&iy[j]);
-    const TC cE = __ldg(&kx[i]) * ixi, cW = __ldg(&kx[i - 1]) * ixi;
-    const TC cN = __ldg(&ky[j]) * iyj, cS = __ldg(&ky[j - 1]) * iyj;
+    const auto ew = __ldg(&LvA<TC>::cew(L)[i]);
+    const auto ns = __ldg(&LvA<TC>::cns(L)[j]);
+    const TC cE = ew.x, cW = ew.y, cN = ns.x, cS = ns.y;
     LapCoef<TC> c;
     c.ce = (bt & B_E) ? cE : (TC)0;
     c.cw = (bt & B_W) ? cW : (TC)0;
@@ -1053,11 +1053,14 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
 }
 
 // Multigrid tile phases.  A tile is 32 columns by 8R rows of one level of
-// one instance; thread (w, lane) handles column i0+lane of rows j0+w+8r,
-// r < R.  Every load uses indices clamped into the level's interior, so all
-// of a thread's loads issue together (no load waits on the stencil byte);
-// results are stored for live cells only.  The arithmetic per cell does not
-// depend on R.
+// one instance.  In the phases without reductions (smoothing, restriction)
+// thread (w, lane) handles column i0+lane of the R consecutive rows from
+// j0+R*w: it loads its column once on rows j0+R*w-1 .. j0+R*w+R and takes
+// the north and south values from there.  Every load uses indices clamped
+// into the level's rows (ghost rows included) and columns, so all of a
+// thread's loads issue together (no load waits on the stencil byte);
+// results are stored for live cells only, each from the same operands and
+// arithmetic whatever R and the row assignment.
 
 // Weighted-Jacobi sweep.  flags: 1 = start from e = 0.
 template <typename T, int R = 1>
@@ -1067,25 +1070,32 @@ __device__ __forceinline__ void smooth_tile(const Tile& t, const LevelDev& L, co
     T* dst = (T*)(src_alt ? L.e : L.e2);
     const T* rr = (const T*)L.r;
     const int P = L.pitch;
-    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + (int)(threadIdx.x >> 5);
+    const int i = t.i0 + (int)(threadIdx.x & 31), jb = t.j0 + R * (int)(threadIdx.x >> 5);
     const int ic = clampi(i, 1, L.NX);
-    int id[R], jcs[R];
+    T col[R + 2];  // column ic on rows jb-1 .. jb+R
+#pragma unroll
+    for (int k = 0; k < R + 2; k++) col[k] = src[ic + clampi(jb - 1 + k, 0, L.NY + 1) * P];
+    int id[R];
     uint8_t bt[R];
     T val[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int j = jb + 8 * r, jc = clampi(j, 1, L.NY);
-        jcs[r] = jc;
+        const int j = jb + r, jc = clampi(j, 1, L.NY);
         id[r] = ic + jc * P;
         bt[r] = (i == ic && j == jc) ? __ldg(&L.bits[id[r]]) : (uint8_t)0;
     }
+    auto fetch = [src](int q) { return (T)src[q]; };
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int jc = jcs[r];
+        const int jc = clampi(jb + r, 1, L.NY);
+        const T eE = src[id[r] + 1], eW = src[id[r] - 1];
         T Le, D;
-        if (L.depth == 0) lap_p<T, T, true>(L, src, ic, jc, id[r], P, bt[r], G, gidx, Le, D);
-        else lap_p<T, T, false>(L, src, ic, jc, id[r], P, bt[r], G, nullptr, Le, D);
-        val[r] = (flags & 1) ? jacobi_from_zero<T>(rr[id[r]], D, om) : jacobi_update<T>(src[id[r]], rr[id[r]], Le, D, om);
+        if (L.depth == 0)
+            lap_vals<T, true>(L, ic, jc, id[r], P, bt[r], G, gidx, eE, eW, col[r + 2], col[r], col[r + 1], fetch, Le, D);
+        else
+            lap_vals<T, false>(L, ic, jc, id[r], P, bt[r], G, nullptr, eE, eW, col[r + 2], col[r], col[r + 1], fetch,
+                               Le, D);
+        val[r] = (flags & 1) ? jacobi_from_zero<T>(rr[id[r]], D, om) : jacobi_update<T>(col[r + 1], rr[id[r]], Le, D, om);
     }
     if (state != ST_ACTIVE) return;
 #pragma unroll
@@ -1111,16 +1121,18 @@ __device__ __forceinline__ void b_smooth_grid(const GridTiles& g, const InstStat
 // Restriction of the fine residual (area weighted) onto the coarse level,
 // fused with the first (zero-start) smoothing sweep of a middle coarse level.
 // One thread per FINE cell: tiles of the fine level start at (1, 1), so the
-// fine cells of a coarse cell share a tile (lanes 2k, 2k+1 when x is coarsened,
-// warps 2w, 2w+1 when y is); each thread forms (r - L e) dA of its cell, pairs
-// are summed in x by shuffle and then in y through shared memory (order:
-// (t00 + t10) + (t01 + t11), as the oracle), and the thread of the first child
-// writes the coarse cell.
+// fine cells of a coarse cell share a tile (lanes 2k, 2k+1 when x is
+// coarsened; when y is, rows 2J-1, 2J are a thread's consecutive rows for
+// R > 1 and warps 2w, 2w+1 for R = 1); each thread forms (r - L e) dA of its
+// cells, pairs are summed in x by shuffle and then in y (in registers, or
+// through shared memory for R = 1) in the order (t00 + t10) + (t01 + t11), as
+// the oracle, and the thread of the first child writes the coarse cell.
 template <typename T, int R = 1>
 __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                            const GhostDev* __restrict__ G, int fine_alt, int vb) {
-    __shared__ T rows[R][TILE_Y][TILE_X];
+    static_assert(R == 1 || R % 2 == 0, "rows per thread: 1 or even");
+    __shared__ T rows[TILE_Y][TILE_X];
     const Tile t = ldg_struct(&tiles[vb]);
     const LevelDev& F = LV[t.lev];
     if (!tile_live(t, F, S)) return;
@@ -1130,52 +1142,65 @@ __device__ __forceinline__ void b_restrict(const Tile* __restrict__ tiles, const
     const int* gidx = F.depth == 0 ? I[t.inst].gidx : nullptr;
     const int FP = F.pitch, cx = C.cx, cy = C.cy;
     const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
-    const int i = t.i0 + lane;
-    const bool inx = i <= F.NX;
-    const int ic = inx ? i : F.NX;
+    const int i = t.i0 + lane, jb = t.j0 + R * w;
+    const int ic = clampi(i, 1, F.NX);
+    T col[R + 2];  // column ic on rows jb-1 .. jb+R
+#pragma unroll
+    for (int k = 0; k < R + 2; k++) col[k] = fe[ic + clampi(jb - 1 + k, 0, F.NY + 1) * FP];
     bool in[R];
-    int id[R], jcs[R];
+    int id[R];
     uint8_t fb[R];
     T term[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        const int j = t.j0 + w + 8 * r;
-        in[r] = inx && j <= F.NY;
-        jcs[r] = j <= F.NY ? j : F.NY;
-        id[r] = ic + jcs[r] * FP;
+        const int j = jb + r;
+        in[r] = i <= F.NX && j <= F.NY;
+        id[r] = ic + clampi(j, 1, F.NY) * FP;
         fb[r] = in[r] ? __ldg(&F.bits[id[r]]) : (uint8_t)0;
     }
+    auto fetch = [fe](int q) { return (T)fe[q]; };
 #pragma unroll
     for (int r = 0; r < R; r++) {
+        const int jc = clampi(jb + r, 1, F.NY);
+        const T eE = fe[id[r] + 1], eW = fe[id[r] - 1];
         T Le, D;
-        if (F.depth == 0) lap_p<T, T, true>(F, fe, ic, jcs[r], id[r], FP, fb[r], G, gidx, Le, D);
-        else lap_p<T, T, false>(F, fe, ic, jcs[r], id[r], FP, fb[r], G, nullptr, Le, D);
-        term[r] = (fb[r] & 0x0F) ? (fr[id[r]] - Le) * (__ldg(&LvA<T>::dw(F)[ic]) * __ldg(&LvA<T>::dh(F)[jcs[r]])) : (T)0;
+        if (F.depth == 0)
+            lap_vals<T, true>(F, ic, jc, id[r], FP, fb[r], G, gidx, eE, eW, col[r + 2], col[r], col[r + 1], fetch, Le, D);
+        else
+            lap_vals<T, false>(F, ic, jc, id[r], FP, fb[r], G, nullptr, eE, eW, col[r + 2], col[r], col[r + 1], fetch,
+                               Le, D);
+        term[r] = (fb[r] & 0x0F) ? (fr[id[r]] - Le) * (__ldg(&LvA<T>::dw(F)[ic]) * __ldg(&LvA<T>::dh(F)[jc])) : (T)0;
     }
     // x pairs: (2I-1, 2I) are lanes (2k, 2k+1); the even lane keeps t0 + t1
     if (cx == 2) {
 #pragma unroll
         for (int r = 0; r < R; r++) term[r] = term[r] + __shfl_xor_sync(0xffffffffu, term[r], 1);
     }
-    // y pairs: rows (2J-1, 2J) are warps (2m, 2m+1)
-    if (cy == 2) {
-        if (w & 1) {
-#pragma unroll
-            for (int r = 0; r < R; r++) rows[r][w][lane] = term[r];
+    // y pairs: rows (2J-1, 2J)
+    bool first[R];  // this row is the first child row of its coarse cell
+    if (R == 1) {
+        // warps (2m, 2m+1)
+        if (cy == 2) {
+            if (w & 1) rows[w][lane] = term[0];
+            __syncthreads();
+            if (!(w & 1)) term[0] = term[0] + rows[w + 1][lane];
         }
-        __syncthreads();
-        if (!(w & 1)) {
+        first[0] = cy != 2 || !(w & 1);
+    } else {
+        // the thread's rows (2m, 2m+1)
 #pragma unroll
-            for (int r = 0; r < R; r++) term[r] = term[r] + rows[r][w + 1][lane];
+        for (int r = 0; r < R; r++) {
+            first[r] = cy != 2 || !(r & 1);
+            if (cy == 2 && !(r & 1)) term[r] = term[r] + term[r + 1];
         }
     }
-    if ((cx == 2 && (lane & 1)) || (cy == 2 && (w & 1))) return;
+    if (cx == 2 && (lane & 1)) return;
     T* rc = (T*)C.r;
     const T om = (T)I[t.inst].omega;
 #pragma unroll
     for (int r = 0; r < R; r++) {
-        if (!in[r]) continue;
-        const int j = t.j0 + w + 8 * r;
+        if (!in[r] || !first[r]) continue;
+        const int j = jb + r;
         const int I0 = cx == 2 ? (i + 1) >> 1 : i, J0 = cy == 2 ? (j + 1) >> 1 : j;
         const int cid = I0 + J0 * C.pitch;
         const uint8_t cb = __ldg(&C.bits[cid]);

@@ -123,6 +123,20 @@ std::vector<float> to_f(const std::vector<double>& v) {
     return r;
 }
 
+// Face-coefficient pairs of one direction: (k[i] inv[i], k[i-1] inv[i]) with
+// both factors first rounded to T, so that each product is the one the
+// kernels would form from the T copies of k and inv.
+template <typename T, typename V2>
+std::vector<V2> face_pairs(const std::vector<double>& k, const std::vector<double>& inv) {
+    std::vector<V2> r(k.size());
+    for (size_t i = 0; i < k.size(); i++) {
+        const T ii = (T)inv[i];
+        r[i].x = (T)k[i] * ii;
+        r[i].y = i > 0 ? (T)k[i - 1] * ii : (T)0;
+    }
+    return r;
+}
+
 int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 // ------------------------------------------------------------- grid
@@ -781,6 +795,10 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             IFX_TRY(dupload(S, &L.d_kxf, to_f(L.kx))); IFX_TRY(dupload(S, &L.d_kyf, to_f(L.ky)));
             IFX_TRY(dupload(S, &L.d_ixf, to_f(L.ix))); IFX_TRY(dupload(S, &L.d_iyf, to_f(L.iy)));
             IFX_TRY(dupload(S, &L.d_dwf, to_f(L.dw))); IFX_TRY(dupload(S, &L.d_dhf, to_f(L.dh)));
+            IFX_TRY(dupload(S, &L.d_cew, face_pairs<double, double2>(L.kx, L.ix)));
+            IFX_TRY(dupload(S, &L.d_cns, face_pairs<double, double2>(L.ky, L.iy)));
+            IFX_TRY(dupload(S, &L.d_cewf, face_pairs<float, float2>(L.kx, L.ix)));
+            IFX_TRY(dupload(S, &L.d_cnsf, face_pairs<float, float2>(L.ky, L.iy)));
             IFX_TRY(dupload(S, &L.d_bits, L.bits));
             if (S->prec == IFX_PREC_FP64) IFX_TRY(alloc_level_fields<double>(S, L));
             else IFX_TRY(alloc_level_fields<float>(S, L));
@@ -799,6 +817,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ld.dirmask = I.dirmask;
             ld.kx = L.d_kx; ld.ky = L.d_ky; ld.ix = L.d_ix; ld.iy = L.d_iy; ld.dw = L.d_dw; ld.dh = L.d_dh;
             ld.kxf = L.d_kxf; ld.kyf = L.d_kyf; ld.ixf = L.d_ixf; ld.iyf = L.d_iyf; ld.dwf = L.d_dwf; ld.dhf = L.d_dhf;
+            ld.cew = L.d_cew; ld.cns = L.d_cns; ld.cewf = L.d_cewf; ld.cnsf = L.d_cnsf;
             ld.bits = L.d_bits;
             ld.e = L.d_e; ld.e2 = L.d_e2; ld.r = L.d_r;
             ld.pI = L.d_pI; ld.pIn = L.d_pIn; ld.pJ = L.d_pJ; ld.pJn = L.d_pJn;
