@@ -16,6 +16,8 @@ IFX_ERR_DIVERGED = 7
 IFX_ERR_BUDGET = 8
 IFX_ERR_STATE = 9
 IFX_ERR_NODEVICE = 10
+IFX_ERR_GEOMETRY = 11
+MOTION_NONE, MOTION_PRESCRIBED = 0, 1
 PPE_JACOBI, PPE_POINT_GS, PPE_LINE_SOR = 0, 1, 2
 
 MODE_REFERENCE = 0
@@ -66,6 +68,10 @@ class Config(C.Structure):
         ("mixed_inner", C.c_int),
         ("force_ref_u", C.c_double), ("force_ref_len", C.c_double),
         ("ppe_method", C.c_int), ("relax_ad", C.c_double), ("relax_ppe", C.c_double),
+        ("motion", C.c_int), ("motion_u", C.c_double), ("motion_v", C.c_double),
+        ("motion_amp_x", C.c_double), ("motion_amp_y", C.c_double), ("motion_amp_deg", C.c_double),
+        ("motion_freq", C.c_double),
+        ("motion_phase_x", C.c_double), ("motion_phase_y", C.c_double), ("motion_phase_deg", C.c_double),
         ("xgrid", C.c_char * PATH_MAX), ("ygrid", C.c_char * PATH_MAX),
     ]
 

@@ -1,8 +1,9 @@
 """Build the CUDA library (libimmerseflow_gb300.so) and the CLI in-tree.
 
 One -gencode for sm_103a, translation units compiled in parallel.  The
-immersed-boundary set-up file is compiled with -fmad=false so that tagging
-and image-point weights are reproducible bit for bit on the CPU.
+immersed-boundary files (set-up, and the per-step geometry of moving bodies)
+are compiled with -fmad=false so that tagging, image-point weights and the
+body pose are reproducible bit for bit on the CPU.
 """
 import os
 import subprocess
@@ -25,6 +26,7 @@ SOURCES = [
     ("kernels_persist.cu", []),
     ("kernels_cluster.cu", []),
     ("kernels_ibm.cu", ["-fmad=false"]),
+    ("kernels_move.cu", ["-fmad=false"]),
     ("kernels_ref.cu", []),
     ("solver.cu", []),
     ("io.cpp", ["-x", "cu"]),

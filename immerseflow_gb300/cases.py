@@ -95,6 +95,19 @@ def external(nx, ny, lx, ly, cx, cy, a, b, angle_deg, re, dt, precision=capi.PRE
     return c, tanh_faces(nx, lx, cx, ratio, width), tanh_faces(ny, ly, cy, ratio, width)
 
 
+def set_motion(c, u=0.0, v=0.0, amp_x=0.0, amp_y=0.0, amp_deg=0.0, freq=0.0, phase_x=0.0, phase_y=0.0,
+               phase_deg=0.0):
+    """Prescribed rigid motion of the configuration's body: centre
+    (body_cx + u t + amp_x (sin(2 pi (freq t + phase_x/360)) - sin(2 pi phase_x/360)),
+    likewise y), angle likewise with amp_deg and phase_deg."""
+    c.motion = capi.MOTION_PRESCRIBED
+    c.motion_u, c.motion_v = u, v
+    c.motion_amp_x, c.motion_amp_y, c.motion_amp_deg = amp_x, amp_y, amp_deg
+    c.motion_freq = freq
+    c.motion_phase_x, c.motion_phase_y, c.motion_phase_deg = phase_x, phase_y, phase_deg
+    return c
+
+
 def cylinder(nx=384, ny=256, re=100.0, dt=5e-3, precision=capi.PREC_FP64):
     return external(nx, ny, 30.0, 20.0, 10.0, 10.0, 0.5, 0.5, 0.0, re, dt, precision)
 

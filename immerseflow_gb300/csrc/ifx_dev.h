@@ -181,6 +181,7 @@ struct alignas(16) LevelDev {
     const double2 *cew, *cns;
     const float2 *cewf, *cnsf;
     const uint8_t* bits;
+    uint8_t* act;  // coarse level of a moving body's instance: cells taking part (else null)
     void* e;   // correction, T*
     void* e2;  // Jacobi partner, T*
     void* r;   // right-hand side, T*
@@ -260,6 +261,18 @@ struct alignas(16) InstDev {
     const unsigned char* sub_img;
     int sub_img_bytes;
     int hist_cap, hist_w, nprobe;
+    // prescribed body motion: the pose at t = nstep dt follows from these
+    // (centre x0 + u t + ax (sin(2 pi (f t + phx)) - sin(2 pi phx)), likewise y
+    // and the angle; angles and phases in turns, w = 2 pi f); bcx, bcy, bcs,
+    // bsn above hold the current pose and bu, bv, bw the current velocity of
+    // the centre and the rotation rate
+    int moving;
+    int ibm_beg, ibm_cap;        // this instance's IBM ghost slots in the ghost table
+    int sub_lb;                  // LevelDev offset (from lev0) of the first sub-cycle level, 0: none
+    double mo_x0, mo_y0, mo_th0, mo_u, mo_v, mo_ax, mo_ay, mo_ath, mo_f, mo_w, mo_phx, mo_phy, mo_pha;
+    double bu, bv, bw;
+    int* fresh;                  // step in which the cell last turned fluid (0: never)
+    const double* fsb;           // body-frame force samples: lx, ly, nlx, nly, ds each
 };
 
 // Device-resident per-instance iteration state and diagnostics.
@@ -273,6 +286,10 @@ struct InstState {
     double rel_restart;                       // mixed path: true relative residual at the last restart
     long long nstep;                          // time steps this instance has done
     long long hist_n;                         // time-history records written
+    // moving body: cell box (i0, i1, j0, j1) of the body at the current pose,
+    // IBM ghosts in use, and a geometry error (1 left the domain, 2 ghost slots full)
+    int bb[4];
+    int n_ibm, geo_err;
 };
 
 // Loop control for device-side convergence: reduce kernels vote, the last

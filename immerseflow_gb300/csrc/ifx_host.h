@@ -29,6 +29,7 @@ struct HostLevel {
     double2 *d_cew = nullptr, *d_cns = nullptr;
     float2 *d_cewf = nullptr, *d_cnsf = nullptr;
     uint8_t* d_bits = nullptr;
+    uint8_t* d_act = nullptr;        // coarse levels of a moving body's instance
     void *d_e = nullptr, *d_e2 = nullptr, *d_r = nullptr;
     int *d_pI = nullptr, *d_pIn = nullptr, *d_pJ = nullptr, *d_pJn = nullptr;
     double *d_pwx = nullptr, *d_pwy = nullptr;
@@ -49,6 +50,8 @@ struct Instance {
     int dirmask = 0;
     double cs = 1.0, sn = 0.0, ia2 = 1.0, ib2 = 1.0;
     int qstride = 0;
+    bool moving = false;             // prescribed body motion: geometry redone every step
+    int ibm_beg = 0, ibm_cap = 0;    // its IBM ghost slots in the ghost table
     InstDev dev{};                   // device pointers (host copy of the InstDev entry)
 };
 
@@ -84,6 +87,10 @@ struct ifx_solver {
     ifx::GhostDev* dG = nullptr;
     int ng = 0, nibm = 0;
     int* dIbm = nullptr;             // global indices of IBM ghost entries
+    int* dMv = nullptr;              // instances with a moving body
+    int nmv = 0;
+    int* dMvSlots = nullptr;         // their IBM ghost slots (global indices)
+    int nmvslots = 0;
     double* dGval = nullptr;         // ghost gather scratch, 3 per entry
     double* dBiIp = nullptr;         // BI/IP per IBM ghost (diagnostics, tests)
     ifx::Tile* dT0 = nullptr;        // finest-level tiles of every instance

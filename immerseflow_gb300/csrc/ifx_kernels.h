@@ -95,6 +95,10 @@ cudaError_t launch_tag(const InstDev* I, int inst, int n_cells, uint8_t* type, c
 cudaError_t launch_mark_ghosts(const InstDev* I, int inst, int n_interior, uint8_t* type, cudaStream_t s);
 cudaError_t launch_ghost_weights(GhostDev* G, const int* ibm, int nibm, const InstDev* I, double* bi_ip,
                                  cudaStream_t s);
+// ---- moving bodies (kernels_move.cu)
+cudaError_t launch_move_geometry(InstDev* I, InstState* S, const LevelDev* LV, GhostDev* G, const int* mv, int nmv,
+                                 cudaStream_t s);
+cudaError_t launch_move_init(InstDev* I, InstState* S, const int* mv, int nmv, const int* n_ibm, cudaStream_t s);
 
 // ---- reference path (kernels_ref.cu), one instance, dense rows (pitch = nx)
 struct RefDev {

@@ -45,6 +45,7 @@ extern "C" const char* ifx_status_string(ifx_status s) {
         case IFX_ERR_BUDGET: return "HBM budget exceeded";
         case IFX_ERR_STATE: return "invalid state";
         case IFX_ERR_NODEVICE: return "no CUDA device";
+        case IFX_ERR_GEOMETRY: return "moving body left the domain or outgrew its ghost slots";
     }
     return "unknown status";
 }

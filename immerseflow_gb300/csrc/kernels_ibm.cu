@@ -16,19 +16,11 @@
 // ghost list and the weights match the CPU restatement bit for bit.
 #include <cuda_runtime.h>
 
+#include "ibm_geom.cuh"
 #include "ifx_dev.h"
 #include "ifx_kernels.h"
 
 namespace ifx {
-
-__device__ __forceinline__ int inside_body(const InstDev& in, double x, double y) {
-    const double ddx = __dsub_rn(x, in.bcx);
-    const double ddy = __dsub_rn(y, in.bcy);
-    const double xr = __dadd_rn(__dmul_rn(ddx, in.bcs), __dmul_rn(ddy, in.bsn));
-    const double yr = __dsub_rn(__dmul_rn(ddy, in.bcs), __dmul_rn(ddx, in.bsn));
-    const double f = __dadd_rn(__dmul_rn(__dmul_rn(xr, xr), in.bia2), __dmul_rn(__dmul_rn(yr, yr), in.bib2));
-    return f < 1.0 ? 1 : 0;
-}
 
 __global__ void k_tag(const InstDev* __restrict__ I, int inst, uint8_t* __restrict__ type) {
     const InstDev& in = I[inst];
@@ -162,22 +154,12 @@ __device__ bool solve4(double m[4][4], const double rhs[4], double out[4]) {
     return true;
 }
 
-// last index in [1, n-2] with c[idx] <= x (0 if none), as std::upper_bound - 1
-__device__ __forceinline__ int ub_index(const double* c, int n, double x) {
-    int lo = 1, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (c[mid] <= x) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo - 1;
-}
-
 __global__ void k_ghost_weights(GhostDev* __restrict__ G, const int* __restrict__ ibm, int nibm,
                                 const InstDev* __restrict__ I, double* __restrict__ bi_ip) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nibm) return;
     GhostDev& g = G[ibm[q]];
+    if (g.cell < 0) return;  // an unused slot of a moving body's instance
     const InstDev& in = I[g.inst];
     const int P = in.pitch, nx = in.nx, ny = in.ny;
     const int i = g.cell % P, j = g.cell / P;
@@ -260,7 +242,17 @@ __global__ void k_ghost_weights(GhostDev* __restrict__ G, const int* __restrict_
         g.wv[k] = -wD[k];
         g.wp[k] = (in.type[g.nb[k]] != T_GHOST) ? wN[k] / keep : 0.0;
     }
+    // Dirichlet value at BI: the wall velocity (zero for a body at rest).  The
+    // ghost is q_G = 2 q_BI - q_IP with q_IP = w_G q_BI + sum_k w_k q_k when G
+    // is a node of the image-point cell (w_G = 0 otherwise), so its constant is
+    // (2 - w_G) q_BI.
     g.cu = g.cv = 0.0;
+    if (in.moving) {
+        const double wg = 2.0 - (gk >= 0 ? wD[gk] : 0.0);
+        const double ub = in.bu - in.bw * (BIy - in.bcy), vb = in.bv + in.bw * (BIx - in.bcx);
+        g.cu = wg * ub;
+        g.cv = wg * vb;
+    }
 }
 
 cudaError_t launch_tag(const InstDev* I, int inst, int n_cells, uint8_t* type, cudaStream_t s) {

@@ -175,9 +175,10 @@ __device__ __forceinline__ double ghost_const(const GhostDev& g, const double* q
 // cells only, so this is an exact linear function of the fluid values.
 template <typename TC, typename Fetch>
 __device__ __forceinline__ TC ghost_eval_f(const GhostDev* G, int gid, Fetch fetch, int self, TC& ws) {
-    const GhostDev& g = G[gid];
     TC acc = (TC)0;
     ws = (TC)0;
+    if (gid < 0) return acc;  // a moving body's ghost beyond its slots (instance retired after the step)
+    const GhostDev& g = G[gid];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const TC w = (TC)g.wp[k];
@@ -352,6 +353,7 @@ __device__ __forceinline__ void b_ghost_gather(const GhostDev* __restrict__ G, i
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const GhostDev& gh = G[g];
+    if (gh.cell < 0) return;  // unused slot of a moving body
     const InstDev& in = I[gh.inst];
     if (in.retired) return;
     if (comps & 1) {
@@ -379,6 +381,7 @@ __device__ __forceinline__ void b_ghost_scatter(const GhostDev* __restrict__ G, 
     int g = vb * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const GhostDev& gh = G[g];
+    if (gh.cell < 0) return;
     const InstDev& in = I[gh.inst];
     if (in.retired) return;
     if (comps & 1) in.u[gh.cell] = gval[3 * (size_t)g];
@@ -415,7 +418,8 @@ __device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const
     const double vn = v[id] * gyj + v[id + P] * fyj, vs = v[id - P] * gys + v[id] * fys;
     const double Nu = (ue * Ue - uw * Uw) * ixi + (un * Vn - us * Vs) * iyj;
     const double Nv = (ve * Ue - vw * Uw) * ixi + (vn * Vn - vs * Vs) * iyj;
-    const bool ab2 = S[t.inst].have_nold != 0;
+    // AB2, Euler on the first step and in cells that turned fluid in this step
+    const bool ab2 = S[t.inst].have_nold != 0 && !(in.fresh && in.fresh[id] == (int)S[t.inst].nstep);
     const double cu = ab2 ? 1.5 * Nu - 0.5 * in.Nu[id] : Nu;
     const double cv = ab2 ? 1.5 * Nv - 0.5 * in.Nv[id] : Nv;
     in.ru[id] = u[id] - in.dt * cu;
@@ -474,6 +478,7 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
         const GhostDev& gh = G[g];
+        if (gh.cell < 0) return;
         const InstDev& in = I[gh.inst];
         const int st = S[gh.inst].pred_state;
         if (st == ST_DONE) return;
@@ -594,6 +599,7 @@ __device__ __forceinline__ void b_pred_refresh(const Tile* __restrict__ tiles, i
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
         const GhostDev* gh = &G[g];
+        if (gh->cell < 0) return;
         const InstDev& in = I[gh->inst];
         if (in.retired) return;
         if (!finalize && !pred_refresh_due(in, S[gh->inst])) return;
@@ -668,6 +674,7 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
         const int g = ((int)vb - ntiles) * blockDim.x + threadIdx.x;
         if (g >= ng) return;
         const GhostDev& gh = G[g];
+        if (gh.cell < 0) return;
         const InstDev& in = I[gh.inst];
         const int st = S[gh.inst].pred_state;
         if (st == ST_DONE) return;
@@ -1838,8 +1845,15 @@ __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstStat
         for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
             const ForceSample f = ldg_struct(&in.fs[q]);
             const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
-            const double up = bil(in.u, f.c1, P, f.xi1, f.et1);
-            const double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
+            double up = bil(in.u, f.c1, P, f.xi1, f.et1);
+            double vp = bil(in.v, f.c1, P, f.xi1, f.et1);
+            if (in.moving) {
+                // velocity relative to the wall at the sample point
+                const double* b = in.fsb + 5 * (size_t)q;
+                const double rx = b[0] * in.bcs - b[1] * in.bsn, ry = b[0] * in.bsn + b[1] * in.bcs;
+                up = up - (in.bu - in.bw * ry);
+                vp = vp - (in.bv + in.bw * rx);
+            }
             F[0] += (-ps * f.nx + mu * up / f.del) * f.ds;
             F[1] += (-ps * f.ny + mu * vp / f.del) * f.ds;
         }

@@ -23,6 +23,7 @@
 
 #include "ifx_host.h"
 #include "ifx_kernels.h"
+#include "motion.h"
 
 using namespace ifx;
 
@@ -365,13 +366,31 @@ void build_levels(Instance& I) {
     }
 }
 
+// IBM ghost stub of cell id (weights follow on the device).
+GhostDev ibm_stub(int id, int inst) {
+    GhostDev g;
+    std::memset(&g, 0, sizeof(g));
+    g.cell = id;
+    g.inst = inst;
+    g.side = -1;
+    g.qi[0] = g.qi[1] = -1;
+    g.qown = -1;
+    g.adj = -1;
+    for (int k = 0; k < 4; k++) g.nb[k] = id;
+    return g;
+}
+
 // Domain ghost relations (wall/inflow/slip/outflow per side, corners from the
-// diagonal interior cell) and IBM ghost stubs, in row-major cell order.
+// diagonal interior cell) and IBM ghost stubs, in row-major cell order.  A
+// moving body's instance instead gets its IBM ghosts after the domain ghosts,
+// in a fixed number of slots (the current ghosts in row-major order, then
+// empty slots, cell -1) that the device refills every step.
 void build_ghosts(Instance& I, int inst, std::vector<GhostDev>& out, std::vector<int>& ibm_list) {
     const int nx = I.nx, ny = I.ny, P = I.pitch;
     const ifx_config& c = I.cfg;
     I.ghost_beg = (int)out.size();
     I.n_ibm = 0;
+    std::vector<int> ibm_cells;
     auto rule = [&](int side, int k_along, double* wu, double* wv, double* wp, double* cu, double* cv, int* qi,
                     double* qf) {
         const int bt = c.bc_type[side];
@@ -409,6 +428,10 @@ void build_ghosts(Instance& I, int inst, std::vector<GhostDev>& out, std::vector
             g.adj = -1;
             for (int k = 0; k < 4; k++) g.nb[k] = id;
             if (t == T_GHOST) {
+                if (I.moving) {
+                    ibm_cells.push_back(id);
+                    continue;
+                }
                 g.side = -1;
                 ibm_list.push_back((int)out.size());
                 I.n_ibm++;
@@ -458,12 +481,52 @@ void build_ghosts(Instance& I, int inst, std::vector<GhostDev>& out, std::vector
             }
             out.push_back(g);
         }
+    if (I.moving) {
+        // slots: four times the ghosts now, and at least four per finest cell
+        // width along the body's perimeter (Ramanujan's approximation)
+        double h = 1e300;
+        for (int i = 1; i <= I.NX; i++) h = std::min(h, I.dx[i]);
+        for (int j = 1; j <= I.NY; j++) h = std::min(h, I.dy[j]);
+        const double a = c.body_a, b = c.body_b;
+        const double per = M_PI * (3.0 * (a + b) - std::sqrt((3.0 * a + b) * (a + 3.0 * b)));
+        I.ibm_cap = (int)std::min(4.0 * I.NX * (double)I.NY,
+                                  std::max(4.0 * (double)ibm_cells.size(), 4.0 * per / h)) + 64;
+        I.ibm_beg = (int)out.size();
+        I.n_ibm = (int)ibm_cells.size();
+        for (int s = 0; s < I.ibm_cap; s++) {
+            GhostDev g = ibm_stub(s < I.n_ibm ? ibm_cells[s] : -1, inst);
+            ibm_list.push_back((int)out.size());
+            out.push_back(g);
+        }
+    }
     I.ghost_cnt = (int)out.size() - I.ghost_beg;
 }
 
-// Body-surface samples for drag/lift: parametric points on the ellipse,
-// outward normal, arc-length weight, and bilinear bases/weights of the
-// pressure sample and of the velocity probe (same formulas as the oracle).
+// Body-surface samples in the body frame: parametric point on the ellipse,
+// outward unit normal and arc-length weight (lx, ly, nlx, nly, ds) each.
+std::vector<double> force_body_frame(const Instance& I) {
+    const double a = I.cfg.body_a, b = I.cfg.body_b;
+    const double dth = 2.0 * M_PI / FORCE_SAMPLES;
+    std::vector<double> out(5 * (size_t)FORCE_SAMPLES);
+    for (int k = 0; k < FORCE_SAMPLES; k++) {
+        double t = dth * (k + 0.5);
+        double ct = std::cos(t), st = std::sin(t);
+        double nlx = ct / a, nly = st / b;
+        double nl = std::sqrt(nlx * nlx + nly * nly);
+        double* o = out.data() + 5 * (size_t)k;
+        o[0] = a * ct;
+        o[1] = b * st;
+        o[2] = nlx / nl;
+        o[3] = nly / nl;
+        o[4] = std::sqrt(a * a * st * st + b * b * ct * ct) * dth;
+    }
+    return out;
+}
+
+// Body-surface samples for drag/lift at the current pose: the body-frame
+// samples placed on the grid, with the bilinear bases/weights of the pressure
+// sample and of the velocity probe (same formulas as the oracle; the device
+// redoes them every step for a moving body).
 std::vector<ForceSample> build_force_table(const Instance& I) {
     std::vector<ForceSample> out;
     if (I.cfg.body != IFX_BODY_ELLIPSE) return out;
@@ -472,21 +535,14 @@ std::vector<ForceSample> build_force_table(const Instance& I) {
         int i0 = (int)(std::upper_bound(cc.begin() + 1, cc.begin() + n - 1, x) - cc.begin()) - 1;
         return std::min(std::max(i0, 0), n - 2);
     };
-    const double a = I.cfg.body_a, b = I.cfg.body_b;
-    const double dth = 2.0 * M_PI / FORCE_SAMPLES;
+    const std::vector<double> bf = force_body_frame(I);
     out.resize(FORCE_SAMPLES);
     for (int k = 0; k < FORCE_SAMPLES; k++) {
-        double t = dth * (k + 0.5);
-        double ct = std::cos(t), st = std::sin(t);
-        double lx = a * ct, ly = b * st;
-        double nlx = ct / a, nly = st / b;
-        double nl = std::sqrt(nlx * nlx + nly * nly);
-        nlx /= nl;
-        nly /= nl;
+        const double* o = bf.data() + 5 * (size_t)k;
+        double lx = o[0], ly = o[1], nlx = o[2], nly = o[3], ds = o[4];
         double xs = I.cfg.body_cx + lx * I.cs - ly * I.sn;
         double ys = I.cfg.body_cy + lx * I.sn + ly * I.cs;
         double nxw = nlx * I.cs - nly * I.sn, nyw = nlx * I.sn + nly * I.cs;
-        double ds = std::sqrt(a * a * st * st + b * b * ct * ct) * dth;
         int i0 = locate(I.xc, nx, xs), j0 = locate(I.yc, ny, ys);
         double h = std::max(I.dx[i0], I.dy[j0]);
         double del = 1.5 * h;
@@ -543,6 +599,19 @@ ifx_status validate(const ifx_config* c) {
     if (c->ppe_method != IFX_PPE_JACOBI)
         return set_error(IFX_ERR_ARG, "PPE-Method point-gs / line-sor selects the REFERENCE-mode pressure solve; "
                                       "method mode solves the pressure with multigrid-preconditioned BiCGSTAB");
+    if (c->motion != IFX_MOTION_NONE) {
+        if (c->motion != IFX_MOTION_PRESCRIBED) return set_error(IFX_ERR_ARG, "bad motion type");
+        if (c->body != IFX_BODY_ELLIPSE) return set_error(IFX_ERR_ARG, "body motion needs a body");
+        bool outflow = false;
+        for (int s = 0; s < 4; s++) outflow = outflow || c->bc_type[s] == IFX_BC_OUTFLOW;
+        // in a closed domain the pressure is fixed up to a constant by the
+        // fluid area, which a moving body changes
+        if (!outflow) return set_error(IFX_ERR_ARG, "a moving body needs an outflow side");
+        const double m[9] = {c->motion_u, c->motion_v, c->motion_amp_x, c->motion_amp_y, c->motion_amp_deg,
+                             c->motion_freq, c->motion_phase_x, c->motion_phase_y, c->motion_phase_deg};
+        for (double x : m)
+            if (!std::isfinite(x)) return set_error(IFX_ERR_ARG, "motion parameters must be finite");
+    }
     return IFX_OK;
 }
 
@@ -643,6 +712,16 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             I.ia2 = 1.0 / (I.cfg.body_a * I.cfg.body_a);
             I.ib2 = 1.0 / (I.cfg.body_b * I.cfg.body_b);
         }
+        I.moving = I.cfg.motion == IFX_MOTION_PRESCRIBED;
+        MotionDef mo{};
+        if (I.moving) {
+            // the pose at t = 0 from the same function as every later step
+            mo = motion_def(I.cfg);
+            const Pose p0 = pose_at(mo.x0, mo.y0, mo.th0, mo.u, mo.v, mo.ax, mo.ay, mo.ath, mo.f, mo.w, mo.phx, mo.phy,
+                                    mo.pha, 0.0);
+            I.cs = p0.c;
+            I.sn = p0.s;
+        }
         InstDev& d = I.dev;
         std::memset(&d, 0, sizeof(d));
         d.NX = I.NX; d.NY = I.NY; d.nx = I.nx; d.ny = I.ny; d.pitch = I.pitch;
@@ -661,6 +740,15 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         d.uc = I.cfg.outflow_uc;
         d.bcx = I.cfg.body_cx; d.bcy = I.cfg.body_cy; d.ba = I.cfg.body_a; d.bb = I.cfg.body_b;
         d.bcs = I.cs; d.bsn = I.sn; d.bia2 = I.ia2; d.bib2 = I.ib2;
+        if (I.moving) {
+            d.moving = 1;
+            d.mo_x0 = mo.x0; d.mo_y0 = mo.y0; d.mo_th0 = mo.th0; d.mo_u = mo.u; d.mo_v = mo.v;
+            d.mo_ax = mo.ax; d.mo_ay = mo.ay; d.mo_ath = mo.ath; d.mo_f = mo.f; d.mo_w = mo.w;
+            d.mo_phx = mo.phx; d.mo_phy = mo.phy; d.mo_pha = mo.pha;
+            int* fresh = nullptr;
+            IFX_TRY(dalloc(S, &fresh, I.ncell));
+            d.fresh = fresh;
+        }
         d.fref = 0.5 * I.cfg.force_ref_u * I.cfg.force_ref_u * I.cfg.force_ref_len;
         const size_t nc = I.ncell;
         IFX_TRY(dalloc(S, &d.u, nc)); IFX_TRY(dalloc(S, &d.v, nc));
@@ -750,7 +838,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         I.lev_base = (int)hLV.size();
         std::vector<int> gidx(I.ncell, -1);
         for (int g = I.ghost_beg; g < I.ghost_beg + I.ghost_cnt; g++)
-            if (hG[g].side < 0) gidx[hG[g].cell] = g;
+            if (hG[g].side < 0 && hG[g].cell >= 0) gidx[hG[g].cell] = g;
         int* gidx_d = nullptr;
         IFX_TRY(dupload(S, &gidx_d, gidx));
         d.gidx = gidx_d;
@@ -800,6 +888,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             IFX_TRY(dupload(S, &L.d_cewf, face_pairs<float, float2>(L.kx, L.ix)));
             IFX_TRY(dupload(S, &L.d_cnsf, face_pairs<float, float2>(L.ky, L.iy)));
             IFX_TRY(dupload(S, &L.d_bits, L.bits));
+            if (I.moving && l > 0) IFX_TRY(dupload(S, &L.d_act, L.act));
             if (S->prec == IFX_PREC_FP64) IFX_TRY(alloc_level_fields<double>(S, L));
             else IFX_TRY(alloc_level_fields<float>(S, L));
             if (l + 1 < nl) {
@@ -819,6 +908,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ld.kxf = L.d_kxf; ld.kyf = L.d_kyf; ld.ixf = L.d_ixf; ld.iyf = L.d_iyf; ld.dwf = L.d_dwf; ld.dhf = L.d_dhf;
             ld.cew = L.d_cew; ld.cns = L.d_cns; ld.cewf = L.d_cewf; ld.cnsf = L.d_cnsf;
             ld.bits = L.d_bits;
+            ld.act = L.d_act;
             ld.e = L.d_e; ld.e2 = L.d_e2; ld.r = L.d_r;
             ld.pI = L.d_pI; ld.pIn = L.d_pIn; ld.pJ = L.d_pJ; ld.pJn = L.d_pJn;
             ld.pwx = L.d_pwx; ld.pwy = L.d_pwy; ld.pwxf = L.d_pwxf; ld.pwyf = L.d_pwyf;
@@ -875,7 +965,15 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             ForceSample* fs_d = nullptr;
             if (!fs.empty()) IFX_TRY(dupload(S, &fs_d, fs));
             d.fs = fs_d;
+            if (I.moving) {
+                double* fsb = nullptr;
+                IFX_TRY(dupload(S, &fsb, force_body_frame(I)));
+                d.fsb = fsb;
+            }
         }
+        d.ibm_beg = I.ibm_beg;
+        d.ibm_cap = I.ibm_cap;
+        d.sub_lb = (lb >= 1 && lb < nl) ? lb : 0;
         d.kx = I.lev[0].d_kx; d.ky = I.lev[0].d_ky; d.ix = I.lev[0].d_ix; d.iy = I.lev[0].d_iy;
         hI[k] = d;
     }
@@ -946,6 +1044,26 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     // image-point weights of the IBM ghosts
     CUDA_TRY(launch_ghost_weights(S->dG, S->dIbm, S->nibm, S->dI, S->dBiIp, S->stream));
     S->launches++;
+    {   // moving bodies: their instances, their IBM ghost slots, body boxes
+        std::vector<int> mv, slots, nibm;
+        for (int k = 0; k < n; k++) {
+            const Instance& I = S->inst[k];
+            if (!I.moving) continue;
+            mv.push_back(k);
+            nibm.push_back(I.n_ibm);
+            for (int s = 0; s < I.ibm_cap; s++) slots.push_back(I.ibm_beg + s);
+        }
+        S->nmv = (int)mv.size();
+        S->nmvslots = (int)slots.size();
+        if (S->nmv) {
+            int* dn = nullptr;
+            IFX_TRY(dupload(S, &S->dMv, mv));
+            IFX_TRY(dupload(S, &S->dMvSlots, slots));
+            IFX_TRY(dupload(S, &dn, nibm));
+            CUDA_TRY(launch_move_init(S->dI, S->dS, S->dMv, S->nmv, dn, S->stream));
+            S->launches++;
+        }
+    }
     // initial field, outflow face values, ghosts and faces
     for (int k = 0; k < n; k++) {
         Instance& I = S->inst[k];
@@ -1082,6 +1200,11 @@ void seq_pre(Seq& q) {
     cudaStream_t st = S->stream;
     const int n = (int)S->inst.size();
     q.add(launch_step_begin(S->dI, S->dS, n, S->dCtl, st));
+    if (S->nmv) {
+        // moving bodies: geometry at the new pose, then the new ghosts' weights
+        q.add(launch_move_geometry(S->dI, S->dS, S->dLV, S->dG, S->dMv, S->nmv, st));
+        q.add(launch_ghost_weights(S->dG, S->dMvSlots, S->nmvslots, S->dI, nullptr, st));
+    }
     q.add(launch_outflow(S->dG, S->ng, S->dI, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;  // ghost fill is two kernels
@@ -1304,7 +1427,13 @@ ifx_status check_states(ifx_solver* S) {
         Instance& I = S->inst[k];
         if (I.dev.retired) continue;
         const InstState& s = S->hS[k];
-        if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric)) {
+        if (s.geo_err) {
+            // a moving body left the domain or outgrew its ghost slots
+            S->inst_status[k] = IFX_ERR_GEOMETRY;
+            I.dev.retired = 1;
+            CUDA_TRY(cudaMemcpyAsync(&S->dI[k].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
+            if (worst == IFX_OK) worst = IFX_ERR_GEOMETRY;
+        } else if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric)) {
             S->inst_status[k] = IFX_ERR_DIVERGED;
             I.dev.retired = 1;
             CUDA_TRY(cudaMemcpyAsync(&S->dI[k].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
@@ -1319,7 +1448,7 @@ ifx_status check_states(ifx_solver* S) {
 
 // Execution mode from IFX_EXEC: "persistent" (default when cooperative
 // launch is available), "graph", or "host" (IFX_NO_GRAPH=1 also selects host).
-int exec_mode(const ifx_solver* S) {
+int exec_mode_selected(const ifx_solver* S) {
     if (S->exec_override == 0 && S->persist_grid > 0) return 0;
     if (S->exec_override == 1 || S->exec_override == 2) return S->exec_override;
     const char* e = std::getenv("IFX_EXEC");
@@ -1328,6 +1457,12 @@ int exec_mode(const ifx_solver* S) {
     if (e && std::strcmp(e, "host") == 0) return 2;
     if (e && std::strcmp(e, "graph") == 0) return 1;
     return S->persist_grid > 0 ? 0 : 1;
+}
+// The persistent kernel has no phase for moving bodies: their solvers run as
+// a graph instead.
+int exec_mode(const ifx_solver* S) {
+    const int m = exec_mode_selected(S);
+    return (m == 0 && S->nmv > 0) ? 1 : m;
 }
 
 // Issues nsteps time steps on the solver's stream.  The host-loop mode reads
@@ -1384,6 +1519,8 @@ ifx_status step_finish(ifx_solver* S) {
         S->launches += (long long)nsteps * (S->graph_nodes_pre + pairs * S->graph_nodes_pred + S->graph_nodes_mid +
                                             bodies * S->graph_nodes_ppe + S->graph_nodes_post);
     }
+    if (st == IFX_ERR_GEOMETRY)
+        return set_error(st, "a moving body left the domain or outgrew its ghost slots (the instance is retired)");
     if (st != IFX_OK) return set_error(st, "non-finite value in the solver state (the instance is retired)");
     return IFX_OK;
 }
@@ -2000,6 +2137,12 @@ extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
     return IFX_OK;
 }
 
+// IBM ghosts of an instance now: a moving body's count is kept on the device.
+static int current_ibm(const ifx_solver* S, int inst) {
+    const Instance& I = S->inst[inst];
+    return (I.moving && S->hS && S->hS[inst].nstep > 0) ? S->hS[inst].n_ibm : I.n_ibm;
+}
+
 extern "C" ifx_status ifx_get_stats(ifx_solver* S, int inst, ifx_stats* out) {
     if (!S || !out || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_stats: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));
@@ -2027,7 +2170,7 @@ extern "C" ifx_status ifx_get_stats(ifx_solver* S, int inst, ifx_stats* out) {
     out->mass_flux_in = s.flux_in;
     out->mass_flux_out = s.flux_out;
     out->n_fluid = I.n_fluid;
-    out->n_ibm_ghost = I.n_ibm;
+    out->n_ibm_ghost = current_ibm(S, inst);
     out->mg_levels = (int)I.lev.size();
     out->status = inst < (int)S->inst_status.size() ? S->inst_status[inst] : IFX_OK;
     return IFX_OK;
@@ -2046,7 +2189,7 @@ extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* 
     if (!S || !count || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_ibm_ghosts: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));
     const Instance& I = S->inst[inst];
-    *count = (S->mode == IFX_MODE_METHOD) ? I.n_ibm : 0;
+    *count = (S->mode == IFX_MODE_METHOD) ? current_ibm(S, inst) : 0;
     if (*count == 0 || cap <= 0) return IFX_OK;
     CUDA_TRY(cudaSetDevice(S->device));
     std::vector<GhostDev> g(I.ghost_cnt);
@@ -2056,11 +2199,11 @@ extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* 
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     // position of this instance's first IBM ghost in the global IBM list
     int ibase = 0;
-    for (int k = 0; k < inst; k++) ibase += S->inst[k].n_ibm;
+    for (int k = 0; k < inst; k++) ibase += S->inst[k].moving ? S->inst[k].ibm_cap : S->inst[k].n_ibm;
     auto dense = [&](int c) { return (c % I.pitch) + (c / I.pitch) * I.nx; };
     int q = 0;
     for (const GhostDev& e : g) {
-        if (e.side >= 0) continue;
+        if (e.side >= 0 || e.cell < 0) continue;
         if (q >= cap) break;
         if (cells) cells[q] = dense(e.cell);
         for (int k = 0; k < 4; k++) {
@@ -2068,8 +2211,9 @@ extern "C" ifx_status ifx_get_ibm_ghosts(ifx_solver* S, int inst, int cap, int* 
             if (wu) wu[4 * q + k] = e.wu[k];
             if (wp) wp[4 * q + k] = e.wp[k];
         }
-        if (bi_ip)
-            for (int k = 0; k < 4; k++) bi_ip[4 * q + k] = bip[4 * (size_t)(ibase + q) + k];
+        if (bi_ip)  // recorded at creation: not kept for a moving body
+            for (int k = 0; k < 4; k++)
+                bi_ip[4 * q + k] = I.moving ? std::nan("") : bip[4 * (size_t)(ibase + q) + k];
         q++;
     }
     return IFX_OK;

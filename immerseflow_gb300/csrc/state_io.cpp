@@ -110,6 +110,14 @@ ifx_status check_inst(const ifx_solver* S, int inst, const char* fn) {
     if (!S || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, std::string(fn) + ": bad argument");
     return IFX_OK;
 }
+// The same for saving or restoring a state: the geometry of a moving body
+// (cell types, ghost slots, stencil bytes of every level) is not part of it.
+ifx_status check_restartable(const ifx_solver* S, int inst, const char* fn) {
+    SIO_TRY(check_inst(S, inst, fn));
+    if (S->inst[inst].moving)
+        return set_error(IFX_ERR_STATE, std::string(fn) + ": not supported for a moving body's instance");
+    return IFX_OK;
+}
 
 // The seven METHOD-mode cell arrays of a checkpoint, in order.
 void method_fields(const InstDev& d, double* (&f)[7]) {
@@ -166,14 +174,14 @@ bool read_file(const std::string& path, std::vector<char>& data) {
 // ------------------------------------------------------------ checkpoints
 
 extern "C" ifx_status ifx_checkpoint_bytes(const ifx_solver* S, int inst, size_t* bytes) {
-    SIO_TRY(check_inst(S, inst, "ifx_checkpoint_bytes"));
+    SIO_TRY(check_restartable(S, inst, "ifx_checkpoint_bytes"));
     if (!bytes) return set_error(IFX_ERR_ARG, "ifx_checkpoint_bytes: bad argument");
     *bytes = sizeof(CkptHeader) + payload_bytes(S, S->inst[inst]);
     return IFX_OK;
 }
 
 extern "C" ifx_status ifx_checkpoint_save(ifx_solver* S, int inst, void* buf, size_t n) {
-    SIO_TRY(check_inst(S, inst, "ifx_checkpoint_save"));
+    SIO_TRY(check_restartable(S, inst, "ifx_checkpoint_save"));
     size_t need = 0;
     SIO_TRY(ifx_checkpoint_bytes(S, inst, &need));
     if (!buf || n < need) return set_error(IFX_ERR_ARG, "ifx_checkpoint_save: buffer smaller than ifx_checkpoint_bytes");
@@ -224,7 +232,7 @@ extern "C" ifx_status ifx_checkpoint_save(ifx_solver* S, int inst, void* buf, si
 }
 
 extern "C" ifx_status ifx_checkpoint_load(ifx_solver* S, int inst, const void* buf, size_t n) {
-    SIO_TRY(check_inst(S, inst, "ifx_checkpoint_load"));
+    SIO_TRY(check_restartable(S, inst, "ifx_checkpoint_load"));
     if (!buf || n < sizeof(CkptHeader)) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_load: not a checkpoint (too short)");
     CkptHeader h;
     std::memcpy(&h, buf, sizeof(h));
@@ -365,7 +373,7 @@ extern "C" ifx_status ifx_write_snapshot_ascii(ifx_solver* S, int inst, const ch
 }
 
 extern "C" ifx_status ifx_read_snapshot_ascii(ifx_solver* S, int inst, const char* path) {
-    SIO_TRY(check_inst(S, inst, "ifx_read_snapshot_ascii"));
+    SIO_TRY(check_restartable(S, inst, "ifx_read_snapshot_ascii"));
     if (!path) return set_error(IFX_ERR_ARG, "ifx_read_snapshot_ascii: bad argument");
     std::ifstream in(path);
     if (!in) return set_error(IFX_ERR_IO, std::string("ifx_read_snapshot_ascii: cannot read ") + path);

@@ -40,6 +40,9 @@ typedef int ifx_status;
 #define IFX_ERR_BUDGET         8  /* request does not fit the HBM budget       */
 #define IFX_ERR_STATE          9  /* call not valid in the current state       */
 #define IFX_ERR_NODEVICE      10  /* no CUDA device                            */
+#define IFX_ERR_GEOMETRY      11  /* a moving body left the domain, or its IBM
+                                     ghosts outgrew their slots (the instance is
+                                     retired, like IFX_ERR_DIVERGED)            */
 
 /* ---------------------------------------------------------------- enums */
 #define IFX_MODE_REFERENCE 0  /* ADsolver-only semantics of the reference      */
@@ -85,6 +88,17 @@ typedef int ifx_status;
 #define IFX_PPE_POINT_GS 1    /* red-black point Gauss-Seidel / SOR (w-PPE)     */
 #define IFX_PPE_LINE_SOR 2    /* zebra x-line SOR, tridiagonal row solves (w-PPE) */
 
+/* Body motion (METHOD mode, ellipse body).  IFX_MOTION_PRESCRIBED moves the
+ * body rigidly: at time t = n dt (step n) the centre and the angle are
+ *   x(t) = body_cx + motion_u t + motion_amp_x (sin(w t + phx) - sin(phx))
+ *   y(t) = body_cy + motion_v t + motion_amp_y (sin(w t + phy) - sin(phy))
+ *   a(t) = body_angle_deg + motion_amp_deg (sin(w t + pha) - sin(pha))
+ * with w = 2 pi motion_freq and the phases in degrees, so that t = 0 is the
+ * configured pose.  The reference claims moving boundaries (README.md:7,11)
+ * but has no code for them. */
+#define IFX_MOTION_NONE       0
+#define IFX_MOTION_PRESCRIBED 1
+
 #define IFX_PATH_MAX 512
 
 /* --------------------------------------------------------------- config */
@@ -118,6 +132,11 @@ typedef struct ifx_config {
     double force_ref_u, force_ref_len;   /* drag/lift normalisation          */
     int    ppe_method;             /* IFX_PPE_*: REFERENCE-mode pressure solve  */
     double relax_ad, relax_ppe;    /* w-AD, w-PPE as read (0 or 1: none)        */
+    int    motion;                 /* IFX_MOTION_*                              */
+    double motion_u, motion_v;     /* constant velocity of the centre           */
+    double motion_amp_x, motion_amp_y, motion_amp_deg;  /* harmonic amplitudes  */
+    double motion_freq;            /* harmonic frequency (1/time)               */
+    double motion_phase_x, motion_phase_y, motion_phase_deg;  /* degrees        */
     char   xgrid[IFX_PATH_MAX];    /* face-coordinate files (<idx> <coord>)     */
     char   ygrid[IFX_PATH_MAX];
 } ifx_config;

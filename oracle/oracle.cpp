@@ -515,6 +515,11 @@ struct orc_solver {
     std::vector<int> gidx;   // cell -> index into ghosts (IBM ghosts), -1 otherwise
     ifx_stats st;
     double cs = 1, sn = 0, ia2 = 1, ib2 = 1;
+    // body pose: centre and velocities (a moving body updates them every step)
+    double bx = 0, by = 0, bu = 0, bv = 0, bw = 0;
+    bool moving = false;
+    long long nstep = 0;
+    std::vector<long long> fresh;  // step in which a cell last turned fluid
 };
 
 namespace {
@@ -608,12 +613,12 @@ void build_ghosts(orc_solver* S) {
                 g.qown = -1;
                 g.adj = -1;
                 // body frame
-                double px = S->xc[i] - c.body_cx, py = S->yc[j] - c.body_cy;
+                double px = S->xc[i] - S->bx, py = S->yc[j] - S->by;
                 double lx = px * S->cs + py * S->sn, ly = -px * S->sn + py * S->cs;
                 double bx, by, nlx, nly;
                 ellipse_closest(c.body_a, c.body_b, lx, ly, &bx, &by, &nlx, &nly);
-                double BIx = c.body_cx + bx * S->cs - by * S->sn;
-                double BIy = c.body_cy + bx * S->sn + by * S->cs;
+                double BIx = S->bx + bx * S->cs - by * S->sn;
+                double BIy = S->by + bx * S->sn + by * S->cs;
                 double nwx = nlx * S->cs - nly * S->sn, nwy = nlx * S->sn + nly * S->cs;
                 double IPx = 2.0 * BIx - S->xc[i], IPy = 2.0 * BIy - S->yc[j];
                 g.bi[0] = BIx; g.bi[1] = BIy; g.ip[0] = IPx; g.ip[1] = IPy;
@@ -678,6 +683,13 @@ void build_ghosts(orc_solver* S) {
                     g.wu[k] = -wD[k];
                     g.wv[k] = -wD[k];
                     g.wp[k] = (S->type[g.nb[k]] != T_GHOST) ? wN[k] / keep : 0.0;
+                }
+                // moving wall: q_G = 2 q_BI - q_IP with q_IP = w_G q_BI + sum_k w_k q_k
+                if (S->moving) {
+                    double wg = 2.0 - (gk >= 0 ? wD[gk] : 0.0);
+                    double ub = S->bu - S->bw * (BIy - S->by), vb = S->bv + S->bw * (BIx - S->bx);
+                    g.cu = wg * ub;
+                    g.cv = wg * vb;
                 }
                 S->ghosts.push_back(g);
             }
@@ -1038,8 +1050,8 @@ void compute_forces(orc_solver* S) {
         double nlx = ct / a, nly = st / b;
         double nl = std::sqrt(nlx * nlx + nly * nly);
         nlx /= nl; nly /= nl;
-        double xs = c.body_cx + lx * S->cs - ly * S->sn;
-        double ys = c.body_cy + lx * S->sn + ly * S->cs;
+        double xs = S->bx + lx * S->cs - ly * S->sn;
+        double ys = S->by + lx * S->sn + ly * S->cs;
         double nxw = nlx * S->cs - nly * S->sn, nyw = nlx * S->sn + nly * S->cs;
         double ds = std::sqrt(a * a * st * st + b * b * ct * ct) * dth;
         int i0 = locate(S->xc, nx, xs), j0 = locate(S->yc, ny, ys);
@@ -1048,6 +1060,11 @@ void compute_forces(orc_solver* S) {
         double ps = sample(S->p, xs, ys);
         double up = sample(S->u, xs + del * nxw, ys + del * nyw);
         double vp = sample(S->v, xs + del * nxw, ys + del * nyw);
+        if (S->moving) {  // velocity relative to the wall at the sample point
+            double rx = lx * S->cs - ly * S->sn, ry = lx * S->sn + ly * S->cs;
+            up = up - (S->bu - S->bw * ry);
+            vp = vp - (S->bv + S->bw * rx);
+        }
         double tx = -ps * nxw + mu * up / del;
         double ty = -ps * nyw + mu * vp / del;
         Fx += tx * ds;
@@ -1058,17 +1075,132 @@ void compute_forces(orc_solver* S) {
     S->st.cl = Fy / q;
 }
 
+// ---- prescribed body motion (no reference counterpart; the reference claims
+// moving boundaries, README.md:7,11, without code).  sin and cos of 2 pi x for
+// x in turns: x - floor(x), quadrant and octant mirror (exact), then the
+// Taylor series on [0, pi/4] to degree 19, every operation rounded on its own
+// (this file is built with -ffp-contract=off), as the CUDA path does.
+void sincos_turns(double x, double* s, double* c) {
+    double r = x - std::floor(x);
+    double r4 = r * 4.0;
+    int q = (int)r4;
+    double f = r4 - (double)q;
+    bool mirror = f > 0.5;
+    if (mirror) f = 1.0 - f;
+    double a = f * (3.14159265358979323846 / 2.0);
+    double a2 = a * a;
+    // 1/n! for n = 19, 17, ..., 3 and 16, 14, ..., 2
+    const double is[9] = {1.0 / 121645100408832000.0, 1.0 / 355687428096000.0, 1.0 / 1307674368000.0,
+                          1.0 / 6227020800.0, 1.0 / 39916800.0, 1.0 / 362880.0, 1.0 / 5040.0, 1.0 / 120.0, 1.0 / 6.0};
+    const double ic[8] = {1.0 / 20922789888000.0, 1.0 / 87178291200.0, 1.0 / 479001600.0, 1.0 / 3628800.0,
+                          1.0 / 40320.0, 1.0 / 720.0, 1.0 / 24.0, 1.0 / 2.0};
+    double ps = is[0];
+    for (int k = 1; k < 9; k++) ps = is[k] - a2 * ps;
+    ps = 1.0 - a2 * ps;
+    double pc = ic[0];
+    for (int k = 1; k < 8; k++) pc = ic[k] - a2 * pc;
+    pc = 1.0 - a2 * pc;
+    double sa = a * ps, ca = pc;
+    if (mirror) std::swap(sa, ca);
+    if (q == 0) { *s = sa; *c = ca; }
+    else if (q == 1) { *s = ca; *c = -sa; }
+    else if (q == 2) { *s = -sa; *c = -ca; }
+    else { *s = -ca; *c = sa; }
+}
+
+// Pose at time t (IFX_MOTION_PRESCRIBED): centre, cos/sin of the angle,
+// velocity of the centre and rotation rate.
+void body_pose(orc_solver* S, double t) {
+    const ifx_config& c = S->cfg;
+    const double f = c.motion_freq, w = (2.0 * 3.14159265358979323846) * c.motion_freq;
+    const double phx = c.motion_phase_x / 360.0, phy = c.motion_phase_y / 360.0, pha = c.motion_phase_deg / 360.0;
+    const double th0 = c.body_angle_deg / 360.0, ath = c.motion_amp_deg / 360.0;
+    const double ft = f * t;
+    double s0, c0, s1, c1;
+    sincos_turns(phx, &s0, &c0);
+    sincos_turns(ft + phx, &s1, &c1);
+    S->bx = (c.body_cx + c.motion_u * t) + c.motion_amp_x * (s1 - s0);
+    S->bu = c.motion_u + (c.motion_amp_x * w) * c1;
+    sincos_turns(phy, &s0, &c0);
+    sincos_turns(ft + phy, &s1, &c1);
+    S->by = (c.body_cy + c.motion_v * t) + c.motion_amp_y * (s1 - s0);
+    S->bv = c.motion_v + (c.motion_amp_y * w) * c1;
+    sincos_turns(pha, &s0, &c0);
+    sincos_turns(ft + pha, &s1, &c1);
+    double th = th0 + ath * (s1 - s0);
+    S->bw = ((ath * (2.0 * 3.14159265358979323846)) * w) * c1;
+    sincos_turns(th, &S->sn, &S->cs);
+}
+
+// Cell types of the interior at the current pose: solid / fluid by the body
+// predicate, then ghosts (solid with a fluid cell among the 8 neighbours).
+// Cells that turn fluid are stamped with the step number.
+void tag_interior(orc_solver* S) {
+    const ifx_config& c = S->cfg;
+    const int nx = S->nx, ny = S->ny;
+    for (int j = 1; j < ny - 1; j++)
+        for (int i = 1; i < nx - 1; i++) {
+            int id = IDX(i, j, nx);
+            int ins = c.body == IFX_BODY_ELLIPSE
+                          ? orc_inside(S->xc[i], S->yc[j], S->bx, S->by, S->cs, S->sn, S->ia2, S->ib2)
+                          : 0;
+            uint8_t old = S->type[id], nw = ins ? T_SOLID : T_FLUID;
+            S->iblank[id] = ins ? 0.0 : 1.0;
+            S->type[id] = nw;
+            if (S->moving && old != T_FLUID && nw == T_FLUID) S->fresh[id] = S->nstep;
+        }
+    for (int j = 1; j < ny - 1; j++)
+        for (int i = 1; i < nx - 1; i++) {
+            int id = IDX(i, j, nx);
+            if (S->type[id] != T_SOLID) continue;
+            bool g = false;
+            for (int dj = -1; dj <= 1; dj++)
+                for (int di = -1; di <= 1; di++) {
+                    int a = i + di, b = j + dj;
+                    if (a < 1 || a > nx - 2 || b < 1 || b > ny - 2) continue;
+                    if (S->type[IDX(a, b, nx)] == T_FLUID) g = true;
+                }
+            if (g) S->type[id] = T_GHOST;
+        }
+}
+
+// A moving body's geometry at step nstep: pose, cell types, the face
+// velocities of fresh cells (the initial face interpolation; the cell keeps
+// the ghost value it had), ghost relations and weights, multigrid levels.
+void move_body(orc_solver* S) {
+    const int nx = S->nx, ny = S->ny;
+    body_pose(S, (double)S->nstep * S->cfg.dt);
+    tag_interior(S);
+    for (int j = 1; j < ny - 1; j++)
+        for (int i = 1; i < nx - 1; i++) {
+            int id = IDX(i, j, nx);
+            if (S->fresh[id] != S->nstep) continue;
+            S->U[id] = S->u[id] * S->gx[i] + S->u[id + 1] * S->fx[i];
+            S->U[id - 1] = S->u[id - 1] * S->gx[i - 1] + S->u[id] * S->fx[i - 1];
+            S->V[id] = S->v[id] * S->gy[j] + S->v[id + nx] * S->fy[j];
+            S->V[id - nx] = S->v[id - nx] * S->gy[j - 1] + S->v[id] * S->fy[j - 1];
+        }
+    build_ghosts(S);
+    S->gidx.assign(S->n, -1);
+    for (size_t q = 0; q < S->ghosts.size(); q++) if (S->ghosts[q].side < 0) S->gidx[S->ghosts[q].cell] = (int)q;
+    build_levels(S);
+    S->st.n_ibm_ghost = S->n_ibm;
+}
+
 void method_step(orc_solver* S) {
     const ifx_config& c = S->cfg;
     const int nx = S->nx, ny = S->ny, n = S->n;
     const double dt = c.dt, dtre = c.dt / c.re;
+    S->nstep++;
+    if (S->moving) move_body(S);
     const Level& l0 = S->L[0];
     // 1. outflow face values and ghosts of u^n, v^n
     update_outflow(S);
     fill_ghosts(S, S->u.data(), 0);
     fill_ghosts(S, S->v.data(), 1);
-    // 2. convective term and predictor right-hand side (AB2; Euler on the first step)
-    const bool ab2 = S->have_nold;
+    // 2. convective term and predictor right-hand side (AB2; Euler on the first
+    // step and in cells that turned fluid in this step)
+    const bool ab2_all = S->have_nold;
 #pragma omp parallel for schedule(static) num_threads(S->nthreads)
     for (int j = 1; j < ny - 1; j++)
         for (int i = 1; i < nx - 1; i++) {
@@ -1085,6 +1217,7 @@ void method_step(orc_solver* S) {
             double vs = S->v[id - nx] * S->gy[j - 1] + S->v[id] * S->fy[j - 1];
             double Nu = (ue * Ue - uw * Uw) * l0.ix[i] + (un * Vn - us * Vs) * l0.iy[j];
             double Nv = (ve * Ue - vw * Uw) * l0.ix[i] + (vn * Vn - vs * Vs) * l0.iy[j];
+            bool ab2 = ab2_all && !(S->moving && S->fresh[id] == S->nstep);
             double cu = ab2 ? 1.5 * Nu - 0.5 * S->Nu[id] : Nu;
             double cv = ab2 ? 1.5 * Nv - 0.5 * S->Nv[id] : Nv;
             S->ru[id] = S->u[id] - dt * cu;
@@ -1318,37 +1451,33 @@ extern "C" orc_solver* orc_create(const ifx_config* cfg, const double* xf, const
         S->gy[j] = S->dy[j + 1] / (S->dy[j] + S->dy[j + 1]);
     }
     // tagging
+    S->bx = cfg->body_cx;
+    S->by = cfg->body_cy;
     if (cfg->body == IFX_BODY_ELLIPSE) {
         double th = cfg->body_angle_deg * M_PI / 180.0;
         S->cs = std::cos(th); S->sn = std::sin(th);
         S->ia2 = 1.0 / (cfg->body_a * cfg->body_a);
         S->ib2 = 1.0 / (cfg->body_b * cfg->body_b);
     }
+    S->moving = cfg->motion == IFX_MOTION_PRESCRIBED;
+    if (S->moving) {
+        body_pose(S, 0.0);  // the configured pose, from the same function as every step
+        S->fresh.assign(n, 0);
+    }
     S->iblank.assign(n, 1.0);
     S->type.assign(n, T_FLUID);
     for (int j = 0; j < ny; j++)
         for (int i = 0; i < nx; i++) {
+            bool ring = i == 0 || j == 0 || i == nx - 1 || j == ny - 1;
+            if (!ring) continue;
             int id = IDX(i, j, nx);
             int ins = cfg->body == IFX_BODY_ELLIPSE
-                          ? orc_inside(S->xc[i], S->yc[j], cfg->body_cx, cfg->body_cy, S->cs, S->sn, S->ia2, S->ib2)
+                          ? orc_inside(S->xc[i], S->yc[j], S->bx, S->by, S->cs, S->sn, S->ia2, S->ib2)
                           : 0;
             S->iblank[id] = ins ? 0.0 : 1.0;
-            bool ring = i == 0 || j == 0 || i == nx - 1 || j == ny - 1;
-            S->type[id] = ring ? T_DOMAIN : (ins ? T_SOLID : T_FLUID);
+            S->type[id] = T_DOMAIN;
         }
-    for (int j = 1; j < ny - 1; j++)
-        for (int i = 1; i < nx - 1; i++) {
-            int id = IDX(i, j, nx);
-            if (S->type[id] != T_SOLID) continue;
-            bool g = false;
-            for (int dj = -1; dj <= 1; dj++)
-                for (int di = -1; di <= 1; di++) {
-                    int a = i + di, b = j + dj;
-                    if (a < 1 || a > nx - 2 || b < 1 || b > ny - 2) continue;
-                    if (S->type[IDX(a, b, nx)] == T_FLUID) g = true;
-                }
-            if (g) S->type[id] = T_GHOST;
-        }
+    tag_interior(S);
     S->n_fluid = 0;
     for (int id = 0; id < n; id++) S->n_fluid += S->type[id] == T_FLUID;
     for (int sd = 0; sd < 4; sd++) S->dir[sd] = cfg->bc_type[sd] == IFX_BC_OUTFLOW;
@@ -1456,5 +1585,13 @@ extern "C" int orc_ghosts(orc_solver* S, int* cells, int* nb, double* wu, double
 }
 
 extern "C" int orc_mg_levels(orc_solver* S) { return (int)S->L.size(); }
+
+extern "C" void orc_sincos_turns(double x, double* s, double* c) { sincos_turns(x, s, c); }
+
+// Current body pose: centre, cos and sin of the angle, centre velocity, rotation rate.
+extern "C" void orc_body(orc_solver* S, double* out) {
+    out[0] = S->bx; out[1] = S->by; out[2] = S->cs; out[3] = S->sn;
+    out[4] = S->bu; out[5] = S->bv; out[6] = S->bw;
+}
 
 extern "C" void orc_destroy(orc_solver* S) { delete S; }

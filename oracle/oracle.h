@@ -83,6 +83,10 @@ int  orc_ghosts(orc_solver* s, int* cells, int* nb, double* wu, double* wp,
                 double* bi, double* ip);
 int  orc_mg_levels(orc_solver* s);
 void orc_destroy(orc_solver* s);
+/* Prescribed body motion: sin, cos of 2 pi x (x in turns), and the current
+ * pose (x, y, cos, sin, u, v, rotation rate). */
+void orc_sincos_turns(double x, double* s, double* c);
+void orc_body(orc_solver* s, double* out);
 
 #ifdef __cplusplus
 }

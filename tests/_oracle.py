@@ -33,6 +33,14 @@ class Oracle:
         L.orc_ghosts.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.orc_mg_levels.argtypes = [C.c_void_p]
         L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_sincos_turns.argtypes = [C.c_double, _dp, _dp]
+        L.orc_body.argtypes = [C.c_void_p, _dp]
+
+    def sincos_turns(self, x):
+        """sin and cos of 2 pi x as the moving-body pose forms them."""
+        s, c = np.zeros(1), np.zeros(1)
+        self.lib.orc_sincos_turns(float(x), s, c)
+        return s[0], c[0]
 
     # ---- reference primitives
     def grid(self, nx, ny, xf, yf):
@@ -108,6 +116,12 @@ class OracleSolver:
 
     def levels(self):
         return self.o.lib.orc_mg_levels(self.h)
+
+    def body(self):
+        """Current body pose: x, y, cos, sin of the angle, u, v, rotation rate."""
+        out = np.zeros(7)
+        self.o.lib.orc_body(self.h, out)
+        return out
 
     def __del__(self):
         try:
