@@ -714,11 +714,11 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         }
         I.moving = I.cfg.motion == IFX_MOTION_PRESCRIBED;
         MotionDef mo{};
+        Pose p0{};
         if (I.moving) {
             // the pose at t = 0 from the same function as every later step
             mo = motion_def(I.cfg);
-            const Pose p0 = pose_at(mo.x0, mo.y0, mo.th0, mo.u, mo.v, mo.ax, mo.ay, mo.ath, mo.f, mo.w, mo.phx, mo.phy,
-                                    mo.pha, 0.0);
+            p0 = pose_at(mo.x0, mo.y0, mo.th0, mo.u, mo.v, mo.ax, mo.ay, mo.ath, mo.f, mo.w, mo.phx, mo.phy, mo.pha, 0.0);
             I.cs = p0.c;
             I.sn = p0.s;
         }
@@ -745,6 +745,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             d.mo_x0 = mo.x0; d.mo_y0 = mo.y0; d.mo_th0 = mo.th0; d.mo_u = mo.u; d.mo_v = mo.v;
             d.mo_ax = mo.ax; d.mo_ay = mo.ay; d.mo_ath = mo.ath; d.mo_f = mo.f; d.mo_w = mo.w;
             d.mo_phx = mo.phx; d.mo_phy = mo.phy; d.mo_pha = mo.pha;
+            d.bu = p0.u; d.bv = p0.v; d.bw = p0.w;  // the initial ghosts see the wall velocity at t = 0
             int* fresh = nullptr;
             IFX_TRY(dalloc(S, &fresh, I.ncell));
             d.fresh = fresh;
