@@ -35,6 +35,8 @@ ellipse   : the large single-instance configuration (1024x768 ellipse,
             Re 300), autotuned, mixed and plain FP64;
 long_run_accuracy: the cylinder over 1000 steps in both precisions: largest
             drag and lift deviation of any step, velocity error at the end;
+moving_body: the cylinder heaving (prescribed motion, geometry redone on the
+            device every step), mixed and plain FP64, beside the cylinder at rest;
 reference_path: the REFERENCE-mode step (the reference's own scheme) at 52^2,
             130^2 and 514^2 cells, GPU and one CPU thread;
 served    : a seeded Poisson request stream through the continuous-batching
@@ -363,6 +365,38 @@ def ellipse_line(ifx, capi, cases, steps=10):
     return out
 
 
+def moving_line(ifx, capi, cases, steps=50):
+    """A body in prescribed motion: the cylinder configuration (384x256, Re 100,
+    dt 5e-3) heaving with amplitude 0.25 D at frequency 0.2, its geometry redone
+    on the device every step; mixed and plain FP64, and the same cylinder at
+    rest for the cost of the per-step geometry (device time, CUDA events)."""
+    out = {"workload": "cylinder D=1, 30x20 domain, 384x256 tanh-stretched, Re 100, dt 5e-3, "
+                       "heaving y = 0.25 sin(2 pi 0.2 t)", "unit": METRIC, "steps": steps}
+    fields = {}
+    for name, prec, moving in (("mixed", capi.PREC_MIXED, True), ("fp64", capi.PREC_FP64, True),
+                               ("mixed_at_rest", capi.PREC_MIXED, False)):
+        cfg, xf, yf = cases.cylinder(precision=prec)
+        if moving:
+            cases.set_motion(cfg, amp_y=0.25, freq=0.2)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.step(1)
+        s.autotune(steps=1)
+        s.step(2)
+        s.step(steps)
+        ms = s.last_step_ms()
+        st = s.stats()
+        out[name] = {"value": cfg.nx * cfg.ny * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
+                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters, "cd": st.cd, "cl": st.cl,
+                     "ibm_ghosts": st.n_ibm_ghost}
+        if moving:
+            fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
+        s.close()
+    out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["rel_l2_velocity_vs_fp64"] = rel_l2(fields["mixed"], fields["fp64"])
+    out["motion_overhead_ms_per_step"] = out["mixed"]["ms_per_step"] - out["mixed_at_rest"]["ms_per_step"]
+    return out
+
+
 def reference_path(ifx, capi, cases, steps=20, cpu=True):
     """The REFERENCE-mode time step (the reference's ADsolver: vortex IC,
     explicit convection, backward-Euler diffusion by Jacobi to the L1 stop rule,
@@ -605,6 +639,7 @@ def main():
     if rank == 0 and world == 1:
         line["ellipse"] = ellipse_line(ifx, capi, cases)
         line["long_run_accuracy"] = long_run_accuracy(ifx, capi, cases)
+        line["moving_body"] = moving_line(ifx, capi, cases)
         line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)

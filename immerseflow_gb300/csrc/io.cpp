@@ -190,6 +190,20 @@ extern "C" ifx_status ifx_config_read(const char* path, ifx_config* c) {
                 if (!(iss >> c->bc_u[s] >> c->bc_v[s])) return bad("Boundary-Velocity");
         } else if (line.find("Outflow-Speed") != std::string::npos) {
             if (!next() || !(iss >> c->outflow_uc)) return bad("Outflow-Speed");
+        } else if (line.find("Body-Motion") != std::string::npos) {
+            // none | prescribed u v amp_x amp_y amp_deg freq phase_x phase_y phase_deg
+            std::string w;
+            if (!next() || !(iss >> w)) return bad("Body-Motion");
+            if (w == "none") {
+                c->motion = IFX_MOTION_NONE;
+            } else if (w == "prescribed") {
+                c->motion = IFX_MOTION_PRESCRIBED;
+                if (!(iss >> c->motion_u >> c->motion_v >> c->motion_amp_x >> c->motion_amp_y >> c->motion_amp_deg >>
+                      c->motion_freq >> c->motion_phase_x >> c->motion_phase_y >> c->motion_phase_deg))
+                    return bad("Body-Motion");
+            } else {
+                return bad("Body-Motion");
+            }
         } else if (line.find("Body") != std::string::npos) {
             std::string w;
             if (!next() || !(iss >> w)) return bad("Body");

@@ -118,6 +118,25 @@ def test_relaxation_factors_and_ppe_method(golden_dir, tmp_path):
     assert e.value.status == capi.IFX_ERR_PARSE
 
 
+def test_body_motion_keyword(golden_dir, tmp_path):
+    """Body-Motion (extension): none, or prescribed with the nine motion
+    parameters; it does not shadow the Body keyword."""
+    src = open(os.path.join(golden_dir, "inputs", "inputs.txt")).read()
+    p = tmp_path / "inputs.txt"
+    p.write_text(src + "Body\ncircle 4 4 0.5\nBody-Motion\nprescribed 0.5 0 0 0.25 10 0.2 0 90 45\n")
+    c = ifx.config_read(str(p))
+    assert c.body == capi.BODY_ELLIPSE and (c.body_cx, c.body_cy, c.body_a) == (4.0, 4.0, 0.5)
+    assert c.motion == capi.MOTION_PRESCRIBED
+    assert (c.motion_u, c.motion_v, c.motion_amp_x, c.motion_amp_y, c.motion_amp_deg) == (0.5, 0.0, 0.0, 0.25, 10.0)
+    assert (c.motion_freq, c.motion_phase_x, c.motion_phase_y, c.motion_phase_deg) == (0.2, 0.0, 90.0, 45.0)
+    p.write_text(src + "Body-Motion\nprescribed 0.5 0\n")
+    with pytest.raises(ifx.IFXError) as e:
+        ifx.config_read(str(p))
+    assert e.value.status == capi.IFX_ERR_PARSE
+    p.write_text(src + "Body-Motion\nnone\n")
+    assert ifx.config_read(str(p)).motion == capi.MOTION_NONE
+
+
 def test_missing_inputs_is_io_error(tmp_path):
     with pytest.raises(ifx.IFXError) as e:
         ifx.config_read(str(tmp_path / "nope.txt"))
