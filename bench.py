@@ -85,8 +85,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=16.0, help="served stream arrival rate [1/s]")
     ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
-    ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch"],
-                    help="workload of --profile: the cylinder, or the batched sweep of --batch instances")
+    ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch", "moving"],
+                    help="workload of --profile: the cylinder, the cylinder heaving (moving), or the batched sweep of --batch instances")
     ap.add_argument("--profile-rows", type=int, default=1, choices=[1, 4],
                     help="rows per thread of the multigrid tile phases under --profile")
     return ap.parse_args()
@@ -509,6 +509,8 @@ def main():
             s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
         else:
             cfg, _, _ = cases.cylinder(precision=prec)
+            if args.profile_workload == "moving":  # heaving as in the moving_body line
+                cases.set_motion(cfg, amp_y=0.25, freq=0.2)
             s = ifx.Solver.create(cfg, xf, yf)
         s.set_mg_tile_rows(args.profile_rows)
         s.step(args.warmup)

@@ -93,12 +93,15 @@ cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_
 // ---- immersed-boundary set-up (kernels_ibm.cu, built without FMA contraction)
 cudaError_t launch_tag(const InstDev* I, int inst, int n_cells, uint8_t* type, cudaStream_t s);
 cudaError_t launch_mark_ghosts(const InstDev* I, int inst, int n_interior, uint8_t* type, cudaStream_t s);
+// threads: block size; small blocks spread the FP64 latency chains of the
+// ghosts over more SMs (the per-step refresh of moving bodies uses 32)
 cudaError_t launch_ghost_weights(GhostDev* G, const int* ibm, int nibm, const InstDev* I, double* bi_ip,
-                                 cudaStream_t s);
+                                 cudaStream_t s, int threads = 128);
 // ---- moving bodies (kernels_move.cu)
 cudaError_t launch_move_geometry(InstDev* I, InstState* S, const LevelDev* LV, GhostDev* G, const int* mv, int nmv,
                                  cudaStream_t s);
 cudaError_t launch_move_init(InstDev* I, InstState* S, const int* mv, int nmv, const int* n_ibm, cudaStream_t s);
+cudaError_t launch_move_forces(const InstDev* I, const InstState* S, const int* mv, int nmv, cudaStream_t s);
 
 // ---- reference path (kernels_ref.cu), one instance, dense rows (pitch = nx)
 struct RefDev {

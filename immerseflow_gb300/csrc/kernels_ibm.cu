@@ -264,9 +264,9 @@ cudaError_t launch_mark_ghosts(const InstDev* I, int inst, int n_interior, uint8
     return cudaGetLastError();
 }
 cudaError_t launch_ghost_weights(GhostDev* G, const int* ibm, int nibm, const InstDev* I, double* bi_ip,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int threads) {
     if (nibm == 0) return cudaSuccess;
-    k_ghost_weights<<<(nibm + 127) / 128, 128, 0, s>>>(G, ibm, nibm, I, bi_ip);
+    k_ghost_weights<<<(nibm + threads - 1) / threads, threads, 0, s>>>(G, ibm, nibm, I, bi_ip);
     return cudaGetLastError();
 }
 

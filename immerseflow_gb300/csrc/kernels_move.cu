@@ -16,9 +16,9 @@
 //      instance's ghost slots (a block prefix sum, so the order is that of the
 //      static set-up), slots left over emptied;
 //   E  every coarser level's cells in use (any child in use) and stencil bytes,
-//      also in the sub-cycle's image of the small levels;
-//   F  the body-surface force samples at the new pose.
-// The image-point weights of the new ghosts follow in k_ghost_weights.  The
+//      also in the sub-cycle's image of the small levels.
+// The image-point weights of the new ghosts (k_ghost_weights) and the force
+// samples at the new pose (k_move_forces) follow as kernels of their own.  The
 // CPU restatement rebuilds the same tables on the whole grid; the rules are
 // local, so the results are the same.
 //
@@ -280,34 +280,44 @@ __global__ void __launch_bounds__(MOVE_THREADS) k_move_geometry(InstDev* __restr
         }
         f = c;
     }
-    // F: force samples at the new pose (the static table's formulas)
-    ForceSample* fs = const_cast<ForceSample*>(in.fs);
-    for (int q = tid; q < FORCE_SAMPLES; q += nt) {
-        const double* b = in.fsb + 5 * (size_t)q;
-        const double lx = b[0], ly = b[1], nlx = b[2], nly = b[3];
-        const double xs = cx + lx * cs - ly * sn;
-        const double ys = cy + lx * sn + ly * cs;
-        const double nxw = nlx * cs - nly * sn, nyw = nlx * sn + nly * cs;
-        int i0 = min(max(ub_index(in.xc, in.nx, xs), 0), in.nx - 2);
-        int j0 = min(max(ub_index(in.yc, in.ny, ys), 0), in.ny - 2);
-        const double h = fmax(in.dx[i0], in.dy[j0]);
-        const double del = 1.5 * h;
-        ForceSample e;
-        e.c0 = i0 + j0 * P;
-        e.xi0 = (xs - in.xc[i0]) / (in.xc[i0 + 1] - in.xc[i0]);
-        e.et0 = (ys - in.yc[j0]) / (in.yc[j0 + 1] - in.yc[j0]);
-        const double xq = xs + del * nxw, yq = ys + del * nyw;
-        const int i1 = min(max(ub_index(in.xc, in.nx, xq), 0), in.nx - 2);
-        const int j1 = min(max(ub_index(in.yc, in.ny, yq), 0), in.ny - 2);
-        e.c1 = i1 + j1 * P;
-        e.xi1 = (xq - in.xc[i1]) / (in.xc[i1 + 1] - in.xc[i1]);
-        e.et1 = (yq - in.yc[j1]) / (in.yc[j1 + 1] - in.yc[j1]);
-        e.nx = nxw;
-        e.ny = nyw;
-        e.ds = b[4];
-        e.del = del;
-        fs[q] = e;
-    }
+}
+
+// The body-surface force samples at the new pose (the static table's
+// formulas), one thread per sample over many small blocks: the binary
+// searches and FP64 divisions are latency chains, and GB300's FP64 pipe is
+// narrow, so the work is spread over the SMs.
+__global__ void k_move_forces(const InstDev* __restrict__ I, const InstState* __restrict__ S, const int* __restrict__ mv) {
+    const int k = mv[blockIdx.y];
+    const InstDev& in = I[k];
+    if (in.retired || S[k].geo_err) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= FORCE_SAMPLES) return;
+    const int P = in.pitch;
+    const double cx = in.bcx, cy = in.bcy, cs = in.bcs, sn = in.bsn;
+    const double* b = in.fsb + 5 * (size_t)q;
+    const double lx = b[0], ly = b[1], nlx = b[2], nly = b[3];
+    const double xs = cx + lx * cs - ly * sn;
+    const double ys = cy + lx * sn + ly * cs;
+    const double nxw = nlx * cs - nly * sn, nyw = nlx * sn + nly * cs;
+    const int i0 = min(max(ub_index(in.xc, in.nx, xs), 0), in.nx - 2);
+    const int j0 = min(max(ub_index(in.yc, in.ny, ys), 0), in.ny - 2);
+    const double h = fmax(in.dx[i0], in.dy[j0]);
+    const double del = 1.5 * h;
+    ForceSample e;
+    e.c0 = i0 + j0 * P;
+    e.xi0 = (xs - in.xc[i0]) / (in.xc[i0 + 1] - in.xc[i0]);
+    e.et0 = (ys - in.yc[j0]) / (in.yc[j0 + 1] - in.yc[j0]);
+    const double xq = xs + del * nxw, yq = ys + del * nyw;
+    const int i1 = min(max(ub_index(in.xc, in.nx, xq), 0), in.nx - 2);
+    const int j1 = min(max(ub_index(in.yc, in.ny, yq), 0), in.ny - 2);
+    e.c1 = i1 + j1 * P;
+    e.xi1 = (xq - in.xc[i1]) / (in.xc[i1 + 1] - in.xc[i1]);
+    e.et1 = (yq - in.yc[j1]) / (in.yc[j1 + 1] - in.yc[j1]);
+    e.nx = nxw;
+    e.ny = nyw;
+    e.ds = b[4];
+    e.del = del;
+    const_cast<ForceSample*>(in.fs)[q] = e;
 }
 
 // Body box of every moving instance at its current pose (set-up).
@@ -329,6 +339,11 @@ cudaError_t launch_move_geometry(InstDev* I, InstState* S, const LevelDev* LV, G
                                  cudaStream_t s) {
     if (nmv == 0) return cudaSuccess;
     k_move_geometry<<<nmv, MOVE_THREADS, 0, s>>>(I, S, LV, G, mv);
+    return cudaGetLastError();
+}
+cudaError_t launch_move_forces(const InstDev* I, const InstState* S, const int* mv, int nmv, cudaStream_t s) {
+    if (nmv == 0) return cudaSuccess;
+    k_move_forces<<<dim3((FORCE_SAMPLES + 31) / 32, nmv), 32, 0, s>>>(I, S, mv);
     return cudaGetLastError();
 }
 cudaError_t launch_move_init(InstDev* I, InstState* S, const int* mv, int nmv, const int* n_ibm, cudaStream_t s) {

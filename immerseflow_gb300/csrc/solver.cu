@@ -1052,7 +1052,15 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             if (!I.moving) continue;
             mv.push_back(k);
             nibm.push_back(I.n_ibm);
-            for (int s = 0; s < I.ibm_cap; s++) slots.push_back(I.ibm_beg + s);
+            // the slots in use are the first ones: listed column-wise over
+            // 32-wide rows, consecutive slots land in different blocks of the
+            // per-step weight kernel (32 threads each), i.e. on different SMs
+            const int nb = (I.ibm_cap + 31) / 32;
+            for (int b = 0; b < nb; b++)
+                for (int l = 0; l < 32; l++) {
+                    const int s = b + l * nb;
+                    if (s < I.ibm_cap) slots.push_back(I.ibm_beg + s);
+                }
         }
         S->nmv = (int)mv.size();
         S->nmvslots = (int)slots.size();
@@ -1204,7 +1212,8 @@ void seq_pre(Seq& q) {
     if (S->nmv) {
         // moving bodies: geometry at the new pose, then the new ghosts' weights
         q.add(launch_move_geometry(S->dI, S->dS, S->dLV, S->dG, S->dMv, S->nmv, st));
-        q.add(launch_ghost_weights(S->dG, S->dMvSlots, S->nmvslots, S->dI, nullptr, st));
+        q.add(launch_ghost_weights(S->dG, S->dMvSlots, S->nmvslots, S->dI, nullptr, st, 32));
+        q.add(launch_move_forces(S->dI, S->dS, S->dMv, S->nmv, st));
     }
     q.add(launch_outflow(S->dG, S->ng, S->dI, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
