@@ -26,6 +26,7 @@ constexpr int MG_ROWS_WIDE = 4;  // rows per thread of the wide multigrid tiles 
 constexpr int GHOST_BLOCK = 256;
 constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
+constexpr int TMA_MAPS_PER_LEVEL = 8;  // tensor maps per level: e, e2, r, bits for 32x8 tiles, then for wide tiles
 constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
 constexpr double COARSE_OMEGA = 1.5;
 // Threads of the block that runs an instance's small levels in the graph and

@@ -1,5 +1,6 @@
 // ifx_host.h -- host-side solver object behind the C ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -87,6 +88,8 @@ struct ifx_solver {
     ifx::GhostDev* dG = nullptr;
     int ng = 0, nibm = 0;
     int* dIbm = nullptr;             // global indices of IBM ghost entries
+    CUtensorMap* dTmap = nullptr;    // TMA tensor maps of the multigrid levels (null: plain tile loads)
+    unsigned* dErr = nullptr;        // set by a kernel whose TMA copy did not complete
     int* dMv = nullptr;              // instances with a moving body
     int nmv = 0;
     int* dMvSlots = nullptr;         // their IBM ghost slots (global indices)

@@ -1,5 +1,6 @@
 // ifx_kernels.h -- host-callable launchers of the CUDA kernels.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "ifx_dev.h"
@@ -54,6 +55,13 @@ cudaError_t launch_bicg_x(const Tile* t, int nt, const LevelDev* LV, const InstD
 template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s);
+// The same sweep with each tile staged in shared memory by TMA loads (tm:
+// TMA_MAPS_PER_LEVEL tensor maps per LevelDev entry); *err is set when a copy
+// does not complete.
+template <typename T>
+cudaError_t launch_smooth_tma(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
+                              const GhostDev* G, const CUtensorMap* tm, int flags, int src_alt, int rows, unsigned* err,
+                              cudaStream_t s);
 // Smoothing sweep of one level of a one-instance solver (tiles from the grid).
 template <typename T>
 cudaError_t launch_smooth_grid(const GridTiles& g, int nt, const InstState* S, const GhostDev* G, int flags,

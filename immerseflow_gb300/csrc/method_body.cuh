@@ -27,6 +27,7 @@
 
 #include "ifx_dev.h"
 #include "ifx_kernels.h"
+#include "tma.cuh"
 
 
 namespace ifx {
@@ -1118,6 +1119,74 @@ __device__ __forceinline__ void b_smooth(const Tile* __restrict__ tiles, const L
     if (!tile_live(t, L, S)) return;
     smooth_tile<T, R>(t, L, (T)I[t.inst].omega, L.depth == 0 ? I[t.inst].gidx : nullptr, G, flags, src_alt, ST_ACTIVE);
 }
+// The same sweep with the tile staged in shared memory by the tensor memory
+// accelerator: one thread issues three 2-D tile loads on an mbarrier (the
+// correction with a one-cell halo, from 16 bytes left of the tile so that the
+// box start is aligned; the right-hand side; the stencil bytes), and the
+// block computes from shared memory.  The loads of a tile no longer cost
+// registers, so more of them are in flight.  Out-of-range box parts read
+// zero; every stored cell (stencil byte non-zero, so inside the level) takes
+// the same operands and arithmetic as smooth_tile.  A copy that does not
+// complete within the wait limit sets *err and the block leaves.
+template <typename T, int R>
+struct SmoothStage {
+    static constexpr int PAD = 16 / (int)sizeof(T);
+    static constexpr int BX = TILE_X + 2 * PAD, BY = TILE_Y * R + 2;
+    alignas(128) T e[BY][BX];
+    alignas(128) T r[TILE_Y * R][TILE_X];
+    alignas(128) uint8_t b[TILE_Y * R][TILE_X];
+    unsigned long long bar;
+};
+template <typename T, int R>
+__device__ __forceinline__ void b_smooth_tma(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                             const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm,
+                                             int flags, int src_alt, unsigned* err, int vb) {
+    using St = SmoothStage<T, R>;
+    __shared__ St sm;
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev& L = LV[t.lev];
+    if (!tile_live(t, L, S)) return;
+    const bool zero = (flags & 1) != 0;
+    const CUtensorMap* m = tm + (size_t)t.lev * TMA_MAPS_PER_LEVEL + (R == 1 ? 0 : 4);
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        const unsigned bytes = (zero ? 0u : (unsigned)sizeof(sm.e)) + (unsigned)sizeof(sm.r) + (unsigned)sizeof(sm.b);
+        mbar_expect_tx(&sm.bar, bytes);
+        if (!zero) tma_load_2d(&sm.e[0][0], &m[src_alt ? 1 : 0], t.i0 - St::PAD, t.j0 - 1, &sm.bar);
+        tma_load_2d(&sm.r[0][0], &m[2], t.i0, t.j0, &sm.bar);
+        tma_load_2d(&sm.b[0][0], &m[3], t.i0, t.j0, &sm.bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(&sm.bar, 0)) {
+        if (threadIdx.x == 0) atomicExch(err, 1u);
+        mbar_wait(&sm.bar, 0);  // the copies in flight, bounded again
+        return;
+    }
+    const T* src = (const T*)(src_alt ? L.e2 : L.e);
+    T* dst = (T*)(src_alt ? L.e : L.e2);
+    const int P = L.pitch, lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+    const int ic = clampi(t.i0 + lane, 1, L.NX);
+    const T om = (T)I[t.inst].omega;
+    const int* gidx = L.depth == 0 ? I[t.inst].gidx : nullptr;
+    auto fetch = [src](int q) { return (T)src[q]; };
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int row = R * w + r;
+        const int jc = clampi(t.j0 + row, 1, L.NY), id = ic + jc * P;
+        const uint8_t bt = sm.b[row][lane];
+        const int x = lane + St::PAD;
+        const T eP = sm.e[row + 1][x], eN = sm.e[row + 2][x], eS = sm.e[row][x];
+        const T eE = sm.e[row + 1][x + 1], eW = sm.e[row + 1][x - 1];
+        T Le, D;
+        if (L.depth == 0) lap_vals<T, true>(L, ic, jc, id, P, bt, G, gidx, eE, eW, eN, eS, eP, fetch, Le, D);
+        else lap_vals<T, false>(L, ic, jc, id, P, bt, G, nullptr, eE, eW, eN, eS, eP, fetch, Le, D);
+        const T rv = sm.r[row][lane];
+        const T val = zero ? jacobi_from_zero<T>(rv, D, om) : jacobi_update<T>(eP, rv, Le, D, om);
+        if (bt & 0x0F) dst[id] = val;
+    }
+}
+
 template <typename T, int R = 1>
 __device__ __forceinline__ void b_smooth_grid(const GridTiles& g, const InstState* __restrict__ S,
                                               const GhostDev* __restrict__ G, int flags, int src_alt, int vb) {

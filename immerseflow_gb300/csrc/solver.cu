@@ -124,6 +124,50 @@ std::vector<float> to_f(const std::vector<double>& v) {
     return r;
 }
 
+// TMA tensor maps of every multigrid level for the staged smoothing sweep
+// (launch_smooth_tma): per level e, e2, r (type T) and the stencil bytes, for
+// 32x8 tiles and for wide tiles; the box of e carries a one-cell halo and
+// starts 16 bytes left of the tile.  Returns false when the driver cannot
+// encode them (the plain tile kernels are used then).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+bool tensor_maps(const std::vector<LevelDev>& lv, int ts, std::vector<CUtensorMap>& out) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p) {
+        cudaGetLastError();
+        return false;
+    }
+    const EncodeTiledFn enc = (EncodeTiledFn)p;
+    const CUtensorMapDataType dt = ts == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    out.assign(lv.size() * TMA_MAPS_PER_LEVEL, CUtensorMap{});
+    for (size_t v = 0; v < lv.size(); v++) {
+        const LevelDev& L = lv[v];
+        const cuuint64_t dims[2] = {(cuuint64_t)L.pitch, (cuuint64_t)L.ny};
+        const cuuint64_t st_t[1] = {(cuuint64_t)L.pitch * ts}, st_b[1] = {(cuuint64_t)L.pitch};
+        const cuuint32_t es[2] = {1, 1};
+        for (int w = 0; w < 2; w++) {
+            const int rows = w ? MG_ROWS_WIDE : 1, pad = 16 / ts;
+            const cuuint32_t be[2] = {(cuuint32_t)(TILE_X + 2 * pad), (cuuint32_t)(TILE_Y * rows + 2)};
+            const cuuint32_t bt[2] = {(cuuint32_t)TILE_X, (cuuint32_t)(TILE_Y * rows)};
+            CUtensorMap* m = &out[v * TMA_MAPS_PER_LEVEL + 4 * w];
+            void* arr[3] = {L.e, L.e2, L.r};
+            for (int a = 0; a < 3; a++)
+                if (enc(&m[a], dt, 2, arr[a], dims, st_t, a < 2 ? be : bt, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return false;
+            if (enc(&m[3], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)L.bits, dims, st_b, bt, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return false;
+        }
+    }
+    return true;
+}
+
 // Face-coefficient pairs of one direction: (k[i] inv[i], k[i-1] inv[i]) with
 // both factors first rounded to T, so that each product is the one the
 // kernels would form from the T copies of k and inv.
@@ -980,6 +1024,14 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     }
     IFX_TRY(dupload(S, &S->dLV, hLV));
     S->hLV = hLV;
+    {   // staged smoothing (TMA); IFX_TMA=0 keeps the plain tile loads
+        const char* e = std::getenv("IFX_TMA");
+        std::vector<CUtensorMap> maps;
+        if (!(e && e[0] == '0') && tensor_maps(hLV, S->prec == IFX_PREC_FP64 ? 8 : 4, maps)) {
+            IFX_TRY(dupload(S, &S->dTmap, maps));
+            IFX_TRY(dalloc(S, &S->dErr, 1));
+        }
+    }
     IFX_TRY(dupload(S, &S->dT0, hT0));
     S->nt0 = (int)hT0.size();
     S->dTsm.assign(lmax, nullptr);
@@ -1151,8 +1203,10 @@ int seq_vcycle(Seq& q, bool first_done = false) {
     const int R = S->mg_rows;
     const bool one = S->inst.size() == 1;  // one instance: tiles from the block index
     auto smooth = [&](const Tile* tl, int nt, int l, int flags, int src_alt) {
-        return one ? launch_smooth_grid<T>(grid_of(S, l, R), nt, S->dS, S->dG, flags, src_alt, R, st)
-                   : launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, flags, src_alt, R, st);
+        if (one) return launch_smooth_grid<T>(grid_of(S, l, R), nt, S->dS, S->dG, flags, src_alt, R, st);
+        if (S->dTmap)
+            return launch_smooth_tma<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, S->dTmap, flags, src_alt, R, S->dErr, st);
+        return launch_smooth<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, flags, src_alt, R, st);
     };
     const bool W = R == MG_ROWS_WIDE;
     const Tile* t0 = W ? S->dT0W : S->dT0;
@@ -1515,6 +1569,13 @@ ifx_status step_finish(ifx_solver* S) {
         if (err) {
             S->poisoned = true;
             return set_error(IFX_ERR_CUDA, "persistent step: grid barrier timed out");
+        }
+    } else if (S->dErr) {
+        unsigned int err = 0;
+        CUDA_TRY(cudaMemcpy(&err, S->dErr, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err) {
+            S->poisoned = true;
+            return set_error(IFX_ERR_CUDA, "a TMA tile copy did not complete");
         }
     }
     ifx_status st = check_states(S);
