@@ -62,6 +62,11 @@ template <typename T>
 cudaError_t launch_smooth_tma(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                               const GhostDev* G, const CUtensorMap* tm, int flags, int src_alt, int rows, unsigned* err,
                               cudaStream_t s);
+// The same with each tile staged by TMA (see launch_smooth_tma).
+template <typename T>
+cudaError_t launch_smooth_grid_tma(const GridTiles& g, int nt, const InstState* S, const GhostDev* G,
+                                   const CUtensorMap* tm, int flags, int src_alt, int rows, unsigned* err,
+                                   cudaStream_t s);
 // Smoothing sweep of one level of a one-instance solver (tiles from the grid).
 template <typename T>
 cudaError_t launch_smooth_grid(const GridTiles& g, int nt, const InstState* S, const GhostDev* G, int flags,

@@ -151,6 +151,13 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_smooth_tma(co
                          const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm, int flags, int src_alt,
                          unsigned* err) { b_smooth_tma<T, R>(tiles, LV, I, S, G, tm, flags, src_alt, err, blockIdx.x); }
 template <typename T, int R>
+__global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid_tma(const GridTiles g, const InstState* __restrict__ S,
+                                                                    const GhostDev* __restrict__ G,
+                                                                    const CUtensorMap* __restrict__ tm, int flags,
+                                                                    int src_alt, unsigned* err) {
+    b_smooth_grid_tma<T, R>(g, S, G, tm, flags, src_alt, err, blockIdx.x);
+}
+template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid(const GridTiles g, const InstState* __restrict__ S,
                                                                 const GhostDev* __restrict__ G, int flags,
                                                                 int src_alt) {
@@ -324,6 +331,19 @@ template cudaError_t launch_smooth_tma<double>(const Tile*, int, const LevelDev*
                                                const GhostDev*, const CUtensorMap*, int, int, int, unsigned*, cudaStream_t);
 template cudaError_t launch_smooth_tma<float>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
                                               const GhostDev*, const CUtensorMap*, int, int, int, unsigned*, cudaStream_t);
+template <typename T>
+cudaError_t launch_smooth_grid_tma(const GridTiles& g, int nt, const InstState* S, const GhostDev* G,
+                                   const CUtensorMap* tm, int flags, int src_alt, int rows, unsigned* err,
+                                   cudaStream_t s) {
+    if (nt == 0) return cudaSuccess;
+    if (rows == MG_ROWS_WIDE) k_smooth_grid_tma<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(g, S, G, tm, flags, src_alt, err);
+    else k_smooth_grid_tma<T, 1><<<nt, TILE_THREADS, 0, s>>>(g, S, G, tm, flags, src_alt, err);
+    return cudaGetLastError();
+}
+template cudaError_t launch_smooth_grid_tma<double>(const GridTiles&, int, const InstState*, const GhostDev*,
+                                                    const CUtensorMap*, int, int, int, unsigned*, cudaStream_t);
+template cudaError_t launch_smooth_grid_tma<float>(const GridTiles&, int, const InstState*, const GhostDev*,
+                                                   const CUtensorMap*, int, int, int, unsigned*, cudaStream_t);
 template <typename T>
 cudaError_t launch_smooth_grid(const GridTiles& g, int nt, const InstState* S, const GhostDev* G, int flags,
                                int src_alt, int rows, cudaStream_t s) {

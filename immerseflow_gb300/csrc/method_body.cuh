@@ -1137,16 +1137,13 @@ struct SmoothStage {
     alignas(128) uint8_t b[TILE_Y * R][TILE_X];
     unsigned long long bar;
 };
+// state: the instance's pressure-solve state (stores only while active).
 template <typename T, int R>
-__device__ __forceinline__ void b_smooth_tma(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
-                                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                                             const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm,
-                                             int flags, int src_alt, unsigned* err, int vb) {
+__device__ __forceinline__ void smooth_tile_tma(const Tile& t, const LevelDev& L, const T om, const int* gidx,
+                                                const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm,
+                                                int flags, int src_alt, unsigned* err, int state) {
     using St = SmoothStage<T, R>;
     __shared__ St sm;
-    const Tile t = ldg_struct(&tiles[vb]);
-    const LevelDev& L = LV[t.lev];
-    if (!tile_live(t, L, S)) return;
     const bool zero = (flags & 1) != 0;
     const CUtensorMap* m = tm + (size_t)t.lev * TMA_MAPS_PER_LEVEL + (R == 1 ? 0 : 4);
     if (threadIdx.x == 0) {
@@ -1163,12 +1160,11 @@ __device__ __forceinline__ void b_smooth_tma(const Tile* __restrict__ tiles, con
         mbar_wait(&sm.bar, 0);  // the copies in flight, bounded again
         return;
     }
+    if (state != ST_ACTIVE) return;
     const T* src = (const T*)(src_alt ? L.e2 : L.e);
     T* dst = (T*)(src_alt ? L.e : L.e2);
     const int P = L.pitch, lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
     const int ic = clampi(t.i0 + lane, 1, L.NX);
-    const T om = (T)I[t.inst].omega;
-    const int* gidx = L.depth == 0 ? I[t.inst].gidx : nullptr;
     auto fetch = [src](int q) { return (T)src[q]; };
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -1185,6 +1181,26 @@ __device__ __forceinline__ void b_smooth_tma(const Tile* __restrict__ tiles, con
         const T val = zero ? jacobi_from_zero<T>(rv, D, om) : jacobi_update<T>(eP, rv, Le, D, om);
         if (bt & 0x0F) dst[id] = val;
     }
+}
+template <typename T, int R>
+__device__ __forceinline__ void b_smooth_tma(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+                                             const InstDev* __restrict__ I, const InstState* __restrict__ S,
+                                             const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm,
+                                             int flags, int src_alt, unsigned* err, int vb) {
+    const Tile t = ldg_struct(&tiles[vb]);
+    const LevelDev& L = LV[t.lev];
+    if (!tile_live(t, L, S)) return;
+    smooth_tile_tma<T, R>(t, L, (T)I[t.inst].omega, L.depth == 0 ? I[t.inst].gidx : nullptr, G, tm, flags, src_alt,
+                          err, ST_ACTIVE);
+}
+// One level of a one-instance solver (tiles from the block index, x0 = 0).
+template <typename T, int R>
+__device__ __forceinline__ void b_smooth_grid_tma(const GridTiles& g, const InstState* __restrict__ S,
+                                                  const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm,
+                                                  int flags, int src_alt, unsigned* err, int vb) {
+    const int state = S[g.inst].ppe_state;
+    smooth_tile_tma<T, R>(g.tile(vb), g.L, (T)g.omega, g.L.depth == 0 ? g.gidx : nullptr, G, tm, flags, src_alt, err,
+                          state);
 }
 
 template <typename T, int R = 1>

@@ -1024,10 +1024,11 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     }
     IFX_TRY(dupload(S, &S->dLV, hLV));
     S->hLV = hLV;
-    {   // staged smoothing (TMA); IFX_TMA=0 keeps the plain tile loads
+    {   // staged smoothing (TMA) on the mixed path, where it measured faster
+        // (FP64 32x8 tiles: no gain); IFX_TMA=0 keeps the plain tile loads
         const char* e = std::getenv("IFX_TMA");
         std::vector<CUtensorMap> maps;
-        if (!(e && e[0] == '0') && tensor_maps(hLV, S->prec == IFX_PREC_FP64 ? 8 : 4, maps)) {
+        if (S->prec == IFX_PREC_MIXED && !(e && e[0] == '0') && tensor_maps(hLV, 4, maps)) {
             IFX_TRY(dupload(S, &S->dTmap, maps));
             IFX_TRY(dalloc(S, &S->dErr, 1));
         }
@@ -1203,6 +1204,8 @@ int seq_vcycle(Seq& q, bool first_done = false) {
     const int R = S->mg_rows;
     const bool one = S->inst.size() == 1;  // one instance: tiles from the block index
     auto smooth = [&](const Tile* tl, int nt, int l, int flags, int src_alt) {
+        if (one && S->dTmap)
+            return launch_smooth_grid_tma<T>(grid_of(S, l, R), nt, S->dS, S->dG, S->dTmap, flags, src_alt, R, S->dErr, st);
         if (one) return launch_smooth_grid<T>(grid_of(S, l, R), nt, S->dS, S->dG, flags, src_alt, R, st);
         if (S->dTmap)
             return launch_smooth_tma<T>(tl, nt, S->dLV, S->dI, S->dS, S->dG, S->dTmap, flags, src_alt, R, S->dErr, st);
