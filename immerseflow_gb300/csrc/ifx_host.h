@@ -110,6 +110,12 @@ struct ifx_solver {
     int mg_rows = 1;                 // rows per thread of the multigrid tile phases: 1 or MG_ROWS_WIDE
     size_t cmg_bytes = 0;            // cluster V-cycle: shared memory per CTA (largest instance)
     int cmg_ok = 0, cmg_use = 0;     // it fits / graph and host-loop modes use it
+    // host copies of the full tile lists (every instance, instance order); the
+    // device lists hold the tiles of the instances in in_lists only
+    std::vector<ifx::Tile> hT0full, hT0Wfull;
+    std::vector<std::vector<ifx::Tile>> hTsmFull, hTreFull, hTsmWFull, hTreWFull;
+    std::vector<char> in_lists;
+    int listed = 0;
     ifx::Tile* dTall = nullptr;      // tiles of every level of every instance
     int* dSub = nullptr;             // LevelDev index of each instance's first small level
     int lmax = 0;

@@ -1057,6 +1057,14 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         S->ntreW[l] = (int)treW[l].size();
         S->ntsmW[l] = (int)tsmW[l].size();
     }
+    S->hT0full = hT0;
+    S->hT0Wfull = hT0W;
+    S->hTsmFull = tsm;
+    S->hTreFull = tre;
+    S->hTsmWFull = tsmW;
+    S->hTreWFull = treW;
+    S->in_lists.assign(n, 1);
+    S->listed = n;
     IFX_TRY(dupload(S, &S->dTall, hTall));
     IFX_TRY(dupload(S, &S->dSub, hSub));
     {   // shared-memory images of the small levels, one buffer for all instances
@@ -1947,6 +1955,66 @@ extern "C" ifx_status ifx_get_exec_mode(ifx_solver* S, int* mode) {
     return IFX_OK;
 }
 
+// Tile lists of the instances still active, written over the device lists
+// (which they never outgrow): a retired instance's tiles would only start
+// blocks that leave at once.  Each listed instance's level-0 partial sums move
+// with its tiles (tile_beg).  The step graph is rebuilt; the persistent
+// kernel takes the new counts.  Results do not change.
+static ifx_status compact_tiles(ifx_solver* S) {
+    const int n = (int)S->inst.size();
+    std::vector<char> keep(n);
+    for (int k = 0; k < n; k++) keep[k] = S->inst[k].dev.retired ? 0 : 1;
+    auto filt = [&](const std::vector<Tile>& v) {
+        std::vector<Tile> o;
+        for (const Tile& t : v)
+            if (keep[t.inst]) o.push_back(t);
+        return o;
+    };
+    auto put = [&](Tile* d, const std::vector<Tile>& v) -> cudaError_t {
+        return v.empty() ? cudaSuccess
+                         : cudaMemcpyAsync(d, v.data(), v.size() * sizeof(Tile), cudaMemcpyHostToDevice, S->stream);
+    };
+    const std::vector<Tile> t0 = filt(S->hT0full), t0w = filt(S->hT0Wfull);
+    CUDA_TRY(put(S->dT0, t0));
+    CUDA_TRY(put(S->dT0W, t0w));
+    S->nt0 = (int)t0.size();
+    S->nt0W = (int)t0w.size();
+    for (int l = 1; l < S->lmax; l++) {
+        const std::vector<Tile> a = filt(S->hTsmFull[l]), b = filt(S->hTreFull[l]);
+        const std::vector<Tile> c = filt(S->hTsmWFull[l]), d = filt(S->hTreWFull[l]);
+        CUDA_TRY(put(S->dTsm[l], a));
+        CUDA_TRY(put(S->dTre[l], b));
+        CUDA_TRY(put(S->dTsmW[l], c));
+        CUDA_TRY(put(S->dTreW[l], d));
+        S->ntsm[l] = (int)a.size();
+        S->ntre[l] = (int)b.size();
+        S->ntsmW[l] = (int)c.size();
+        S->ntreW[l] = (int)d.size();
+        S->plan.ntsm[l] = S->ntsm[l];
+        S->plan.ntre[l] = S->ntre[l];
+    }
+    S->plan.nt0 = S->nt0;
+    for (size_t q = 0; q < t0.size(); q++) {
+        const int k = t0[q].inst;
+        if (q > 0 && t0[q - 1].inst == k) continue;
+        Instance& I = S->inst[k];
+        I.tile_beg = (int)q;
+        I.dev.tile_beg = (int)q;
+        CUDA_TRY(cudaMemcpyAsync(&S->dI[k].tile_beg, &I.dev.tile_beg, sizeof(int), cudaMemcpyHostToDevice, S->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    S->in_lists = keep;
+    S->listed = 0;
+    for (char c : keep) S->listed += c;
+    if (S->gexec) {
+        cudaGraphExecDestroy(S->gexec);
+        cudaGraphDestroy(S->graph);
+        S->gexec = nullptr;
+        S->graph = nullptr;
+    }
+    return IFX_OK;
+}
+
 extern "C" ifx_status ifx_set_instance_active(ifx_solver* S, int inst, int active) {
     if (!S || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_set_instance_active: bad argument");
     if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_set_instance_active needs a METHOD-mode solver");
@@ -1956,6 +2024,12 @@ extern "C" ifx_status ifx_set_instance_active(ifx_solver* S, int inst, int activ
     I.dev.retired = active ? 0 : 1;
     CUDA_TRY(cudaMemcpyAsync(&S->dI[inst].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
     CUDA_TRY(cudaStreamSynchronize(S->stream));
+    // list the active instances only, once half of the listed ones are gone
+    // (or when an instance that is not listed comes back)
+    int nact = 0;
+    for (const Instance& J : S->inst) nact += J.dev.retired ? 0 : 1;
+    if ((active && !S->in_lists[inst]) || (!active && nact > 0 && S->inst.size() > 1 && 2 * nact <= S->listed))
+        IFX_TRY(compact_tiles(S));
     return IFX_OK;
 }
 

@@ -140,3 +140,34 @@ def test_server_fails_only_the_diverged_request():
         for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
             assert np.array_equal(v.result(rid, f), ref[f]), (rid, f)
     v.close()
+
+
+@pytest.mark.parametrize("prec,rows", [(capi.PREC_FP64, 1), (capi.PREC_MIXED, 1), (capi.PREC_MIXED, 4)])
+def test_retired_instances_leave_the_tile_lists(prec, rows):
+    """Retiring three of five instances compacts the device tile lists to the two
+    left (their partial sums move with them); an instance set active again is
+    listed again.  Every result equals the same case run alone."""
+    specs = [case(64, 48, prec=prec), case(56, 40, re=150.0, b=0.25, angle=15.0, prec=prec),
+             case(72, 40, re=200.0, b=0.35, angle=10.0, prec=prec), case(40, 40, re=60.0, prec=prec),
+             case(48, 48, re=120.0, prec=prec)]
+    s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+    s.set_mg_tile_rows(rows)
+    s.step(2)
+    for k in (0, 2, 3):
+        s.set_active(k, False)
+    s.step(3)
+    for k in (1, 4):
+        ref = alone(*specs[k], 5)
+        for f, a in ref.items():
+            assert np.array_equal(s.get(f, inst=k), a), (k, f)
+    s.set_active(2, True)
+    s.step(2)
+    for k, n in ((2, 4), (1, 7), (4, 7)):
+        ref = alone(*specs[k], n)
+        for f, a in ref.items():
+            assert np.array_equal(s.get(f, inst=k), a), (k, f)
+    s.set_exec_mode(ifx.EXEC_PERSISTENT)  # the persistent kernel on the compacted lists
+    s.step(1)
+    ref = alone(*specs[2], 5)
+    for f, a in ref.items():
+        assert np.array_equal(s.get(f, inst=2), a), f
