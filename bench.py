@@ -627,7 +627,7 @@ def main():
                      "peak_source": peak_kind, "traffic": traffic,
                      "bytes_per_launch": step_bytes_total / args.steps, "ms_per_launch": total_ms / args.steps,
                      "note": "working set ~30 MB is L2-resident; launch/barrier latency bound at this size"},
-        "phase_roofline": {"kernel": "k_smooth<float> finest level, launched alone", "bytes_per_cell": 13,
+        "phase_roofline": {"kernel": "finest-level smoothing sweep as the step launches it (k_smooth_grid_tma<float>), launched alone", "bytes_per_cell": 13,
                            "cells_per_launch": k_cells, "ms_per_launch": k_ms, "achieved_gbs": k_bw,
                            "frac": k_bw / peak, "grid_barrier_us": bar_us},
         "iterations": {"ppe_mean": sum(pits) / len(pits), "predictor_mean": sum(adits) / len(adits),

@@ -393,7 +393,9 @@ void       ifx_server_destroy(ifx_server* v);
 /* Measurement hook (no reference counterpart): launches one kernel of the
  * time step `reps` times back to back on the solver's stream and returns the
  * mean device time per launch (CUDA events).  kernel: 0 finest-level
- * multigrid smoothing sweep, 1 FP64 pressure operator apply (BiCGSTAB),
+ * multigrid smoothing sweep (the variant the step launches: from the block
+ * index for one instance, TMA-staged on the mixed path), 1 FP64 pressure
+ * operator apply (BiCGSTAB),
  * 2 predictor Jacobi sweep, 3 convection / predictor right-hand side,
  * 4 one grid barrier of the persistent per-step kernel (time per barrier),
  * 5 the small-level multigrid sub-cycle (one block per instance).
