@@ -228,6 +228,11 @@ struct alignas(16) ForceSample {
     double xi0, et0, xi1, et1, nx, ny, ds, del;
 };
 
+// The geometry arrays below that are declared const (cell types, ghost map,
+// force samples, sub-cycle image; and the stencil bytes of LevelDev) are read
+// only by every kernel except the per-step geometry of a moving body
+// (k_move_geometry, k_move_forces), which rewrites them between the steps'
+// phases.
 struct alignas(16) InstDev {
     int NX, NY, nx, ny, pitch;
     int singular, dirmask, body, lev0, nlev;
