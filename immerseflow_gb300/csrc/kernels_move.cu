@@ -301,7 +301,7 @@ __global__ void k_move_forces(const InstDev* __restrict__ I, const InstState* __
     const double nxw = nlx * cs - nly * sn, nyw = nlx * sn + nly * cs;
     const int i0 = min(max(ub_index(in.xc, in.nx, xs), 0), in.nx - 2);
     const int j0 = min(max(ub_index(in.yc, in.ny, ys), 0), in.ny - 2);
-    const double h = fmax(in.dx[i0], in.dy[j0]);
+    const double h = fmax(fmax(in.dx[i0], in.dx[i0 + 1]), fmax(in.dy[j0], in.dy[j0 + 1]));
     const double del = 1.5 * h;
     ForceSample e;
     e.c0 = i0 + j0 * P;

@@ -588,7 +588,9 @@ std::vector<ForceSample> build_force_table(const Instance& I) {
         double ys = I.cfg.body_cy + lx * I.sn + ly * I.cs;
         double nxw = nlx * I.cs - nly * I.sn, nyw = nlx * I.sn + nly * I.cs;
         int i0 = locate(I.xc, nx, xs), j0 = locate(I.yc, ny, ys);
-        double h = std::max(I.dx[i0], I.dy[j0]);
+        // the larger width of the two bracketing cells per direction: the same
+        // for a surface point and its mirror image on a symmetric grid
+        double h = std::max(std::max(I.dx[i0], I.dx[i0 + 1]), std::max(I.dy[j0], I.dy[j0 + 1]));
         double del = 1.5 * h;
         ForceSample f;
         f.c0 = i0 + j0 * P;

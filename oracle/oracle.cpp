@@ -1055,7 +1055,8 @@ void compute_forces(orc_solver* S) {
         double nxw = nlx * S->cs - nly * S->sn, nyw = nlx * S->sn + nly * S->cs;
         double ds = std::sqrt(a * a * st * st + b * b * ct * ct) * dth;
         int i0 = locate(S->xc, nx, xs), j0 = locate(S->yc, ny, ys);
-        double h = std::max(S->dx[i0], S->dy[j0]);
+        // larger width of the two bracketing cells per direction (mirror-invariant)
+        double h = std::max(std::max(S->dx[i0], S->dx[i0 + 1]), std::max(S->dy[j0], S->dy[j0 + 1]));
         double del = 1.5 * h;
         double ps = sample(S->p, xs, ys);
         double up = sample(S->u, xs + del * nxw, ys + del * nyw);
