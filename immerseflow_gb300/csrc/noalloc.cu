@@ -1,10 +1,10 @@
 // noalloc.cu -- a pressure solve that allocates nothing.
 //
 // Some callers cannot call cudaMalloc: a plug-in running inside a host
-// application that owns every device allocation through its own pool, code
-// that issues work while a stream is being captured into a CUDA graph (where
-// allocation calls are not permitted), or a service that accounts every byte
-// of device memory up front and forbids allocation on its request path.
+// application that owns every device allocation through its own pool, a
+// service that accounts every byte of device memory up front and forbids
+// allocation on its request path, or a latency-bound loop that cannot afford
+// the device-wide synchronisation that cudaFree implies.
 // ifx_ppe_reference_noalloc serves them: the caller passes its own device
 // buffers for the inputs and the output, and the solver's scratch (second
 // pressure buffer, stencil coefficients, reduction partials) lives in the

@@ -256,9 +256,9 @@ ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
  * cavity configuration.  Its scratch is ~0.84 MB of device memory per GPU. */
 #define IFX_NOALLOC_MAX_CELLS (132 * 132)
 /* Pressure solve for callers that cannot allocate device memory (a plug-in
- * whose host application owns every device allocation, work issued while a
- * stream is captured into a graph, a service that budgets device memory up
- * front).  No counterpart in the reference: it is the solve of ifx_ppe_reference
+ * whose host application owns every device allocation, a service that budgets
+ * device memory up front, a latency-bound loop that cannot afford the device
+ * synchronisation cudaFree implies).  No counterpart in the reference: it is the solve of ifx_ppe_reference
  * (PPESolver's Jacobi Laplace with p = 100 on the i=0 / j=0 ghosts, stopped when
  * the signed residual sum drops to tol or after itermax sweeps) run on buffers
  * the caller owns: d_dx, d_dy (nx*ny each, the full width arrays of readGridData,

@@ -2,9 +2,10 @@
 
 ifx_ppe_reference_noalloc exists for callers that cannot allocate device
 memory themselves: a plug-in inside a host application that owns every device
-allocation, work issued while a stream is being captured into a graph, or a
-service with a fixed device-memory budget.  Here the caller's buffers come
-from torch; the result is compared with ifx_ppe_reference on a solver handle
+allocation, a service with a fixed device-memory budget, or a latency-bound
+loop that cannot afford the device synchronisation of cudaFree.  Here the
+caller's buffers come from torch; the result is compared with
+ifx_ppe_reference on a solver handle
 (same kernels, so the tolerance of the other reference-mode tests, 1e-12
 relative, holds), on two calls in a row so that leftovers in the shared
 scratch array cannot go unnoticed.  The file name sorts last, so a run that
