@@ -96,6 +96,19 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """Largest x over the ranks: each rank times its own replica and the job
+    ends with the slowest one.  With one rank, x itself."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -431,8 +444,8 @@ def reference_path(ifx, capi, cases, steps=20, cpu=True):
     return {"workload": "REFERENCE mode (the reference's ADsolver step), uniform grids on [0,1]^2, "
                         "vortex IC, Re 150, dt 1e-3, AD_itermax 25",
             "unit": METRIC, "lines": lines,
-            "note": "the reference's own CUDA executable builds from its sources, which do not travel to "
-                    "the GPU box; this is the drop-in REFERENCE mode on the same scheme"}
+            "note": "the reference's own CUDA executable builds from its sources, which are not present on "
+                    "the GPU host; this is the drop-in REFERENCE mode on the same scheme"}
 
 
 def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
@@ -562,14 +575,12 @@ def main():
     st = s.stats()
     u_m, v_m = s.get(capi.FIELD_U), s.get(capi.FIELD_V)
     cd_m, cl_m = st.cd, st.cl
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world)
     value = world * cells * args.steps / (total_ms * 1e-3) / 1e6
 
     # plain FP64 path on the same steps
     s64, total64, launches64, _, _, pits64, _ = timed(capi.PREC_FP64)
+    total64 = max_over_ranks(total64, world)
     st64 = s64.stats()
     u64, v64 = s64.get(capi.FIELD_U), s64.get(capi.FIELD_V)
     err_u = float(np.sqrt(np.sum((u_m - u64) ** 2 + (v_m - v64) ** 2) / np.sum(u64 ** 2 + v64 ** 2)))
@@ -591,7 +602,7 @@ def main():
             lib_out = s.get(f).ravel()
             a[:] = lib_out
     barrier()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * cells * args.steps / e2e_s / 1e6
     nbytes = 3 * nx * ny * 8
 

@@ -1,6 +1,6 @@
 // oracle.cpp -- CPU FP64 restatement of the ImmerseFlow++ hot path.
 //
-// TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+// TEST INFRASTRUCTURE ONLY: the oracle for the CUDA path and the timed CPU
 // baseline.  Nothing in the product library links or calls this file.
 //
 // Parity is pinned against the reference's result files (results/uc.dat,

@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU FP64 restatement of the ImmerseFlow++ hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle for the CUDA path:
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it;
  * the product library never links or calls it.
  *
