@@ -267,8 +267,10 @@ ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
  * It calls no cudaMalloc/cudaFree: its scratch is one fixed device array inside
  * this library, present on every GPU that loads the library until exit, so
  * nx*ny above IFX_NOALLOC_MAX_CELLS returns IFX_ERR_ARG.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the array, so
+ * device looks up that array's device address (cudaGetSymbolAddress) and keeps
+ * it for the life of the process; make that first call before any stream
+ * capture, and do not cudaDeviceReset a device between calls (the kept
+ * address would no longer be valid).  All calls share the array, so
  * calls that overlap on the GPU (other streams, other threads) race: serialise
  * them. */
 ifx_status ifx_ppe_reference_noalloc(const double* d_dx, const double* d_dy, int nx, int ny, double* d_p,
