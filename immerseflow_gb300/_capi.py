@@ -43,6 +43,7 @@ FIELD_XC = 8
 FIELD_YC = 9
 
 PATH_MAX = 512
+MAX_CELLS = 1 << 28  # IFX_MAX_CELLS: largest instance, cells including the ghost ring
 
 
 class Config(C.Structure):

@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <exception>
 #include <vector>
 
 #include "ifx_host.h"
@@ -635,6 +636,8 @@ void initial_field(const Instance& I, std::vector<double>& u, std::vector<double
 
 ifx_status validate(const ifx_config* c) {
     if (c->nx < 4 || c->ny < 4) return set_error(IFX_ERR_ARG, "method mode needs nx, ny >= 4");
+    if ((c->nx + 2LL) * (c->ny + 2LL) > IFX_MAX_CELLS)
+        return set_error(IFX_ERR_ARG, "nx, ny give more than IFX_MAX_CELLS cells");
     if (!(c->dt > 0) || !(c->re > 0)) return set_error(IFX_ERR_ARG, "dt and Re must be positive");
     if (c->mg_pre < 1 || c->mg_post < 1) return set_error(IFX_ERR_ARG, "multigrid sweeps must be >= 1");
     if (c->ad_itermax < 1 || c->ppe_itermax < 0) return set_error(IFX_ERR_ARG, "bad iteration caps");
@@ -1874,8 +1877,11 @@ extern "C" ifx_status ifx_create_batch(int n, const ifx_config* cfgs, const doub
                                        const double* const* yfs, ifx_solver** out) {
     if (!out || n < 1 || !cfgs || !xfs || !yfs) return set_error(IFX_ERR_ARG, "ifx_create_batch: bad argument");
     *out = nullptr;
-    for (int k = 0; k < n; k++)
+    for (int k = 0; k < n; k++) {
         if (!xfs[k] || !yfs[k]) return set_error(IFX_ERR_ARG, "ifx_create_batch: null grid");
+        if (cfgs[k].nx < 1 || cfgs[k].ny < 1 || (cfgs[k].nx + 2LL) * (cfgs[k].ny + 2LL) > IFX_MAX_CELLS)
+            return set_error(IFX_ERR_ARG, "ifx_create_batch: nx, ny must be >= 1 and give at most IFX_MAX_CELLS cells");
+    }
     ifx_solver* S = nullptr;
     IFX_TRY(new_solver(&S));
     ifx_status st;
@@ -1899,8 +1905,14 @@ extern "C" ifx_status ifx_create(const ifx_config* cfg, const double* xf, const 
 
 extern "C" ifx_status ifx_create_from_file(const char* inputs_path, ifx_solver** out) {
     ifx_config c;
-    IFX_TRY(ifx_config_read(inputs_path, &c));
-    std::vector<double> xf(c.nx + 1), yf(c.ny + 1);
+    IFX_TRY(ifx_config_read(inputs_path, &c));  // bounds nx, ny by IFX_MAX_CELLS
+    std::vector<double> xf, yf;
+    try {
+        xf.resize((size_t)c.nx + 1);
+        yf.resize((size_t)c.ny + 1);
+    } catch (const std::exception&) {
+        return set_error(IFX_ERR_NOMEM, "ifx_create_from_file: host grid arrays");
+    }
     IFX_TRY(ifx_grid_read(c.xgrid, c.nx + 1, xf.data()));
     IFX_TRY(ifx_grid_read(c.ygrid, c.ny + 1, yf.data()));
     return ifx_create(&c, xf.data(), yf.data(), out);

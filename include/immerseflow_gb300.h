@@ -185,6 +185,11 @@ ifx_status ifx_write_tecplot(const char* path, int nx, int ny, const double* x,
 /* ----------------------------------------------------------------- solver */
 typedef struct ifx_solver ifx_solver;
 
+/* Largest instance, in cells including the ghost ring ((nx+2)*(ny+2)): the
+ * kernels index an instance's cells with 32-bit integers.  ifx_config_read
+ * refuses larger grids with IFX_ERR_PARSE, the create calls with IFX_ERR_ARG. */
+#define IFX_MAX_CELLS (1 << 28)
+
 /* allocation + readGridData + initializeData (src/main.cu:86-90,
  * src/include/preSim.cu:147-240).  xf has cfg->nx+1 entries, yf cfg->ny+1. */
 ifx_status ifx_create(const ifx_config* cfg, const double* xf, const double* yf,

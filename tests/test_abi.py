@@ -36,8 +36,8 @@ def test_python_bindings_cover_the_header():
 def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "immerseflow_gb300.h"\n'
-                   'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(ifx_config), sizeof(ifx_stats),'
-                   ' offsetof(ifx_config, xgrid), offsetof(ifx_stats, status)); return 0;}\n')
+                   'int main(void){printf("%zu %zu %zu %zu %d\\n", sizeof(ifx_config), sizeof(ifx_stats),'
+                   ' offsetof(ifx_config, xgrid), offsetof(ifx_stats, status), IFX_MAX_CELLS); return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
@@ -45,6 +45,7 @@ def test_struct_layout_matches_header(tmp_path):
     assert int(out[1]) == C.sizeof(capi.Stats)
     assert int(out[2]) == capi.Config.xgrid.offset
     assert int(out[3]) == capi.Stats.status.offset
+    assert int(out[4]) == capi.MAX_CELLS
 
 
 def test_config_default_matches_python_mirror():
