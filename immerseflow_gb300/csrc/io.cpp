@@ -282,7 +282,7 @@ extern "C" ifx_status ifx_write_tecplot(const char* path, int nx, int ny, const 
     std::fprintf(fp, "VARIABLES = \"X\",\"Y\",\"T\"\n");
     std::fprintf(fp, "ZONE T=\"BIG ZONE\", I=%d, J=%d, DATAPACKING=POINT\n", nx, ny);
     for (int j = 0; j < ny; j++)
-        for (int i = 0; i < nx; i++) std::fprintf(fp, "%f,%f,%f\n", x[i], y[j], q[i + j * nx]);
+        for (int i = 0; i < nx; i++) std::fprintf(fp, "%f,%f,%f\n", x[i], y[j], q[i + (size_t)j * nx]);
     if (std::fclose(fp) != 0) return set_error(IFX_ERR_IO, std::string("Error closing file: ") + path);
     return IFX_OK;
 }
