@@ -63,3 +63,15 @@ def test_status_strings_and_no_device_error():
     L = ifx.lib()
     assert L.ifx_status_string(capi.IFX_ERR_PARSE) == b"parse error"
     assert L.ifx_version().startswith(b"immerseflow_gb300")
+
+
+def test_noalloc_solve_refuses_bad_arguments_before_device_access():
+    # null buffers, too-small grids and grids above IFX_NOALLOC_MAX_CELLS are
+    # refused by the host checks that precede any CUDA call
+    lib = ifx.lib()
+    d = C.c_void_p(16)
+    cases = [(None, d, 10, 10, d), (d, None, 10, 10, d), (d, d, 10, 10, None), (d, d, 2, 10, d), (d, d, 10, 2, d),
+             (d, d, 200, 200, d), (d, d, 133, 132, d)]
+    for dx, dy, nx, ny, p in cases:
+        st = lib.ifx_ppe_reference_noalloc(dx, dy, nx, ny, p, 10, 1e-6, None, None)
+        assert st == capi.IFX_ERR_ARG, (nx, ny)
