@@ -29,23 +29,36 @@ roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
 cpu_baseline: the CPU oracle (same scheme, FP64, all host threads);
 batched   : the batched sweep (256 seeded instances of uneven grid, Re and
             ellipse, one batched solver each for mixed and plain FP64,
-            execution mode picked by the autotuner), Mcell-updates/s, solves/s
-            of 500-step runs, error of mixed vs FP64 per instance;
+            execution mode picked by the autotuner): Mcell-updates/s and
+            roofline over the same window of steps in both precisions, error
+            of mixed vs FP64 per instance, and solves/s measured over a full
+            500-step mixed run (batched.solve);
 ellipse   : the large single-instance configuration (1024x768 ellipse,
-            Re 300), autotuned, mixed and plain FP64;
+            Re 300), autotuned, mixed and plain FP64, both against the CPU
+            oracle after the same steps (Linf velocity and divergence errors);
+cavity    : the lid-driven cavity (128x128, Re 100, dt 1e-3, pressure to
+            1e-8) over 2000 steps from rest, mixed and plain FP64, both against
+            the CPU oracle after the same 2000 steps;
 long_run_accuracy: the cylinder over 1000 steps in both precisions: largest
             drag and lift deviation of any step, velocity error at the end;
 moving_body: the cylinder heaving (prescribed motion, geometry redone on the
             device every step), mixed and plain FP64, beside the cylinder at rest;
 reference_path: the REFERENCE-mode step (the reference's own scheme) at 52^2,
             130^2 and 514^2 cells, GPU and one CPU thread;
-served    : a seeded Poisson request stream through the continuous-batching
-            server (real-time arrivals, cohorts admitted by device memory),
-            solves/s, Mcell-updates/s and p50/p99 latency, the two smallest
-            requests re-run alone in FP64 for the error; the same stream
-            served in plain FP64 (served.fp64), and both precisions with every
-            request arriving at t = 0 (served.capacity: the server's
-            throughput, mixed over FP64).
+reference_cuda: the reference's own AD-only CUDA executable (oracle/_ref,
+            built on this machine from the staged reference sources) on the
+            same three grids, per-step wall time with its printing to a file
+            and to /dev/null;
+served    : the first 16 requests of the seeded served stream (cylinder or
+            ellipse, grids log-uniform 64^2..1024^2, Re U[50,1000], 200..2000
+            steps) through the continuous-batching server, Poisson arrivals at
+            1/s in real time, cohorts admitted by device memory: solves/s,
+            Mcell-updates/s and p50/p99 latency in mixed precision and in plain
+            FP64 (served.fp64), every request's mixed velocity against its FP64
+            result, and both precisions with every request arriving at t = 0
+            (served.capacity: the server's throughput, mixed over FP64);
+summary   : the headline figures of all blocks in a few hundred bytes, the
+            last key of the line.
 
 --impl reference times the CPU restatement of the reference scheme (the
 reference's pressure solver does not compile and it has no projection or
@@ -81,8 +94,13 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch", type=int, default=256, help="instances of the batched sweep (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5)
-    ap.add_argument("--serve", type=int, default=48, help="requests of the served stream (0: skip)")
-    ap.add_argument("--rate", type=float, default=16.0, help="served stream arrival rate [1/s]")
+    ap.add_argument("--batch-solve-steps", type=int, default=500,
+                    help="steps of the mixed batched run that solves/s is measured over")
+    ap.add_argument("--serve", type=int, default=16, help="requests of the served stream (0: skip)")
+    ap.add_argument("--rate", type=float, default=1.0, help="served stream arrival rate [1/s]")
+    ap.add_argument("--cavity-steps", type=int, default=2000, help="steps of the cavity line (0: skip)")
+    ap.add_argument("--no-reference-build", action="store_true",
+                    help="skip the timing of the reference's own CUDA executable")
     ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
     ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch", "moving"],
@@ -214,17 +232,22 @@ def copy_cfg(cfg, precision):
     return c
 
 
-def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
+def batched_sweep(ifx, capi, cases, n_inst, steps, solve_steps, peak):
     """Batched sweep: n_inst uneven instances (seeded), mixed vs plain FP64, each
-    advanced in one batch; execution mode chosen by the autotuner."""
+    advanced in one batch; execution mode chosen by the autotuner (which restores
+    the state).  Both precisions time the same window (steps 3 .. 2 + steps from
+    the impulsive start) for the rate and the roofline; the mixed batch then runs
+    on to `solve_steps` steps, and solves/s is measured over that whole run."""
     res, fields = {}, {}
     for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
         specs = cases.batch_sample(count=n_inst, seed=0, precision=prec)
         ncell = sum(c.nx * c.ny for c, _, _ in specs)
         s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
-        s.step(max(1, warm - 2))
         mode, _ = s.autotune(steps=1)
+        s.synchronize()
+        w0 = time.perf_counter()
         s.step(2)
+        ms_head = s.last_step_ms()
         l0 = s.stats().kernel_launches
         s.step(steps)
         ms = s.last_step_ms()
@@ -242,6 +265,14 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
                      "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes(),
                      "roofline": {"bound": "hbm", "achieved": nbytes / (ms / steps * 1e-3) / 1e9, "unit": "GB/s",
                                   "bytes_per_step": nbytes, "peak": peak, "frac": nbytes / (ms / steps * 1e-3) / 1e9 / peak}}
+        if name == "mixed" and solve_steps > 2 + steps:
+            s.step(solve_steps - 2 - steps)
+            dev_ms = ms_head + ms + s.last_step_ms()
+            s.synchronize()
+            wall = time.perf_counter() - w0
+            res["solve"] = {"steps": solve_steps, "device_s": dev_ms * 1e-3, "wall_s": wall,
+                            "solves_per_s": n_inst / wall, "value": ncell * solve_steps / wall / 1e6,
+                            "unit": METRIC, "all_finite": bool(all(np.isfinite(s.stats(k).cd) for k in range(n_inst)))}
         res["cells"] = ncell
         s.close()
     errs = [rel_l2(np.concatenate([um.ravel(), vm.ravel()]), np.concatenate([u6.ravel(), v6.ravel()]))
@@ -251,22 +282,26 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, warm, peak):
                             "Re U[50,300], ellipse aspect U[0.1,1], angle U[-30,30] deg",
                 "instances": n_inst, "timed_steps": steps,
                 "speedup_mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
-                "solves_per_s_500_steps": n_inst / (res["mixed"]["ms_per_step"] * 1e-3 * 500),
                 "accuracy_vs_fp64": {"rel_l2_velocity_max": max(errs), "rel_l2_velocity_median": float(np.median(errs)),
-                                     "cd_rel_err_max": max(cds)},
+                                     "cd_rel_err_max": max(cds), "after_steps": 2 + steps},
                 "l2": "inputs larger than L2 (device_bytes)"})
     return res
 
 
-def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True, max_cohort=32):
-    """Served stream through the continuous-batching server: seeded arrivals
-    (Poisson at `rate` per second in real time, or all at t = 0 when rate is
-    None: the server's capacity); latency = completion - arrival."""
-    stream = cases.served_stream(nreq, rate or 1.0, seed=0, precision=prec, nmin=64, nmax=512, smin=20, smax=200)
+def served_stream(ifx, capi, cases, nreq, rate, budget, prec, max_cohort=32, keep=False):
+    """Served stream through the continuous-batching server: the first `nreq`
+    requests of the seeded C5 stream (cylinder or ellipse, grids log-uniform
+    64^2..1024^2, Re U[50,1000], 200..2000 steps), arriving in real time as a
+    Poisson process at `rate` per second, or all at t = 0 when rate is None
+    (the server's capacity); latency = completion - arrival.  With `keep`, the
+    velocity and drag of every finished request are returned for the accuracy
+    comparison."""
+    stream = cases.served_stream(nreq, rate or 1.0, seed=0, precision=prec)
     if rate is None:
         stream = [(0.0,) + tuple(r[1:]) for r in stream]
     srv = ifx.Server(budget, max_cohort=max_cohort)
-    arr, done, work, spec_of = {}, {}, 0, {}
+    arr, done, work, index = {}, {}, 0, {}
+    kept = {}
     t0 = time.perf_counter()
     i = 0
     ticks = 0
@@ -277,7 +312,7 @@ def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True, max_co
             t_arr, cfg, xf, yf, n = stream[i]
             rid = srv.submit(cfg, xf, yf, n)
             arr[rid] = t_arr
-            spec_of[rid] = (cfg, xf, yf, n)
+            index[rid] = i
             work += cfg.nx * cfg.ny * n
             i += 1
         info = srv.info()
@@ -291,40 +326,44 @@ def served_stream(ifx, capi, cases, nreq, rate, budget, prec, check=True, max_co
         tnow = time.perf_counter() - t0
         for rid in srv.poll():
             done[rid] = tnow
+            if keep:
+                st = srv.stats(rid)
+                kept[index[rid]] = (np.concatenate([srv.result(rid, capi.FIELD_U).ravel(),
+                                                    srv.result(rid, capi.FIELD_V).ravel()]), st.cd, st.cl)
+            srv.release(rid)
     lat = np.array([done[r] - arr[r] for r in arr]) * 1e3
     span = max(done.values()) - stream[0][0]
-    out = {"workload": f"served stream: {nreq} requests (seed 0), "
-                       + (f"Poisson arrivals at {rate}/s" if rate else "all arriving at t = 0 (capacity)")
-                       + ", cylinder or ellipse, grids log-uniform 64^2..512^2, Re U[50,1000], 20..200 steps each",
-           "requests": nreq, "solves_per_s": nreq / span, "value": work / span / 1e6, "unit": METRIC,
+    sizes = [c.nx for _, c, _, _, _ in stream]
+    nsteps = [n for _, _, _, _, n in stream]
+    out = {"workload": f"served stream: the first {nreq} requests of the seeded stream (seed 0) with grids "
+                       "log-uniform 64^2..1024^2, Re U[50,1000], 200..2000 steps, cylinder or ellipse; "
+                       + (f"Poisson arrivals at {rate}/s" if rate else "all arriving at t = 0 (capacity)"),
+           "requests": nreq, "grid_range": [min(sizes), max(sizes)], "steps_range": [min(nsteps), max(nsteps)],
+           "cell_steps": work, "solves_per_s": nreq / span, "value": work / span / 1e6, "unit": METRIC,
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
            "ticks": ticks, "peak_cohorts": peak_cohorts, "hbm_budget_bytes": budget,
            "precision": "mixed" if prec == capi.PREC_MIXED else "fp64"}
-    if check:
-        # accuracy: the two smallest requests re-run alone in plain FP64
-        small = sorted(arr, key=lambda r: spec_of[r][0].nx * spec_of[r][0].ny)[:2]
-        errs = []
-        for r in small:
-            cfg, xf, yf, n = spec_of[r]
-            s = ifx.Solver.create(copy_cfg(cfg, capi.PREC_FP64), xf, yf)
-            s.step(n)
-            a = np.concatenate([srv.result(r, capi.FIELD_U).ravel(), srv.result(r, capi.FIELD_V).ravel()])
-            b = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
-            errs.append(rel_l2(a, b))
-            s.close()
-        out["accuracy_vs_fp64"] = {"rel_l2_velocity_max": max(errs), "requests_checked": len(errs)}
     srv.close()
-    return out
+    return (out, kept) if keep else out
 
 
 def served_lines(ifx, capi, cases, nreq, rate, budget):
     """The Poisson stream (latency) and the all-at-once stream (capacity), each
-    served in mixed precision and in plain FP64."""
-    res = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_MIXED)
-    res["fp64"] = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_FP64, check=False)
-    cap = {"mixed": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_MIXED, check=False),
-           "fp64": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_FP64, check=False)}
+    served in mixed precision and in plain FP64.  Every request's mixed result
+    is compared with its plain FP64 result (a request's result does not depend
+    on its cohort, so the FP64 stream gives the FP64 answer of each request)."""
+    res, km = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_MIXED, keep=True)
+    res["fp64"], k6 = served_stream(ifx, capi, cases, nreq, rate, budget, capi.PREC_FP64, keep=True)
+    errs = {k: rel_l2(km[k][0], k6[k][0]) for k in km}
+    cds = {k: abs(km[k][1] - k6[k][1]) / max(abs(k6[k][1]), 1e-12) for k in km}
+    big = max(km, key=lambda k: km[k][0].size)
+    res["accuracy_vs_fp64"] = {"requests_checked": len(errs), "rel_l2_velocity_max": max(errs.values()),
+                               "rel_l2_velocity_median": float(np.median(list(errs.values()))),
+                               "cd_rel_err_max": max(cds.values()),
+                               "largest_request": {"cells": km[big][0].size // 2, "rel_l2_velocity": errs[big]}}
+    cap = {"mixed": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_MIXED),
+           "fp64": served_stream(ifx, capi, cases, nreq, None, budget, capi.PREC_FP64)}
     cap["speedup_mixed_over_fp64"] = cap["mixed"]["value"] / cap["fp64"]["value"]
     res["capacity"] = cap
     return res
@@ -352,13 +391,44 @@ def long_run_accuracy(ifx, capi, cases, steps=1000):
             "cd_final": float(h6[-1, 1]), "cl_final": float(h6[-1, 2])}
 
 
-def ellipse_line(ifx, capi, cases, steps=10):
+def _oracle_solver(cfg, xf, yf):
+    """The CPU oracle (FP64 restatement of the same scheme) on all host threads:
+    the checker of the accuracy lines."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle
+
+    return _oracle.Oracle().method(cfg, xf, yf, os.cpu_count() or 1)
+
+
+def vs_oracle(capi, get, stats, o):
+    """Errors of a GPU result against the oracle after the same steps: Linf of
+    u and v relative to the oracle's largest |velocity|, relative L2 of the
+    velocity, Linf of the per-cell divergence field (absolute), both max |div|,
+    and drag / lift relative to the oracle's drag."""
+    ug, vg = get(capi.FIELD_U), get(capi.FIELD_V)
+    uo, vo = o.get(capi.FIELD_U), o.get(capi.FIELD_V)
+    vmax = max(float(np.abs(uo).max()), float(np.abs(vo).max()), 1e-300)
+    so = o.stats()
+    out = {"linf_velocity": float(max(np.abs(ug - uo).max(), np.abs(vg - vo).max()) / vmax),
+           "rel_l2_velocity": rel_l2(np.concatenate([ug.ravel(), vg.ravel()]), np.concatenate([uo.ravel(), vo.ravel()])),
+           "linf_divergence": float(np.abs(get(capi.FIELD_DIV) - o.get(capi.FIELD_DIV)).max()),
+           "max_div": stats.max_div, "max_div_oracle": so.max_div}
+    if abs(so.cd) > 0:
+        out["cd_rel_err"] = abs(stats.cd - so.cd) / abs(so.cd)
+        out["cl_err_rel_to_cd"] = abs(stats.cl - so.cl) / abs(so.cd)
+    return out
+
+
+def ellipse_line(ifx, capi, cases, steps=10, oracle=True):
     """The large single-instance configuration: ellipse of aspect 0.2 and chord
     1 at 10 deg, 1024x768 cells on a 20x12 domain, Re 300, dt 2e-3; autotuned,
-    mixed and plain FP64 (device time, CUDA events)."""
+    mixed and plain FP64 (device time, CUDA events).  Both results are compared
+    with the CPU oracle after the same 3 + `steps` steps (Linf velocity and
+    divergence errors)."""
     out = {"workload": "ellipse aspect 0.2, chord 1, 10 deg, 20x12 domain, 1024x768 tanh-stretched, Re 300, dt 2e-3",
            "unit": METRIC, "steps": steps}
     fields = {}
+    solvers = {}
     for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
         cfg, xf, yf = cases.ellipse(precision=prec)
         s = ifx.Solver.create(cfg, xf, yf)
@@ -372,10 +442,81 @@ def ellipse_line(ifx, capi, cases, steps=10):
                      "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters,
                      "predictor_iters_last": st.last_ad_iters, "cd": st.cd}
         fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
-        s.close()
+        solvers[name] = s
     out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["rel_l2_velocity_vs_fp64"] = rel_l2(fields["mixed"], fields["fp64"])
+    if oracle:
+        cfg, xf, yf = cases.ellipse(precision=capi.PREC_FP64)
+        o = _oracle_solver(cfg, xf, yf)
+        o.step(3 + steps)
+        out["vs_oracle"] = {name: vs_oracle(capi, s.get, s.stats(), o) for name, s in solvers.items()}
+        out["vs_oracle"]["steps"] = 3 + steps
+    for s in solvers.values():
+        s.close()
     return out
+
+
+def cavity_line(ifx, capi, cases, steps=2000, oracle=True):
+    """Lid-driven cavity: unit square, uniform 128x128, lid u = 1, no-slip
+    walls, Re 100, dt 1e-3, pressure to 1e-8, `steps` steps from rest (device
+    time of the last steps - 1, CUDA events), mixed and plain FP64; both against
+    the CPU oracle after the same steps."""
+    out = {"workload": "lid-driven cavity, unit square, uniform 128x128, lid u=1, Re 100, dt 1e-3, "
+                       f"pressure to 1e-8, {steps} steps", "unit": METRIC, "steps": steps}
+    solvers = {}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        cfg, xf, yf = cases.cavity(precision=prec)
+        s = ifx.Solver.create(cfg, xf, yf)
+        s.step(1)
+        s.autotune(steps=1)
+        s.step(steps - 1)
+        ms = s.last_step_ms()
+        st = s.stats()
+        out[name] = {"value": cfg.nx * cfg.ny * (steps - 1) / (ms * 1e-3) / 1e6, "ms_per_step": ms / (steps - 1),
+                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters,
+                     "predictor_iters_last": st.last_ad_iters, "max_div": st.max_div}
+        solvers[name] = s
+    out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    gm, g6 = solvers["mixed"], solvers["fp64"]
+    out["rel_l2_velocity_mixed_vs_fp64"] = rel_l2(
+        np.concatenate([gm.get(capi.FIELD_U).ravel(), gm.get(capi.FIELD_V).ravel()]),
+        np.concatenate([g6.get(capi.FIELD_U).ravel(), g6.get(capi.FIELD_V).ravel()]))
+    if oracle:
+        cfg, xf, yf = cases.cavity(precision=capi.PREC_FP64)
+        o = _oracle_solver(cfg, xf, yf)
+        t0 = time.perf_counter()
+        o.step(steps)
+        dt = time.perf_counter() - t0
+        out["vs_oracle"] = {name: vs_oracle(capi, s.get, s.stats(), o) for name, s in solvers.items()}
+        out["cpu_oracle"] = {"value": cfg.nx * cfg.ny * steps / dt / 1e6, "cores": os.cpu_count() or 1}
+    for s in solvers.values():
+        s.close()
+    return out
+
+
+def reference_cuda(steps=(50, 20, 6)):
+    """The reference's own AD-only CUDA executable (oracle/_ref, built from the
+    staged, unmodified sources) on the REFERENCE-mode workload at 52^2, 130^2
+    and 514^2 cells (ghosts included): seconds per ADsolver step as the
+    difference of two runs of k and 2k steps over k, with its per-iteration
+    printing sent to a file (as shipped) and to /dev/null.  Each of its steps
+    also writes uc.dat and vc.dat (src/include/ADSolver.cu:374-375)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_run
+
+    if not ref_run.available():
+        return {"unavailable": "reference executable not built (its sources were not staged)"}
+    lines = []
+    with tempfile.TemporaryDirectory() as d:
+        for n, k in zip((50, 128, 512), steps):
+            row = {"grid": [n + 2, n + 2], "steps": k}
+            for name, dest in (("stdout_file", os.path.join(d, "stdout.txt")), ("stdout_devnull", os.devnull)):
+                sec, t1, t2 = ref_run.time_per_step(os.path.join(d, f"c{n}"), n, k, stdout_path=dest)
+                row[name] = {"value": n * n / sec / 1e6, "ms_per_step": sec * 1e3, "run_s": [t1, t2]}
+            lines.append(row)
+    return {"workload": "the reference's ADsolver (src/include/ADSolver.cu:268-395), uniform grids on [0,1]^2, "
+                        "vortex IC, Re 150, dt 1e-3, AD_itermax 25", "unit": METRIC, "lines": lines,
+            "build": "oracle/ref.mk: nvcc -gencode arch=compute_103a,code=sm_103a, cudaMalloc padded (oracle/ref_guard.h)"}
 
 
 def moving_line(ifx, capi, cases, steps=50):
@@ -443,9 +584,61 @@ def reference_path(ifx, capi, cases, steps=20, cpu=True):
         s.close()
     return {"workload": "REFERENCE mode (the reference's ADsolver step), uniform grids on [0,1]^2, "
                         "vortex IC, Re 150, dt 1e-3, AD_itermax 25",
-            "unit": METRIC, "lines": lines,
-            "note": "the reference's own CUDA executable builds from its sources, which are not present on "
-                    "the GPU host; this is the drop-in REFERENCE mode on the same scheme"}
+            "unit": METRIC, "lines": lines}
+
+
+def bench_config(cells, world):
+    """The workload's config, identical in both arms of the bench."""
+    return {"workload": WORKLOAD, "grid": [384, 256], "cells": cells, "parallelism": f"replicas x{world}",
+            "ppe_tol": 1e-8, "l2": "flushed before every timed GPU step (256 MB write)"}
+
+
+def _r(x, d=3):
+    return None if x is None else float(f"{x:.{d}g}")
+
+
+def summary(line):
+    """The figures of the long blocks in a few hundred bytes, as the last key of
+    the line: Mcell-updates/s (M), mixed/FP64 ratios (x), errors, fractions."""
+    out = {"cyl": {"M": _r(line["value"]), "fp64_M": _r(line["plain_fp64"]["value"]),
+                   "x": _r(line["plain_fp64"]["speedup_mixed_over_fp64"]), "e2e_M": _r(line["e2e"]["value"]),
+                   "frac": _r(line["roofline"]["frac"]), "err": _r(line["accuracy_vs_fp64"]["rel_l2_velocity"], 2)},
+           "sweep_frac": _r(line["phase_roofline"]["frac"])}
+    if "cavity" in line:
+        c = line["cavity"]
+        out["cavity"] = {"M": _r(c["mixed"]["value"]), "fp64_M": _r(c["fp64"]["value"]),
+                         "x": _r(c["speedup_mixed_over_fp64"])}
+        if "vs_oracle" in c:
+            out["cavity"]["linf_vs_oracle"] = [_r(c["vs_oracle"]["fp64"]["linf_velocity"], 2),
+                                               _r(c["vs_oracle"]["mixed"]["linf_velocity"], 2)]
+    if "ellipse" in line:
+        e = line["ellipse"]
+        out["ellipse"] = {"M": _r(e["mixed"]["value"]), "fp64_M": _r(e["fp64"]["value"]),
+                          "x": _r(e["speedup_mixed_over_fp64"])}
+        if "vs_oracle" in e:
+            out["ellipse"]["linf_vs_oracle"] = [_r(e["vs_oracle"]["fp64"]["linf_velocity"], 2),
+                                                _r(e["vs_oracle"]["mixed"]["linf_velocity"], 2)]
+            out["ellipse"]["linf_div"] = [_r(e["vs_oracle"]["fp64"]["linf_divergence"], 2),
+                                          _r(e["vs_oracle"]["mixed"]["linf_divergence"], 2)]
+    if "batched" in line:
+        b = line["batched"]
+        out["batch"] = {"M": _r(b["mixed"]["value"]), "fp64_M": _r(b["fp64"]["value"]),
+                        "x": _r(b["speedup_mixed_over_fp64"]), "frac": _r(b["mixed"]["roofline"]["frac"]),
+                        "err": _r(b["accuracy_vs_fp64"]["rel_l2_velocity_max"], 2)}
+        if "solve" in b:
+            out["batch"]["solves_s"] = _r(b["solve"]["solves_per_s"])
+    if "served" in line:
+        v = line["served"]
+        out["served"] = {"n": v["requests"], "solves_s": _r(v["solves_per_s"]),
+                         "p50_ms": _r(v["latency_ms"]["p50"]), "p99_ms": _r(v["latency_ms"]["p99"]),
+                         "fp64_p50_ms": _r(v["fp64"]["latency_ms"]["p50"]),
+                         "fp64_p99_ms": _r(v["fp64"]["latency_ms"]["p99"]),
+                         "cap_x": _r(v["capacity"]["speedup_mixed_over_fp64"]),
+                         "err": _r(v["accuracy_vs_fp64"]["rel_l2_velocity_max"], 2)}
+    if "reference_cuda" in line and "lines" in line["reference_cuda"]:
+        out["ref_cuda_M"] = [_r(r["stdout_devnull"]["value"]) for r in line["reference_cuda"]["lines"]]
+        out["ref_mode_M"] = [_r(r["gpu_value"]) for r in line["reference_path"]["lines"]]
+    return out
 
 
 def cpu_oracle_run(cfg, xf, yf, seconds, min_steps=3, warm=1, nthreads=None):
@@ -492,7 +685,7 @@ def main():
         line = {"metric": METRIC, "value": val, "unit": METRIC, "impl": "reference", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "grid": [384, 256], "solver": "CPU restatement (oracle), FP64"},
+                "config": bench_config(cells, world), "solver": "CPU restatement (oracle), FP64, all host threads",
                 "cpu_baseline": {"value": val, "unit": METRIC, "cores": nth, "kind": "port",
                                  "sample": f"{args.steps} time steps after {args.warmup} warm-up steps"},
                 "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -623,13 +816,8 @@ def main():
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 multigrid + f64 BiCGSTAB/state", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [384, 256], "cells": cells, "parallelism": f"replicas x{world}",
-                   "precision": "mixed", "ppe_tol": cfg_m.ppe_tol, "l2": "flushed before every timed step (256 MB write)",
-                   "execution": exec_name(s)},
-        "plain_fp64": {"value": value64, "ms_per_step": total64 / args.steps, "gpu_launches": launches64,
-                       "execution": exec_name(s64),
-                       "speedup_mixed_over_fp64": value / value64},
-        "accuracy_vs_fp64": {"rel_l2_velocity": err_u, "cd_rel_err": err_cd, "cd": cd_m, "cd_fp64": st64.cd},
+        "config": bench_config(cells, world),
+        "precision": "mixed", "execution": exec_name(s),
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": ("k_persist_step<float> (one launch per time step)" if persistent else
@@ -638,27 +826,37 @@ def main():
                      "peak_source": peak_kind, "traffic": traffic,
                      "bytes_per_launch": step_bytes_total / args.steps, "ms_per_launch": total_ms / args.steps,
                      "note": "working set ~30 MB is L2-resident; launch/barrier latency bound at this size"},
-        "phase_roofline": {"kernel": "finest-level smoothing sweep as the step launches it (k_smooth_grid_tma<float>), launched alone", "bytes_per_cell": 13,
-                           "cells_per_launch": k_cells, "ms_per_launch": k_ms, "achieved_gbs": k_bw,
-                           "frac": k_bw / peak, "grid_barrier_us": bar_us},
-        "iterations": {"ppe_mean": sum(pits) / len(pits), "predictor_mean": sum(adits) / len(adits),
-                       "ppe_mean_fp64": sum(pits64) / len(pits64)},
         "clocks": clocks,
     }
+    # long detail blocks first; the short summary is the last key of the line
+    if rank == 0 and world == 1:
+        line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
+        if not args.no_reference_build:
+            line["reference_cuda"] = reference_cuda()
+        line["moving_body"] = moving_line(ifx, capi, cases)
+        line["long_run_accuracy"] = long_run_accuracy(ifx, capi, cases)
+        line["ellipse"] = ellipse_line(ifx, capi, cases, oracle=not args.no_cpu)
+        if args.cavity_steps > 1:
+            line["cavity"] = cavity_line(ifx, capi, cases, steps=args.cavity_steps, oracle=not args.no_cpu)
     if args.batch > 0:
-        line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.warmup, peak)
+        line["batched"] = batched_sweep(ifx, capi, cases, args.batch, args.batch_steps, args.batch_solve_steps, peak)
     if args.serve > 0:
         line["served"] = served_lines(ifx, capi, cases, args.serve, args.rate, 64 << 30)
-    if rank == 0 and world == 1:
-        line["ellipse"] = ellipse_line(ifx, capi, cases)
-        line["long_run_accuracy"] = long_run_accuracy(ifx, capi, cases)
-        line["moving_body"] = moving_line(ifx, capi, cases)
-        line["reference_path"] = reference_path(ifx, capi, cases, cpu=not args.no_cpu)
+    line["phase_roofline"] = {"kernel": "finest-level smoothing sweep as the step launches it (k_smooth_grid_tma<float>), "
+                                        "launched alone", "bytes_per_cell": 13,
+                              "cells_per_launch": k_cells, "ms_per_launch": k_ms, "achieved_gbs": k_bw,
+                              "frac": k_bw / peak, "grid_barrier_us": bar_us}
+    line["iterations"] = {"ppe_mean": sum(pits) / len(pits), "predictor_mean": sum(adits) / len(adits),
+                          "ppe_mean_fp64": sum(pits64) / len(pits64)}
+    line["accuracy_vs_fp64"] = {"rel_l2_velocity": err_u, "cd_rel_err": err_cd, "cd": cd_m, "cd_fp64": st64.cd}
+    line["plain_fp64"] = {"value": value64, "ms_per_step": total64 / args.steps, "gpu_launches": launches64,
+                          "execution": exec_name(s64), "speedup_mixed_over_fp64": value / value64}
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
         n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)
         line["cpu_baseline"] = {"value": cells * n / dt / 1e6, "unit": METRIC, "cores": nth, "kind": "port",
                                 "sample": f"{n} time steps of the same workload after 1 warm-up step ({dt:.1f} s)"}
+    line["summary"] = summary(line)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
