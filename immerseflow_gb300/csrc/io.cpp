@@ -242,7 +242,7 @@ extern "C" ifx_status ifx_config_read(const char* path, ifx_config* c) {
         }
     }
     if (c->nx < 1 || c->ny < 1) return set_error(IFX_ERR_PARSE, std::string(path) + ": nx, ny must be >= 1");
-    if ((long long)(c->nx + 2LL) * (c->ny + 2LL) > IFX_MAX_CELLS)
+    if (IFX_PADDED_CELLS(c->nx, c->ny) > IFX_MAX_CELLS)
         return set_error(IFX_ERR_PARSE, std::string(path) + ": nx, ny give more than IFX_MAX_CELLS cells");
     const std::string d = dir_of(path);
     auto full = [&](const std::string& g) { return (!g.empty() && g[0] == '/') ? g : d + "/" + g; };

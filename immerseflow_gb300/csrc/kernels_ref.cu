@@ -4,9 +4,10 @@
 // Laplace solve that PPESolver intends (src/include/PPESolver.cu:13-71,
 // 137-205), one instance, dense rows (index i + j*nx as in the reference).
 // The arithmetic of every kernel follows the reference expression by
-// expression; what changes is the launch structure: 2-D tiles instead of
-// 1-D grid-stride loops, no cudaMalloc/cudaFree per step, and residual sums
-// reduced on the device in a fixed order (no per-iteration allocation).
+// expression; what changes is the launch structure: one thread per cell
+// (no grid-stride loop), no cudaMalloc/cudaFree per step, residual sums
+// reduced on the device in a fixed order (no per-iteration allocation), and
+// the whole step in one cooperative launch (k_ref_steps).
 #include <cuda_runtime.h>
 
 #include <algorithm>

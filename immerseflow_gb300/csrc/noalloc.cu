@@ -61,7 +61,9 @@ ifx_status scratch_address(int dev, double** out) {
 extern "C" ifx_status ifx_ppe_reference_noalloc(const double* d_dx, const double* d_dy, int nx, int ny,
                                                 double* d_p, int itermax, double tol, int* iters,
                                                 void* stream) {
-    if (!d_dx || !d_dy || !d_p || nx < 3 || ny < 3 || itermax < 0)
+    // a NaN tolerance would end the loop before the first sweep and report a
+    // converged solve, so it is refused with the other bad arguments
+    if (!d_dx || !d_dy || !d_p || nx < 3 || ny < 3 || itermax < 0 || !(tol == tol))
         return ifx::set_error(IFX_ERR_ARG, "ifx_ppe_reference_noalloc: bad argument");
     if ((long long)nx * ny > kMaxCells)
         return ifx::set_error(IFX_ERR_ARG, "ifx_ppe_reference_noalloc: nx*ny = " + std::to_string((long long)nx * ny) +

@@ -636,8 +636,8 @@ void initial_field(const Instance& I, std::vector<double>& u, std::vector<double
 
 ifx_status validate(const ifx_config* c) {
     if (c->nx < 4 || c->ny < 4) return set_error(IFX_ERR_ARG, "method mode needs nx, ny >= 4");
-    if ((c->nx + 2LL) * (c->ny + 2LL) > IFX_MAX_CELLS)
-        return set_error(IFX_ERR_ARG, "nx, ny give more than IFX_MAX_CELLS cells");
+    if (IFX_PADDED_CELLS(c->nx, c->ny) > IFX_MAX_CELLS)
+        return set_error(IFX_ERR_ARG, "nx, ny give more than IFX_MAX_CELLS cells (rows padded to 32)");
     if (!(c->dt > 0) || !(c->re > 0)) return set_error(IFX_ERR_ARG, "dt and Re must be positive");
     if (c->mg_pre < 1 || c->mg_post < 1) return set_error(IFX_ERR_ARG, "multigrid sweeps must be >= 1");
     if (c->ad_itermax < 1 || c->ppe_itermax < 0) return set_error(IFX_ERR_ARG, "bad iteration caps");
@@ -1879,7 +1879,7 @@ extern "C" ifx_status ifx_create_batch(int n, const ifx_config* cfgs, const doub
     *out = nullptr;
     for (int k = 0; k < n; k++) {
         if (!xfs[k] || !yfs[k]) return set_error(IFX_ERR_ARG, "ifx_create_batch: null grid");
-        if (cfgs[k].nx < 1 || cfgs[k].ny < 1 || (cfgs[k].nx + 2LL) * (cfgs[k].ny + 2LL) > IFX_MAX_CELLS)
+        if (cfgs[k].nx < 1 || cfgs[k].ny < 1 || IFX_PADDED_CELLS(cfgs[k].nx, cfgs[k].ny) > IFX_MAX_CELLS)
             return set_error(IFX_ERR_ARG, "ifx_create_batch: nx, ny must be >= 1 and give at most IFX_MAX_CELLS cells");
     }
     ifx_solver* S = nullptr;

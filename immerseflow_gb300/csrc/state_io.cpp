@@ -231,8 +231,12 @@ extern "C" ifx_status ifx_checkpoint_save(ifx_solver* S, int inst, void* buf, si
     return IFX_OK;
 }
 
-extern "C" ifx_status ifx_checkpoint_load(ifx_solver* S, int inst, const void* buf, size_t n) {
-    SIO_TRY(check_restartable(S, inst, "ifx_checkpoint_load"));
+namespace {
+
+// Every check of a checkpoint record against instance inst (header, format,
+// mode, grid and geometry hash, sizes, payload checksum), on the host only:
+// nothing on the device changes until a record has passed.
+ifx_status validate_checkpoint(const ifx_solver* S, int inst, const void* buf, size_t n, CkptHeader* out) {
     if (!buf || n < sizeof(CkptHeader)) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_load: not a checkpoint (too short)");
     CkptHeader h;
     std::memcpy(&h, buf, sizeof(h));
@@ -247,6 +251,18 @@ extern "C" ifx_status ifx_checkpoint_load(ifx_solver* S, int inst, const void* b
         return set_error(IFX_ERR_PARSE, "ifx_checkpoint_load: truncated or mismatched checkpoint");
     const char* pay = (const char*)buf + sizeof(CkptHeader);
     if (fnv1a(pay, h.payload_bytes) != h.payload_hash) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_load: checksum mismatch");
+    if (out) *out = h;
+    return IFX_OK;
+}
+
+}  // namespace
+
+extern "C" ifx_status ifx_checkpoint_load(ifx_solver* S, int inst, const void* buf, size_t n) {
+    SIO_TRY(check_restartable(S, inst, "ifx_checkpoint_load"));
+    CkptHeader h;
+    SIO_TRY(validate_checkpoint(S, inst, buf, n, &h));
+    const Instance& I = S->inst[inst];
+    const char* pay = (const char*)buf + sizeof(CkptHeader);
     SIO_CUDA(cudaSetDevice(S->device));
     SIO_TRY(finish_pending(S));
     // aligned copy of the payload (the caller's buffer may be unaligned)
@@ -312,16 +328,24 @@ extern "C" ifx_status ifx_checkpoint_read(ifx_solver* S, const char* path) {
     std::memcpy(&count, in.data() + 12, 4);
     if (ver != kVersion) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_read: unknown checkpoint version");
     if (count != S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_checkpoint_read: instance count differs");
+    // every record is checked before any instance is loaded, so a file with a
+    // bad record leaves the whole handle as it was
+    std::vector<std::pair<size_t, size_t>> rec(count);
     size_t at = 16;
     for (int k = 0; k < (int)count; k++) {
+        SIO_TRY(check_restartable(S, k, "ifx_checkpoint_read"));
         uint64_t nb = 0;
         if (at + 8 > in.size()) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_read: truncated file");
         std::memcpy(&nb, in.data() + at, 8);
         at += 8;
         if (nb > in.size() - at) return set_error(IFX_ERR_PARSE, "ifx_checkpoint_read: truncated file");
-        SIO_TRY(ifx_checkpoint_load(S, k, in.data() + at, (size_t)nb));
+        ifx_status st = validate_checkpoint(S, k, in.data() + at, (size_t)nb, nullptr);
+        if (st != IFX_OK)
+            return set_error(st, "ifx_checkpoint_read: record " + std::to_string(k) + ": " + ifx_last_error());
+        rec[k] = {at, (size_t)nb};
         at += nb;
     }
+    for (int k = 0; k < (int)count; k++) SIO_TRY(ifx_checkpoint_load(S, k, in.data() + rec[k].first, rec[k].second));
     return IFX_OK;
 }
 

@@ -185,10 +185,13 @@ ifx_status ifx_write_tecplot(const char* path, int nx, int ny, const double* x,
 /* ----------------------------------------------------------------- solver */
 typedef struct ifx_solver ifx_solver;
 
-/* Largest instance, in cells including the ghost ring ((nx+2)*(ny+2)): the
- * kernels index an instance's cells with 32-bit integers.  ifx_config_read
- * refuses larger grids with IFX_ERR_PARSE, the create calls with IFX_ERR_ARG. */
+/* Largest instance: the kernels index an instance's cells with 32-bit
+ * integers over rows padded to a multiple of 32 cells, so the bound applies to
+ * IFX_PADDED_CELLS(nx, ny) = roundup(nx+2, 32) * (ny+2), which is at least
+ * the cell count with the ghost ring, (nx+2)*(ny+2).  ifx_config_read refuses
+ * larger grids with IFX_ERR_PARSE, the create calls with IFX_ERR_ARG. */
 #define IFX_MAX_CELLS (1 << 28)
+#define IFX_PADDED_CELLS(nx, ny) ((((long long)(nx) + 2 + 31) / 32 * 32) * ((long long)(ny) + 2))
 
 /* allocation + readGridData + initializeData (src/main.cu:86-90,
  * src/include/preSim.cu:147-240).  xf has cfg->nx+1 entries, yf cfg->ny+1. */
@@ -257,8 +260,9 @@ ifx_status ifx_device_bytes(const ifx_solver* s, size_t* bytes);
 ifx_status ifx_ppe_reference(ifx_solver* s, int* iters);
 
 /* Largest grid (cells including the ghost ring, nx*ny) that
- * ifx_ppe_reference_noalloc accepts: 132 x 132, i.e. the 128 x 128 interior of the
- * cavity configuration.  Its scratch is ~0.84 MB of device memory per GPU. */
+ * ifx_ppe_reference_noalloc accepts: 132 x 132 including the ghost ring, a
+ * 130 x 130 interior (the 128 x 128 cavity, 130 x 130 with its ring, fits).
+ * Its scratch is ~0.84 MB of device memory per GPU. */
 #define IFX_NOALLOC_MAX_CELLS (132 * 132)
 /* Pressure solve for callers that cannot allocate device memory (a plug-in
  * whose host application owns every device allocation, a service that budgets

@@ -11,7 +11,7 @@ printed, %f precision) plus the SHA-256 of each original file, and copies the
 small input files verbatim.  It reads the reference only here, at fixture
 generation time; the tests use the committed fixtures.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py <reference checkout>
 """
 import hashlib
 import os
@@ -57,4 +57,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>")
+    main(sys.argv[1])

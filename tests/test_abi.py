@@ -75,3 +75,6 @@ def test_noalloc_solve_refuses_bad_arguments_before_device_access():
     for dx, dy, nx, ny, p in cases:
         st = lib.ifx_ppe_reference_noalloc(dx, dy, nx, ny, p, 10, 1e-6, None, None)
         assert st == capi.IFX_ERR_ARG, (nx, ny)
+    # a NaN tolerance would stop the loop before its first sweep
+    st = lib.ifx_ppe_reference_noalloc(d, d, 10, 10, d, 10, float("nan"), None, None)
+    assert st == capi.IFX_ERR_ARG

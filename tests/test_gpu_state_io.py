@@ -73,6 +73,28 @@ def test_checkpoint_file_of_a_batch_and_member_into_own_handle(tmp_path):
     same(a, c, 2, 0)
 
 
+def test_checkpoint_file_with_a_corrupt_record_changes_nothing(tmp_path):
+    """A checkpoint file whose second record is corrupt is refused, and the
+    first instance keeps its state: every record is checked before any is
+    loaded."""
+    specs = [cyl(), cases.cavity(n=40)]
+    cfgs, xfs, yfs = [c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs]
+    a = ifx.Solver.batch(cfgs, xfs, yfs)
+    a.step(1)
+    path = str(tmp_path / "batch.ifx")
+    a.checkpoint_write(path)
+    data = bytearray(open(path, "rb").read())
+    data[-100] ^= 0xFF  # a payload byte of the last (second) record
+    open(path, "wb").write(bytes(data))
+    a.step(2)
+    before = {f: a.get(f, inst=0) for f in FIELDS}
+    with pytest.raises(ifx.IFXError) as e:
+        a.checkpoint_read(path)
+    assert e.value.status == capi.IFX_ERR_PARSE and "record 1" in str(e.value)
+    for f, v in before.items():
+        assert np.array_equal(a.get(f, inst=0), v), f
+
+
 def test_checkpoint_across_precision_and_rejections():
     cfg64, xf, yf = cyl()
     cfg32, _, _ = cyl(capi.PREC_MIXED)

@@ -84,10 +84,13 @@ def test_probes_read_survives_garbage_and_keeps_to_its_buffer(tmp_path):
             assert n.value >= 0
 
 
-@pytest.mark.parametrize("nxny", ["2147483647 50", "50 2147483647", "20000 20000", "2147483647 2147483647"])
+@pytest.mark.parametrize("nxny", ["2147483647 50", "50 2147483647", "20000 20000", "2147483647 2147483647",
+                                  "1 80000000"])
 def test_oversized_grid_is_refused_before_any_allocation(golden_dir, tmp_path, nxny):
-    # (nx+2)*(ny+2) above IFX_MAX_CELLS: a parse error from the file surface and
-    # an argument error from the create call, both before any device access
+    # more than IFX_MAX_CELLS cells in the padded device layout (the last case
+    # has 3 x 80000002 < 2^28 cells, but rows padded to 32 give 2.56e9): a parse
+    # error from the file surface and an argument error from the create call,
+    # both before any device access
     with open(os.path.join(golden_dir, "inputs", "inputs.txt")) as fh:
         lines = fh.read().splitlines()
     k = next(i for i, l in enumerate(lines) if "nx" in l)

@@ -7,7 +7,8 @@ loop that cannot afford the device synchronisation of cudaFree.  Here the
 caller's buffers come from torch; the result is compared with
 ifx_ppe_reference on a solver handle
 (same kernels, so the tolerance of the other reference-mode tests, 1e-12
-relative, holds), on two calls in a row so that leftovers in the shared
+relative, holds) and with the reference's own result file p.dat (to its %f
+print precision, 5e-7), on two calls in a row so that leftovers in the shared
 scratch array cannot go unnoticed.  The file name sorts last, so a run that
 stops at the first failure has run every other test first.
 """
@@ -41,7 +42,7 @@ def _full_widths(xf, yf):
     return np.tile(dx, (ny, 1)).ravel(), np.tile(dy[:, None], (1, nx)).ravel()
 
 
-def test_noalloc_matches_solver_solve_twice(golden_dir):
+def test_noalloc_matches_solver_solve_twice(golden_dir, golden):
     torch = pytest.importorskip("torch")
     c, xf, yf = _grid(golden_dir)
     s = ifx.Solver.create(c, xf, yf)
@@ -64,6 +65,8 @@ def test_noalloc_matches_solver_solve_twice(golden_dir):
         p = d_p.cpu().numpy().reshape(ny, nx)
         assert it.value == it_ref, (call, it.value, it_ref)
         assert np.abs(p - p_ref).max() <= 1e-12 * np.abs(p_ref).max(), call
+        # and on its own against the reference's result file p.dat (printed with %f)
+        assert np.abs(p - golden["p"]).max() <= 5.0e-7 + 1e-12, call
 
 
 def test_noalloc_rejects_grids_above_the_fixed_scratch():
