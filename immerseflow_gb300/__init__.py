@@ -50,6 +50,7 @@ _SIGS = {
     "ifx_synchronize": (C.c_int, [C.c_void_p]),
     "ifx_trace_step": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int)]),
     "ifx_profile_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_longlong)]),
+    "ifx_set_barrier_fault": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int]),
     "ifx_destroy": (None, [C.c_void_p]),
     "ifx_step_async": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),

@@ -7,8 +7,6 @@
 
 namespace ifx {
 
-constexpr long long kSpinLimit = 1ll << 23;  // x ~50-100 ns per poll: well under a second per barrier
-
 __device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(const volatile unsigned int*)p; }
 
 // Flat barrier on a monotonically increasing 64-bit arrival counter: the
@@ -16,8 +14,11 @@ __device__ __forceinline__ unsigned int vload(const unsigned int* p) { return *(
 // gridDim.x * k.  Arrival is a release add, the wait an acquire poll, so the
 // critical path is one atomic and one poll; the counter never needs a reset
 // inside the launch (the host zeroes it before each launch).
+// The wait gives up after spin_limit polls: it sets the error flag and every
+// block returns, so a lost block ends the launch with an error the host reads
+// instead of a hang.
 __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epoch, long long* trace = nullptr,
-                                             int cap = 0) {
+                                             int cap = 0, long long spin_limit = kSpinLimit) {
     __syncthreads();
     epoch += 1;
     if (threadIdx.x == 0) {
@@ -28,7 +29,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned long long& epo
         while (true) {
             asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(&b->count) : "memory");
             if (v >= target) break;
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 atomicExch(&b->err, 1u);
                 break;
             }

@@ -7,6 +7,9 @@
 namespace ifx {
 
 constexpr int kMaxLevels = 16;
+// polls of a grid barrier before it gives up (x ~50-100 ns per poll: well
+// under a second per barrier)
+constexpr long long kSpinLimit = 1ll << 23;
 
 // Grid barrier state (zeroed once at allocation; counters return to zero
 // after every barrier, the generation only grows).
@@ -37,6 +40,9 @@ struct PersistPlan {
     long long* trace;   // optional: SM clock of block 0 after every barrier
     int trace_cap;
     int sub_bytes;      // dynamic shared memory of the sub-cycle (largest instance)
+    long long spin_limit;     // polls before a grid barrier gives up (kSpinLimit)
+    int withhold_arrival;     // failure-detection hook: the arrival counter starts
+                              // one short, so the first barrier never completes
 };
 
 template <typename T>

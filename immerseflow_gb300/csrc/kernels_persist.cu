@@ -57,7 +57,7 @@ __device__ __forceinline__ bool any_ppe_active(const InstState* S, int n) {
 
 #define BAR()                                          \
     do {                                               \
-        if (!grid_barrier(P.bar, ep, P.trace, P.trace_cap)) return false; \
+        if (!grid_barrier(P.bar, ep, P.trace, P.trace_cap, P.spin_limit)) return false; \
     } while (0)
 #define FOR_VB(n) for (int vb = blockIdx.x; vb < (n); vb += gridDim.x)
 
@@ -244,7 +244,8 @@ cudaError_t launch_barrier_bench(GridBar* bar, int grid, int reps, cudaStream_t 
 
 template <typename T>
 cudaError_t launch_persist_step(const PersistPlan& P, int grid, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(&P.bar->count, 0, sizeof(P.bar->count), s);
+    // all bits set: 2^64 - 1, one arrival short of zero (the counter wraps)
+    cudaError_t e = cudaMemsetAsync(&P.bar->count, P.withhold_arrival ? 0xFF : 0, sizeof(P.bar->count), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&P};
     return cudaLaunchCooperativeKernel((const void*)k_persist_step<T>, dim3(grid), dim3(TILE_THREADS), args,

@@ -720,6 +720,8 @@ ifx_status setup_persistent(ifx_solver* S) {
     P.mg_pre = S->mg_pre;
     P.mg_post = S->mg_post;
     P.sub_bytes = S->sub_bytes;
+    P.spin_limit = kSpinLimit;
+    P.withhold_arrival = 0;
     P.pred_pairs = max_pred_pairs(S);
     P.ppe_bodies = max_ppe_bodies(S);
     CUDA_TRY(cudaStreamSynchronize(S->stream));
@@ -1557,7 +1559,11 @@ ifx_status step_launch(ifx_solver* S, int nsteps) {
     CUDA_TRY(cudaEventRecord(S->ev0, S->stream));
     if (mode == 0) {
         S->plan.nsteps = nsteps;
-        CUDA_TRY(launch_persist_step<T>(S->plan, S->persist_grid, S->stream));
+        const cudaError_t e = launch_persist_step<T>(S->plan, S->persist_grid, S->stream);
+        // a barrier fault set by ifx_set_barrier_fault applies to this launch only
+        S->plan.spin_limit = kSpinLimit;
+        S->plan.withhold_arrival = 0;
+        CUDA_TRY(e);
         S->launches += 1;
     } else if (S->use_graph) {
         if (!S->gexec) IFX_TRY(build_graph<T>(S));
@@ -2438,6 +2444,15 @@ extern "C" ifx_status ifx_profile_kernel(ifx_solver* S, int kernel, int reps, do
     return profile_kernel<float>(S, kernel, reps, ms_per_launch);
 }
 
+extern "C" ifx_status ifx_set_barrier_fault(ifx_solver* S, long long spin_limit, int withhold_arrival) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_set_barrier_fault: bad argument");
+    if (S->mode != IFX_MODE_METHOD || S->persist_grid == 0)
+        return set_error(IFX_ERR_STATE, "ifx_set_barrier_fault needs the persistent kernel");
+    S->plan.spin_limit = spin_limit > 0 ? spin_limit : kSpinLimit;
+    S->plan.withhold_arrival = withhold_arrival != 0;
+    return IFX_OK;
+}
+
 extern "C" ifx_status ifx_trace_step(ifx_solver* S, int cap, double* us, int* n) {
     if (!S || !us || !n || cap < 1) return set_error(IFX_ERR_ARG, "ifx_trace_step: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));
@@ -2453,6 +2468,8 @@ extern "C" ifx_status ifx_trace_step(ifx_solver* S, int cap, double* us, int* n)
                                              : launch_persist_step<float>(S->plan, S->persist_grid, S->stream);
     S->plan.trace = nullptr;
     S->plan.trace_cap = 0;
+    S->plan.spin_limit = kSpinLimit;
+    S->plan.withhold_arrival = 0;
     if (e != cudaSuccess) return cuerr(e, "ifx_trace_step");
     std::vector<long long> h(cap + 1);
     CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(long long) * (cap + 1), cudaMemcpyDeviceToHost, S->stream));

@@ -418,6 +418,15 @@ ifx_status ifx_profile_kernel(ifx_solver* s, int kernel, int reps, double* ms_pe
  * grid barrier; us[k] receives the time between barrier k and k+1 in
  * microseconds (SM clock rate), *n the number of intervals (<= cap). */
 ifx_status ifx_trace_step(ifx_solver* s, int cap, double* us, int* n);
+/* Failure-detection hook (no reference counterpart): the next persistent
+ * launch of this handle (IFX_EXEC_PERSISTENT) polls each grid barrier at most
+ * spin_limit times (<= 0: the default, about 2^23 polls, well under a second)
+ * and, if withhold_arrival is non-zero, starts its arrival counter one short,
+ * as if one block of the launch had been lost.  The first barrier then never
+ * completes: every block gives up after spin_limit polls, sets the error flag
+ * and returns, the step reports IFX_ERR_CUDA and the handle refuses further
+ * steps (IFX_ERR_STATE); the device stays usable.  Applies to one launch. */
+ifx_status ifx_set_barrier_fault(ifx_solver* s, long long spin_limit, int withhold_arrival);
 void       ifx_destroy(ifx_solver* s);
 
 #ifdef __cplusplus
