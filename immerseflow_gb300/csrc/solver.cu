@@ -645,17 +645,21 @@ ifx_status validate(const ifx_config* c) {
         return set_error(IFX_ERR_ARG, "body semi-axes must be positive");
     for (int s = 0; s < 4; s++)
         if (c->bc_type[s] < 0 || c->bc_type[s] > 3) return set_error(IFX_ERR_ARG, "bad boundary type");
+    bool outflow = false;
+    for (int s = 0; s < 4; s++) outflow = outflow || c->bc_type[s] == IFX_BC_OUTFLOW;
+    // Without an outflow side the pressure is fixed only up to a constant, and
+    // the solve makes the right-hand side compatible by removing its
+    // area-weighted mean.  With a body the eliminated ghost rows make the
+    // operator non-symmetric: its compatibility condition is no longer the
+    // area-weighted mean, and the solve stalls at its iteration cap.
+    if (c->body != IFX_BODY_NONE && !outflow)
+        return set_error(IFX_ERR_ARG, "a body needs an outflow side (Dirichlet pressure) in method mode");
     if (c->ppe_method != IFX_PPE_JACOBI)
         return set_error(IFX_ERR_ARG, "PPE-Method point-gs / line-sor selects the REFERENCE-mode pressure solve; "
                                       "method mode solves the pressure with multigrid-preconditioned BiCGSTAB");
     if (c->motion != IFX_MOTION_NONE) {
         if (c->motion != IFX_MOTION_PRESCRIBED) return set_error(IFX_ERR_ARG, "bad motion type");
         if (c->body != IFX_BODY_ELLIPSE) return set_error(IFX_ERR_ARG, "body motion needs a body");
-        bool outflow = false;
-        for (int s = 0; s < 4; s++) outflow = outflow || c->bc_type[s] == IFX_BC_OUTFLOW;
-        // in a closed domain the pressure is fixed up to a constant by the
-        // fluid area, which a moving body changes
-        if (!outflow) return set_error(IFX_ERR_ARG, "a moving body needs an outflow side");
         const double m[9] = {c->motion_u, c->motion_v, c->motion_amp_x, c->motion_amp_y, c->motion_amp_deg,
                              c->motion_freq, c->motion_phase_x, c->motion_phase_y, c->motion_phase_deg};
         for (double x : m)

@@ -48,12 +48,17 @@ def test_reference_mode_case_is_refused():
 
 
 @pytest.mark.parametrize("field,value", [("re", -1.0), ("dt", 0.0), ("mg_pre", 0), ("ppe_method", capi.PPE_LINE_SOR),
-                                         ("nx", 1 << 28)])
+                                         ("nx", 1 << 28), ("closed_box_body", None)])
 def test_invalid_request_refused_at_submit(field, value):
     """A configuration the solver would refuse is refused at submit, not when its
     cohort is created (which would fail the requests admitted with it)."""
     cfg, xf, yf = small(48, 32)
-    setattr(cfg, field, value)
+    if field == "closed_box_body":
+        # a body with no outflow side: the pressure problem is refused (its
+        # compatibility condition is not the area-weighted mean)
+        cfg.bc_type[capi.SIDE_E] = capi.BC_WALL
+    else:
+        setattr(cfg, field, value)
     srv = ifx.Server(1 << 30, max_cohort=4)
     with pytest.raises(ifx.IFXError) as e:
         srv.submit(cfg, xf, yf, nsteps=3)
