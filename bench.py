@@ -215,11 +215,11 @@ def cell_step_bytes(ad_iters, ppe_iters, mixed):
     return 81 + pred * ad_iters + 41 + start + restarts + 81 + per_it * ppe_iters
 
 
-def exec_name(s):
+def exec_name(s, tuned=True):
     mode = {0: "persistent", 1: "graph", 2: "host"}.get(s.exec_mode(), "?")
     rows = s.mg_tile_rows()
     cmg = s.cluster_vcycle()[1]
-    return f"{mode}, multigrid tiles 32x{8 * rows}" + (", cluster V-cycle" if cmg else "") + " (autotuned)"
+    return f"{mode}, multigrid tiles 32x{8 * rows}" + (", cluster V-cycle" if cmg else "") + (" (autotuned)" if tuned else "")
 
 
 def rel_l2(a, b):
@@ -244,6 +244,7 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, solve_steps, peak):
         ncell = sum(c.nx * c.ny for c, _, _ in specs)
         s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
         mode, _ = s.autotune(steps=1)
+        sched, _ = s.autotune_schedule(steps=1)
         s.synchronize()
         w0 = time.perf_counter()
         s.step(2)
@@ -260,6 +261,7 @@ def batched_sweep(ifx, capi, cases, n_inst, steps, solve_steps, peak):
         fields[name] = [(s.get(capi.FIELD_U, inst=k), s.get(capi.FIELD_V, inst=k), s.stats(k).cd) for k in range(n_inst)]
         res[name] = {"value": ncell * steps / (ms * 1e-3) / 1e6, "unit": METRIC, "ms_per_step": ms / steps,
                      "exec": {0: "persistent", 1: "graph"}.get(mode, str(mode)), "mg_tile_rows": s.mg_tile_rows(),
+                     "schedule": sched.as_dict(),
                      "gpu_launches": launches,
                      "ppe_iters_mean": float(np.mean(its)), "ppe_iters_max": int(max(its)),
                      "predictor_iters_max": int(max(ads)), "device_bytes": s.device_bytes(),
@@ -434,12 +436,13 @@ def ellipse_line(ifx, capi, cases, steps=10, oracle=True):
         s = ifx.Solver.create(cfg, xf, yf)
         s.step(1)
         s.autotune(steps=1)
+        sched, _ = s.autotune_schedule(steps=1)
         s.step(2)
         s.step(steps)
         ms = s.last_step_ms()
         st = s.stats()
         out[name] = {"value": cfg.nx * cfg.ny * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
-                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters,
+                     "execution": exec_name(s), "schedule": sched.as_dict(), "ppe_iters_last": st.last_ppe_iters,
                      "predictor_iters_last": st.last_ad_iters, "cd": st.cd}
         fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
         solvers[name] = s
@@ -469,11 +472,12 @@ def cavity_line(ifx, capi, cases, steps=2000, oracle=True):
         s = ifx.Solver.create(cfg, xf, yf)
         s.step(1)
         s.autotune(steps=1)
+        sched, _ = s.autotune_schedule(steps=2)
         s.step(steps - 1)
         ms = s.last_step_ms()
         st = s.stats()
         out[name] = {"value": cfg.nx * cfg.ny * (steps - 1) / (ms * 1e-3) / 1e6, "ms_per_step": ms / (steps - 1),
-                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters,
+                     "execution": exec_name(s), "schedule": sched.as_dict(), "ppe_iters_last": st.last_ppe_iters,
                      "predictor_iters_last": st.last_ad_iters, "max_div": st.max_div}
         solvers[name] = s
     out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
@@ -533,14 +537,17 @@ def moving_line(ifx, capi, cases, steps=50):
         if moving:
             cases.set_motion(cfg, amp_y=0.25, freq=0.2)
         s = ifx.Solver.create(cfg, xf, yf)
+        # the autotuners refuse moving bodies (their trial steps would move
+        # the geometry); graph mode with 32x8 tiles, the cylinder's choice
+        s.set_exec_mode(ifx.EXEC_GRAPH)
+        s.set_mg_tile_rows(1)
         s.step(1)
-        s.autotune(steps=1)
         s.step(2)
         s.step(steps)
         ms = s.last_step_ms()
         st = s.stats()
         out[name] = {"value": cfg.nx * cfg.ny * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
-                     "execution": exec_name(s), "ppe_iters_last": st.last_ppe_iters, "cd": st.cd, "cl": st.cl,
+                     "execution": exec_name(s, tuned=False), "ppe_iters_last": st.last_ppe_iters, "cd": st.cd, "cl": st.cl,
                      "ibm_ghosts": st.n_ibm_ghost}
         if moving:
             fields[name] = np.concatenate([s.get(capi.FIELD_U).ravel(), s.get(capi.FIELD_V).ravel()])
@@ -741,6 +748,7 @@ def main():
         s = ifx.Solver.create(cfg, xf, yf)
         s.step(1)
         s.autotune(steps=2)  # execution mode and tile shape; the state is restored afterwards
+        s.autotune_schedule(steps=2)  # sweep schedule, the same way
         for _ in range(args.warmup):
             flush()
             s.step(1)
@@ -817,7 +825,7 @@ def main():
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 multigrid + f64 BiCGSTAB/state", "data": "synthetic",
         "config": bench_config(cells, world),
-        "precision": "mixed", "execution": exec_name(s),
+        "precision": "mixed", "execution": exec_name(s), "schedule": s.schedule().as_dict(),
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": ("k_persist_step<float> (one launch per time step)" if persistent else
@@ -850,7 +858,8 @@ def main():
                           "ppe_mean_fp64": sum(pits64) / len(pits64)}
     line["accuracy_vs_fp64"] = {"rel_l2_velocity": err_u, "cd_rel_err": err_cd, "cd": cd_m, "cd_fp64": st64.cd}
     line["plain_fp64"] = {"value": value64, "ms_per_step": total64 / args.steps, "gpu_launches": launches64,
-                          "execution": exec_name(s64), "speedup_mixed_over_fp64": value / value64}
+                          "execution": exec_name(s64), "schedule": s64.schedule().as_dict(),
+                          "speedup_mixed_over_fp64": value / value64}
     if rank == 0 and world == 1 and not args.no_cpu:
         cfg64, _, _ = cases.cylinder(precision=capi.PREC_FP64)
         n, dt, nth = cpu_oracle_run(cfg64, xf, yf, args.cpu_seconds)

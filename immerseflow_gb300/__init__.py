@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from . import _capi as capi
-from ._capi import Config, Stats, default_config
+from ._capi import Config, Schedule, Stats, default_config
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libimmerseflow_gb300.so")
@@ -51,6 +51,9 @@ _SIGS = {
     "ifx_trace_step": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int)]),
     "ifx_profile_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "ifx_set_barrier_fault": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int]),
+    "ifx_set_schedule": (C.c_int, [C.c_void_p, C.POINTER(Schedule)]),
+    "ifx_get_schedule": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Schedule)]),
+    "ifx_autotune_schedule": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Schedule), _dp]),
     "ifx_destroy": (None, [C.c_void_p]),
     "ifx_step_async": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
@@ -292,6 +295,22 @@ class Solver:
         _check(lib().ifx_autotune(self._h, int(steps), C.byref(m), C.byref(ms)))
         return m.value, ms.value
 
+    def schedule(self, inst=0):
+        """Sweep schedule of an instance (capi.Schedule)."""
+        s = Schedule()
+        _check(lib().ifx_get_schedule(self._h, int(inst), C.byref(s)))
+        return s
+
+    def set_schedule(self, sched):
+        _check(lib().ifx_set_schedule(self._h, C.byref(sched)))
+
+    def autotune_schedule(self, steps=2):
+        """Pick the fastest valid sweep schedule by timing; state is restored.
+        Returns (capi.Schedule, ms/step)."""
+        s, ms = Schedule(), C.c_double()
+        _check(lib().ifx_autotune_schedule(self._h, int(steps), C.byref(s), C.byref(ms)))
+        return s, ms.value
+
     def set_mg_tile_rows(self, rows):
         _check(lib().ifx_set_mg_tile_rows(self._h, int(rows)))
 
@@ -461,5 +480,5 @@ class Server:
 
 from .interface import ImmerseFlow  # noqa: E402  (mirror of the reference object)
 
-__all__ = ["Config", "Stats", "default_config", "Solver", "Server", "ImmerseFlow", "IFXError", "config_read",
+__all__ = ["Config", "Schedule", "Stats", "default_config", "Solver", "Server", "ImmerseFlow", "IFXError", "config_read",
            "grid_read", "write_tecplot", "probes_read", "estimate_bytes", "lib", "capi"]

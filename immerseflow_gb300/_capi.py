@@ -73,8 +73,20 @@ class Config(C.Structure):
         ("motion_amp_x", C.c_double), ("motion_amp_y", C.c_double), ("motion_amp_deg", C.c_double),
         ("motion_freq", C.c_double),
         ("motion_phase_x", C.c_double), ("motion_phase_y", C.c_double), ("motion_phase_deg", C.c_double),
+        ("coarse_sweeps", C.c_int), ("restart_drop", C.c_double), ("restart_every", C.c_int),
         ("xgrid", C.c_char * PATH_MAX), ("ygrid", C.c_char * PATH_MAX),
     ]
+
+
+class Schedule(C.Structure):
+    _fields_ = [
+        ("mg_pre", C.c_int), ("mg_post", C.c_int), ("mg_omega", C.c_double),
+        ("coarse_sweeps", C.c_int), ("mixed_inner", C.c_int),
+        ("restart_drop", C.c_double), ("restart_every", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(C.Structure):
@@ -114,6 +126,7 @@ def default_config():
     c.mg_pre, c.mg_post = 2, 2
     c.mg_omega = 0.8
     c.mixed_inner = 8
+    c.coarse_sweeps, c.restart_drop, c.restart_every = 40, 1e-4, 25
     c.force_ref_u, c.force_ref_len = 1.0, 1.0
     c.ppe_method, c.relax_ad, c.relax_ppe = PPE_JACOBI, 1.0, 1.0
     c.xgrid = b"xgrid.dat2"

@@ -27,8 +27,7 @@ constexpr int GHOST_BLOCK = 256;
 constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
 constexpr int TMA_MAPS_PER_LEVEL = 8;  // tensor maps per level: e, e2, r, bits for 32x8 tiles, then for wide tiles
-constexpr int COARSE_SWEEPS = 40;    // RB-SOR sweeps on the coarsest level
-constexpr double COARSE_OMEGA = 1.5;
+constexpr double COARSE_OMEGA = 1.5;  // RB-SOR factor on the coarsest level
 // Threads of the block that runs an instance's small levels in the graph and
 // host-loop modes (the persistent kernel runs them with its own blocks).
 constexpr int SUB_THREADS = 512;
@@ -36,11 +35,6 @@ constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one
 constexpr int SUB_SMEM_MAX = 96 * 1024;  // shared memory for those levels (fields, metrics, tables)
 constexpr int kSubLevels = 16;           // at most this many levels per instance
 constexpr int SUB_COARSE_PER_THREAD = 4;  // coarsest-level cells per thread in the RB-SOR solve
-// Mixed path: the FP32 BiCGSTAB restarts from the FP64 true residual once its
-// recursive residual fell by this factor since the last restart, or after
-// this many iterations.
-constexpr double PPE_RESTART_DROP = 1e-4;
-constexpr int PPE_RESTART_EVERY = 25;
 
 enum CellType : uint8_t { T_SOLID = 0, T_FLUID = 1, T_GHOST = 2, T_DOMAIN = 3 };
 // per-cell stencil bits: open faces, and (finest level) faces to an IBM ghost
@@ -242,6 +236,12 @@ struct alignas(16) InstDev {
     double dt, re, dtre, idt, omega;
     double ad_lim, ppe_tol;
     int ad_itermax, ppe_itermax, n_fluid, mixed_inner;
+    // sweep schedule: coarsest-level RB-SOR sweeps; mixed path: the FP32
+    // BiCGSTAB restarts from the FP64 true residual once its recursive
+    // residual fell by restart_drop since the last restart, or after
+    // restart_every iterations
+    int coarse_sweeps, restart_every;
+    double restart_drop;
     double uc;                   // convective outflow speed
     double area;                 // sum of fluid-cell areas
     double *u, *v, *u2, *v2, *Us, *Vs, *U, *V, *Nu, *Nv, *ru, *rv, *p, *b, *div, *iblank;

@@ -90,6 +90,9 @@ extern "C" void ifx_config_default(ifx_config* c) {
     c->mg_post = 2;
     c->mg_omega = 0.8;
     c->mixed_inner = 8;
+    c->coarse_sweeps = 40;
+    c->restart_drop = 1e-4;
+    c->restart_every = 25;
     c->force_ref_u = 1.0;
     c->force_ref_len = 1.0;
     c->ppe_method = IFX_PPE_JACOBI;
@@ -228,6 +231,10 @@ extern "C" ifx_status ifx_config_read(const char* path, ifx_config* c) {
             if (!next() || !(iss >> c->mg_pre >> c->mg_post >> c->mg_omega)) return bad("Multigrid");
         } else if (line.find("Mixed-Inner") != std::string::npos) {
             if (!next() || !(iss >> c->mixed_inner)) return bad("Mixed-Inner");
+        } else if (line.find("Coarse-Sweeps") != std::string::npos) {
+            if (!next() || !(iss >> c->coarse_sweeps)) return bad("Coarse-Sweeps");
+        } else if (line.find("Defect-Correction") != std::string::npos) {
+            if (!next() || !(iss >> c->restart_drop >> c->restart_every)) return bad("Defect-Correction");
         } else if (line.find("Force-Reference") != std::string::npos) {
             if (!next() || !(iss >> c->force_ref_u >> c->force_ref_len)) return bad("Force-Reference");
         } else if (line.find("PPE-Method") != std::string::npos) {

@@ -830,8 +830,8 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
 // (start == 0 only).  start: 1 after the initial residual, 2 after a mixed-path
 // restart (instances without one are skipped), 0 after an iteration.  mixed:
 // the recursive FP32 residual is never accepted; a restart is scheduled when
-// it fell by PPE_RESTART_DROP (or below the tolerance) since the last one, or
-// after PPE_RESTART_EVERY iterations.
+// it fell by in.restart_drop (or below the tolerance) since the last one, or
+// after in.restart_every iterations.
 __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                                 const double* __restrict__ part, int start, int mixed,
                                                 LoopCtl* ctl, unsigned long long handle, int vb) {
@@ -865,8 +865,8 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
             const bool true_res = start != 0 || !mixed;
             if ((true_res && rel <= in.ppe_tol) || st.ppe_iters >= in.ppe_itermax) {
                 st.ppe_state = ST_DONE;
-            } else if (!true_res && (rel <= in.ppe_tol || rel <= PPE_RESTART_DROP * st.rel_restart ||
-                                     st.ppe_iters - st.restart_it >= PPE_RESTART_EVERY)) {
+            } else if (!true_res && (rel <= in.ppe_tol || rel <= in.restart_drop * st.rel_restart ||
+                                     st.ppe_iters - st.restart_it >= in.restart_every)) {
                 st.restart = 1;
                 active = true;
                 due = true;
@@ -1596,7 +1596,7 @@ __device__ __forceinline__ void sub_sync(int n) {
 // operator of its cells (at most SUB_COARSE_PER_THREAD) in registers; only
 // the warps that own cells take part.
 template <typename T>
-__device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g) {
+__device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g, int sweeps) {
     const T om = (T)COARSE_OMEGA;
     const int NX = g.NX, nx = g.nx, NXY = g.NX * g.NY;
     const int nthr = min((int)blockDim.x, (NXY + 31) & ~31);
@@ -1617,7 +1617,7 @@ __device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g) {
             const int col = (i + j) & 1;
             const bool hasE = i < NX, hasW = i > 1, hasN = j < g.NY, hasS = j > 1;
             T e = (T)0;
-            for (int it = 0; it < COARSE_SWEEPS; it++) {
+            for (int it = 0; it < sweeps; it++) {
 #pragma unroll
                 for (int cc = 0; cc < 2; cc++) {
                     const T vE = __shfl_down_sync(0xffffffffu, e, 1), vW = __shfl_up_sync(0xffffffffu, e, 1);
@@ -1659,7 +1659,7 @@ __device__ __forceinline__ void sub_coarse_solve(const SubGeo<T>& g) {
             }
         }
         T* e = g.e;
-        for (int it = 0; it < COARSE_SWEEPS; it++) {
+        for (int it = 0; it < sweeps; it++) {
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
 #pragma unroll
@@ -1745,7 +1745,7 @@ __device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const Le
             __syncthreads();
         }
         if (g.child < 0) {
-            sub_coarse_solve<T>(g);
+            sub_coarse_solve<T>(g, I[k].coarse_sweeps);
             break;
         }
         int cur = 0;

@@ -93,6 +93,12 @@ static ifx_status admit(ifx_server* V) {
             continue;
         }
         if (V->used + want + r.est > V->budget) break;
+        // a batch shares its precision and multigrid sweep counts: the first
+        // request that differs from the cohort's first one starts the next cohort
+        if (!take.empty()) {
+            const ifx_config& a = V->reqs[take[0]].cfg;
+            if (r.cfg.precision != a.precision || r.cfg.mg_pre != a.mg_pre || r.cfg.mg_post != a.mg_post) break;
+        }
         want += r.est;
         take.push_back(r.id);
         V->waiting.pop_front();
@@ -222,9 +228,13 @@ extern "C" ifx_status ifx_server_tick(ifx_server* V, int* n_finished) {
         ifx_status st = ifx_step_async(c.s, c.pending);
         if (st != IFX_OK) worst = st;
     }
-    {
+    // cohorts of compatible requests, while requests at the head of the queue
+    // fit the budget
+    for (int guard = 0; guard < 64 && !V->waiting.empty(); guard++) {
+        const size_t nc = V->cohorts.size(), nw = V->waiting.size();
         ifx_status st = admit(V);
         if (st != IFX_OK) worst = st;
+        if (V->cohorts.size() == nc && V->waiting.size() == nw) break;
     }
     size_t idx = 0;
     for (auto it = V->cohorts.begin(); it != V->cohorts.end(); idx++) {

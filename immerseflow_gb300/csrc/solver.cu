@@ -640,6 +640,11 @@ ifx_status validate(const ifx_config* c) {
         return set_error(IFX_ERR_ARG, "nx, ny give more than IFX_MAX_CELLS cells (rows padded to 32)");
     if (!(c->dt > 0) || !(c->re > 0)) return set_error(IFX_ERR_ARG, "dt and Re must be positive");
     if (c->mg_pre < 1 || c->mg_post < 1) return set_error(IFX_ERR_ARG, "multigrid sweeps must be >= 1");
+    if (!(c->mg_omega > 0 && c->mg_omega < 2)) return set_error(IFX_ERR_ARG, "multigrid omega must lie in (0, 2)");
+    if (c->coarse_sweeps < 1 || c->coarse_sweeps > 10000) return set_error(IFX_ERR_ARG, "coarse sweeps must lie in 1..10000");
+    if (c->mixed_inner < 1) return set_error(IFX_ERR_ARG, "mixed_inner must be >= 1");
+    if (!(c->restart_drop > 0 && c->restart_drop < 1) || c->restart_every < 1)
+        return set_error(IFX_ERR_ARG, "defect correction: restart_drop in (0, 1), restart_every >= 1");
     if (c->ad_itermax < 1 || c->ppe_itermax < 0) return set_error(IFX_ERR_ARG, "bad iteration caps");
     if (c->body == IFX_BODY_ELLIPSE && !(c->body_a > 0 && c->body_b > 0))
         return set_error(IFX_ERR_ARG, "body semi-axes must be positive");
@@ -792,6 +797,9 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         d.ad_itermax = I.cfg.ad_itermax;
         d.ppe_itermax = I.cfg.ppe_itermax;
         d.mixed_inner = I.cfg.mixed_inner;
+        d.coarse_sweeps = I.cfg.coarse_sweeps;
+        d.restart_drop = I.cfg.restart_drop;
+        d.restart_every = I.cfg.restart_every;
         d.uc = I.cfg.outflow_uc;
         d.bcx = I.cfg.body_cx; d.bcy = I.cfg.body_cy; d.ba = I.cfg.body_a; d.bb = I.cfg.body_b;
         d.bcs = I.cs; d.bsn = I.sn; d.bia2 = I.ia2; d.bib2 = I.ib2;
@@ -2119,6 +2127,12 @@ struct StateSnapshot {
 extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double* ms_per_step) {
     if (!S || steps < 1) return set_error(IFX_ERR_ARG, "ifx_autotune: bad argument");
     if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_autotune needs a METHOD-mode solver");
+    // the trial steps of a moving body rewrite its geometry (cell types, ghost
+    // slots, stencil bytes) for later poses, and the snapshot restores only the
+    // flow state
+    if (S->nmv > 0)
+        return set_error(IFX_ERR_STATE, "ifx_autotune: a moving body's trial steps would move its geometry, which the "
+                                        "restored state does not include; set the execution mode directly");
     CUDA_TRY(cudaSetDevice(S->device));
     IFX_TRY(step_finish(S));
     StateSnapshot snap;
@@ -2164,6 +2178,190 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
     set_mg_rows(S, best.rows);
     set_cluster_mg(S, best.cmg);
     if (chosen) *chosen = best.mode;
+    if (ms_per_step) *ms_per_step = best_ms;
+    return IFX_OK;
+}
+
+// ------------------------------------------------------------ sweep schedule
+
+namespace {
+ifx_schedule schedule_of(const ifx_config& c) {
+    ifx_schedule s;
+    s.mg_pre = c.mg_pre;
+    s.mg_post = c.mg_post;
+    s.mg_omega = c.mg_omega;
+    s.coarse_sweeps = c.coarse_sweeps;
+    s.mixed_inner = c.mixed_inner;
+    s.restart_drop = c.restart_drop;
+    s.restart_every = c.restart_every;
+    return s;
+}
+bool same_schedule(const ifx_schedule& a, const ifx_schedule& b) {
+    return a.mg_pre == b.mg_pre && a.mg_post == b.mg_post && a.mg_omega == b.mg_omega &&
+           a.coarse_sweeps == b.coarse_sweeps && a.mixed_inner == b.mixed_inner && a.restart_drop == b.restart_drop &&
+           a.restart_every == b.restart_every;
+}
+ifx_status check_schedule(const ifx_schedule* s) {
+    if (!s) return set_error(IFX_ERR_ARG, "schedule: null");
+    if (s->mg_pre < 1 || s->mg_post < 1 || s->mg_pre > 16 || s->mg_post > 16)
+        return set_error(IFX_ERR_ARG, "schedule: multigrid sweeps must lie in 1..16");
+    if (!(s->mg_omega > 0 && s->mg_omega < 2)) return set_error(IFX_ERR_ARG, "schedule: omega must lie in (0, 2)");
+    if (s->coarse_sweeps < 1 || s->coarse_sweeps > 10000)
+        return set_error(IFX_ERR_ARG, "schedule: coarse sweeps must lie in 1..10000");
+    if (s->mixed_inner < 1) return set_error(IFX_ERR_ARG, "schedule: mixed_inner must be >= 1");
+    if (!(s->restart_drop > 0 && s->restart_drop < 1) || s->restart_every < 1)
+        return set_error(IFX_ERR_ARG, "schedule: restart_drop in (0, 1), restart_every >= 1");
+    return IFX_OK;
+}
+// Every instance takes the schedule: host configuration, device descriptor
+// (omega, coarse sweeps, restart rule, mixed_inner), the persistent plan's
+// sweep counts; the step graph is rebuilt on next use (it holds the sweep
+// counts and omega as launch parameters).  The descriptors are read back from
+// the device first: a moving body's pose lives there.
+ifx_status apply_schedule(ifx_solver* S, const ifx_schedule& s) {
+    std::vector<InstDev> h(S->inst.size());
+    CUDA_TRY(cudaMemcpyAsync(h.data(), S->dI, h.size() * sizeof(InstDev), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    for (size_t k = 0; k < S->inst.size(); k++) {
+        Instance& I = S->inst[k];
+        I.cfg.mg_pre = s.mg_pre;
+        I.cfg.mg_post = s.mg_post;
+        I.cfg.mg_omega = s.mg_omega;
+        I.cfg.coarse_sweeps = s.coarse_sweeps;
+        I.cfg.mixed_inner = s.mixed_inner;
+        I.cfg.restart_drop = s.restart_drop;
+        I.cfg.restart_every = s.restart_every;
+        I.dev.omega = s.mg_omega;
+        I.dev.coarse_sweeps = s.coarse_sweeps;
+        I.dev.mixed_inner = s.mixed_inner;
+        I.dev.restart_drop = s.restart_drop;
+        I.dev.restart_every = s.restart_every;
+        h[k].omega = s.mg_omega;
+        h[k].coarse_sweeps = s.coarse_sweeps;
+        h[k].mixed_inner = s.mixed_inner;
+        h[k].restart_drop = s.restart_drop;
+        h[k].restart_every = s.restart_every;
+        h[k].retired = I.dev.retired;
+    }
+    CUDA_TRY(cudaMemcpyAsync(S->dI, h.data(), h.size() * sizeof(InstDev), cudaMemcpyHostToDevice, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    drop_graph(S);
+    S->mg_pre = S->plan.mg_pre = s.mg_pre;
+    S->mg_post = S->plan.mg_post = s.mg_post;
+    return IFX_OK;
+}
+}  // namespace
+
+extern "C" ifx_status ifx_set_schedule(ifx_solver* S, const ifx_schedule* sched) {
+    if (!S) return set_error(IFX_ERR_ARG, "ifx_set_schedule: null solver");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_set_schedule needs a METHOD-mode solver");
+    IFX_TRY(check_schedule(sched));
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    return apply_schedule(S, *sched);
+}
+
+extern "C" ifx_status ifx_get_schedule(const ifx_solver* S, int inst, ifx_schedule* out) {
+    if (!S || !out || inst < 0 || inst >= (int)S->inst.size()) return set_error(IFX_ERR_ARG, "ifx_get_schedule: bad argument");
+    *out = schedule_of(S->inst[inst].cfg);
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_autotune_schedule(ifx_solver* S, int steps, ifx_schedule* chosen, double* ms_per_step) {
+    if (!S || steps < 1) return set_error(IFX_ERR_ARG, "ifx_autotune_schedule: bad argument");
+    if (S->mode != IFX_MODE_METHOD) return set_error(IFX_ERR_STATE, "ifx_autotune_schedule needs a METHOD-mode solver");
+    if (S->nmv > 0)
+        return set_error(IFX_ERR_STATE, "ifx_autotune_schedule: a moving body's trial steps would move its geometry, "
+                                        "which the restored state does not include; set the schedule directly");
+    CUDA_TRY(cudaSetDevice(S->device));
+    IFX_TRY(step_finish(S));
+    StateSnapshot snap;
+    IFX_TRY(snap.take(S));
+    const long long steps0 = S->steps_done;
+    const int n = (int)S->inst.size();
+    std::vector<int> retired0(n), status0(S->inst_status.begin(), S->inst_status.end());
+    for (int k = 0; k < n; k++) retired0[k] = S->inst[k].dev.retired;
+    const ifx_schedule start = schedule_of(S->inst[0].cfg);
+    // one candidate: a warm-up step (rebuilds the graph), `steps` timed steps
+    // from the same state, then the state, the statuses and the retirements
+    // are put back; a schedule is valid when every pressure solve of the timed
+    // steps met its stop rule and no instance diverged
+    auto trial = [&](const ifx_schedule& c, double* ms) -> ifx_status {
+        IFX_TRY(apply_schedule(S, c));
+        ifx_status st = ifx_step(S, 1);
+        if (st == IFX_OK) st = ifx_step(S, steps);
+        bool ok = st == IFX_OK;
+        *ms = S->last_ms / steps;
+        for (int k = 0; k < n && ok; k++)
+            ok = retired0[k] || (S->inst_status[k] == status0[k] && S->hS[k].ppe_rel <= S->inst[k].cfg.ppe_tol);
+        if (!ok) *ms = 1e300;
+        if (S->poisoned) return set_error(IFX_ERR_CUDA, "ifx_autotune_schedule: a grid barrier timed out");
+        IFX_TRY(snap.restore(S));
+        for (int k = 0; k < n; k++) {
+            S->inst[k].dev.retired = retired0[k];
+            S->inst_status[k] = status0[k];
+        }
+        S->steps_done = steps0;
+        return IFX_OK;  // apply_schedule of the next trial uploads the descriptors (retired flags included)
+    };
+    ifx_schedule best = start;
+    double best_ms = 1e300;
+    ifx_status st = trial(best, &best_ms);
+    // coordinate search, one pass: a change is kept when it is faster by more
+    // than 1 % (timing noise)
+    auto consider = [&](ifx_schedule c) {
+        if (st != IFX_OK || same_schedule(c, best)) return;
+        double ms = 0;
+        st = trial(c, &ms);
+        if (st == IFX_OK && ms < 0.99 * best_ms) {
+            best = c;
+            best_ms = ms;
+        }
+    };
+    const int pp[5][2] = {{1, 1}, {2, 2}, {1, 2}, {2, 1}, {3, 3}};
+    const ifx_schedule b0 = best;
+    for (auto& q : pp) {
+        ifx_schedule c = b0;
+        c.mg_pre = q[0];
+        c.mg_post = q[1];
+        consider(c);
+    }
+    const ifx_schedule b1 = best;
+    for (double om : {0.6, 0.7, 0.8, 0.9}) {
+        ifx_schedule c = b1;
+        c.mg_omega = om;
+        consider(c);
+    }
+    const ifx_schedule b2 = best;
+    for (int cs : {10, 20, 40, 80}) {
+        ifx_schedule c = b2;
+        c.coarse_sweeps = cs;
+        consider(c);
+    }
+    if (S->prec == IFX_PREC_MIXED) {
+        const ifx_schedule b3 = best;
+        for (int mi : {4, 8, 16}) {
+            ifx_schedule c = b3;
+            c.mixed_inner = mi;
+            consider(c);
+        }
+        const ifx_schedule b4 = best;
+        for (double rd : {1e-3, 1e-4, 1e-5}) {
+            ifx_schedule c = b4;
+            c.restart_drop = rd;
+            consider(c);
+        }
+    }
+    if (st != IFX_OK) {
+        apply_schedule(S, start);
+        return st;
+    }
+    if (best_ms >= 1e300) {
+        IFX_TRY(apply_schedule(S, start));
+        return set_error(IFX_ERR_NOT_CONVERGED, "ifx_autotune_schedule: no schedule met the stop rule");
+    }
+    IFX_TRY(apply_schedule(S, best));
+    if (chosen) *chosen = best;
     if (ms_per_step) *ms_per_step = best_ms;
     return IFX_OK;
 }

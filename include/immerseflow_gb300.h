@@ -137,6 +137,12 @@ typedef struct ifx_config {
     double motion_amp_x, motion_amp_y, motion_amp_deg;  /* harmonic amplitudes  */
     double motion_freq;            /* harmonic frequency (1/time)               */
     double motion_phase_x, motion_phase_y, motion_phase_deg;  /* degrees        */
+    int    coarse_sweeps;          /* red-black SOR sweeps on the coarsest
+                                      multigrid level                           */
+    double restart_drop;           /* mixed path: the FP32 Krylov recursion is
+                                      restarted from the FP64 true residual once
+                                      its residual fell by this factor ...      */
+    int    restart_every;          /* ... or after this many iterations         */
     char   xgrid[IFX_PATH_MAX];    /* face-coordinate files (<idx> <coord>)     */
     char   ygrid[IFX_PATH_MAX];
 } ifx_config;
@@ -233,8 +239,42 @@ ifx_status ifx_get_exec_mode(ifx_solver* s, int* mode);
 /* Autotuner (no reference counterpart): times `steps` steps in each available
  * execution mode and multigrid tile shape (after one warm-up step each),
  * restores the solver state afterwards, and keeps the fastest.  All of them
- * give bit-identical results, so tuning never changes an answer. */
+ * give bit-identical results, so tuning never changes an answer.  A handle with
+ * a moving body is refused (IFX_ERR_STATE): trial steps would move its
+ * geometry, which the restored state does not hold. */
 ifx_status ifx_autotune(ifx_solver* s, int steps, int* chosen_mode, double* ms_per_step);
+/* Sweep schedule of a METHOD-mode step (no reference counterpart: the
+ * reference reads solver settings in inputs.txt that it never uses,
+ * inputs/inputs.txt:14, src/main.cu:39-42).  The pressure solve stops on the
+ * same rule whatever the schedule (FP64 true residual <= ppe_tol ||b||), so a
+ * schedule changes the fields only within that tolerance; it changes how many
+ * iterations, and how much time, the solve takes. */
+typedef struct ifx_schedule {
+    int    mg_pre, mg_post;        /* weighted-Jacobi sweeps before / after the
+                                      coarse-grid correction of the V-cycle     */
+    double mg_omega;               /* weighted-Jacobi factor                    */
+    int    coarse_sweeps;          /* red-black SOR sweeps on the coarsest level */
+    int    mixed_inner;            /* mixed path: FP32 predictor sweeps per FP64
+                                      defect                                    */
+    double restart_drop;           /* mixed path: FP32 Krylov recursion restarted
+                                      from the FP64 true residual after this drop */
+    int    restart_every;          /* ... or after this many iterations         */
+} ifx_schedule;
+/* Every instance of the handle takes the schedule (the configuration fields of
+ * the same names). */
+ifx_status ifx_set_schedule(ifx_solver* s, const ifx_schedule* sched);
+ifx_status ifx_get_schedule(const ifx_solver* s, int inst, ifx_schedule* out);
+/* Autotuner of the sweep schedule (no reference counterpart): a one-pass
+ * coordinate search over the pre/post sweep pair, omega, the coarsest-level
+ * sweeps and, in mixed precision, mixed_inner and the restart drop.  Each
+ * candidate runs a warm-up step and `steps` timed steps from the same saved
+ * state; a candidate counts only if every pressure solve met its stop rule and
+ * no instance diverged, and it replaces the current best only when it is more
+ * than 1% faster.  The state is restored afterwards and the fastest valid
+ * schedule is kept (*chosen, device ms per step).  Run it after
+ * ifx_autotune, in the execution mode that will be used.  A handle with a
+ * moving body is refused (IFX_ERR_STATE), as by ifx_autotune. */
+ifx_status ifx_autotune_schedule(ifx_solver* s, int steps, ifx_schedule* chosen, double* ms_per_step);
 /* Multigrid tile shape of the graph and host-loop modes: 1 = 32x8 cells (one
  * row per thread), 4 = 32x32 cells (four rows per thread, more loads in flight;
  * suits large batches).  Results do not depend on it.  The autotuner sets it. */

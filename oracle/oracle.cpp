@@ -901,7 +901,7 @@ void coarse_solve(orc_solver* S, int l) {
     Level& v = S->L[l];
     std::fill(v.e.begin(), v.e.end(), 0.0);
     const double om = 1.5;
-    for (int it = 0; it < 40; it++)
+    for (int it = 0; it < S->cfg.coarse_sweeps; it++)
         for (int col = 0; col < 2; col++)
             for (int j = 1; j <= v.NY; j++)
                 for (int i = 1; i <= v.NX; i++) {

@@ -126,3 +126,32 @@ def test_body_leaving_the_domain_is_retired():
     s = run(other, failed_at + 2)
     for f in FIELDS:
         assert np.array_equal(bt.get(f, inst=1), s.get(f)), f
+
+
+def test_autotuners_refuse_a_moving_body():
+    # their trial steps would move the geometry, which the restored state lacks
+    s = ifx.Solver.create(*heaving())
+    s.step(1)
+    with pytest.raises(ifx.IFXError) as e:
+        s.autotune(steps=1)
+    assert e.value.status == capi.IFX_ERR_STATE
+    with pytest.raises(ifx.IFXError) as e:
+        s.autotune_schedule(steps=1)
+    assert e.value.status == capi.IFX_ERR_STATE
+
+
+def test_set_schedule_keeps_the_device_pose():
+    # the schedule fields are written into the device descriptors without
+    # touching the pose the moving body keeps there: re-setting the same
+    # schedule mid-run changes nothing, bit for bit
+    a = ifx.Solver.create(*heaving())
+    a.set_exec_mode(ifx.EXEC_GRAPH)
+    b = ifx.Solver.create(*heaving())
+    b.set_exec_mode(ifx.EXEC_GRAPH)
+    a.step(3)
+    b.step(3)
+    b.set_schedule(b.schedule())
+    a.step(3)
+    b.step(3)
+    for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_CELLTYPE):
+        assert np.array_equal(a.get(f), b.get(f)), f

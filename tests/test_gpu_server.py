@@ -171,3 +171,27 @@ def test_retired_instances_leave_the_tile_lists(prec, rows):
     ref = alone(*specs[2], 5)
     for f, a in ref.items():
         assert np.array_equal(s.get(f, inst=2), a), f
+
+
+def test_server_stream_of_mixed_precisions():
+    """FP64 and mixed-precision requests interleaved in one queue: a cohort
+    holds one precision (a batch shares it), so each cohort stops at the first
+    request of the other precision; every request finishes and equals its
+    alone run."""
+    stream = [(case(48, 40, prec=capi.PREC_MIXED), 3), (case(56, 40, prec=capi.PREC_FP64), 2),
+              (case(40, 48, prec=capi.PREC_MIXED), 2), (case(48, 48, prec=capi.PREC_FP64), 3)]
+    srv = ifx.Server(1 << 33, max_cohort=8)
+    ids = {srv.submit(*spec, nsteps=n): (spec, n) for spec, n in stream}
+    done = []
+    for _ in range(20):
+        srv.tick()
+        done += srv.poll()
+        if len(done) == len(stream):
+            break
+    assert sorted(done) == sorted(ids)
+    for rid, (spec, n) in ids.items():
+        assert srv.state(rid)[0] == ifx.REQ_FINISHED
+        ref = alone(*spec, n)
+        for f, a in ref.items():
+            assert np.array_equal(srv.result(rid, f), a), (rid, f)
+    srv.close()
