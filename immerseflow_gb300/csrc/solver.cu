@@ -2603,16 +2603,17 @@ static ifx_status profile_kernel(ifx_solver* S, int kernel, int reps, double* ms
     CUDA_TRY(launch_step_begin(S->dI, S->dS, n, S->dCtl, st));
     auto one = [&]() -> cudaError_t {
         switch (kernel) {
-            case 0:  // the finest-level sweep as the step launches it (32x8 tiles)
+            case 0: {  // the finest-level sweep as the step launches it (the handle's tile shape)
+                const int R = S->mg_rows;
+                const Tile* t0 = R == MG_ROWS_WIDE ? S->dT0W : S->dT0;
+                const int nt0 = R == MG_ROWS_WIDE ? S->nt0W : S->nt0;
                 if (S->inst.size() == 1 && S->dTmap)
-                    return launch_smooth_grid_tma<T>(grid_of(S, 0, 1), S->nt0, S->dS, S->dG, S->dTmap, 0, 0, 1,
-                                                     S->dErr, st);
-                if (S->inst.size() == 1)
-                    return launch_smooth_grid<T>(grid_of(S, 0, 1), S->nt0, S->dS, S->dG, 0, 0, 1, st);
+                    return launch_smooth_grid_tma<T>(grid_of(S, 0, R), nt0, S->dS, S->dG, S->dTmap, 0, 0, R, S->dErr, st);
+                if (S->inst.size() == 1) return launch_smooth_grid<T>(grid_of(S, 0, R), nt0, S->dS, S->dG, 0, 0, R, st);
                 if (S->dTmap)
-                    return launch_smooth_tma<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dTmap, 0, 0, 1,
-                                                S->dErr, st);
-                return launch_smooth<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, 1, st);
+                    return launch_smooth_tma<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dTmap, 0, 0, R, S->dErr, st);
+                return launch_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 0, 0, R, st);
+            }
             case 1: return launch_bicg_apply<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, 0, 1, st);
             case 2: return launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st);
             case 4: return launch_barrier_bench(S->dBar, S->persist_grid, 1000, st);
