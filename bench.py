@@ -393,12 +393,17 @@ def long_run_accuracy(ifx, capi, cases, steps=1000):
             "cd_final": float(h6[-1, 1]), "cl_final": float(h6[-1, 2])}
 
 
-def _oracle_solver(cfg, xf, yf):
+def _oracle_solver(cfg, xf, yf, schedule=None):
     """The CPU oracle (FP64 restatement of the same scheme) on all host threads:
-    the checker of the accuracy lines."""
+    the checker of the accuracy lines; `schedule` (a tuned capi.Schedule) sets
+    its sweep schedule, which the oracle follows like the GPU."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
 
+    if schedule is not None:
+        cfg = type(cfg).from_buffer_copy(cfg)
+        for k, v in schedule.as_dict().items():
+            setattr(cfg, k, v)
     return _oracle.Oracle().method(cfg, xf, yf, os.cpu_count() or 1)
 
 
@@ -426,7 +431,9 @@ def ellipse_line(ifx, capi, cases, steps=10, oracle=True):
     1 at 10 deg, 1024x768 cells on a 20x12 domain, Re 300, dt 2e-3; autotuned,
     mixed and plain FP64 (device time, CUDA events).  Both results are compared
     with the CPU oracle after the same 3 + `steps` steps (Linf velocity and
-    divergence errors)."""
+    divergence errors); the oracle follows the FP64 run's tuned schedule, so the
+    mixed run's errors include its own schedule's difference (within the
+    pressure tolerance)."""
     out = {"workload": "ellipse aspect 0.2, chord 1, 10 deg, 20x12 domain, 1024x768 tanh-stretched, Re 300, dt 2e-3",
            "unit": METRIC, "steps": steps}
     fields = {}
@@ -450,7 +457,7 @@ def ellipse_line(ifx, capi, cases, steps=10, oracle=True):
     out["rel_l2_velocity_vs_fp64"] = rel_l2(fields["mixed"], fields["fp64"])
     if oracle:
         cfg, xf, yf = cases.ellipse(precision=capi.PREC_FP64)
-        o = _oracle_solver(cfg, xf, yf)
+        o = _oracle_solver(cfg, xf, yf, solvers["fp64"].schedule())
         o.step(3 + steps)
         out["vs_oracle"] = {name: vs_oracle(capi, s.get, s.stats(), o) for name, s in solvers.items()}
         out["vs_oracle"]["steps"] = 3 + steps
@@ -463,7 +470,7 @@ def cavity_line(ifx, capi, cases, steps=2000, oracle=True):
     """Lid-driven cavity: unit square, uniform 128x128, lid u = 1, no-slip
     walls, Re 100, dt 1e-3, pressure to 1e-8, `steps` steps from rest (device
     time of the last steps - 1, CUDA events), mixed and plain FP64; both against
-    the CPU oracle after the same steps."""
+    the CPU oracle after the same steps (with the FP64 run's tuned schedule)."""
     out = {"workload": "lid-driven cavity, unit square, uniform 128x128, lid u=1, Re 100, dt 1e-3, "
                        f"pressure to 1e-8, {steps} steps", "unit": METRIC, "steps": steps}
     solvers = {}
@@ -487,7 +494,7 @@ def cavity_line(ifx, capi, cases, steps=2000, oracle=True):
         np.concatenate([g6.get(capi.FIELD_U).ravel(), g6.get(capi.FIELD_V).ravel()]))
     if oracle:
         cfg, xf, yf = cases.cavity(precision=capi.PREC_FP64)
-        o = _oracle_solver(cfg, xf, yf)
+        o = _oracle_solver(cfg, xf, yf, solvers["fp64"].schedule())
         t0 = time.perf_counter()
         o.step(steps)
         dt = time.perf_counter() - t0
