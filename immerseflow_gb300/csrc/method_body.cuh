@@ -142,6 +142,15 @@ __device__ __forceinline__ void inst_sum(const double* part, int beg, int cnt, d
 __device__ __forceinline__ void loop_vote(LoopCtl* ctl, bool active, unsigned long long handle, bool due = false) {
     // thread 0 of each voting block; no-op inside the persistent kernel (ctl == nullptr)
     if (!ctl) return;
+    if (gridDim.x == 1) {
+        // the only voting block (a one-instance solver): the vote is its own,
+        // with no other block to count or to order against; the counters stay
+        // at zero and the next kernel sees the result at the kernel boundary
+        ctl->result = active ? 1 : 0;
+        ctl->due_result = due ? 1 : 0;
+        if (handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, active ? 1u : 0u);
+        return;
+    }
     if (active) atomicAdd(&ctl->active, 1);
     if (due) atomicAdd(&ctl->due, 1);
     __threadfence();
