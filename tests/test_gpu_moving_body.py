@@ -155,3 +155,19 @@ def test_set_schedule_keeps_the_device_pose():
     b.step(3)
     for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P, capi.FIELD_CELLTYPE):
         assert np.array_equal(a.get(f), b.get(f)), f
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_galilean_consistency_of_the_towed_cylinder(prec):
+    """The GPU's towed cylinder against its fixed cylinder in a uniform stream
+    (tests/_galilean.py): the time-averaged drag difference falls under
+    refinement (128 -> 192 cells across) and is below 3% on the finer grid."""
+    import _galilean as gl
+
+    diffs = []
+    for n in (128, 192):
+        fixed = ifx.Solver.create(*gl.case(n, False, prec))
+        towed = ifx.Solver.create(*gl.case(n, True, prec))
+        f, t = gl.mean_drag(fixed), gl.mean_drag(towed)
+        diffs.append(abs(t - f) / abs(f))
+    assert diffs[0] > diffs[1] and diffs[1] < 0.03, diffs
