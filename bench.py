@@ -17,7 +17,8 @@ plain_fp64: the same steps with every kernel in FP64;
 roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
             launch per step, or the persistent per-step kernel); achieved =
             algorithmic bytes of the step / its event time; traffic = the DRAM
-            bytes of one warm-cache step from the committed ncu launch list.
+            bytes of one step from the committed one-launch ncu capture of the
+            persistent per-step kernel (the same phases in one launch).
             Algorithmic bytes per interior cell (s = 4 B FP32 multigrid
             word, state words 8 B, stencil byte 1 B):
               convection+AB2 rhs 81, predictor sweep 49 (x sweeps),
@@ -180,14 +181,13 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def committed_traffic(persistent):
-    """DRAM bytes per step of the cylinder step from the committed ncu summary:
-    the persistent kernel's launch, or the sum over the step's kernels."""
-    name = "persist_step_cylinder_384x256.md" if persistent else "launch_list_cylinder_384x256_host.md"
-    key = "traffic_bytes_per_launch:" if persistent else "traffic_bytes_per_step:"
+def committed_traffic():
+    """DRAM bytes of one cylinder step from the committed ncu summary of the
+    persistent per-step kernel: one launch runs every phase of the step, so a
+    single-launch capture gives the step's traffic."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", name)):
-            if line.startswith(key):
+        for line in open(os.path.join(ROOT, "profiles", "persist_step_cylinder_384x256.md")):
+            if line.startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":")[1])
     except Exception:
         pass
@@ -807,8 +807,7 @@ def main():
             s.set(f, a)
         s.step(1)
         for f, a in host.items():
-            lib_out = s.get(f).ravel()
-            a[:] = lib_out
+            s.get(f, out=a)  # straight into the pinned buffer
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * cells * args.steps / e2e_s / 1e6
@@ -817,7 +816,7 @@ def main():
     # roofline of the dominant kernel: the per-step kernel (persistent mode)
     peak, peak_kind = measured_peak()
     persistent = s.exec_mode() == 0
-    traffic = committed_traffic(persistent)
+    traffic = committed_traffic()
     achieved = step_bytes_total / (total_ms * 1e-3) / 1e9
     # one phase alone: the finest-level smoothing sweep, FP32 in the mixed path
     k_ms, k_cells = s.profile_kernel(0, reps=200)

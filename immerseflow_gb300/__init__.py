@@ -207,12 +207,18 @@ class Solver:
         _check(lib().ifx_ppe_reference(self._h, C.byref(it)))
         return it.value
 
-    def get(self, field, inst=0):
-        """Copy a field to the host; cell fields come back as [ny, nx]."""
+    def get(self, field, inst=0, out=None):
+        """Copy a field to the host; cell fields come back as [ny, nx].  With
+        `out` (a C-contiguous float64 array of the field's size, e.g. a pinned
+        buffer reused every step) the field is copied straight into it."""
         nx, ny = self.grid_dims(inst)
         shp = {capi.FIELD_UF: (ny - 2, nx - 1), capi.FIELD_VF: (ny - 1, nx - 2),
                capi.FIELD_XC: (nx,), capi.FIELD_YC: (ny,)}.get(field, (ny, nx))
-        out = np.zeros(int(np.prod(shp)))
+        n = int(np.prod(shp))
+        if out is None:
+            out = np.zeros(n)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != n:
+            raise ValueError(f"out must be a C-contiguous float64 array of {n} values")
         _check(lib().ifx_get_field_i(self._h, inst, field, _dptr(out), out.size))
         return out.reshape(shp)
 
