@@ -24,7 +24,7 @@ cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng
                                 int stage, int finalize, const LoopCtl* ctl, int rows, cudaStream_t s);
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
                                LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
-cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
+cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, double* part, int to_final,
                             cudaStream_t s);
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
 template <typename T>

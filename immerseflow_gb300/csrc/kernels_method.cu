@@ -65,7 +65,9 @@ __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restri
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle) { b_pred_reduce(I, S, part, parity, ctl, handle, blockIdx.x); }
 __global__ void __launch_bounds__(TILE_THREADS, 8) k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
-                           double* __restrict__ part, int to_final) { b_face_rhs(tiles, I, part, to_final, blockIdx.x); }
+                           const InstState* __restrict__ S, double* __restrict__ part, int to_final) {
+    b_face_rhs(tiles, I, S, part, to_final, blockIdx.x);
+}
 __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part) { b_rhs_reduce(I, S, part, blockIdx.x); }
 // restart_only: for a chunk of blockDim instances at a time, every block forms
@@ -242,9 +244,9 @@ cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* par
     k_pred_reduce<<<ninst, 256, 0, s>>>(I, S, part, parity, ctl, handle);
     return cudaGetLastError();
 }
-cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, double* part, int to_final,
+cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, double* part, int to_final,
                             cudaStream_t s) {
-    k_face_rhs<<<nt, TILE_THREADS, 0, s>>>(t, I, part, to_final);
+    k_face_rhs<<<nt, TILE_THREADS, 0, s>>>(t, I, S, part, to_final);
     return cudaGetLastError();
 }
 cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s) {

@@ -162,7 +162,7 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
         BAR();
     }
     if (!ghost_fill(P, 3, ep)) return false;
-    FOR_VB(P.nt0) b_face_rhs(P.t0, P.I, P.part, 0, vb);
+    FOR_VB(P.nt0) b_face_rhs(P.t0, P.I, P.S, P.part, 0, vb);
     BAR();
     FOR_VB(n) b_rhs_reduce(P.I, P.S, P.part, vb);
     BAR();

@@ -822,6 +822,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dalloc(S, &d.Nu, nc)); IFX_TRY(dalloc(S, &d.Nv, nc));
         IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
         IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
+        IFX_TRY(dalloc(S, &d.pold, nc));
         IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
         if (S->prec == IFX_PREC_MIXED)
             for (float** a : {&d.du, &d.dv, &d.du2, &d.dv2, &d.rfu, &d.rfv}) IFX_TRY(dalloc(S, a, nc));
@@ -1173,7 +1174,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         CUDA_TRY(cudaStreamSynchronize(S->stream));  // host vectors go out of scope
     }
     CUDA_TRY(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, S->stream));
-    CUDA_TRY(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 1, S->stream));
+    CUDA_TRY(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dS, S->dPart, 1, S->stream));
     S->launches += 3;
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     IFX_TRY(setup_persistent(S));
@@ -1340,7 +1341,7 @@ void seq_mid(Seq& q) {
                                   nullptr, S->mg_rows, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
-    q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dPart, 0, st));
+    q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dS, S->dPart, 0, st));
     q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
     q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, nullptr, n, st));
     q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st));
@@ -2096,7 +2097,8 @@ struct StateSnapshot {
         for (const Instance& I : S->inst) {
             const InstDev& d = I.dev;
             const size_t nc = I.ncell * sizeof(double), nq = 4 * (size_t)I.qstride * sizeof(double);
-            for (void* p : {(void*)d.u, (void*)d.v, (void*)d.U, (void*)d.V, (void*)d.Nu, (void*)d.Nv, (void*)d.p})
+            for (void* p : {(void*)d.u, (void*)d.v, (void*)d.U, (void*)d.V, (void*)d.Nu, (void*)d.Nv, (void*)d.p,
+                            (void*)d.pold})
                 items.push_back({p, nc});
             items.push_back({(void*)d.qbu, nq});
             items.push_back({(void*)d.qbv, nq});

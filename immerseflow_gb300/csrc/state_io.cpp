@@ -50,7 +50,7 @@ namespace {
 
 constexpr char kMagic[8] = {'I', 'F', 'X', 'C', 'K', 'P', 'T', '1'};
 constexpr char kSetMagic[8] = {'I', 'F', 'X', 'C', 'K', 'S', 'E', 'T'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;  // 2: the pressure of the step before (initial-guess extrapolation)
 
 struct CkptHeader {
     char magic[8];
@@ -91,9 +91,13 @@ bool method(const ifx_solver* S) { return S->mode == IFX_MODE_METHOD; }
 
 size_t cells(const Instance& I) { return (size_t)I.nx * I.ny; }
 
+// Cell fields a METHOD-mode checkpoint carries: u, v, U, V, the convection
+// history Nu, Nv, p and the pressure of the step before.
+constexpr int kMethodFields = 8;
+
 size_t payload_bytes(const ifx_solver* S, const Instance& I) {
     if (!method(S)) return 3 * cells(I) * sizeof(double);
-    return 7 * cells(I) * sizeof(double) + 2 * 4 * (size_t)I.qstride * sizeof(double) + sizeof(InstState);
+    return kMethodFields * cells(I) * sizeof(double) + 2 * 4 * (size_t)I.qstride * sizeof(double) + sizeof(InstState);
 }
 
 // Pitched device field <-> dense host rows.
@@ -120,8 +124,8 @@ ifx_status check_restartable(const ifx_solver* S, int inst, const char* fn) {
 }
 
 // The seven METHOD-mode cell arrays of a checkpoint, in order.
-void method_fields(const InstDev& d, double* (&f)[7]) {
-    f[0] = d.u; f[1] = d.v; f[2] = d.U; f[3] = d.V; f[4] = d.Nu; f[5] = d.Nv; f[6] = d.p;
+void method_fields(const InstDev& d, double* (&f)[kMethodFields]) {
+    f[0] = d.u; f[1] = d.v; f[2] = d.U; f[3] = d.V; f[4] = d.Nu; f[5] = d.Nv; f[6] = d.p; f[7] = d.pold;
 }
 
 // REFERENCE-mode arrays (dense rows).
@@ -207,10 +211,10 @@ extern "C" ifx_status ifx_checkpoint_save(ifx_solver* S, int inst, void* buf, si
     double* q = (double*)pay;
     const size_t nc = cells(I);
     if (method(S)) {
-        double* f[7];
+        double* f[kMethodFields];
         method_fields(I.dev, f);
-        for (int k = 0; k < 7; k++) SIO_TRY(field_out(S, I, f[k], I.pitch, q + k * nc));
-        double* qb = q + 7 * nc;
+        for (int k = 0; k < kMethodFields; k++) SIO_TRY(field_out(S, I, f[k], I.pitch, q + k * nc));
+        double* qb = q + kMethodFields * nc;
         SIO_CUDA(cudaMemcpyAsync(qb, I.dev.qbu, 4 * (size_t)I.qstride * 8, cudaMemcpyDeviceToHost, S->stream));
         SIO_CUDA(cudaMemcpyAsync(qb + 4 * (size_t)I.qstride, I.dev.qbv, 4 * (size_t)I.qstride * 8, cudaMemcpyDeviceToHost,
                                  S->stream));
@@ -270,13 +274,13 @@ extern "C" ifx_status ifx_checkpoint_load(ifx_solver* S, int inst, const void* b
     std::memcpy(q.data(), pay, h.payload_bytes);
     const size_t nc = cells(I);
     if (method(S)) {
-        double* f[7];
+        double* f[kMethodFields];
         method_fields(I.dev, f);
-        for (int k = 0; k < 7; k++) SIO_TRY(field_in(S, I, f[k], I.pitch, q.data() + k * nc));
+        for (int k = 0; k < kMethodFields; k++) SIO_TRY(field_in(S, I, f[k], I.pitch, q.data() + k * nc));
         // Jacobi partners start equal to the state, as at creation
         SIO_TRY(field_in(S, I, I.dev.u2, I.pitch, q.data()));
         SIO_TRY(field_in(S, I, I.dev.v2, I.pitch, q.data() + nc));
-        const double* qb = q.data() + 7 * nc;
+        const double* qb = q.data() + kMethodFields * nc;
         SIO_CUDA(cudaMemcpyAsync(I.dev.qbu, qb, 4 * (size_t)I.qstride * 8, cudaMemcpyHostToDevice, S->stream));
         SIO_CUDA(cudaMemcpyAsync(I.dev.qbv, qb + 4 * (size_t)I.qstride, 4 * (size_t)I.qstride * 8, cudaMemcpyHostToDevice,
                                  S->stream));
@@ -442,6 +446,7 @@ extern "C" ifx_status ifx_read_snapshot_ascii(ifx_solver* S, int inst, const cha
         SIO_CUDA(cudaMemcpyAsync(&st, S->dS + inst, sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
         SIO_CUDA(cudaStreamSynchronize(S->stream));
         st.have_nold = 0;  // no convection history in this format
+        st.pold_n = 0;     // nor the pressure of the step before
         if (steps >= 0) st.nstep = steps;
         SIO_CUDA(cudaMemcpyAsync(S->dS + inst, &st, sizeof(InstState), cudaMemcpyHostToDevice, S->stream));
     } else {
