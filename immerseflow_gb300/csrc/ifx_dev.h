@@ -245,7 +245,7 @@ struct alignas(16) InstDev {
     double uc;                   // convective outflow speed
     double area;                 // sum of fluid-cell areas
     double *u, *v, *u2, *v2, *Us, *Vs, *U, *V, *Nu, *Nv, *ru, *rv, *p, *b, *div, *iblank;
-    double* pold;                // pressure of the step before (initial-guess extrapolation)
+    double *pold, *pold2;        // pressures of the two steps before (initial-guess extrapolation)
     const double *dx, *dy, *fx, *gx, *fy, *gy, *xc, *yc, *xf, *yf;
     const double *kx, *ky, *ix, *iy;   // finest-level face coefficients and 1/width
     const uint8_t* type;
@@ -286,7 +286,7 @@ struct alignas(16) InstDev {
 struct InstState {
     int pred_state, pred_iters, ppe_state, ppe_iters;
     int status, have_nold;
-    int pold_n, pad_pold;                     // steps that stored the pressure of the step before (saturates at 3)
+    int pold_n, pad_pold;                     // steps that stored their pressure for the extrapolation (saturates at 4)
     int restart, restart_it;                  // mixed path: FP64 residual due next body; iteration of the last one
     double pred_metric, ppe_rel, bmean, bnorm, pmean;
     double rho, alpha, omega, beta;           // BiCGSTAB scalars

@@ -336,7 +336,7 @@ __device__ __forceinline__ void b_step_begin(const InstDev* __restrict__ I, Inst
     const int st = I[k].retired ? ST_DONE : ST_ACTIVE;
     if (st == ST_ACTIVE) {
         S[k].nstep++;
-        if (S[k].pold_n < 3) S[k].pold_n++;
+        if (S[k].pold_n < 4) S[k].pold_n++;
     }
     S[k].pred_state = st;
     S[k].pred_iters = 0;
@@ -725,11 +725,12 @@ __device__ __forceinline__ double face_v(const InstDev& in, const double* v, int
 
 // Face velocities of the predicted field (into Us,Vs, or into U,V when
 // to_final), the pressure source div(U*)/dt and its area-weighted sum.
-// Also sets the pressure solve's initial guess: from the third step of an
-// instance on, the linear extrapolation 2 p^(n-1) - p^(n-2) of its last two
-// pressures (the solve from the last pressure alone starts O(dt) away, the
-// extrapolation O(dt^2): fewer Krylov iterations under the same stop rule).
-// 2 p is exact, so the value does not depend on multiply-add contraction.
+// Also sets the pressure solve's initial guess: the extrapolation of the
+// instance's last pressures, 3 p^(n-1) - 3 p^(n-2) + p^(n-3) from its fourth
+// step on, 2 p^(n-1) - p^(n-2) on its third (the solve from the last pressure
+// alone starts O(dt) away, the quadratic extrapolation O(dt^3): fewer Krylov
+// iterations under the same stop rule).  Each operation is rounded on its
+// own, as in the oracle.
 __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S, double* __restrict__ part, int to_final, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
@@ -752,8 +753,11 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
             in.b[id] = b;
             acc[0] = b * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
             if (!to_final) {
-                const double po = in.p[id];
-                if (S[t.inst].pold_n >= 3) in.p[id] = 2.0 * po - in.pold[id];
+                const double po = in.p[id], p2 = in.pold[id];
+                const int m = S[t.inst].pold_n;
+                if (m >= 4) in.p[id] = __dadd_rn(__dsub_rn(__dmul_rn(3.0, po), __dmul_rn(3.0, p2)), in.pold2[id]);
+                else if (m >= 3) in.p[id] = __dsub_rn(__dmul_rn(2.0, po), p2);
+                in.pold2[id] = p2;
                 in.pold[id] = po;
             }
         } else {

@@ -31,7 +31,7 @@
 namespace ifx {
 
 // Device bytes of one METHOD-mode instance (the allocations of create_method:
-// 25 FP64 cell fields, cell types, ghost index map, two multigrid buffers and
+// 26 FP64 cell fields, cell types, ghost index map, two multigrid buffers and
 // a residual per level in T plus stencil bytes), rounded up by 10% for the
 // ghost tables, 1-D metrics and per-level tables.
 size_t estimate_instance_bytes(const ifx_config& c) {
@@ -39,7 +39,7 @@ size_t estimate_instance_bytes(const ifx_config& c) {
     const size_t pitch = (nx + 31) / 32 * 32;
     const size_t cells = pitch * ny;
     const size_t ts = c.precision == IFX_PREC_FP64 ? 8 : 4;
-    const size_t per_cell = 25 * 8 + 1 + 4;
+    const size_t per_cell = 26 * 8 + 1 + 4;
     const size_t levels = cells * 4 / 3 * (3 * ts + 1);
     return (cells * per_cell + levels) * 11 / 10 + (1u << 20);
 }

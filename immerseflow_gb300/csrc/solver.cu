@@ -822,7 +822,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dalloc(S, &d.Nu, nc)); IFX_TRY(dalloc(S, &d.Nv, nc));
         IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
         IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
-        IFX_TRY(dalloc(S, &d.pold, nc));
+        IFX_TRY(dalloc(S, &d.pold, nc)); IFX_TRY(dalloc(S, &d.pold2, nc));
         IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
         if (S->prec == IFX_PREC_MIXED)
             for (float** a : {&d.du, &d.dv, &d.du2, &d.dv2, &d.rfu, &d.rfv}) IFX_TRY(dalloc(S, a, nc));
@@ -2098,7 +2098,7 @@ struct StateSnapshot {
             const InstDev& d = I.dev;
             const size_t nc = I.ncell * sizeof(double), nq = 4 * (size_t)I.qstride * sizeof(double);
             for (void* p : {(void*)d.u, (void*)d.v, (void*)d.U, (void*)d.V, (void*)d.Nu, (void*)d.Nv, (void*)d.p,
-                            (void*)d.pold})
+                            (void*)d.pold, (void*)d.pold2})
                 items.push_back({p, nc});
             items.push_back({(void*)d.qbu, nq});
             items.push_back({(void*)d.qbv, nq});

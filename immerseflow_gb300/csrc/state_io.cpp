@@ -50,7 +50,7 @@ namespace {
 
 constexpr char kMagic[8] = {'I', 'F', 'X', 'C', 'K', 'P', 'T', '1'};
 constexpr char kSetMagic[8] = {'I', 'F', 'X', 'C', 'K', 'S', 'E', 'T'};
-constexpr uint32_t kVersion = 2;  // 2: the pressure of the step before (initial-guess extrapolation)
+constexpr uint32_t kVersion = 2;  // 2: the pressures of the two steps before (initial-guess extrapolation)
 
 struct CkptHeader {
     char magic[8];
@@ -92,8 +92,8 @@ bool method(const ifx_solver* S) { return S->mode == IFX_MODE_METHOD; }
 size_t cells(const Instance& I) { return (size_t)I.nx * I.ny; }
 
 // Cell fields a METHOD-mode checkpoint carries: u, v, U, V, the convection
-// history Nu, Nv, p and the pressure of the step before.
-constexpr int kMethodFields = 8;
+// history Nu, Nv, p and the pressures of the two steps before.
+constexpr int kMethodFields = 9;
 
 size_t payload_bytes(const ifx_solver* S, const Instance& I) {
     if (!method(S)) return 3 * cells(I) * sizeof(double);
@@ -126,6 +126,7 @@ ifx_status check_restartable(const ifx_solver* S, int inst, const char* fn) {
 // The seven METHOD-mode cell arrays of a checkpoint, in order.
 void method_fields(const InstDev& d, double* (&f)[kMethodFields]) {
     f[0] = d.u; f[1] = d.v; f[2] = d.U; f[3] = d.V; f[4] = d.Nu; f[5] = d.Nv; f[6] = d.p; f[7] = d.pold;
+    f[8] = d.pold2;
 }
 
 // REFERENCE-mode arrays (dense rows).
@@ -446,7 +447,7 @@ extern "C" ifx_status ifx_read_snapshot_ascii(ifx_solver* S, int inst, const cha
         SIO_CUDA(cudaMemcpyAsync(&st, S->dS + inst, sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
         SIO_CUDA(cudaStreamSynchronize(S->stream));
         st.have_nold = 0;  // no convection history in this format
-        st.pold_n = 0;     // nor the pressure of the step before
+        st.pold_n = 0;     // nor the pressures of the steps before
         if (steps >= 0) st.nstep = steps;
         SIO_CUDA(cudaMemcpyAsync(S->dS + inst, &st, sizeof(InstState), cudaMemcpyHostToDevice, S->stream));
     } else {

@@ -509,9 +509,10 @@ struct orc_solver {
     std::vector<double> qbu, qbv;                       // outflow face values, [side*qstride + k]
     int qstride = 0;
     bool have_nold = false;
-    // pressure of the step before (the initial guess of step n >= 3 is the
-    // linear extrapolation 2 p^(n-1) - p^(n-2)) and the steps that stored one
-    std::vector<double> pold;
+    // pressures of the two steps before: the initial guess of the pressure
+    // solve is the extrapolation of the last three pressures (quadratic from an
+    // instance's fourth step, linear on its third); pold_n counts the steps
+    std::vector<double> pold, pold2;
     int pold_n = 0;
     bool singular = true;
     bool dir[4] = {false, false, false, false};
@@ -1197,7 +1198,7 @@ void method_step(orc_solver* S) {
     const int nx = S->nx, ny = S->ny, n = S->n;
     const double dt = c.dt, dtre = c.dt / c.re;
     S->nstep++;
-    if (S->pold_n < 3) S->pold_n++;
+    if (S->pold_n < 4) S->pold_n++;
     if (S->moving) move_body(S);
     const Level& l0 = S->L[0];
     // 1. outflow face values and ghosts of u^n, v^n
@@ -1286,11 +1287,13 @@ void method_step(orc_solver* S) {
             if (S->type[id] != T_FLUID) { S->b[id] = 0.0; continue; }
             double d = (S->U[id] - S->U[id - 1]) * l0.ix[i] + (S->V[id] - S->V[id - nx]) * l0.iy[j];
             S->b[id] = d / dt;
-            // initial guess of the pressure solve: from the third step on, the
-            // linear extrapolation of the last two pressures (2 p is exact, so
-            // a fused multiply-add gives the same value)
+            // initial guess of the pressure solve: the extrapolation of the last
+            // pressures, 3 p1 - 3 p2 + p3 from the fourth step on, 2 p1 - p2 on
+            // the third (each operation rounded on its own, as the kernels do)
             const double po = S->p[id];
-            if (S->pold_n >= 3) S->p[id] = 2.0 * po - S->pold[id];
+            if (S->pold_n >= 4) S->p[id] = (3.0 * po - 3.0 * S->pold[id]) + S->pold2[id];
+            else if (S->pold_n >= 3) S->p[id] = 2.0 * po - S->pold[id];
+            S->pold2[id] = S->pold[id];
             S->pold[id] = po;
             bsum += S->b[id] * (S->dx[i] * S->dy[j]);
             asum += S->dx[i] * S->dy[j];
@@ -1500,7 +1503,7 @@ extern "C" orc_solver* orc_create(const ifx_config* cfg, const double* xf, const
     for (size_t q = 0; q < S->ghosts.size(); q++) if (S->ghosts[q].side < 0) S->gidx[S->ghosts[q].cell] = (int)q;
     build_levels(S);
     // state
-    S->u.assign(n, 0.0); S->v.assign(n, 0.0); S->p.assign(n, 0.0); S->pold.assign(n, 0.0);
+    S->u.assign(n, 0.0); S->v.assign(n, 0.0); S->p.assign(n, 0.0); S->pold.assign(n, 0.0); S->pold2.assign(n, 0.0);
     S->U.assign(n, 0.0); S->V.assign(n, 0.0);
     S->Nu.assign(n, 0.0); S->Nv.assign(n, 0.0);
     S->ru.assign(n, 0.0); S->rv.assign(n, 0.0);
