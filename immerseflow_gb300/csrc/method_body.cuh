@@ -86,9 +86,14 @@ __device__ __forceinline__ void tile_ij(const Tile& t, int& i, int& j) {
 // Deterministic block sum of NV values; result valid in thread 0..NV-1 as out[k].
 // RT: arithmetic of the in-warp stage (float on the mixed path, whose Krylov
 // vectors are FP32: FP64 butterfly adds on every lane are slow on GB300); the
-// warp results are summed in FP64.
-template <int NV, typename RT = double>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double* out) {
+// warp results are summed in FP64.  The values may be given as float: a
+// product or sum of two floats formed in FP64 and rounded to float equals
+// the FP32 operation (53 >= 2*24 + 2 bits, so the double rounding is
+// innocuous), and GB300 issues FP64 operations and conversions at 1/61 of
+// the FP32 rate (2 FP64 FMA per SM and clock), so the mixed path forms its
+// FP32 partials in FP32.
+template <int NV, typename RT = double, typename VT>
+__device__ __forceinline__ void block_sum(VT (&v)[NV], double* out) {
     __shared__ double sh[NV][32];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
@@ -313,9 +318,9 @@ __device__ __forceinline__ size_t sub_slot(const InstDev& in, const LevelDev& L,
     ok = row < nty;
     return (size_t)in.tile_beg + (size_t)row * ntx + t.i0 / TILE_X;
 }
-template <int NV, typename RT, int R>
+template <int NV, typename RT, int R, typename VT>
 __device__ __forceinline__ void write_sub_partials(const InstDev& in, const LevelDev& L, const Tile& t,
-                                                   double (&acc)[R][NV], double* __restrict__ part) {
+                                                   VT (&acc)[R][NV], double* __restrict__ part) {
 #pragma unroll
     for (int r = 0; r < R; r++) {
         __shared__ double out[NV];
@@ -663,7 +668,7 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
         const float dtre = (float)in.dtre;
         const float ixi = __ldg(&L.ixf[ic]);
         const float aE = dtre * (__ldg(&L.kxf[ic]) * ixi), aW = dtre * (__ldg(&L.kxf[ic - 1]) * ixi);
-        double m[R][1];
+        float m[R][1];
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int q = id[r];
@@ -675,11 +680,11 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
                               aP * su[q]) * di;
             const float dV = (in.rfv[q] + aE * sv[q + 1] + aW * sv[q - 1] + aN * sv[q + P] + aS * sv[q - P] -
                               aP * sv[q]) * di;
-            m[r][0] = 0.0;
+            m[r][0] = 0.0f;
             if (fl[r]) {
                 du[q] = su[q] + dU;
                 dv[q] = sv[q] + dV;
-                m[r][0] = (double)fabsf(dU) + (double)fabsf(dV);
+                m[r][0] = fabsf(dU) + fabsf(dV);
             }
         }
         write_sub_partials<1, float, R>(in, L, t, m, part);
@@ -713,6 +718,18 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
 
 // -------------------------------------------------- faces and PPE source
 
+// Face values of a 32x8 tile (b_face_rhs, b_correct): x faces i0-1 .. i0+31
+// of its rows and y faces j0-1 .. j0+7 of its columns, two fields each.  One
+// shared allocation serves both phases (a function-scope __shared__ object).
+struct TileFaces {
+    double x[2][TILE_Y][TILE_X + 1];
+    double y[2][TILE_Y + 1][TILE_X];
+};
+__device__ __forceinline__ TileFaces& tile_faces() {
+    __shared__ TileFaces f;
+    return f;
+}
+
 __device__ __forceinline__ double face_u(const InstDev& in, const double* u, int i, int id) {
     if (__ldg(&in.type[id]) == T_FLUID || __ldg(&in.type[id + 1]) == T_FLUID) return u[id] * __ldg(&in.gx[i]) + u[id + 1] * __ldg(&in.fx[i]);
     return 0.0;
@@ -730,28 +747,48 @@ __device__ __forceinline__ double face_v(const InstDev& in, const double* v, int
 // step on, 2 p^(n-1) - p^(n-2) on its third (the solve from the last pressure
 // alone starts O(dt) away, the quadratic extrapolation O(dt^3): fewer Krylov
 // iterations under the same stop rule).  Each operation is rounded on its
-// own, as in the oracle.
+// own, as in the oracle.  Every face value is formed once, as in b_correct:
+// thread (w, lane) forms the east and north faces of its cell, warps 0 and 1
+// the south faces of the first row and the west faces of the first column.
 __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S, double* __restrict__ part, int to_final, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     if (in.retired) return;
+    TileFaces& F = tile_faces();
+    auto& sU = F.x[0];
+    auto& sV = F.y[0];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     int i, j;
     tile_ij(t, i, j);
-    const int P = in.pitch, id = i + j * P;
+    const int P = in.pitch, id = i + j * P, NX = in.NX, NY = in.NY;
+    const bool row = j >= 1 && j <= NY, col = i >= 1 && i <= NX;
     double* Uo = to_final ? in.U : in.Us;
     double* Vo = to_final ? in.V : in.Vs;
-    if (i <= in.nx - 2 && j >= 1 && j <= in.NY) Uo[id] = face_u(in, in.u, i, id);
-    if (j <= in.ny - 2 && i >= 1 && i <= in.NX) Vo[id] = face_v(in, in.v, j, id);
+    {
+        double Ue = 0.0, Vn = 0.0;
+        if (row && i <= NX) Uo[id] = Ue = face_u(in, in.u, i, id);
+        if (col && j <= NY) Vo[id] = Vn = face_v(in, in.v, j, id);
+        sU[w][l + 1] = Ue;
+        sV[w + 1][l] = Vn;
+    }
+    if (w == 0) {
+        const int js = t.j0 - 1;
+        sV[0][l] = (js >= 0 && col) ? face_v(in, in.v, js, i + js * P) : 0.0;
+    } else if (w == 1 && l < TILE_Y) {
+        const int iw = t.i0 - 1, jw = t.j0 + l;
+        sU[l][0] = (iw >= 0 && jw >= 1 && jw <= NY) ? face_u(in, in.u, iw, iw + jw * P) : 0.0;
+    }
+    __syncthreads();
     double acc[1] = {0.0};
-    if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
+    if (row && col) {
         if (__ldg(&in.type[id]) == T_FLUID) {
-            const double Ue = face_u(in, in.u, i, id), Uw = face_u(in, in.u, i - 1, id - 1);
-            const double Vn = face_v(in, in.v, j, id), Vs = face_v(in, in.v, j - 1, id - P);
+            const double Ue = sU[w][l + 1], Uw = sU[w][l];
+            const double Vn = sV[w + 1][l], Vs = sV[w][l];
             const double d = (Ue - Uw) * __ldg(&in.ix[i]) + (Vn - Vs) * __ldg(&in.iy[j]);
             const double b = d / in.dt;
             in.b[id] = b;
-            acc[0] = b * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
+            if (in.singular) acc[0] = b * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
             if (!to_final) {
                 const double po = in.p[id], p2 = in.pold[id];
                 const int m = S[t.inst].pold_n;
@@ -764,9 +801,11 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
             in.b[id] = 0.0;
         }
     }
+    // the area-weighted source serves the mean removal of a singular operator only
     __shared__ double out[1];
-    block_sum<1>(acc, out);
-    if (threadIdx.x == 0) part[(size_t)vb * NPART] = out[0];
+    if (in.singular) block_sum<1>(acc, out);
+    else __syncthreads();  // the block's next tile rewrites the face arrays
+    if (threadIdx.x == 0) part[(size_t)vb * NPART] = in.singular ? out[0] : 0.0;
 }
 
 __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
@@ -831,7 +870,7 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
     int i, j, id;
     uint8_t bt;
     tile_ij(t, i, j);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    T acc[4] = {(T)0, (T)0, (T)0, (T)0};
     if (live0(L, i, j, id, bt)) {
         double Lp, D;
         lap<double, double, true>(L, in.p, i, j, id, bt, G, in.gidx, Lp, D);
@@ -842,10 +881,10 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
         ((T*)in.krh)[id] = rt;
         ((T*)in.kp)[id] = (T)0;
         ((T*)in.kv)[id] = (T)0;
-        acc[0] = r * r;
-        acc[1] = bb * bb;
-        acc[2] = (double)rt * (double)rt;
-        acc[3] = in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j]));
+        acc[0] = (T)(r * r);
+        acc[1] = (T)(bb * bb);
+        acc[2] = rt * rt;
+        if (in.singular) acc[3] = (T)(in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j])));
     }
     __shared__ double out[4];
     block_sum<4, T>(acc, out);
@@ -953,16 +992,14 @@ __device__ __forceinline__ void b_bicg_dir_smooth(const Tile* __restrict__ tiles
     const T* src = (const T*)L.e;
     T* dst = (T*)L.e2;
     const T om = (T)in.omega;
+    // the instance's scalars, converted once per thread
+    const T c1 = which == 0 ? (T)st.beta : (T)st.alpha, omg = which == 0 ? (T)st.omega : (T)0;
     T val[R], e1[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int id = q.id[r];
-        if (which == 0) {
-            const T beta = (T)st.beta, omg = (T)st.omega;
-            val[r] = kr[id] + beta * (((const T*)in.kp)[id] - omg * kv[id]);
-        } else {
-            val[r] = kr[id] - (T)st.alpha * kv[id];
-        }
+        if (which == 0) val[r] = kr[id] + c1 * (((const T*)in.kp)[id] - omg * kv[id]);
+        else val[r] = kr[id] - c1 * kv[id];
         T Le, D;
         lap_p<T, T, true>(L, src, q.ic, q.jc[r], id, L.pitch, q.bt[r], G, in.gidx, Le, D);
         e1[r] = jacobi_from_zero<T>(val[r], D, om);
@@ -993,21 +1030,21 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
     const T* w2 = (const T*)(which == 0 ? in.krh : in.ks);
     Rows0<R> q;
     rows0<R>(L, t, q);
-    double acc[R][2];
+    T acc[R][2];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         T Lz, D;
         lap_p<T, T, true>(L, z, q.ic, q.jc[r], q.id[r], L.pitch, q.bt[r], G, in.gidx, Lz, D);
         const T zc = z[q.id[r]], wv = w2[q.id[r]];
-        acc[r][0] = acc[r][1] = 0.0;
+        acc[r][0] = acc[r][1] = (T)0;
         if (q.bt[r] & 0x0F) {
             zo[q.id[r]] = zc;
             y[q.id[r]] = Lz;
             if (which == 0) {
-                acc[r][0] = (double)wv * (double)Lz;
+                acc[r][0] = wv * Lz;
             } else {
-                acc[r][0] = (double)Lz * (double)wv;
-                acc[r][1] = (double)Lz * (double)Lz;
+                acc[r][0] = Lz * wv;
+                acc[r][1] = Lz * Lz;
             }
         }
     }
@@ -1065,22 +1102,23 @@ __device__ __forceinline__ void b_bicg_x(const Tile* __restrict__ tiles, const L
     Rows0<R> q;
     rows0<R>(L, t, q);
     const double alpha = st.alpha, omega = st.omega;
+    const T omf = (T)omega;
     const double dxi = __ldg(&in.dx[q.ic]);
-    double acc[R][4];
+    const bool sing = in.singular;  // the area-weighted sum of p serves the nullspace projection only
+    T acc[R][4];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int id = q.id[r];
         const double pn = in.p[id] + alpha * (double)((const T*)in.kph)[id] + omega * (double)((const T*)in.ksh)[id];
-        const T rv = ((const T*)in.ks)[id] - (T)omega * ((const T*)in.kt)[id];
+        const T rv = ((const T*)in.ks)[id] - omf * ((const T*)in.kt)[id];
         const T rh = ((const T*)in.krh)[id];
-        const double dyj = __ldg(&in.dy[q.jc[r]]);
-        acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = 0.0;
+        acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = (T)0;
         if (q.bt[r] & 0x0F) {
             in.p[id] = pn;
             ((T*)in.kr)[id] = rv;
-            acc[r][0] = (double)rv * (double)rv;
-            acc[r][2] = (double)rh * (double)rv;
-            acc[r][3] = pn * (dxi * dyj);
+            acc[r][0] = rv * rv;
+            acc[r][2] = rh * rv;
+            if (sing) acc[r][3] = (T)(pn * (dxi * __ldg(&in.dy[q.jc[r]])));
         }
     }
     write_sub_partials<4, T, R>(in, L, t, acc, part);
@@ -1839,53 +1877,117 @@ __device__ __forceinline__ double corr_v(const InstDev& in, int j, int id) {
     return in.Vs[id] - in.dt * __ldg(&in.ky[j]) * (in.p[id + P] - in.p[id]);
 }
 
+// Largest |d| of a block (thread 0), with NaN counted as 0 like fmax: the
+// absolute values are compared as 64-bit integers, which order non-negative
+// doubles as their values do, with no FP64 operation.
+__device__ __forceinline__ double block_max_abs(double d) {
+    __shared__ unsigned long long sh[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    unsigned long long v = (unsigned long long)__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFull;
+    if (v > 0x7FF0000000000000ull) v = 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+        v = x > v ? x : v;
+    }
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    unsigned long long m = 0ull;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nw; q++) m = sh[q] > m ? sh[q] : m;
+    __syncthreads();
+    return __longlong_as_double((long long)m);
+}
+
 // Projection of cell and face velocities; divergence and boundary fluxes.
+// Every face value is formed once: thread (w, lane) forms the east face U
+// and the north face V of its cell and the interpolated pressures there;
+// warp 0 forms the south faces of the tile's first row, warp 1 the west faces
+// of its first column; the cells take their west and south values from
+// shared memory.  The operands and operations of each value are those of the
+// cell-by-cell form, so the results are the same.
 __device__ __forceinline__ void b_correct(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                           double* __restrict__ part, int vb) {
     const Tile t = ldg_struct(&tiles[vb]);
     const InstDev& in = I[t.inst];
     if (in.retired) return;
+    TileFaces& F = tile_faces();
+    auto& sU = F.x[0];   // U and the interpolated pressure on the x faces
+    auto& sPe = F.x[1];
+    auto& sV = F.y[0];   // V and the interpolated pressure on the y faces
+    auto& sPn = F.y[1];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     int i, j;
     tile_ij(t, i, j);
-    const int P = in.pitch, id = i + j * P;
-    double dmax = 0.0, fl[2] = {0.0, 0.0};
-    if (i <= in.nx - 2 && j >= 1 && j <= in.NY) {
-        const double Un = corr_u(in, i, id);
-        in.U[id] = Un;
-        if (i == 0) fl[0] += Un * __ldg(&in.dy[j]);
-        if (i == in.nx - 2) fl[1] += Un * __ldg(&in.dy[j]);
+    const int P = in.pitch, id = i + j * P, NX = in.NX, NY = in.NY;
+    const double* p = in.p;
+    const bool row = j >= 1 && j <= NY, col = i >= 1 && i <= NX;
+    double fl[2] = {0.0, 0.0};
+    {
+        double Un = 0.0, pe = 0.0;
+        if (row && i <= NX) {
+            Un = corr_u(in, i, id);
+            in.U[id] = Un;
+            if (i == 0) fl[0] += Un * __ldg(&in.dy[j]);
+            if (i == NX) fl[1] += Un * __ldg(&in.dy[j]);
+            pe = p[id] * __ldg(&in.gx[i]) + p[id + 1] * __ldg(&in.fx[i]);
+        }
+        sU[w][l + 1] = Un;
+        sPe[w][l + 1] = pe;
     }
-    if (j <= in.ny - 2 && i >= 1 && i <= in.NX) {
-        const double Vn = corr_v(in, j, id);
-        in.V[id] = Vn;
-        if (j == 0) fl[0] += Vn * __ldg(&in.dx[i]);
-        if (j == in.ny - 2) fl[1] += Vn * __ldg(&in.dx[i]);
+    {
+        double Vn = 0.0, pn = 0.0;
+        if (col && j <= NY) {
+            Vn = corr_v(in, j, id);
+            in.V[id] = Vn;
+            if (j == 0) fl[0] += Vn * __ldg(&in.dx[i]);
+            if (j == NY) fl[1] += Vn * __ldg(&in.dx[i]);
+            pn = p[id] * __ldg(&in.gy[j]) + p[id + P] * __ldg(&in.fy[j]);
+        }
+        sV[w + 1][l] = Vn;
+        sPn[w + 1][l] = pn;
     }
-    if (i >= 1 && i <= in.NX && j >= 1 && j <= in.NY) {
+    if (w == 0) {  // south faces of the first row
+        const int js = t.j0 - 1, ids = i + js * P;
+        double Vs = 0.0, ps = 0.0;
+        if (js >= 0 && col) {
+            Vs = corr_v(in, js, ids);
+            ps = p[ids] * __ldg(&in.gy[js]) + p[ids + P] * __ldg(&in.fy[js]);
+        }
+        sV[0][l] = Vs;
+        sPn[0][l] = ps;
+    } else if (w == 1 && l < TILE_Y) {  // west faces of the first column
+        const int iw = t.i0 - 1, jw = t.j0 + l, idw = iw + jw * P;
+        double Uw = 0.0, pw = 0.0;
+        if (iw >= 0 && jw >= 1 && jw <= NY) {
+            Uw = corr_u(in, iw, idw);
+            pw = p[idw] * __ldg(&in.gx[iw]) + p[idw + 1] * __ldg(&in.fx[iw]);
+        }
+        sU[l][0] = Uw;
+        sPe[l][0] = pw;
+    }
+    __syncthreads();
+    double d = 0.0;
+    if (row && col) {
         if (__ldg(&in.type[id]) == T_FLUID) {
-            const double* p = in.p;
             const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
-            const double pe = p[id] * __ldg(&in.gx[i]) + p[id + 1] * __ldg(&in.fx[i]);
-            const double pw = p[id - 1] * __ldg(&in.gx[i - 1]) + p[id] * __ldg(&in.fx[i - 1]);
-            const double pn = p[id] * __ldg(&in.gy[j]) + p[id + P] * __ldg(&in.fy[j]);
-            const double ps = p[id - P] * __ldg(&in.gy[j - 1]) + p[id] * __ldg(&in.fy[j - 1]);
-            in.u[id] -= in.dt * (pe - pw) * ixi;
-            in.v[id] -= in.dt * (pn - ps) * iyj;
-            const double d = (corr_u(in, i, id) - corr_u(in, i - 1, id - 1)) * ixi +
-                             (corr_v(in, j, id) - corr_v(in, j - 1, id - P)) * iyj;
+            in.u[id] -= in.dt * (sPe[w][l + 1] - sPe[w][l]) * ixi;
+            in.v[id] -= in.dt * (sPn[w + 1][l] - sPn[w][l]) * iyj;
+            d = (sU[w][l + 1] - sU[w][l]) * ixi + (sV[w + 1][l] - sV[w][l]) * iyj;
             in.div[id] = d;
-            dmax = fabs(d);
         } else {
             in.div[id] = 0.0;
         }
     }
-    const double m = block_max(dmax);
+    const double m = block_max_abs(d);
+    // boundary mass fluxes: tiles that hold a boundary face only
+    const bool edge = t.i0 == 0 || t.i0 + TILE_X > NX || t.j0 == 0 || t.j0 + TILE_Y > NY;
     __shared__ double out[2];
-    block_sum<2>(fl, out);
+    if (edge) block_sum<2>(fl, out);
     if (threadIdx.x == 0) {
         part[(size_t)vb * NPART] = m;
-        part[(size_t)vb * NPART + 1] = out[0];
-        part[(size_t)vb * NPART + 2] = out[1];
+        part[(size_t)vb * NPART + 1] = edge ? out[0] : 0.0;
+        part[(size_t)vb * NPART + 2] = edge ? out[1] : 0.0;
     }
 }
 
