@@ -248,6 +248,10 @@ struct alignas(16) InstDev {
     double *pold, *pold2;        // pressures of the two steps before (initial-guess extrapolation)
     const double *dx, *dy, *fx, *gx, *fy, *gy, *xc, *yc, *xf, *yf;
     const double *kx, *ky, *ix, *iy;   // finest-level face coefficients and 1/width
+    // implicit predictor coefficients: column i (a_E, a_W) = dt/Re (kx[i] ix[i],
+    // kx[i-1] ix[i]) with pcs[i] = (1 + a_E) + a_W, row j (a_N, a_S) likewise
+    const double2 *pax, *pay;
+    const double* pcs;
     const uint8_t* type;
     const int* gidx;             // cell -> global ghost index (IBM ghosts), -1 otherwise
     double *qbu, *qbv;

@@ -94,20 +94,36 @@ __device__ __forceinline__ void tile_ij(const Tile& t, int& i, int& j) {
 // FP32 partials in FP32.
 template <int NV, typename RT = double, typename VT>
 __device__ __forceinline__ void block_sum(VT (&v)[NV], double* out) {
-    __shared__ double sh[NV][32];
+    __shared__ RT sh[NV][32];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
         RT x = (RT)v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (l == 0) sh[k][w] = (double)x;
+        if (l == 0) sh[k][w] = x;
     }
     __syncthreads();
-    if (threadIdx.x < NV) {
-        double s = 0.0;
-        for (int q = 0; q < nw; q++) s += sh[threadIdx.x][q];
-        out[threadIdx.x] = s;
+    if constexpr (sizeof(RT) == sizeof(double)) {
+        if (threadIdx.x < NV) {
+            double s = 0.0;
+            for (int q = 0; q < nw; q++) s += sh[threadIdx.x][q];
+            out[threadIdx.x] = s;
+        }
+    } else {
+        // FP32 warp sums: warp 0 widens all of them at once (one conversion
+        // per lane instead of one per warp and value), then sums them in FP64
+        // in the same order
+        __shared__ double shd[NV][32];
+        if (w == 0) {
+            for (int q = l; q < NV * nw; q += 32) shd[q / nw][q % nw] = (double)sh[q / nw][q % nw];
+            __syncwarp();
+            if (l < NV) {
+                double s = 0.0;
+                for (int q = 0; q < nw; q++) s += shd[l][q];
+                out[l] = s;
+            }
+        }
     }
     __syncthreads();
 }
@@ -476,10 +492,9 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
         }
         double m[1] = {0.0};
         if (fl) {
-            const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
-            const double aE = in.dtre * (__ldg(&in.kx[i]) * ixi), aW = in.dtre * (__ldg(&in.kx[i - 1]) * ixi);
-            const double aN = in.dtre * (__ldg(&in.ky[j]) * iyj), aS = in.dtre * (__ldg(&in.ky[j - 1]) * iyj);
-            const double aP = 1.0 + aE + aW + aN + aS;
+            const double2 ax = __ldg(&in.pax[i]), ay = __ldg(&in.pay[j]);
+            const double aE = ax.x, aW = ax.y, aN = ay.x, aS = ay.y;
+            const double aP = (__ldg(&in.pcs[i]) + aN) + aS;  // 1 + aE + aW + aN + aS, in that order
             const double di = rcpa(aP);
             const double dU = (in.ru[id] + aE * su[id + 1] + aW * su[id - 1] + aN * su[id + P] + aS * su[id - P] -
                                aP * su[id]) * di;
@@ -574,10 +589,9 @@ __device__ __forceinline__ void pred_refresh_cell(const InstDev& in, int cell, c
     const double* v = in.v;
     if (!gh) {
         const int P = in.pitch, id = cell, j = cell / P, i = cell - j * P;
-        const double ixi = __ldg(&in.ix[i]), iyj = __ldg(&in.iy[j]);
-        const double aE = in.dtre * (__ldg(&in.kx[i]) * ixi), aW = in.dtre * (__ldg(&in.kx[i - 1]) * ixi);
-        const double aN = in.dtre * (__ldg(&in.ky[j]) * iyj), aS = in.dtre * (__ldg(&in.ky[j - 1]) * iyj);
-        const double aP = 1.0 + aE + aW + aN + aS;
+        const double2 ax = __ldg(&in.pax[i]), ay = __ldg(&in.pay[j]);
+        const double aE = ax.x, aW = ax.y, aN = ay.x, aS = ay.y;
+        const double aP = (__ldg(&in.pcs[i]) + aN) + aS;  // 1 + aE + aW + aN + aS, in that order
         in.rfu[id] = (float)(in.ru[id] + aE * u[id + 1] + aW * u[id - 1] + aN * u[id + P] + aS * u[id - P] - aP * u[id]);
         in.rfv[id] = (float)(in.rv[id] + aE * v[id + 1] + aW * v[id - 1] + aN * v[id + P] + aS * v[id - P] - aP * v[id]);
     } else {
@@ -882,7 +896,7 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
         ((T*)in.kp)[id] = (T)0;
         ((T*)in.kv)[id] = (T)0;
         acc[0] = (T)(r * r);
-        acc[1] = (T)(bb * bb);
+        if (!restart_only) acc[1] = (T)(bb * bb);  // ||b||: the initial residual only
         acc[2] = rt * rt;
         if (in.singular) acc[3] = (T)(in.p[id] * (__ldg(&in.dx[i]) * __ldg(&in.dy[j])));
     }

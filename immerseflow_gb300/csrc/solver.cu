@@ -1040,6 +1040,27 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         d.ibm_cap = I.ibm_cap;
         d.sub_lb = (lb >= 1 && lb < nl) ? lb : 0;
         d.kx = I.lev[0].d_kx; d.ky = I.lev[0].d_ky; d.ix = I.lev[0].d_ix; d.iy = I.lev[0].d_iy;
+        {   // the implicit predictor's coefficients, each formed as the kernels formed it per cell
+            const HostLevel& L0 = I.lev[0];
+            const double dtre = d.dtre;
+            std::vector<double2> ax(L0.kx.size()), ay(L0.ky.size());
+            std::vector<double> cs(L0.kx.size());
+            for (size_t i = 0; i < ax.size(); i++) {
+                ax[i].x = dtre * (L0.kx[i] * L0.ix[i]);
+                ax[i].y = i > 0 ? dtre * (L0.kx[i - 1] * L0.ix[i]) : 0.0;
+                cs[i] = (1.0 + ax[i].x) + ax[i].y;
+            }
+            for (size_t j = 0; j < ay.size(); j++) {
+                ay[j].x = dtre * (L0.ky[j] * L0.iy[j]);
+                ay[j].y = j > 0 ? dtre * (L0.ky[j - 1] * L0.iy[j]) : 0.0;
+            }
+            double2 *ax_d = nullptr, *ay_d = nullptr;
+            double* cs_d = nullptr;
+            IFX_TRY(dupload(S, &ax_d, ax));
+            IFX_TRY(dupload(S, &ay_d, ay));
+            IFX_TRY(dupload(S, &cs_d, cs));
+            d.pax = ax_d; d.pay = ay_d; d.pcs = cs_d;
+        }
         hI[k] = d;
     }
     IFX_TRY(dupload(S, &S->dLV, hLV));
