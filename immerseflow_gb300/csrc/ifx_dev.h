@@ -32,6 +32,9 @@ constexpr double COARSE_OMEGA = 1.5;  // RB-SOR factor on the coarsest level
 // host-loop modes (the persistent kernel runs them with its own blocks).
 constexpr int SUB_THREADS = 512;
 constexpr int SUB_MAX_CELLS = 2048;  // coarse levels up to this size run in one block per instance
+// ... in the plain FP64 path: one SM issues 2 FP64 FMA per clock, so a sweep of
+// a 1536-cell level in one block takes ~12 us against ~5 us as a tile phase
+constexpr int SUB_MAX_CELLS_FP64 = 512;
 constexpr int SUB_SMEM_MAX = 96 * 1024;  // shared memory for those levels (fields, metrics, tables)
 constexpr int kSubLevels = 16;           // at most this many levels per instance
 constexpr int SUB_COARSE_PER_THREAD = 4;  // coarsest-level cells per thread in the RB-SOR solve
@@ -271,6 +274,13 @@ struct alignas(16) InstDev {
     // staged by one contiguous copy; sub_img_bytes is a multiple of 16
     const unsigned char* sub_img;
     int sub_img_bytes;
+    // the first small level: its global correction buffers and right-hand
+    // side (read by the sub-cycle, the correction written back), their row
+    // pitch, the byte offsets of its e and r in the image, its size (ghost
+    // ring included) and whether it has a coarser level
+    void *sub_ge, *sub_ge2;
+    const void* sub_gr;
+    int sub_gpitch, sub_oe, sub_or, sub_nx, sub_ny, sub_child;
     int hist_cap, hist_w, nprobe;
     // prescribed body motion: the pose at t = nstep dt follows from these
     // (centre x0 + u t + ax (sin(2 pi (f t + phx)) - sin(2 pi phx)), likewise y

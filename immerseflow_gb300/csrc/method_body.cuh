@@ -1779,6 +1779,46 @@ __device__ __forceinline__ void sub_stage_geometry(const int* __restrict__ sub, 
     __syncthreads();
 }
 
+// Asynchronous global -> shared copies (cp.async) of 4, 8 or 16 bytes, and
+// the wait for all of this thread's.
+template <int N>
+__device__ __forceinline__ void cp_async(unsigned dst, const void* src) {
+    static_assert(N == 4 || N == 8 || N == 16, "cp.async size");
+    if constexpr (N == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+    else if constexpr (N == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Stages instance `in`'s small levels for one V-cycle in one round of
+// asynchronous copies: the image (headers, geometry, zero fields) except the
+// first level's e and r, which come from that level's global buffers (e: the
+// zero-start sweep of the tile phase; when the first level is the coarsest,
+// the image's zero e is kept).  The same shared-memory contents as staging
+// the image and then loading e and r, without the round trip in between.
+template <typename T>
+__device__ __forceinline__ void sub_stage_all(const InstDev& in, unsigned char* sm) {
+    const unsigned char* img = in.sub_img;
+    const T* ge = (const T*)in.sub_ge;
+    const T* gr = (const T*)in.sub_gr;
+    const int n16 = in.sub_img_bytes >> 4, nx = in.sub_nx, n = nx * in.sub_ny, gp = in.sub_gpitch;
+    const int oe = in.sub_oe, orr = in.sub_or, span = (int)sub_al16((size_t)n * sizeof(T));
+    const bool load_e = in.sub_child >= 0;
+    const unsigned sb = (unsigned)__cvta_generic_to_shared(sm);
+    for (int q = threadIdx.x; q < n16; q += blockDim.x) {
+        const int b = q << 4;
+        if ((load_e && b >= oe && b < oe + span) || (b >= orr && b < orr + span)) continue;
+        cp_async<16>(sb + b, img + b);
+    }
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int g = q + (q / nx) * (gp - nx);
+        if (load_e) cp_async<(int)sizeof(T)>(sb + oe + q * (int)sizeof(T), ge + g);
+        cp_async<(int)sizeof(T)>(sb + orr + q * (int)sizeof(T), gr + g);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+}
+
 // Small coarse levels of one instance (vb = instance) in one block, from the
 // first small level (restricted by the tile phase before) down to the RB-SOR
 // solve and back up; the first small level's correction is written back to
@@ -1789,22 +1829,25 @@ template <typename T>
 __device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
                                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                            int pre, int post, unsigned char* sm, bool geometry_staged, int vb) {
+    (void)sub;
+    (void)LV;
     const int k = vb;
     if (S[k].ppe_state != ST_ACTIVE) return;
-    if (!geometry_staged) sub_stage_geometry<T>(sub, LV, I, k, sm);
+    const InstDev& in = I[k];
     const SubHdr* hdr = (const SubHdr*)sm;
-    const int ns = hdr[0].ns;
-    const T om = (T)I[k].omega;
-    const LevelDev& L0 = LV[sub[k]];
-    {
+    if (!geometry_staged) {
+        sub_stage_all<T>(in, sm);
+    } else {
+        // geometry resident from an earlier V-cycle: the first level's e and
+        // r from global memory, every other field zeroed
         const SubGeo<T> g = sub_geo<T>(sm, hdr[0]);
         const int n = g.nx * g.ny;
-        if (g.child >= 0) sub_load_rows<T>(g.e, (const T*)L0.e, g.nx, n, L0.pitch);  // zero-start sweep of the tile phase
+        if (g.child >= 0) sub_load_rows<T>(g.e, (const T*)in.sub_ge, g.nx, n, in.sub_gpitch);  // zero-start sweep of the tile phase
         else
             for (int q = threadIdx.x; q < n; q += blockDim.x) g.e[q] = (T)0;
-        sub_load_rows<T>(g.r, (const T*)L0.r, g.nx, n, L0.pitch);
+        sub_load_rows<T>(g.r, (const T*)in.sub_gr, g.nx, n, in.sub_gpitch);
         for (int q = threadIdx.x; q < n; q += blockDim.x) g.e2[q] = (T)0;
-        for (int s = 1; s < ns; s++) {
+        for (int s = 1; s < hdr[0].ns; s++) {
             const SubGeo<T> c = sub_geo<T>(sm, hdr[s]);
             const int m = c.nx * c.ny;
             for (int q = threadIdx.x; q < m; q += blockDim.x) {
@@ -1812,8 +1855,10 @@ __device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const Le
                 c.e2[q] = (T)0;
             }
         }
+        __syncthreads();
     }
-    __syncthreads();
+    const int ns = hdr[0].ns;
+    const T om = (T)in.omega;
     // descend
     for (int s = 0; s < ns; s++) {
         const SubGeo<T> g = sub_geo<T>(sm, hdr[s]);
@@ -1823,7 +1868,7 @@ __device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const Le
             __syncthreads();
         }
         if (g.child < 0) {
-            sub_coarse_solve<T>(g, I[k].coarse_sweeps);
+            sub_coarse_solve<T>(g, in.coarse_sweeps);
             break;
         }
         int cur = 0;
@@ -1850,11 +1895,11 @@ __device__ __forceinline__ void b_subcycle(const int* __restrict__ sub, const Le
     const SubGeo<T> g = sub_geo<T>(sm, hdr[0]);
     const int res = (g.child < 0) ? 0 : parity_after_post(g.depth, pre, post);
     const T* src = res ? g.e2 : g.e;
-    T* dst = (T*)(res ? L0.e2 : L0.e);
-    const int n = g.nx * g.ny;
+    T* dst = (T*)(res ? in.sub_ge2 : in.sub_ge);
+    const int n = g.nx * g.ny, gp = in.sub_gpitch;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int j = q / g.nx;
-        dst[q + j * (L0.pitch - g.nx)] = src[q];
+        dst[q + j * (gp - g.nx)] = src[q];
     }
     __syncthreads();  // the block may stage another instance in the same memory
 }

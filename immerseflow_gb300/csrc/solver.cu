@@ -909,9 +909,10 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         d.gidx = gidx_d;
         const int nl = (int)I.lev.size();
         // first level handled inside one block per instance (>= 1, <= coarsest): at
-        // most SUB_MAX_CELLS cells, and it and every coarser level staged in
-        // shared memory within SUB_SMEM_MAX bytes
+        // most SUB_MAX_CELLS (FP64: SUB_MAX_CELLS_FP64) cells, and it and every
+        // coarser level staged in shared memory within SUB_SMEM_MAX bytes
         const int tsz = S->prec == IFX_PREC_FP64 ? 8 : 4;
+        const long long sub_max = S->prec == IFX_PREC_FP64 ? SUB_MAX_CELLS_FP64 : SUB_MAX_CELLS;
         auto staged = [&](int from) {
             size_t b = SUB_HDR_BYTES;
             for (int l = from; l < nl; l++) b += sub_level_bytes(I.lev[l].nx, I.lev[l].ny, tsz);
@@ -919,7 +920,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         };
         int lb = nl - 1;
         for (int l = 1; l < nl; l++)
-            if ((long long)I.lev[l].NX * I.lev[l].NY <= SUB_MAX_CELLS && staged(l) <= (size_t)SUB_SMEM_MAX) {
+            if ((long long)I.lev[l].NX * I.lev[l].NY <= sub_max && staged(l) <= (size_t)SUB_SMEM_MAX) {
                 lb = l;
                 break;
             }
@@ -1123,8 +1124,24 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dupload(S, &d_img, all));
         for (int k = 0; k < n; k++) {
             hI[k].sub_img = d_img + at[k];
-            S->inst[k].dev.sub_img = hI[k].sub_img;
-            S->inst[k].dev.sub_img_bytes = hI[k].sub_img_bytes;
+            const LevelDev& L = hLV[hSub[k]];  // the first small level
+            SubHdr h0;
+            std::memcpy(&h0, all.data() + at[k], sizeof(h0));
+            hI[k].sub_ge = L.e;
+            hI[k].sub_ge2 = L.e2;
+            hI[k].sub_gr = L.r;
+            hI[k].sub_gpitch = L.pitch;
+            hI[k].sub_oe = (int)(h0.base + h0.o.e);
+            hI[k].sub_or = (int)(h0.base + h0.o.r);
+            hI[k].sub_nx = h0.nx;
+            hI[k].sub_ny = h0.ny;
+            hI[k].sub_child = h0.child;
+            InstDev& dv = S->inst[k].dev;
+            dv.sub_img = hI[k].sub_img;
+            dv.sub_img_bytes = hI[k].sub_img_bytes;
+            dv.sub_ge = L.e; dv.sub_ge2 = L.e2; dv.sub_gr = L.r; dv.sub_gpitch = L.pitch;
+            dv.sub_oe = hI[k].sub_oe; dv.sub_or = hI[k].sub_or;
+            dv.sub_nx = h0.nx; dv.sub_ny = h0.ny; dv.sub_child = h0.child;
         }
     }
     if (S->prec == IFX_PREC_FP64) CUDA_TRY(subcycle_smem_limit<double>(S->sub_bytes));
