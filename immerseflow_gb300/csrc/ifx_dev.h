@@ -58,12 +58,13 @@ IFX_HD inline int parity_after_pre(int depth, int pre) { return depth == 0 ? (pr
 IFX_HD inline int parity_after_post(int depth, int pre, int post) { return (parity_after_pre(depth, pre) + post) & 1; }
 
 // Shared-memory layout (byte offsets) of one small multigrid level staged for
-// the sub-cycle: fields e, e2, r (n = nx*ny cells of tsize bytes), the 1-D
-// metric arrays kx ix dw (nx) and ky iy dh (ny), the prolongation tables from
-// the next coarser level (pwx pI pIn psx: nx; pwy pJ pJn psy: ny) and the
-// stencil bytes; every array starts on a 16-byte boundary.
+// the sub-cycle: fields e, e2, r (n = nx*ny cells of tsize bytes), the face
+// coefficient pairs cew = (kx[i] ix[i], kx[i-1] ix[i]) and the widths dw (nx),
+// cns and dh (ny), the prolongation tables from the next coarser level (pwx
+// pI pIn psx: nx; pwy pJ pJn psy: ny) and the stencil bytes; every array
+// starts on a 16-byte boundary.
 struct SubLayout {
-    size_t e, e2, r, kx, ix, dw, pwx, ky, iy, dh, pwy, pI, pIn, pJ, pJn, b, psx, psy, bytes;
+    size_t e, e2, r, cew, dw, pwx, cns, dh, pwy, pI, pIn, pJ, pJn, b, psx, psy, bytes;
 };
 IFX_HD inline size_t sub_al16(size_t x) { return (x + 15) & ~(size_t)15; }
 IFX_HD inline SubLayout sub_layout(int nx, int ny, int tsize) {
@@ -73,12 +74,10 @@ IFX_HD inline SubLayout sub_layout(int nx, int ny, int tsize) {
     L.e = o;   o += sub_al16(n * ts);
     L.e2 = o;  o += sub_al16(n * ts);
     L.r = o;   o += sub_al16(n * ts);
-    L.kx = o;  o += sub_al16(X * ts);
-    L.ix = o;  o += sub_al16(X * ts);
+    L.cew = o; o += sub_al16(X * 2 * ts);
     L.dw = o;  o += sub_al16(X * ts);
     L.pwx = o; o += sub_al16(X * ts);
-    L.ky = o;  o += sub_al16(Y * ts);
-    L.iy = o;  o += sub_al16(Y * ts);
+    L.cns = o; o += sub_al16(Y * 2 * ts);
     L.dh = o;  o += sub_al16(Y * ts);
     L.pwy = o; o += sub_al16(Y * ts);
     L.pI = o;  o += sub_al16(X * 4);

@@ -1500,9 +1500,15 @@ __device__ __forceinline__ void b_prolong_sweep(const Tile* __restrict__ tiles, 
 // View of a staged level; the pointers are formed from the dynamic shared
 // memory base and the offsets of its SubHdr, so accesses compile to
 // shared-memory loads and stores.
+template <typename T> struct SubPair;
+template <> struct SubPair<float> { using type = float2; };
+template <> struct SubPair<double> { using type = double2; };
+
 template <typename T>
 struct SubGeo {
-    T *e, *e2, *r, *kx, *ix, *dw, *pwx, *ky, *iy, *dh, *pwy;
+    using T2 = typename SubPair<T>::type;
+    T *e, *e2, *r, *dw, *pwx, *dh, *pwy;
+    T2 *cew, *cns;
     int *pI, *pIn, *pJ, *pJn;
     uint8_t* b;
     signed char *psx, *psy;
@@ -1515,8 +1521,8 @@ __device__ __forceinline__ SubGeo<T> sub_geo(unsigned char* sm, const SubHdr& h)
     const SubLayout& o = h.o;
     SubGeo<T> g;
     g.e = (T*)(p + o.e); g.e2 = (T*)(p + o.e2); g.r = (T*)(p + o.r);
-    g.kx = (T*)(p + o.kx); g.ix = (T*)(p + o.ix); g.dw = (T*)(p + o.dw); g.pwx = (T*)(p + o.pwx);
-    g.ky = (T*)(p + o.ky); g.iy = (T*)(p + o.iy); g.dh = (T*)(p + o.dh); g.pwy = (T*)(p + o.pwy);
+    g.cew = (typename SubGeo<T>::T2*)(p + o.cew); g.dw = (T*)(p + o.dw); g.pwx = (T*)(p + o.pwx);
+    g.cns = (typename SubGeo<T>::T2*)(p + o.cns); g.dh = (T*)(p + o.dh); g.pwy = (T*)(p + o.pwy);
     g.pI = (int*)(p + o.pI); g.pIn = (int*)(p + o.pIn); g.pJ = (int*)(p + o.pJ); g.pJn = (int*)(p + o.pJn);
     g.b = p + o.b;
     g.psx = (signed char*)(p + o.psx); g.psy = (signed char*)(p + o.psy);
@@ -1555,9 +1561,8 @@ __device__ __forceinline__ void sub_load_ro(U* dst, const U* src, int n) {
 
 template <typename T>
 __device__ __forceinline__ LapCoef<T> sub_coef(const SubGeo<T>& g, int i, int j, uint8_t bt) {
-    const T ixi = g.ix[i], iyj = g.iy[j];
-    const T cE = g.kx[i] * ixi, cW = g.kx[i - 1] * ixi;
-    const T cN = g.ky[j] * iyj, cS = g.ky[j - 1] * iyj;
+    const auto ew = g.cew[i], ns = g.cns[j];
+    const T cE = ew.x, cW = ew.y, cN = ns.x, cS = ns.y;
     LapCoef<T> c;
     c.ce = (bt & B_E) ? cE : (T)0;
     c.cw = (bt & B_W) ? cW : (T)0;

@@ -104,8 +104,17 @@ std::vector<unsigned char> sub_image(const Instance& I, int lb) {
             signed char* d = (signed char*)(b + o);
             for (int q = 0; q < n && q < (int)v.size(); q++) d[q] = v[q];
         };
-        put_t(h.o.kx, L.kx, L.nx); put_t(h.o.ix, L.ix, L.nx); put_t(h.o.dw, L.dw, L.nx);
-        put_t(h.o.ky, L.ky, L.ny); put_t(h.o.iy, L.iy, L.ny); put_t(h.o.dh, L.dh, L.ny);
+        // face coefficient pairs: the products of the T copies, as the tile phases form them
+        auto put_pairs = [&](size_t o, const std::vector<double>& k, const std::vector<double>& inv, int n) {
+            T* d = (T*)(b + o);
+            for (int q = 0; q < n && q < (int)k.size(); q++) {
+                const T iq = (T)inv[q];
+                d[2 * q] = (T)k[q] * iq;
+                d[2 * q + 1] = q > 0 ? (T)k[q - 1] * iq : (T)0;
+            }
+        };
+        put_pairs(h.o.cew, L.kx, L.ix, L.nx); put_t(h.o.dw, L.dw, L.nx);
+        put_pairs(h.o.cns, L.ky, L.iy, L.ny); put_t(h.o.dh, L.dh, L.ny);
         if (h.child >= 0) {
             put_t(h.o.pwx, L.pwx, L.nx); put_t(h.o.pwy, L.pwy, L.ny);
             put_i(h.o.pI, L.pI, L.nx); put_i(h.o.pIn, L.pIn, L.nx);
