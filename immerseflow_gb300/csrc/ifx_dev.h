@@ -248,6 +248,7 @@ struct alignas(16) InstDev {
     double area;                 // sum of fluid-cell areas
     double *u, *v, *u2, *v2, *Us, *Vs, *U, *V, *Nu, *Nv, *ru, *rv, *p, *b, *div, *iblank;
     double *pold, *pold2;        // pressures of the two steps before (initial-guess extrapolation)
+    double *dup, *dvp;           // predictor increment q* - q^n of the step before (initial guess)
     const double *dx, *dy, *fx, *gx, *fy, *gy, *xc, *yc, *xf, *yf;
     const double *kx, *ky, *ix, *iy;   // finest-level face coefficients and 1/width
     // implicit predictor coefficients: column i (a_E, a_W) = dt/Re (kx[i] ix[i],

@@ -13,6 +13,7 @@ cudaError_t launch_outflow(const GhostDev* G, int ng, const InstDev* I, cudaStre
 cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int comps, double* gval,
                               cudaStream_t s);
 cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
+cudaError_t launch_pred_guess(const Tile* t, int nt, const InstDev* I, cudaStream_t s);
 cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I,
                               const InstState* S, double* part, int parity, cudaStream_t s);
 // Mixed path: FP32 sweep on the correction, and the FP64 refresh (stage 0:

@@ -41,6 +41,10 @@ __global__ void k_ghost_scatter(const GhostDev* __restrict__ G, int ng, const In
                                 int comps, const double* __restrict__ gval) { b_ghost_scatter(G, ng, I, comps, gval, blockIdx.x); }
 __global__ void __launch_bounds__(TILE_THREADS, 8) k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S) { b_conv_rhs(tiles, I, S, blockIdx.x); }
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_pred_guess(const Tile* __restrict__ tiles,
+                                                                const InstDev* __restrict__ I) {
+    b_pred_guess(tiles, I, blockIdx.x);
+}
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<double>(1)) k_pred_sweep(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G,
                              int ng, const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              double* __restrict__ part, int parity) { b_pred_sweep(tiles, ntiles, G, ng, I, S, part, parity, blockIdx.x); }
@@ -214,6 +218,10 @@ cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int c
     k_ghost_gather<<<nblk(ng, 256), 256, 0, s>>>(G, ng, I, comps, gval);
     CK(cudaGetLastError());
     k_ghost_scatter<<<nblk(ng, 256), 256, 0, s>>>(G, ng, I, comps, gval);
+    return cudaGetLastError();
+}
+cudaError_t launch_pred_guess(const Tile* t, int nt, const InstDev* I, cudaStream_t s) {
+    k_pred_guess<<<nt, TILE_THREADS, 0, s>>>(t, I);
     return cudaGetLastError();
 }
 cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {

@@ -128,6 +128,8 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     if (!ghost_fill(P, 3, ep)) return false;
     FOR_VB(P.nt0) b_conv_rhs(P.t0, P.I, P.S, vb);
     BAR();
+    FOR_VB(P.nt0) b_pred_guess(P.t0, P.I, vb);
+    BAR();
     // predictor: pairs of Jacobi sweeps until every instance converged
     const int npred = P.nt0 + nchunks(P.ng);
     constexpr bool mixed32 = sizeof(T) == 4;

@@ -462,6 +462,28 @@ __device__ __forceinline__ void b_conv_rhs(const Tile* __restrict__ tiles, const
     in.Nv[id] = Nv;
 }
 
+// Initial guess of the predictor: q^n plus the step before's predictor
+// increment q* - q^n in the fluid cells (zero on an instance's first step and
+// in cells that were not fluid then); the increment buffers keep q^n until
+// b_face_rhs forms the new increment.  The predictor's first update then
+// starts O(dt^2) instead of O(dt) away: about 12 -> 9 Jacobi sweeps a step on
+// the cylinder.
+__device__ __forceinline__ void b_pred_guess(const Tile* __restrict__ tiles, const InstDev* __restrict__ I, int vb) {
+    const Tile t = ldg_struct(&tiles[vb]);
+    const InstDev& in = I[t.inst];
+    if (in.retired) return;
+    int i, j;
+    tile_ij(t, i, j);
+    if (i < 1 || i > in.NX || j < 1 || j > in.NY) return;
+    const int id = i + j * in.pitch;
+    if (__ldg(&in.type[id]) != T_FLUID) return;
+    const double un = in.u[id], vn = in.v[id];
+    in.u[id] = un + in.dup[id];
+    in.v[id] = vn + in.dvp[id];
+    in.dup[id] = un;
+    in.dvp[id] = vn;
+}
+
 // One Jacobi sweep of the predictor for u and v, fluid cells and every
 // ghost relation; parity 0 reads (u,v) and writes (u2,v2), parity 1 the
 // reverse.  An instance that converged on the parity-0 sweep copies its
@@ -810,9 +832,13 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
                 else if (m >= 3) in.p[id] = __dsub_rn(__dmul_rn(2.0, po), p2);
                 in.pold2[id] = p2;
                 in.pold[id] = po;
+                // the predictor increment for the next step's initial guess
+                in.dup[id] = in.u[id] - in.dup[id];
+                in.dvp[id] = in.v[id] - in.dvp[id];
             }
         } else {
             in.b[id] = 0.0;
+            if (!to_final) in.dup[id] = in.dvp[id] = 0.0;
         }
     }
     // the area-weighted source serves the mean removal of a singular operator only

@@ -832,6 +832,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         IFX_TRY(dalloc(S, &d.ru, nc)); IFX_TRY(dalloc(S, &d.rv, nc));
         IFX_TRY(dalloc(S, &d.p, nc)); IFX_TRY(dalloc(S, &d.b, nc));
         IFX_TRY(dalloc(S, &d.pold, nc)); IFX_TRY(dalloc(S, &d.pold2, nc));
+        IFX_TRY(dalloc(S, &d.dup, nc)); IFX_TRY(dalloc(S, &d.dvp, nc));
         IFX_TRY(dalloc(S, &d.div, nc)); IFX_TRY(dalloc(S, &d.iblank, nc));
         if (S->prec == IFX_PREC_MIXED)
             for (float** a : {&d.du, &d.dv, &d.du2, &d.dv2, &d.rfu, &d.rfv}) IFX_TRY(dalloc(S, a, nc));
@@ -1351,6 +1352,7 @@ void seq_pre(Seq& q) {
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;  // ghost fill is two kernels
     q.add(launch_conv_rhs(S->dT0, S->nt0, S->dI, S->dS, st));
+    q.add(launch_pred_guess(S->dT0, S->nt0, S->dI, st));
 }
 
 template <typename T>
@@ -2145,7 +2147,7 @@ struct StateSnapshot {
             const InstDev& d = I.dev;
             const size_t nc = I.ncell * sizeof(double), nq = 4 * (size_t)I.qstride * sizeof(double);
             for (void* p : {(void*)d.u, (void*)d.v, (void*)d.U, (void*)d.V, (void*)d.Nu, (void*)d.Nv, (void*)d.p,
-                            (void*)d.pold, (void*)d.pold2})
+                            (void*)d.pold, (void*)d.pold2, (void*)d.dup, (void*)d.dvp})
                 items.push_back({p, nc});
             items.push_back({(void*)d.qbu, nq});
             items.push_back({(void*)d.qbv, nq});

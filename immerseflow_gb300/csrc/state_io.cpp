@@ -50,7 +50,9 @@ namespace {
 
 constexpr char kMagic[8] = {'I', 'F', 'X', 'C', 'K', 'P', 'T', '1'};
 constexpr char kSetMagic[8] = {'I', 'F', 'X', 'C', 'K', 'S', 'E', 'T'};
-constexpr uint32_t kVersion = 2;  // 2: the pressures of the two steps before (initial-guess extrapolation)
+// 2: the pressures of the two steps before (initial-guess extrapolation);
+// 3: the predictor increment of the step before (the predictor's initial guess)
+constexpr uint32_t kVersion = 3;
 
 struct CkptHeader {
     char magic[8];
@@ -92,8 +94,9 @@ bool method(const ifx_solver* S) { return S->mode == IFX_MODE_METHOD; }
 size_t cells(const Instance& I) { return (size_t)I.nx * I.ny; }
 
 // Cell fields a METHOD-mode checkpoint carries: u, v, U, V, the convection
-// history Nu, Nv, p and the pressures of the two steps before.
-constexpr int kMethodFields = 9;
+// history Nu, Nv, p, the pressures of the two steps before and the predictor
+// increment of the step before.
+constexpr int kMethodFields = 11;
 
 size_t payload_bytes(const ifx_solver* S, const Instance& I) {
     if (!method(S)) return 3 * cells(I) * sizeof(double);
@@ -123,10 +126,10 @@ ifx_status check_restartable(const ifx_solver* S, int inst, const char* fn) {
     return IFX_OK;
 }
 
-// The seven METHOD-mode cell arrays of a checkpoint, in order.
+// The METHOD-mode cell arrays of a checkpoint, in order.
 void method_fields(const InstDev& d, double* (&f)[kMethodFields]) {
     f[0] = d.u; f[1] = d.v; f[2] = d.U; f[3] = d.V; f[4] = d.Nu; f[5] = d.Nv; f[6] = d.p; f[7] = d.pold;
-    f[8] = d.pold2;
+    f[8] = d.pold2; f[9] = d.dup; f[10] = d.dvp;
 }
 
 // REFERENCE-mode arrays (dense rows).
@@ -448,6 +451,9 @@ extern "C" ifx_status ifx_read_snapshot_ascii(ifx_solver* S, int inst, const cha
         SIO_CUDA(cudaStreamSynchronize(S->stream));
         st.have_nold = 0;  // no convection history in this format
         st.pold_n = 0;     // nor the pressures of the steps before
+        // nor the predictor increment of the step before
+        SIO_CUDA(cudaMemsetAsync(d.dup, 0, I.ncell * sizeof(double), S->stream));
+        SIO_CUDA(cudaMemsetAsync(d.dvp, 0, I.ncell * sizeof(double), S->stream));
         if (steps >= 0) st.nstep = steps;
         SIO_CUDA(cudaMemcpyAsync(S->dS + inst, &st, sizeof(InstState), cudaMemcpyHostToDevice, S->stream));
     } else {

@@ -353,8 +353,10 @@ ifx_status ifx_synchronize(ifx_solver* s);
  * (src/main.cu:27-30,50-53) without using them; its Fortran predecessor
  * restarts from an ASCII snapshot (test/UTIL_PRE_SIM.f90:120-149).
  * Binary checkpoint of one instance: every array a step carries into the next
- * (METHOD: cell and face velocities, convection history, pressure, outflow
- * boundary values, iteration state; REFERENCE: u, v, p), so that a run
+ * (METHOD: cell and face velocities, convection history, pressure and the
+ * pressures of the two steps before, the predictor increment of the step
+ * before, outflow boundary values, iteration state; REFERENCE: u, v, p), so
+ * that a run
  * restarted from it continues bit for bit.  A checkpoint loads into an
  * instance of the same mode, grid, body and boundary types (any precision,
  * any batch position); a header and a checksum are checked.  Loading into a

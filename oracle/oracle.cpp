@@ -514,6 +514,9 @@ struct orc_solver {
     // instance's fourth step, linear on its third); pold_n counts the steps
     std::vector<double> pold, pold2;
     int pold_n = 0;
+    // the predictor increment q* - q^n of the step before (zero in cells that
+    // were not fluid): the next predictor starts from q^n plus it
+    std::vector<double> dup, dvp;
     bool singular = true;
     bool dir[4] = {false, false, false, false};
     std::vector<Level> L;
@@ -1233,7 +1236,19 @@ void method_step(orc_solver* S) {
             S->Nv[id] = Nv;
         }
     S->have_nold = true;
-    // 3. predictor: Jacobi on (I - dt/Re L) q = rhs, ghosts from the BC relations
+    // 3. predictor: Jacobi on (I - dt/Re L) q = rhs, ghosts from the BC relations,
+    // from q^n plus the previous step's predictor increment in the fluid cells
+    // (the increment buffers keep q^n until the increment is formed again)
+    for (int j = 1; j < ny - 1; j++)
+        for (int i = 1; i < nx - 1; i++) {
+            const int id = IDX(i, j, nx);
+            if (S->type[id] != T_FLUID) continue;
+            const double un = S->u[id], vn = S->v[id];
+            S->u[id] = un + S->dup[id];
+            S->v[id] = vn + S->dvp[id];
+            S->dup[id] = un;
+            S->dvp[id] = vn;
+        }
     S->u2 = S->u;
     S->v2 = S->v;
     int it = 0;
@@ -1277,6 +1292,14 @@ void method_step(orc_solver* S) {
     S->st.last_ad_iters = it;
     S->st.last_ad_metric = metric / std::max(1, S->n_fluid);
     S->st.ad_iters_total += it;
+    // the increment for the next step's initial guess
+    for (int j = 1; j < ny - 1; j++)
+        for (int i = 1; i < nx - 1; i++) {
+            const int id = IDX(i, j, nx);
+            const bool fl = S->type[id] == T_FLUID;
+            S->dup[id] = fl ? S->u[id] - S->dup[id] : 0.0;
+            S->dvp[id] = fl ? S->v[id] - S->dvp[id] : 0.0;
+        }
     // 4. face velocities of the predicted field
     face_interp(S);
     // 5. pressure right-hand side
@@ -1504,6 +1527,7 @@ extern "C" orc_solver* orc_create(const ifx_config* cfg, const double* xf, const
     build_levels(S);
     // state
     S->u.assign(n, 0.0); S->v.assign(n, 0.0); S->p.assign(n, 0.0); S->pold.assign(n, 0.0); S->pold2.assign(n, 0.0);
+    S->dup.assign(n, 0.0); S->dvp.assign(n, 0.0);
     S->U.assign(n, 0.0); S->V.assign(n, 0.0);
     S->Nu.assign(n, 0.0); S->Nv.assign(n, 0.0);
     S->ru.assign(n, 0.0); S->rv.assign(n, 0.0);
