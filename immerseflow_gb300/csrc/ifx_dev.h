@@ -26,6 +26,9 @@ constexpr int MG_ROWS_WIDE = 4;  // rows per thread of the wide multigrid tiles 
 constexpr int GHOST_BLOCK = 256;
 constexpr int NPART = 6;            // partial sums per tile
 constexpr int FORCE_SAMPLES = 2048;  // body-surface samples for drag/lift
+// blocks per instance that evaluate them (an SM issues 2 FP64 FMA per clock:
+// one block took ~30 us for the 2048 samples)
+constexpr int FORCE_BLOCKS = 8;
 constexpr int TMA_MAPS_PER_LEVEL = 8;  // tensor maps per level: e, e2, r, bits for 32x8 tiles, then for wide tiles
 constexpr double COARSE_OMEGA = 1.5;  // RB-SOR factor on the coarsest level
 // Threads of the block that runs an instance's small levels in the graph and

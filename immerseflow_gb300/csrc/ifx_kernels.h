@@ -102,7 +102,8 @@ cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const Ins
 cudaError_t launch_correct(const Tile* t, int nt, const InstDev* I, double* part, cudaStream_t s);
 cudaError_t launch_correct_reduce(const InstDev* I, InstState* S, const double* part, int ninst,
                                   cudaStream_t s);
-cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_t s);
+// fpart: 2 * FORCE_BLOCKS doubles per instance; ftick: one zeroed counter per instance
+cudaError_t launch_forces(const InstDev* I, InstState* S, double* fpart, unsigned* ftick, int ninst, cudaStream_t s);
 
 // ---- immersed-boundary set-up (kernels_ibm.cu, built without FMA contraction)
 cudaError_t launch_tag(const InstDev* I, int inst, int n_cells, uint8_t* type, cudaStream_t s);

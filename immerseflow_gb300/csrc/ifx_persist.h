@@ -27,6 +27,8 @@ struct PersistPlan {
     const GhostDev* G;
     double* gval;
     double* part;
+    double* fpart;      // force partials, 2 * FORCE_BLOCKS per instance
+    unsigned* ftick;    // force tickets, one per instance
     const Tile* t0;
     const Tile* tsm[kMaxLevels];
     const Tile* tre[kMaxLevels];

@@ -195,7 +195,10 @@ __global__ void __launch_bounds__(TILE_THREADS, 8) k_correct(const Tile* __restr
                           double* __restrict__ part) { b_correct(tiles, I, part, blockIdx.x); }
 __global__ void k_correct_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                  const double* __restrict__ part) { b_correct_reduce(I, S, part, blockIdx.x); }
-__global__ void k_forces(const InstDev* __restrict__ I, InstState* __restrict__ S) { b_forces(I, S, blockIdx.x); }
+__global__ void k_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, double* __restrict__ fpart,
+                         unsigned* __restrict__ ftick) {
+    b_forces(I, S, fpart, ftick, blockIdx.x);
+}
 
 // ------------------------------------------------------------ launchers
 
@@ -427,8 +430,8 @@ cudaError_t launch_correct_reduce(const InstDev* I, InstState* S, const double* 
     k_correct_reduce<<<ninst, 256, 0, s>>>(I, S, part);
     return cudaGetLastError();
 }
-cudaError_t launch_forces(const InstDev* I, InstState* S, int ninst, cudaStream_t s) {
-    k_forces<<<ninst, 256, 0, s>>>(I, S);
+cudaError_t launch_forces(const InstDev* I, InstState* S, double* fpart, unsigned* ftick, int ninst, cudaStream_t s) {
+    k_forces<<<ninst * FORCE_BLOCKS, 256, 0, s>>>(I, S, fpart, ftick);
     return cudaGetLastError();
 }
 

@@ -210,7 +210,7 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     FOR_VB(n) b_correct_reduce(P.I, P.S, P.part, vb);
     BAR();
     if (!ghost_fill(P, 3, ep)) return false;
-    FOR_VB(n) b_forces(P.I, P.S, vb);
+    FOR_VB(n * FORCE_BLOCKS) b_forces(P.I, P.S, P.fpart, P.ftick, vb);
     BAR();
     return true;
 }

@@ -2136,16 +2136,21 @@ __device__ __forceinline__ double bil(const double* q, int c, int P, double xi, 
     return (1 - xi) * (1 - et) * q[c] + xi * (1 - et) * q[c + 1] + (1 - xi) * et * q[c + P] + xi * et * q[c + P + 1];
 }
 
-__device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S, int vb) {
-    const int k = vb;
+// vb = instance * FORCE_BLOCKS + b: block b sums its share of the samples
+// into fpart; the last of the instance's blocks to finish (ticket ftick)
+// sums the FORCE_BLOCKS partials in block order and writes the forces and the
+// time-history record.
+__device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstState* __restrict__ S,
+                                         double* __restrict__ fpart, unsigned* __restrict__ ftick, int vb) {
+    const int k = vb / FORCE_BLOCKS, fb = vb - k * FORCE_BLOCKS;
     const InstDev& in = I[k];
     if (in.retired) return;
-    double cd = 0.0, cl = 0.0;  // valid in thread 0
+    constexpr int per = FORCE_SAMPLES / FORCE_BLOCKS;
     if (in.body) {
         const double mu = 1.0 / in.re;
         const int P = in.pitch;
         double F[2] = {0.0, 0.0};
-        for (int q = threadIdx.x; q < FORCE_SAMPLES; q += blockDim.x) {
+        for (int q = fb * per + threadIdx.x; q < (fb + 1) * per; q += blockDim.x) {
             const ForceSample f = ldg_struct(&in.fs[q]);
             const double ps = bil(in.p, f.c0, P, f.xi0, f.et0);
             double up = bil(in.u, f.c1, P, f.xi1, f.et1);
@@ -2163,13 +2168,33 @@ __device__ __forceinline__ void b_forces(const InstDev* __restrict__ I, InstStat
         __shared__ double out[2];
         block_sum<2>(F, out);
         if (threadIdx.x == 0) {
-            cd = out[0] / in.fref;
-            cl = out[1] / in.fref;
+            fpart[2 * (size_t)vb] = out[0];
+            fpart[2 * (size_t)vb + 1] = out[1];
         }
     }
+    __shared__ bool last;
     if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&ftick[k], 1u) == FORCE_BLOCKS - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double cd = 0.0, cl = 0.0;  // valid in thread 0
+    if (threadIdx.x == 0) {
+        if (in.body) {
+            double fx = 0.0, fy = 0.0;
+            const volatile double* fp = fpart + 2 * (size_t)k * FORCE_BLOCKS;
+            for (int b = 0; b < FORCE_BLOCKS; b++) {
+                fx += fp[2 * b];
+                fy += fp[2 * b + 1];
+            }
+            cd = fx / in.fref;
+            cl = fy / in.fref;
+        }
         S[k].cd = cd;
         S[k].cl = cl;
+        ftick[k] = 0u;
     }
     // time-history record of this step: step count, forces, probe values
     if (in.hist_cap > 0) {

@@ -721,6 +721,8 @@ ifx_status setup_persistent(ifx_solver* S) {
     P.G = S->dG;
     P.gval = S->dGval;
     P.part = S->dPart;
+    P.fpart = S->dFpart;
+    P.ftick = S->dFtick;
     P.t0 = S->dT0;
     P.nt0 = S->nt0;
     for (int l = 1; l < S->lmax; l++) {
@@ -1165,6 +1167,8 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
         if (e != cudaSuccess) cudaGetLastError();  // cluster launches unavailable: tile V-cycle only
     }
     IFX_TRY(dalloc(S, &S->dPart, (size_t)S->nt0 * NPART));
+    IFX_TRY(dalloc(S, &S->dFpart, (size_t)n * 2 * FORCE_BLOCKS));
+    IFX_TRY(dalloc(S, &S->dFtick, (size_t)n));
     IFX_TRY(dalloc(S, &S->dS, n));
     IFX_TRY(dalloc(S, &S->dCtl, 1));
     CUDA_TRY(cudaMallocHost((void**)&S->hS, n * sizeof(InstState)));
@@ -1438,7 +1442,7 @@ void seq_post(Seq& q) {
     q.add(launch_correct_reduce(S->dI, S->dS, S->dPart, n, st));
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
-    q.add(launch_forces(S->dI, S->dS, n, st));
+    q.add(launch_forces(S->dI, S->dS, S->dFpart, S->dFtick, n, st));
 }
 
 int max_pred_pairs(const ifx_solver* S) {
