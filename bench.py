@@ -798,17 +798,14 @@ def main():
 
     # end to end through the C ABI: pinned host state in, result out, every step
     nx, ny = s.grid_dims()
-    host = {f: torch.empty(nx * ny, dtype=torch.float64, pin_memory=True).numpy() for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P)}
-    for f, a in host.items():
-        a[:] = s.get(f).ravel()
+    host = tuple(torch.empty(nx * ny, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3))
+    s.get_state(out=host)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for f, a in host.items():
-            s.set(f, a)
+        s.set_state(*host)  # u, v, p in one call (ifx_set_state)
         s.step(1)
-        for f, a in host.items():
-            s.get(f, out=a)  # straight into the pinned buffer
+        s.get_state(out=host)  # straight into the pinned buffers (ifx_get_state)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * cells * args.steps / e2e_s / 1e6

@@ -41,6 +41,8 @@ _SIGS = {
     "ifx_set_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t]),
     "ifx_get_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),
     "ifx_set_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),
+    "ifx_set_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t]),
+    "ifx_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t]),
     "ifx_write_results": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ifx_forces": (C.c_int, [C.c_void_p, _dp, _dp]),
     "ifx_get_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Stats)]),
@@ -225,6 +227,30 @@ class Solver:
     def set(self, field, arr, inst=0):
         a = np.ascontiguousarray(arr, np.float64).ravel()
         _check(lib().ifx_set_field_i(self._h, inst, field, _dptr(a), a.size))
+
+    def set_state(self, u, v, p, inst=0):
+        """Set u, v and p of instance `inst` in one call (each nx*ny values in
+        dense rows, or None to keep that field)."""
+        nx, ny = self.grid_dims(inst)
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64).ravel() for a in (u, v, p)]
+        for a in arrs:
+            if a is not None and a.size != nx * ny:
+                raise ValueError(f"each field must hold {nx * ny} values")
+        ptrs = [None if a is None else _dptr(a) for a in arrs]
+        _check(lib().ifx_set_state(self._h, inst, *ptrs, nx * ny))
+
+    def get_state(self, inst=0, out=None):
+        """(u, v, p) of instance `inst` as [ny, nx] arrays in one call; with
+        `out` (three C-contiguous float64 arrays of nx*ny values, e.g. pinned
+        buffers reused every step) the fields are copied straight into them."""
+        nx, ny = self.grid_dims(inst)
+        if out is None:
+            out = tuple(np.zeros(nx * ny) for _ in range(3))
+        for a in out:
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != nx * ny:
+                raise ValueError(f"out must be three C-contiguous float64 arrays of {nx * ny} values")
+        _check(lib().ifx_get_state(self._h, inst, *[_dptr(a) for a in out], nx * ny))
+        return tuple(a.reshape(ny, nx) for a in out)
 
     def grid_dims(self, inst=0):
         """(nx, ny) including the ghost ring."""

@@ -122,6 +122,7 @@ struct ifx_solver {
     int sub_bytes = 0;  // dynamic shared memory of the small-level sub-cycle
     int mg_pre = 2, mg_post = 2;
     double* dPart = nullptr;         // NPART partials per finest-level tile
+    double* dStage = nullptr;        // state transfers: three dense fields of the largest instance
     double* dFpart = nullptr;        // force partials, 2 * FORCE_BLOCKS per instance
     unsigned* dFtick = nullptr;      // force tickets, one per instance (zero between steps)
     ifx::LoopCtl* dCtl = nullptr;

@@ -14,6 +14,12 @@ cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int c
                               cudaStream_t s);
 cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);
 cudaError_t launch_pred_guess(const Tile* t, int nt, const InstDev* I, cudaStream_t s);
+// u, v, p (pitched; a null field is skipped) <-> stage (dense rows of nx, the
+// three fields one after another)
+cudaError_t launch_state_unpack(const double* stage, double* u, double* v, double* p, int nx, int ny, int pitch,
+                                cudaStream_t s);
+cudaError_t launch_state_pack(const double* u, const double* v, const double* p, double* stage, int nx, int ny,
+                              int pitch, cudaStream_t s);
 cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I,
                               const InstState* S, double* part, int parity, cudaStream_t s);
 // Mixed path: FP32 sweep on the correction, and the FP64 refresh (stage 0:

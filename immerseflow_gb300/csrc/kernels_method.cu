@@ -223,6 +223,38 @@ cudaError_t launch_ghost_fill(const GhostDev* G, int ng, const InstDev* I, int c
     k_ghost_scatter<<<nblk(ng, 256), 256, 0, s>>>(G, ng, I, comps, gval);
     return cudaGetLastError();
 }
+// Dense host rows <-> pitched device fields, three fields at a time through a
+// dense staging buffer (one contiguous copy each way instead of row copies).
+__global__ void k_state_unpack(const double* __restrict__ stage, double* u, double* v, double* p, int nx, int ny,
+                               int pitch) {
+    const int n = nx * ny;
+    double* dst[3] = {u, v, p};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+        const int f = q / n, r = q - f * n, j = r / nx, i = r - j * nx;
+        if (dst[f]) dst[f][i + j * pitch] = stage[q];
+    }
+}
+__global__ void k_state_pack(const double* u, const double* v, const double* p, double* __restrict__ stage, int nx,
+                             int ny, int pitch) {
+    const int n = nx * ny;
+    const double* src[3] = {u, v, p};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+        const int f = q / n, r = q - f * n, j = r / nx, i = r - j * nx;
+        if (src[f]) stage[q] = src[f][i + j * pitch];
+    }
+}
+cudaError_t launch_state_unpack(const double* stage, double* u, double* v, double* p, int nx, int ny, int pitch,
+                                cudaStream_t s) {
+    const int n = 3 * nx * ny, g = (n + 255) / 256;
+    k_state_unpack<<<g < 1216 ? g : 1216, 256, 0, s>>>(stage, u, v, p, nx, ny, pitch);
+    return cudaGetLastError();
+}
+cudaError_t launch_state_pack(const double* u, const double* v, const double* p, double* stage, int nx, int ny,
+                              int pitch, cudaStream_t s) {
+    const int n = 3 * nx * ny, g = (n + 255) / 256;
+    k_state_pack<<<g < 1216 ? g : 1216, 256, 0, s>>>(u, v, p, stage, nx, ny, pitch);
+    return cudaGetLastError();
+}
 cudaError_t launch_pred_guess(const Tile* t, int nt, const InstDev* I, cudaStream_t s) {
     k_pred_guess<<<nt, TILE_THREADS, 0, s>>>(t, I);
     return cudaGetLastError();

@@ -2546,6 +2546,83 @@ extern "C" ifx_status ifx_set_field(ifx_solver* S, int field, const double* host
     return ifx_set_field_i(S, 0, field, host, n);
 }
 
+namespace {
+// The dense staging buffer of the state calls (three fields of the largest
+// instance), allocated on first use in either mode.
+ifx_status state_stage(ifx_solver* S, double** out) {
+    if (!S->dStage) {
+        size_t most = 0;
+        for (const Instance& I : S->inst) most = std::max(most, (size_t)I.nx * I.ny);
+        IFX_TRY(dalloc(S, &S->dStage, 3 * most));
+    }
+    *out = S->dStage;
+    return IFX_OK;
+}
+
+// The device arrays of u, v, p of one instance and their row pitch.
+void state_arrays(ifx_solver* S, const Instance& I, double* (&f)[3], size_t& pitch) {
+    if (S->mode == IFX_MODE_REFERENCE) {
+        f[0] = S->r_cur ? S->r_ut : S->r_u;
+        f[1] = S->r_cur ? S->r_vt : S->r_v;
+        f[2] = S->r_p;
+        pitch = I.nx;
+    } else {
+        f[0] = I.dev.u;
+        f[1] = I.dev.v;
+        f[2] = I.dev.p;
+        pitch = I.pitch;
+    }
+}
+}  // namespace
+
+extern "C" ifx_status ifx_set_state(ifx_solver* S, int inst, const double* u, const double* v, const double* p,
+                                    size_t n) {
+    if (!S || inst < 0 || inst >= (int)S->inst.size() || (!u && !v && !p))
+        return set_error(IFX_ERR_ARG, "ifx_set_state: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
+    const Instance& I = S->inst[inst];
+    if (n != (size_t)I.nx * I.ny) return set_error(IFX_ERR_ARG, "ifx_set_state: size mismatch");
+    CUDA_TRY(cudaSetDevice(S->device));
+    double* f[3];
+    size_t pitch;
+    state_arrays(S, I, f, pitch);
+    double* stage = nullptr;
+    IFX_TRY(state_stage(S, &stage));
+    const double* h[3] = {u, v, p};
+    double* dst[3];
+    for (int k = 0; k < 3; k++) {
+        dst[k] = h[k] ? f[k] : nullptr;
+        if (h[k]) CUDA_TRY(cudaMemcpyAsync(stage + k * n, h[k], n * 8, cudaMemcpyHostToDevice, S->stream));
+    }
+    CUDA_TRY(launch_state_unpack(stage, dst[0], dst[1], dst[2], I.nx, I.ny, (int)pitch, S->stream));
+    S->launches++;
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_state(ifx_solver* S, int inst, double* u, double* v, double* p, size_t n) {
+    if (!S || inst < 0 || inst >= (int)S->inst.size() || (!u && !v && !p))
+        return set_error(IFX_ERR_ARG, "ifx_get_state: bad argument");
+    if (S->pending_steps) IFX_TRY(step_finish(S));
+    const Instance& I = S->inst[inst];
+    if (n != (size_t)I.nx * I.ny) return set_error(IFX_ERR_ARG, "ifx_get_state: size mismatch");
+    CUDA_TRY(cudaSetDevice(S->device));
+    double* f[3];
+    size_t pitch;
+    state_arrays(S, I, f, pitch);
+    double* stage = nullptr;
+    IFX_TRY(state_stage(S, &stage));
+    double* h[3] = {u, v, p};
+    const double* src[3];
+    for (int k = 0; k < 3; k++) src[k] = h[k] ? f[k] : nullptr;
+    CUDA_TRY(launch_state_pack(src[0], src[1], src[2], stage, I.nx, I.ny, (int)pitch, S->stream));
+    S->launches++;
+    for (int k = 0; k < 3; k++)
+        if (h[k]) CUDA_TRY(cudaMemcpyAsync(h[k], stage + k * n, n * 8, cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return IFX_OK;
+}
+
 extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
     if (!S || !dir) return set_error(IFX_ERR_ARG, "ifx_write_results: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));

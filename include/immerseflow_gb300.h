@@ -330,6 +330,14 @@ ifx_status ifx_get_field(ifx_solver* s, int field, double* host, size_t n);
 ifx_status ifx_set_field(ifx_solver* s, int field, const double* host, size_t n);
 ifx_status ifx_get_field_i(ifx_solver* s, int inst, int field, double* host, size_t n);
 ifx_status ifx_set_field_i(ifx_solver* s, int inst, int field, const double* host, size_t n);
+/* The state of one instance in one call: u, v and p, each nx*ny doubles in
+ * dense rows (a null pointer skips that field), staged through one dense
+ * device buffer: one contiguous copy per field, one kernel between the dense
+ * and the pitched layout, one synchronisation (the per-field calls above
+ * synchronise once per field and copy row by row).  For a caller that passes
+ * the whole state in and out every step. */
+ifx_status ifx_set_state(ifx_solver* s, int inst, const double* u, const double* v, const double* p, size_t n);
+ifx_status ifx_get_state(ifx_solver* s, int inst, double* u, double* v, double* p, size_t n);
 /* Writes p.dat, uc.dat, vc.dat, final_results.dat into dir (src/include/postSim.cu:10-66). */
 ifx_status ifx_write_results(ifx_solver* s, const char* dir);
 ifx_status ifx_forces(ifx_solver* s, double* cd, double* cl);

@@ -291,3 +291,33 @@ def test_small_uneven_grids_vs_oracle(oracle, nx, ny, prec):
     _compare(s, o, tol=tol)
     if prec == capi.PREC_FP64:
         assert s.stats().last_ppe_iters == o.stats().last_ppe_iters
+
+
+@pytest.mark.gpu
+def test_state_transfer_matches_field_calls(golden_dir):
+    """ifx_set_state / ifx_get_state move u, v, p like the per-field calls."""
+    specs = [cases.cylinder(nx=96, ny=64, precision=capi.PREC_MIXED),
+             cases.cylinder(nx=64, ny=48, precision=capi.PREC_MIXED)]
+    s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+    s.step(3)
+    for inst in (0, 1):
+        ref = [s.get(f, inst) for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P)]
+        for a, b in zip(ref, s.get_state(inst)):
+            assert np.array_equal(a, b)
+        rng = np.random.default_rng(inst)
+        new = [rng.standard_normal(a.shape) for a in ref]
+        s.set_state(new[0], None, new[2], inst)  # v kept
+        assert np.array_equal(s.get(capi.FIELD_U, inst), new[0])
+        assert np.array_equal(s.get(capi.FIELD_V, inst), ref[1])
+        assert np.array_equal(s.get(capi.FIELD_P, inst), new[2])
+    # REFERENCE mode (dense device arrays): the reference's own inputs
+    c = ifx.config_read(os.path.join(golden_dir, "inputs", "inputs.txt"))
+    xf = ifx.grid_read(c.xgrid.decode(), c.nx + 1)
+    yf = ifx.grid_read(c.ygrid.decode(), c.ny + 1)
+    r = ifx.Solver.create(c, xf, yf)
+    r.step(2)
+    ref = [r.get(f) for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P)]
+    for a, b in zip(ref, r.get_state()):
+        assert np.array_equal(a, b)
+    r.set_state(None, None, ref[2] + 1.0)
+    assert np.array_equal(r.get(capi.FIELD_P), ref[2] + 1.0)
