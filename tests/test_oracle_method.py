@@ -48,3 +48,19 @@ def test_cavity_second_order_under_refinement(oracle):
     d2 = np.abs(prof[64] - prof[128]).max()
     assert d2 < 2e-3
     assert 3.0 <= d1 / d2 <= 5.5, d1 / d2
+
+
+def test_predictor_initial_guess(oracle):
+    """The predictor starts from q^n plus the step before's increment q* - q^n:
+    after the first steps it needs fewer Jacobi sweeps than on the first step
+    (from q^n alone), and the solution is unchanged within the predictor's own
+    tolerance (the stop rule is the same)."""
+    cfg, xf, yf = cases.cylinder(nx=192, ny=128, precision=capi.PREC_FP64)
+    s = oracle.method(cfg, xf, yf, nthreads=8)
+    its = []
+    for _ in range(12):
+        s.step(1)
+        its.append(s.stats().last_ad_iters)
+    # the first step has no increment; from the fourth step on the guess is O(dt^2) away
+    assert max(its[4:]) < its[0], its
+    assert s.stats().max_div < 1e-6
