@@ -172,7 +172,11 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid(const GridTiles
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
-                           const GhostDev* __restrict__ G, int fine_alt) { b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x); }
+                           const GhostDev* __restrict__ G, int fine_alt) {
+    // a programmatically launched sub-cycle may start staging its geometry now
+    asm volatile("griddepcontrol.launch_dependents;");
+    b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x);
+}
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
@@ -446,8 +450,19 @@ template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s) {
     if (ninst == 0) return cudaSuccess;
-    k_subcycle<T><<<ninst, SUB_THREADS, smem_bytes, s>>>(sub, LV, I, S, pre, post);
-    return cudaGetLastError();
+    // programmatic dependent launch: the blocks may start (and stage the
+    // geometry image) while the restriction before them runs
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ninst);
+    cfg.blockDim = dim3(SUB_THREADS);
+    cfg.dynamicSmemBytes = (size_t)smem_bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_subcycle<T>, sub, LV, I, S, pre, post);
 }
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {
     k_p_finalize<<<nt, TILE_THREADS, 0, s>>>(t, I, S);

@@ -1841,6 +1841,11 @@ __device__ __forceinline__ void sub_stage_all(const InstDev& in, unsigned char* 
         if ((load_e && b >= oe && b < oe + span) || (b >= orr && b < orr + span)) continue;
         cp_async<16>(sb + b, img + b);
     }
+    // The first level's e and r are the output of the phase before (the
+    // restriction into it): a programmatic launch of this kernel starts while
+    // that phase runs and waits here, after the geometry copies are issued
+    // (a no-op in a launch without a programmatic dependency).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int g = q + (q / nx) * (gp - nx);
         if (load_e) cp_async<(int)sizeof(T)>(sb + oe + q * (int)sizeof(T), ge + g);
