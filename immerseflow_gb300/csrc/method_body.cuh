@@ -49,6 +49,13 @@ __device__ __forceinline__ S ldg_struct(const S* p) {
 
 // ---------------------------------------------------------------- helpers
 
+// Programmatic dependent launch: a phase lets its dependents launch early
+// (trigger), and a dependent launched that way does its independent work
+// (its instance state, its geometry) before waiting for the phase's output
+// (wait).  Both are no-ops in launches without a programmatic dependency.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ double rcpa(double d) { return (double)__frcp_rn((float)d); }
 __device__ __forceinline__ float rcpa(float d) { return __frcp_rn(d); }
 
@@ -562,11 +569,12 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
                               unsigned long long handle, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
-    const int st = S[k].pred_state;
+    const int st = S[k].pred_state, beg = in.tile_beg, cnt = in.tile_cnt;
+    pdl_wait();  // the sweep's partials; every write below
     bool active = false, due = false;
     if (st == ST_ACTIVE) {
         double r[1];
-        inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
+        inst_sum<1>(part, beg, cnt, r);
         if (threadIdx.x == 0) {
             const int it = S[k].pred_iters + 1;
             S[k].pred_iters = it;
@@ -945,9 +953,11 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
     bool active = false, due = false;
     if (start == 2 && none_due(ctl)) return;
     const bool run = S[k].ppe_state == ST_ACTIVE && (start != 2 || S[k].restart);
+    const int beg = in.tile_beg, cnt = in.tile_cnt;
+    pdl_wait();  // the partials of the phase before; every write below
     if (run) {
         double r[4];
-        inst_sum<4>(part, in.tile_beg, in.tile_cnt, r);
+        inst_sum<4>(part, beg, cnt, r);
         if (threadIdx.x == 0) {
             InstState& st = S[k];
             if (start == 1) {
@@ -1097,8 +1107,10 @@ __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, Ins
     const int k = vb;
     const InstDev& in = I[k];
     if (S[k].ppe_state != ST_ACTIVE) return;
+    const int beg = in.tile_beg, cnt = in.tile_cnt;
+    pdl_wait();  // the operator apply's partials
     double r[2];
-    inst_sum<2>(part, in.tile_beg, in.tile_cnt, r);
+    inst_sum<2>(part, beg, cnt, r);
     if (threadIdx.x == 0) {
         if (which == 0) S[k].alpha = r[0] != 0.0 ? S[k].rho / r[0] : 0.0;
         else S[k].omega = r[1] != 0.0 ? r[0] / r[1] : 0.0;
@@ -1843,9 +1855,8 @@ __device__ __forceinline__ void sub_stage_all(const InstDev& in, unsigned char* 
     }
     // The first level's e and r are the output of the phase before (the
     // restriction into it): a programmatic launch of this kernel starts while
-    // that phase runs and waits here, after the geometry copies are issued
-    // (a no-op in a launch without a programmatic dependency).
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // that phase runs and waits here, after the geometry copies are issued.
+    pdl_wait();
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int g = q + (q / nx) * (gp - nx);
         if (load_e) cp_async<(int)sizeof(T)>(sb + oe + q * (int)sizeof(T), ge + g);
