@@ -101,7 +101,7 @@ cudaError_t cluster_vcycle_setup(int smem_bytes, int ninst, int* ok);
 template <typename T>
 cudaError_t launch_vcycle_cluster(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                                   const GhostDev* G, int pre, int post, int smem_bytes, cudaStream_t s);
-// Allows k_subcycle<T> `bytes` of dynamic shared memory (above the 48 KB default).
+// Allows both k_subcycle<T, MINB> variants `bytes` of dynamic shared memory (above the 48 KB default).
 template <typename T>
 cudaError_t subcycle_smem_limit(int bytes);
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s);

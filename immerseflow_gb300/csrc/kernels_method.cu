@@ -19,6 +19,7 @@
 // path, float for the mixed path).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "method_body.cuh"
@@ -33,13 +34,34 @@ namespace ifx {
 template <typename T>
 constexpr int mg_blocks(int rows) { return rows == 1 ? (sizeof(T) == 8 ? 8 : 4) : 8; }
 
+// Streaming multiprocessors of the current device (read once per device).
+static int device_sm_count() {
+    static std::atomic<int> cnt[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = dev >= 0 && dev < 64 ? dev : 0;
+    int n = cnt[dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+        cnt[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+// The tile kernels that spill within 32 registers (eight resident blocks per
+// SM: the FP64 one-row tiles, the FP64 true residual, the prolongation with
+// its first sweep, the convection) come in two variants: MINB = 8 for grids of
+// many tiles and MINB = 4 (64 registers, no spills), taken for grids of at
+// most four blocks per SM, where the fifth to eighth slots would stay empty.
+static bool few_tiles(int grid) { return grid <= 4 * device_sm_count(); }
+
 __global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl) { b_step_begin(I, S, n, ctl, blockIdx.x); }
 __global__ void k_outflow(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I) { b_outflow(G, ng, I, blockIdx.x); }
 __global__ void k_ghost_gather(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
                                int comps, double* __restrict__ gval) { b_ghost_gather(G, ng, I, comps, gval, blockIdx.x); }
 __global__ void k_ghost_scatter(const GhostDev* __restrict__ G, int ng, const InstDev* __restrict__ I,
                                 int comps, const double* __restrict__ gval) { b_ghost_scatter(G, ng, I, comps, gval, blockIdx.x); }
-__global__ void __launch_bounds__(TILE_THREADS, 8) k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
+template <int MINB>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_conv_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S) { b_conv_rhs(tiles, I, S, blockIdx.x); }
 __global__ void __launch_bounds__(TILE_THREADS, 8) k_pred_guess(const Tile* __restrict__ tiles,
                                                                 const InstDev* __restrict__ I) {
@@ -107,8 +129,8 @@ __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restric
 // whose restart is due (others count 0; each instance's tiles are contiguous
 // in the list), and the grid strides over the concatenated due tiles: the pass
 // costs in proportion to the tiles restarting, spread over the whole grid.
-template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS, 8) k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int MINB>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_bicg_start(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int restart_only,
                              const LoopCtl* ctl, int nt, int ninst) {
@@ -157,14 +179,14 @@ __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __rest
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T, R>(tiles, LV, I, S, blockIdx.x); }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_bicg_dir_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                   const InstDev* __restrict__ I, const InstState* __restrict__ S,
                                   const GhostDev* __restrict__ G, int which) {
     b_bicg_dir_smooth<T, R>(tiles, LV, I, S, G, which, blockIdx.x);
 }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_bicg_apply(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                              const InstDev* __restrict__ I, const InstState* __restrict__ S,
                              const GhostDev* __restrict__ G, double* __restrict__ part, int e_alt, int which) {
     pdl_trigger();
@@ -182,12 +204,12 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_x(const 
     pdl_trigger();
     b_bicg_x<T, R>(tiles, LV, I, S, part, blockIdx.x);
 }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_smooth(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, int flags, int src_alt) { b_smooth<T, R>(tiles, LV, I, S, G, flags, src_alt, blockIdx.x); }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_smooth_tma(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_smooth_tma(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S,
                          const GhostDev* __restrict__ G, const CUtensorMap* __restrict__ tm, int flags, int src_alt,
                          unsigned* err) { b_smooth_tma<T, R>(tiles, LV, I, S, G, tm, flags, src_alt, err, blockIdx.x); }
@@ -204,8 +226,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) k_smooth_grid(const GridTiles
                                                                 int src_alt) {
     b_smooth_grid<T, R>(g, S, G, flags, src_alt, blockIdx.x);
 }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_restrict(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            const GhostDev* __restrict__ G, int fine_alt) {
     pdl_trigger();  // a programmatically launched sub-cycle may start staging its geometry
@@ -214,14 +236,17 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_restrict(cons
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
-template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS, 8) k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int MINB>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                                 const InstDev* __restrict__ I, const InstState* __restrict__ S, int cur,
                                 int coarse_alt) {
     b_prolong_sweep<T>(tiles, LV, I, S, cur, coarse_alt, blockIdx.x);
 }
-template <typename T>
-__global__ void __launch_bounds__(SUB_THREADS) k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
+// MINB = 1 lets the compiler keep the two staged levels' views of a
+// restriction or prolongation in registers (no spills; one block per SM);
+// MINB = 2 fits two blocks per SM for batches of more instances than SMs.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(SUB_THREADS, MINB) k_subcycle(const int* __restrict__ sub, const LevelDev* __restrict__ LV,
                            const InstDev* __restrict__ I, const InstState* __restrict__ S,
                            int pre, int post) {
     extern __shared__ __align__(16) unsigned char sub_smem[];
@@ -298,7 +323,8 @@ cudaError_t launch_pred_guess(const Tile* t, int nt, const InstDev* I, cudaStrea
     return cudaGetLastError();
 }
 cudaError_t launch_conv_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {
-    k_conv_rhs<<<nt, TILE_THREADS, 0, s>>>(t, I, S);
+    if (few_tiles(nt)) k_conv_rhs<4><<<nt, TILE_THREADS, 0, s>>>(t, I, S);
+    else k_conv_rhs<8><<<nt, TILE_THREADS, 0, s>>>(t, I, S);
     return cudaGetLastError();
 }
 cudaError_t launch_pred_sweep(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I,
@@ -338,7 +364,8 @@ cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const I
                               const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, int ninst,
                               cudaStream_t s) {
     const int grid = restart_only && nt > OPT_GRID ? OPT_GRID : nt;
-    k_bicg_start<T><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt, ninst);
+    if (few_tiles(grid)) k_bicg_start<T, 4><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt, ninst);
+    else k_bicg_start<T, 8><<<grid, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, restart_only, ctl, nt, ninst);
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
@@ -357,6 +384,7 @@ template <typename T>
 cudaError_t launch_bicg_dir_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                                    const GhostDev* G, int which, int rows, cudaStream_t s) {
     if (rows == MG_ROWS_WIDE) k_bicg_dir_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, which);
+    else if (sizeof(T) == 8 && few_tiles(nt)) k_bicg_dir_smooth<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, which);
     else k_bicg_dir_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, which);
     return cudaGetLastError();
 }
@@ -368,6 +396,7 @@ template <typename T>
 cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                               const GhostDev* G, double* part, int e_alt, int which, int rows, cudaStream_t s) {
     if (rows == MG_ROWS_WIDE) k_bicg_apply<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
+    else if (sizeof(T) == 8 && few_tiles(nt)) k_bicg_apply<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
     else k_bicg_apply<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, part, e_alt, which);
     return cudaGetLastError();
 }
@@ -394,6 +423,7 @@ cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstD
                           const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
     if (rows == MG_ROWS_WIDE) k_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
+    else if (sizeof(T) == 8 && few_tiles(nt)) k_smooth<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     else k_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     return cudaGetLastError();
 }
@@ -404,6 +434,8 @@ cudaError_t launch_smooth_tma(const Tile* t, int nt, const LevelDev* LV, const I
     if (nt == 0) return cudaSuccess;
     if (rows == MG_ROWS_WIDE)
         k_smooth_tma<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
+    else if (sizeof(T) == 8 && few_tiles(nt))
+        k_smooth_tma<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
     else k_smooth_tma<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
     return cudaGetLastError();
 }
@@ -441,6 +473,7 @@ cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const Ins
                             const GhostDev* G, int fine_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
     if (rows == MG_ROWS_WIDE) k_restrict<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
+    else if (sizeof(T) == 8 && few_tiles(nt)) k_restrict<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     else k_restrict<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     return cudaGetLastError();
 }
@@ -456,7 +489,8 @@ template <typename T>
 cudaError_t launch_prolong_sweep(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                                  int cur, int coarse_alt, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    k_prolong_sweep<T><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, cur, coarse_alt);
+    if (few_tiles(nt)) k_prolong_sweep<T, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, cur, coarse_alt);
+    else k_prolong_sweep<T, 8><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, cur, coarse_alt);
     return cudaGetLastError();
 }
 template cudaError_t launch_prolong_sweep<double>(const Tile*, int, const LevelDev*, const InstDev*, const InstState*,
@@ -473,10 +507,12 @@ cudaError_t subcycle_smem_limit(int bytes) {
     dev = dev >= 0 && dev < 64 ? dev : 0;
     std::lock_guard<std::mutex> g(mu);
     if (bytes <= cur[dev]) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_subcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_subcycle<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_subcycle<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) cur[dev] = bytes;
     return e;
 }
+
 template <typename T>
 cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const InstDev* I, const InstState* S,
                             int pre, int post, int smem_bytes, cudaStream_t s) {
@@ -493,7 +529,10 @@ cudaError_t launch_subcycle(const int* sub, int ninst, const LevelDev* LV, const
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_subcycle<T>, sub, LV, I, S, pre, post);
+    // one block per instance: as many instances as SMs run in one wave of the
+    // one-block-per-SM variant
+    if (ninst <= device_sm_count()) return cudaLaunchKernelEx(&cfg, k_subcycle<T, 1>, sub, LV, I, S, pre, post);
+    return cudaLaunchKernelEx(&cfg, k_subcycle<T, 2>, sub, LV, I, S, pre, post);
 }
 cudaError_t launch_p_finalize(const Tile* t, int nt, const InstDev* I, const InstState* S, cudaStream_t s) {
     k_p_finalize<<<nt, TILE_THREADS, 0, s>>>(t, I, S);
