@@ -328,12 +328,22 @@ size_t cluster_vcycle_bytes(int nd, const int* nx, const int* ny, int tsize, siz
 template <typename T>
 cudaError_t cluster_vcycle_setup(int smem_bytes, int ninst, int* ok) {
     *ok = 0;
+    // the attributes belong to the kernel, shared by every solver on the
+    // device: the shared-memory limit is only raised (a smaller solver set up
+    // after a larger one must not lower it under the larger one's launches)
     static std::mutex mu;
+    static int cur[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = dev >= 0 && dev < 64 ? dev : 0;
     std::lock_guard<std::mutex> g(mu);
     cudaError_t e = cudaFuncSetAttribute(k_vcycle_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_vcycle_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-    if (e != cudaSuccess) return e;
+    if (smem_bytes > cur[dev]) {
+        e = cudaFuncSetAttribute(k_vcycle_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+        if (e != cudaSuccess) return e;
+        cur[dev] = smem_bytes;
+    }
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
