@@ -48,10 +48,11 @@ static int device_sm_count() {
     return n;
 }
 // The tile kernels that spill within 32 registers (eight resident blocks per
-// SM: the FP64 one-row tiles, the FP64 true residual, the prolongation with
-// its first sweep, the convection) come in two variants: MINB = 8 for grids of
-// many tiles and MINB = 4 (64 registers, no spills), taken for grids of at
-// most four blocks per SM, where the fifth to eighth slots would stay empty.
+// SM: the four-row multigrid tiles, the FP64 one-row tiles, the FP64 true
+// residual, the prolongation with its first sweep, the convection) come in
+// two variants: MINB = 8 for grids of many tiles and MINB = 4 (64 registers,
+// no spills), taken for grids of at most four blocks per SM, where the fifth
+// to eighth slots would stay empty.
 static bool few_tiles(int grid) { return grid <= 4 * device_sm_count(); }
 
 __global__ void k_step_begin(const InstDev* __restrict__ I, InstState* S, int n, LoopCtl* ctl) { b_step_begin(I, S, n, ctl, blockIdx.x); }
@@ -233,8 +234,8 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB) k_restrict(const Tile* __r
     pdl_trigger();  // a programmatically launched sub-cycle may start staging its geometry
     b_restrict<T, R>(tiles, LV, I, S, G, fine_alt, blockIdx.x);
 }
-template <typename T, int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
+template <typename T, int R, int MINB = mg_blocks<T>(R)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB) k_prolong(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                           const InstState* __restrict__ S, int fine_alt, int coarse_alt) { b_prolong<T, R>(tiles, LV, S, fine_alt, coarse_alt, blockIdx.x); }
 template <typename T, int MINB>
 __global__ void __launch_bounds__(TILE_THREADS, MINB) k_prolong_sweep(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
@@ -422,7 +423,9 @@ template <typename T>
 cudaError_t launch_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           const GhostDev* G, int flags, int src_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    if (rows == MG_ROWS_WIDE) k_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
+    if (rows == MG_ROWS_WIDE && few_tiles(nt))
+        k_smooth<T, MG_ROWS_WIDE, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
+    else if (rows == MG_ROWS_WIDE) k_smooth<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     else if (sizeof(T) == 8 && few_tiles(nt)) k_smooth<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     else k_smooth<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, flags, src_alt);
     return cudaGetLastError();
@@ -432,7 +435,9 @@ cudaError_t launch_smooth_tma(const Tile* t, int nt, const LevelDev* LV, const I
                               const GhostDev* G, const CUtensorMap* tm, int flags, int src_alt, int rows, unsigned* err,
                               cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    if (rows == MG_ROWS_WIDE)
+    if (rows == MG_ROWS_WIDE && few_tiles(nt))
+        k_smooth_tma<T, MG_ROWS_WIDE, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
+    else if (rows == MG_ROWS_WIDE)
         k_smooth_tma<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
     else if (sizeof(T) == 8 && few_tiles(nt))
         k_smooth_tma<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, tm, flags, src_alt, err);
@@ -472,7 +477,9 @@ template <typename T>
 cudaError_t launch_restrict(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                             const GhostDev* G, int fine_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    if (rows == MG_ROWS_WIDE) k_restrict<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
+    if (rows == MG_ROWS_WIDE && few_tiles(nt))
+        k_restrict<T, MG_ROWS_WIDE, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
+    else if (rows == MG_ROWS_WIDE) k_restrict<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     else if (sizeof(T) == 8 && few_tiles(nt)) k_restrict<T, 1, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     else k_restrict<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, I, S, G, fine_alt);
     return cudaGetLastError();
@@ -481,7 +488,9 @@ template <typename T>
 cudaError_t launch_prolong(const Tile* t, int nt, const LevelDev* LV, const InstState* S, int fine_alt,
                            int coarse_alt, int rows, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    if (rows == MG_ROWS_WIDE) k_prolong<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
+    if (rows == MG_ROWS_WIDE && few_tiles(nt))
+        k_prolong<T, MG_ROWS_WIDE, 4><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
+    else if (rows == MG_ROWS_WIDE) k_prolong<T, MG_ROWS_WIDE><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
     else k_prolong<T, 1><<<nt, TILE_THREADS, 0, s>>>(t, LV, S, fine_alt, coarse_alt);
     return cudaGetLastError();
 }
