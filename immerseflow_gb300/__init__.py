@@ -66,6 +66,8 @@ _SIGS = {
     "ifx_step_wait": (C.c_int, [C.c_void_p]),
     "ifx_set_exec_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "ifx_get_exec_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ifx_set_persistent_grid": (C.c_int, [C.c_void_p, C.c_int]),
+    "ifx_get_persistent_grid": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ifx_set_instance_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ifx_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
     "ifx_checkpoint_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
@@ -320,6 +322,15 @@ class Solver:
         m = C.c_int()
         _check(lib().ifx_get_exec_mode(self._h, C.byref(m)))
         return m.value
+
+    def set_persistent_grid(self, blocks):
+        """Blocks of the persistent mode's launch (0: all co-resident blocks)."""
+        _check(lib().ifx_set_persistent_grid(self._h, int(blocks)))
+
+    def persistent_grid(self):
+        g = C.c_int()
+        _check(lib().ifx_get_persistent_grid(self._h, C.byref(g)))
+        return g.value
 
     def autotune(self, steps=2):
         """Pick the fastest execution mode by timing; state is restored.  Returns (mode, ms/step)."""

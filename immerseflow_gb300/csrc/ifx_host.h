@@ -132,6 +132,8 @@ struct ifx_solver {
     ifx::GridBar* dBar = nullptr;
     ifx::PersistPlan plan{};
     int persist_grid = 0;            // 0: cooperative launch unavailable
+    int persist_full = 0;            // co-resident grid (SMs x blocks per SM, capped): the default
+    int persist_sms = 0;             // SMs of the device
     bool poisoned = false;           // a grid barrier timed out: the handle refuses further steps
 
     // graph execution of one time step (conditional WHILE nodes for the loops)

@@ -712,6 +712,8 @@ ifx_status setup_persistent(ifx_solver* S) {
     if (bps < 1) return IFX_OK;
     S->persist_grid = sms * std::min(bps, 4);
     if (S->persist_grid > 64 * 32) S->persist_grid = 64 * 32;
+    S->persist_full = S->persist_grid;
+    S->persist_sms = sms;
     IFX_TRY(dalloc(S, &S->dBar, 1));
     PersistPlan& P = S->plan;
     std::memset(&P, 0, sizeof(P));
@@ -2035,6 +2037,27 @@ extern "C" ifx_status ifx_set_exec_mode(ifx_solver* S, int mode) {
     return IFX_OK;
 }
 
+// Blocks of the persistent kernel: its phases stride over their tiles, so any
+// grid up to the co-resident one gives the same results; fewer blocks make each
+// grid barrier cheaper (fewer arrivals on its counter) and suit instances with
+// few tiles.
+extern "C" ifx_status ifx_set_persistent_grid(ifx_solver* S, int blocks) {
+    if (!S || blocks < 0) return set_error(IFX_ERR_ARG, "ifx_set_persistent_grid: bad argument");
+    if (S->persist_full == 0) return set_error(IFX_ERR_STATE, "persistent execution is not available for this solver");
+    if (blocks > S->persist_full)
+        return set_error(IFX_ERR_ARG, "ifx_set_persistent_grid: more blocks than can be co-resident (" +
+                                          std::to_string(S->persist_full) + ")");
+    IFX_TRY(step_finish(S));
+    S->persist_grid = blocks == 0 ? S->persist_full : blocks;
+    return IFX_OK;
+}
+
+extern "C" ifx_status ifx_get_persistent_grid(ifx_solver* S, int* blocks) {
+    if (!S || !blocks) return set_error(IFX_ERR_ARG, "ifx_get_persistent_grid: bad argument");
+    *blocks = S->persist_grid;
+    return IFX_OK;
+}
+
 extern "C" ifx_status ifx_get_exec_mode(ifx_solver* S, int* mode) {
     if (!S || !mode) return set_error(IFX_ERR_ARG, "ifx_get_exec_mode: bad argument");
     *mode = S->mode == IFX_MODE_METHOD ? exec_mode(S) : IFX_EXEC_HOST;
@@ -2194,16 +2217,23 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
     IFX_TRY(snap.take(S));
     const long long steps0 = S->steps_done;
     const int saved = S->exec_override, saved_rows = S->mg_rows, saved_cmg = S->cmg_use;
+    const int saved_grid = S->persist_grid;
     // (execution mode, rows per thread of the multigrid tile phases, cluster
-    // V-cycle); the persistent kernel always uses 32x8 tiles
+    // V-cycle, persistent grid); the persistent kernel always uses 32x8 tiles
     struct Cand {
-        int mode, rows, cmg;
+        int mode, rows, cmg, grid;
     };
     std::vector<Cand> cand;
-    if (S->persist_grid > 0) cand.push_back({IFX_EXEC_PERSISTENT, 1, 0});
-    cand.push_back({IFX_EXEC_GRAPH, 1, 0});
-    cand.push_back({IFX_EXEC_GRAPH, MG_ROWS_WIDE, 0});
-    if (S->cmg_ok) cand.push_back({IFX_EXEC_GRAPH, 1, 1});
+    if (S->persist_full > 0) {
+        cand.push_back({IFX_EXEC_PERSISTENT, 1, 0, S->persist_full});
+        // a few instances: also one block per SM (fewer arrivals per grid
+        // barrier; fewer blocks than SMs measured slower on every workload)
+        if (S->inst.size() <= 8 && S->persist_sms < S->persist_full)
+            cand.push_back({IFX_EXEC_PERSISTENT, 1, 0, S->persist_sms});
+    }
+    cand.push_back({IFX_EXEC_GRAPH, 1, 0, saved_grid});
+    cand.push_back({IFX_EXEC_GRAPH, MG_ROWS_WIDE, 0, saved_grid});
+    if (S->cmg_ok) cand.push_back({IFX_EXEC_GRAPH, 1, 1, saved_grid});
     Cand best = cand[0];
     double best_ms = 1e300;
     ifx_status st = IFX_OK;
@@ -2211,6 +2241,7 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
         S->exec_override = c.mode;
         set_mg_rows(S, c.rows);
         set_cluster_mg(S, c.cmg);
+        S->persist_grid = c.grid;
         st = ifx_step(S, 1);  // warm-up (builds the graph on first use)
         if (st == IFX_OK) st = ifx_step(S, steps);
         if (st == IFX_OK) st = snap.restore(S);
@@ -2226,12 +2257,14 @@ extern "C" ifx_status ifx_autotune(ifx_solver* S, int steps, int* chosen, double
         S->exec_override = saved;
         set_mg_rows(S, saved_rows);
         set_cluster_mg(S, saved_cmg);
+        S->persist_grid = saved_grid;
         snap.restore(S);
         return st;
     }
     S->exec_override = best.mode;
     set_mg_rows(S, best.rows);
     set_cluster_mg(S, best.cmg);
+    S->persist_grid = best.grid;
     if (chosen) *chosen = best.mode;
     if (ms_per_step) *ms_per_step = best_ms;
     return IFX_OK;

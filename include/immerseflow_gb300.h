@@ -235,9 +235,17 @@ ifx_status ifx_step_wait(ifx_solver* s);
 #define IFX_EXEC_HOST       2    /* one launch per phase, loops driven by the host  */
 ifx_status ifx_set_exec_mode(ifx_solver* s, int mode);
 ifx_status ifx_get_exec_mode(ifx_solver* s, int* mode);
+/* Blocks of the persistent mode's cooperative launch (no reference
+ * counterpart): 0 = every block that can be co-resident (the default), else at
+ * most that many.  The phases stride over their tiles, so results do not
+ * depend on it; fewer blocks make each grid barrier cheaper.  ifx_autotune
+ * also tries one block per SM for handles of up to eight instances. */
+ifx_status ifx_set_persistent_grid(ifx_solver* s, int blocks);
+ifx_status ifx_get_persistent_grid(ifx_solver* s, int* blocks);
 
 /* Autotuner (no reference counterpart): times `steps` steps in each available
- * execution mode and multigrid tile shape (after one warm-up step each),
+ * execution mode, multigrid tile shape and persistent grid (after one warm-up
+ * step each),
  * restores the solver state afterwards, and keeps the fastest.  All of them
  * give bit-identical results, so tuning never changes an answer.  A handle with
  * a moving body is refused (IFX_ERR_STATE): trial steps would move its

@@ -147,6 +147,33 @@ def test_persistent_batch_equals_graph_batch():
             assert np.array_equal(a.get(f, inst=k), c.get(f, inst=k)), (k, f)
 
 
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_persistent_grid_does_not_change_results(prec):
+    """The persistent kernel's phases stride over their tiles, so a launch of a
+    few blocks gives the graph mode's results bit for bit; with fewer blocks
+    than instances the small levels' geometry is staged in every V-cycle."""
+    specs = [small_cylinder(prec=prec, nx=96, ny=64), cases.cavity(n=40, precision=prec),
+             small_cylinder(prec=prec, nx=70, ny=90, angle=25.0, b=0.25)]
+    ref = _run_mode("graph", specs, 3)
+    for grid in (2, 38):
+        os.environ["IFX_EXEC"] = "persistent"
+        try:
+            s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+            s.set_persistent_grid(grid)
+            assert s.persistent_grid() == grid
+            s.step(3)
+        finally:
+            del os.environ["IFX_EXEC"]
+        for k in range(3):
+            for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_P):
+                assert np.array_equal(s.get(f, inst=k), ref.get(f, inst=k)), (grid, k, f)
+            assert s.stats(k).last_ppe_iters == ref.stats(k).last_ppe_iters
+    with pytest.raises(ifx.IFXError):
+        s.set_persistent_grid(1 << 20)  # more blocks than can be co-resident
+    s.set_persistent_grid(0)
+    assert s.persistent_grid() >= 38
+
+
 def test_batch_member_equals_alone():
     specs = [small_cylinder(nx=96, ny=64), cases.cavity(n=40), small_cylinder(nx=70, ny=90, angle=25.0, b=0.25)]
     batch = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
