@@ -16,7 +16,10 @@ value     : interior cells x steps / device time of the timed steps (CUDA
             start's first ~100 steps (5-8 Krylov iterations a step) a step takes
             2; both arms time the same steps (transient: the first steps);
 e2e       : same metric through the C ABI with the state copied from pinned
-            host buffers and the result copied back every step, wall clock;
+            host buffers and the result copied back every step, wall clock
+            (ifx_step_state: copies in, the step and copies out in one call
+            that waits once; three_calls_value: the same through
+            ifx_set_state, ifx_step and ifx_get_state);
 plain_fp64: the same steps with every kernel in FP64;
 roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
             launch per step, or the persistent per-step kernel); achieved =
@@ -874,13 +877,21 @@ def main():
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s.set_state(*host)  # u, v, p in one call (ifx_set_state)
-        s.step(1)
-        s.get_state(out=host)  # straight into the pinned buffers (ifx_get_state)
+        # u, v, p in, one step, u, v, p out into the same pinned buffers: one call, one wait (ifx_step_state)
+        s.step_state(*host, n=1, out=host)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * cells * args.steps / e2e_s / 1e6
     nbytes = 3 * nx * ny * 8
+    # the same exchange through three calls, each waiting (ifx_set_state, ifx_step, ifx_get_state)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_state(*host)
+        s.step(1)
+        s.get_state(out=host)
+    barrier()
+    e2e3 = world * cells * args.steps / max_over_ranks(time.perf_counter() - t0, world) / 1e6
 
     # roofline of the dominant kernel: the per-step kernel (persistent mode)
     peak, peak_kind = measured_peak()
@@ -901,7 +912,9 @@ def main():
         "dtype": "f32 multigrid + f64 BiCGSTAB/state", "data": "synthetic",
         "config": bench_config(cells, world, args),
         "precision": "mixed", "execution": exec_name(s), "schedule": s.schedule().as_dict(),
-        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "call": "ifx_step_state (state in, one step, state out, one wait) from pinned host buffers",
+                "three_calls_value": e2e3},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": ("k_persist_step<float> (one launch per time step)" if persistent else
                                                 "the step's kernels (one CUDA graph launch per time step)"),

@@ -43,6 +43,7 @@ _SIGS = {
     "ifx_set_field_i": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_size_t]),
     "ifx_set_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t]),
     "ifx_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t]),
+    "ifx_step_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, C.c_size_t]),
     "ifx_write_results": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ifx_forces": (C.c_int, [C.c_void_p, _dp, _dp]),
     "ifx_get_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Stats)]),
@@ -253,6 +254,25 @@ class Solver:
                 raise ValueError(f"out must be three C-contiguous float64 arrays of {nx * ny} values")
         _check(lib().ifx_get_state(self._h, inst, *[_dptr(a) for a in out], nx * ny))
         return tuple(a.reshape(ny, nx) for a in out)
+
+    def step_state(self, u, v, p, n=1, out=None, inst=0):
+        """set_state(u, v, p), step(n) and get_state(out=out) in one call that
+        waits once: each input nx*ny float64 values or None (keep), `out` three
+        C-contiguous float64 arrays of nx*ny values (they may be the inputs) or
+        None (no copy out).  Returns out reshaped to [ny, nx], or None."""
+        nx, ny = self.grid_dims(inst)
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64).ravel() for a in (u, v, p)]
+        for a in arrs:
+            if a is not None and a.size != nx * ny:
+                raise ValueError(f"each field must hold {nx * ny} values")
+        if out is not None:
+            for a in out:
+                if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != nx * ny:
+                    raise ValueError(f"out must be three C-contiguous float64 arrays of {nx * ny} values")
+        ins = [None if a is None else _dptr(a) for a in arrs]
+        outs = [None, None, None] if out is None else [_dptr(a) for a in out]
+        _check(lib().ifx_step_state(self._h, inst, *ins, int(n), *outs, nx * ny))
+        return None if out is None else tuple(a.reshape(ny, nx) for a in out)
 
     def grid_dims(self, inst=0):
         """(nx, ny) including the ghost ring."""

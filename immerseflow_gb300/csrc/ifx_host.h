@@ -70,6 +70,11 @@ struct ifx_solver {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // after ev1: the step's error flag and instance states copied to pinned
+    // host memory, then ev2, so that completing a step takes one wait
+    cudaEvent_t ev2 = nullptr;
+    unsigned int* h_flag = nullptr;  // pinned
+    bool states_enqueued = false;
     double last_ms = 0.0;
     long long launches = 0;
     std::vector<void*> allocs;       // every device allocation, freed at destroy

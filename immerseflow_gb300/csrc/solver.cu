@@ -1175,6 +1175,9 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
     IFX_TRY(dalloc(S, &S->dCtl, 1));
     CUDA_TRY(cudaMallocHost((void**)&S->hS, n * sizeof(InstState)));
     CUDA_TRY(cudaMallocHost((void**)&S->hCtl, sizeof(LoopCtl)));
+    CUDA_TRY(cudaMallocHost((void**)&S->h_flag, sizeof(unsigned int)));
+    *S->h_flag = 0;
+    if (!S->ev2) CUDA_TRY(cudaEventCreateWithFlags(&S->ev2, cudaEventDisableTiming));
     std::memset(S->hS, 0, n * sizeof(InstState));
     CUDA_TRY(cudaMemcpyAsync(S->dI, hI.data(), n * sizeof(InstDev), cudaMemcpyHostToDevice, S->stream));
     // image-point weights of the IBM ghosts
@@ -1570,8 +1573,13 @@ ifx_status build_graph(ifx_solver* S) {
 ifx_status check_states(ifx_solver* S) {
     const int n = (int)S->inst.size();
     if ((int)S->inst_status.size() != n) S->inst_status.assign(n, IFX_OK);
-    CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, n * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
-    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    if (S->states_enqueued) {
+        S->states_enqueued = false;  // copied behind the step, which the caller waited for
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, n * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
+        CUDA_TRY(cudaStreamSynchronize(S->stream));
+    }
+    bool copies = false;
     ifx_status worst = IFX_OK;
     for (int k = 0; k < n; k++) {
         Instance& I = S->inst[k];
@@ -1582,17 +1590,19 @@ ifx_status check_states(ifx_solver* S) {
             S->inst_status[k] = IFX_ERR_GEOMETRY;
             I.dev.retired = 1;
             CUDA_TRY(cudaMemcpyAsync(&S->dI[k].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
+            copies = true;
             if (worst == IFX_OK) worst = IFX_ERR_GEOMETRY;
         } else if (!std::isfinite(s.ppe_rel) || !std::isfinite(s.max_div) || !std::isfinite(s.pred_metric)) {
             S->inst_status[k] = IFX_ERR_DIVERGED;
             I.dev.retired = 1;
             CUDA_TRY(cudaMemcpyAsync(&S->dI[k].retired, &I.dev.retired, sizeof(int), cudaMemcpyHostToDevice, S->stream));
+            copies = true;
             worst = IFX_ERR_DIVERGED;
         } else if (s.ppe_iters >= I.cfg.ppe_itermax && s.ppe_rel > I.cfg.ppe_tol && S->inst_status[k] == IFX_OK) {
             S->inst_status[k] = IFX_ERR_NOT_CONVERGED;
         }
     }
-    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    if (copies) CUDA_TRY(cudaStreamSynchronize(S->stream));  // the host sources of the copies above
     return worst;
 }
 
@@ -1640,6 +1650,14 @@ ifx_status step_launch(ifx_solver* S, int nsteps) {
         for (int s = 0; s < nsteps; s++) IFX_TRY(step_method_host<T>(S));
     }
     CUDA_TRY(cudaEventRecord(S->ev1, S->stream));
+    // the error flag and the instance states follow the steps in the stream,
+    // so that step_finish waits once (ev2) and reads both from pinned memory
+    const unsigned int* flag = mode == 0 ? &S->dBar->err : S->dErr;
+    *S->h_flag = 0;
+    if (flag) CUDA_TRY(cudaMemcpyAsync(S->h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaMemcpyAsync(S->hS, S->dS, S->inst.size() * sizeof(InstState), cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(cudaEventRecord(S->ev2, S->stream));
+    S->states_enqueued = true;
     return IFX_OK;
 }
 
@@ -1648,25 +1666,16 @@ ifx_status step_finish(ifx_solver* S) {
     const int nsteps = S->pending_steps, mode = S->pending_mode;
     if (nsteps == 0) return IFX_OK;
     S->pending_steps = 0;
-    CUDA_TRY(cudaEventSynchronize(S->ev1));
+    CUDA_TRY(cudaEventSynchronize(S->ev2));  // the steps (ev1), then their flag and state copies
     float ms = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
     S->last_ms = ms;
     S->steps_done += nsteps;
-    if (mode == 0) {
-        unsigned int err = 0;
-        CUDA_TRY(cudaMemcpy(&err, &S->dBar->err, sizeof(err), cudaMemcpyDeviceToHost));
-        if (err) {
-            S->poisoned = true;
-            return set_error(IFX_ERR_CUDA, "persistent step: grid barrier timed out");
-        }
-    } else if (S->dErr) {
-        unsigned int err = 0;
-        CUDA_TRY(cudaMemcpy(&err, S->dErr, sizeof(err), cudaMemcpyDeviceToHost));
-        if (err) {
-            S->poisoned = true;
-            return set_error(IFX_ERR_CUDA, "a TMA tile copy did not complete");
-        }
+    if (*S->h_flag) {
+        S->poisoned = true;
+        S->states_enqueued = false;
+        return set_error(IFX_ERR_CUDA, mode == 0 ? "persistent step: grid barrier timed out"
+                                                 : "a TMA tile copy did not complete");
     }
     ifx_status st = check_states(S);
     if (mode == 1) {
@@ -2656,6 +2665,59 @@ extern "C" ifx_status ifx_get_state(ifx_solver* S, int inst, double* u, double* 
     return IFX_OK;
 }
 
+// ifx_set_state, nsteps steps and ifx_get_state in one call: the copies, the
+// layout kernels and the steps are issued back to back on the solver's stream
+// and the call waits once, at the end.
+extern "C" ifx_status ifx_step_state(ifx_solver* S, int inst, const double* u_in, const double* v_in,
+                                     const double* p_in, int nsteps, double* u_out, double* v_out, double* p_out,
+                                     size_t n) {
+    if (!S || inst < 0 || inst >= (int)S->inst.size() || nsteps < 0)
+        return set_error(IFX_ERR_ARG, "ifx_step_state: bad argument");
+    if (S->mode == IFX_MODE_REFERENCE) {  // its step waits on the host every Jacobi sweep anyway
+        if (u_in || v_in || p_in) IFX_TRY(ifx_set_state(S, inst, u_in, v_in, p_in, n));
+        IFX_TRY(ifx_step(S, nsteps));
+        return (u_out || v_out || p_out) ? ifx_get_state(S, inst, u_out, v_out, p_out, n) : IFX_OK;
+    }
+    if (S->pending_steps) IFX_TRY(step_finish(S));
+    const Instance& I = S->inst[inst];
+    if (n != (size_t)I.nx * I.ny) return set_error(IFX_ERR_ARG, "ifx_step_state: size mismatch");
+    CUDA_TRY(cudaSetDevice(S->device));
+    double* f[3];
+    size_t pitch;
+    state_arrays(S, I, f, pitch);
+    double* stage = nullptr;
+    IFX_TRY(state_stage(S, &stage));
+    const double* hi[3] = {u_in, v_in, p_in};
+    if (u_in || v_in || p_in) {
+        double* dst[3];
+        for (int k = 0; k < 3; k++) {
+            dst[k] = hi[k] ? f[k] : nullptr;
+            if (hi[k]) CUDA_TRY(cudaMemcpyAsync(stage + k * n, hi[k], n * 8, cudaMemcpyHostToDevice, S->stream));
+        }
+        CUDA_TRY(launch_state_unpack(stage, dst[0], dst[1], dst[2], I.nx, I.ny, (int)pitch, S->stream));
+        S->launches++;
+    }
+    ifx_status st = IFX_OK;
+    if (nsteps > 0) {
+        st = S->prec == IFX_PREC_FP64 ? step_launch<double>(S, nsteps) : step_launch<float>(S, nsteps);
+        if (st != IFX_OK) {
+            cudaStreamSynchronize(S->stream);  // the input copies read the caller's buffers
+            return st;
+        }
+    }
+    double* ho[3] = {u_out, v_out, p_out};
+    if (u_out || v_out || p_out) {
+        const double* src[3];
+        for (int k = 0; k < 3; k++) src[k] = ho[k] ? f[k] : nullptr;
+        CUDA_TRY(launch_state_pack(src[0], src[1], src[2], stage, I.nx, I.ny, (int)pitch, S->stream));
+        S->launches++;
+        for (int k = 0; k < 3; k++)
+            if (ho[k]) CUDA_TRY(cudaMemcpyAsync(ho[k], stage + k * n, n * 8, cudaMemcpyDeviceToHost, S->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    return step_finish(S);  // the steps' status (its wait has already passed)
+}
+
 extern "C" ifx_status ifx_write_results(ifx_solver* S, const char* dir) {
     if (!S || !dir) return set_error(IFX_ERR_ARG, "ifx_write_results: bad argument");
     if (S->pending_steps) IFX_TRY(step_finish(S));
@@ -2871,10 +2933,12 @@ extern "C" void ifx_destroy(ifx_solver* S) {
     for (void* p : S->allocs) cudaFree(p);
     if (S->hS) cudaFreeHost(S->hS);
     if (S->hCtl) cudaFreeHost(S->hCtl);
+    if (S->h_flag) cudaFreeHost(S->h_flag);
     if (S->h_out) cudaFreeHost(S->h_out);
     if (S->r_iters_h) cudaFreeHost(S->r_iters_h);
     if (S->ev0) cudaEventDestroy(S->ev0);
     if (S->ev1) cudaEventDestroy(S->ev1);
+    if (S->ev2) cudaEventDestroy(S->ev2);
     if (S->stream) cudaStreamDestroy(S->stream);
     delete S;
 }

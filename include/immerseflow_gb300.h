@@ -346,6 +346,16 @@ ifx_status ifx_set_field_i(ifx_solver* s, int inst, int field, const double* hos
  * the whole state in and out every step. */
 ifx_status ifx_set_state(ifx_solver* s, int inst, const double* u, const double* v, const double* p, size_t n);
 ifx_status ifx_get_state(ifx_solver* s, int inst, double* u, double* v, double* p, size_t n);
+/* ifx_set_state, ifx_step(nsteps) and ifx_get_state in one call (no reference
+ * counterpart): the state copies, the steps and the result copies are issued
+ * back to back on the solver's stream and the call waits once, at the end, so
+ * a caller that exchanges the state every step pays one host round trip instead
+ * of three.  NULL inputs keep the device values; NULL outputs are not copied;
+ * inputs and outputs may be the same buffers.  The outputs are written also
+ * when the steps report an error (a diverged instance is flagged, as by
+ * ifx_step); the return value is the steps' status. */
+ifx_status ifx_step_state(ifx_solver* s, int inst, const double* u_in, const double* v_in, const double* p_in,
+                          int nsteps, double* u_out, double* v_out, double* p_out, size_t n);
 /* Writes p.dat, uc.dat, vc.dat, final_results.dat into dir (src/include/postSim.cu:10-66). */
 ifx_status ifx_write_results(ifx_solver* s, const char* dir);
 ifx_status ifx_forces(ifx_solver* s, double* cd, double* cl);

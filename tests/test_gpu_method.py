@@ -348,3 +348,36 @@ def test_state_transfer_matches_field_calls(golden_dir):
         assert np.array_equal(a, b)
     r.set_state(None, None, ref[2] + 1.0)
     assert np.array_equal(r.get(capi.FIELD_P), ref[2] + 1.0)
+
+
+@pytest.mark.parametrize("mode", ["persistent", "graph", "host"])
+def test_step_state_equals_separate_calls(mode):
+    """ifx_step_state (state in, steps, state out, one wait) gives what
+    ifx_set_state + ifx_step + ifx_get_state give, in every execution mode,
+    also with the same buffers for input and output."""
+    c, x, y = small_cylinder(prec=capi.PREC_MIXED)
+    os.environ["IFX_EXEC"] = mode
+    try:
+        a, b = ifx.Solver.create(c, x, y), ifx.Solver.create(c, x, y)
+    finally:
+        del os.environ["IFX_EXEC"]
+    a.step(2)
+    b.step(2)
+    nx, ny = a.grid_dims()
+    state = [f.ravel().copy() for f in a.get_state()]
+    state[0] += 1e-3 * np.sin(np.arange(nx * ny))  # a perturbed velocity passed in
+    for _ in range(3):
+        a.set_state(*state)
+        a.step(2)
+        ra = [f.ravel().copy() for f in a.get_state()]
+        buf = tuple(s.copy() for s in state)
+        rb = b.step_state(*buf, n=2, out=buf)  # in place
+        for u, w in zip(ra, rb):
+            assert np.array_equal(u, w.ravel())
+        assert a.stats().last_ppe_iters == b.stats().last_ppe_iters
+        state = ra
+    # outputs only, and inputs only
+    out = tuple(np.zeros(nx * ny) for _ in range(3))
+    assert b.step_state(None, None, None, n=0, out=out) is not None
+    assert all(np.array_equal(u, w) for u, w in zip(state, out))
+    assert b.step_state(*state, n=1) is None
