@@ -120,8 +120,9 @@ def parse():
                     help="skip the timing of the reference's own CUDA executable")
     ap.add_argument("--profile", default=None, choices=["mixed", "fp64"],
                     help="profiler driver: warm-up steps, then --steps steps inside the NVTX range 'step', no output")
-    ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch", "moving"],
-                    help="workload of --profile: the cylinder, the cylinder heaving (moving), or the batched sweep of --batch instances")
+    ap.add_argument("--profile-workload", default="cylinder", choices=["cylinder", "batch", "moving", "ellipse"],
+                    help="workload of --profile: the cylinder, the cylinder heaving (moving), the 1024x768 "
+                         "ellipse, or the batched sweep of --batch instances")
     ap.add_argument("--profile-rows", type=int, default=1, choices=[1, 4],
                     help="rows per thread of the multigrid tile phases under --profile")
     return ap.parse_args()
@@ -799,6 +800,8 @@ def main():
         if args.profile_workload == "batch":
             specs = cases.batch_sample(count=args.batch, seed=0, precision=prec)
             s = ifx.Solver.batch([c for c, _, _ in specs], [x for _, x, _ in specs], [y for _, _, y in specs])
+        elif args.profile_workload == "ellipse":
+            s = ifx.Solver.create(*cases.ellipse(precision=prec))
         else:
             cfg, _, _ = cases.cylinder(precision=prec)
             if args.profile_workload == "moving":  # heaving as in the moving_body line
