@@ -138,6 +138,7 @@ struct ifx_solver {
     ifx::PersistPlan plan{};
     int persist_grid = 0;            // 0: cooperative launch unavailable
     int persist_full = 0;            // co-resident grid (SMs x blocks per SM, capped): the default
+    int wide_sums = 0;               // some instance has >= 1024 level-0 tile partials (batched reduction loads)
     int persist_sms = 0;             // SMs of the device
     bool poisoned = false;           // a grid barrier timed out: the handle refuses further steps
 

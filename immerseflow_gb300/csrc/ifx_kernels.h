@@ -29,17 +29,20 @@ cudaError_t launch_pred_sweep32(const Tile* t, int nt, const GhostDev* G, int ng
                                 const InstState* S, double* part, int parity, int rows, cudaStream_t s);
 cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng, const InstDev* I, const InstState* S,
                                 int stage, int finalize, const LoopCtl* ctl, int rows, cudaStream_t s);
+// One-block-per-instance reductions of the level-0 tile partials; wide: an
+// instance has thousands of tiles (loads batched four rows at a time).
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
-                               LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
+                               LoopCtl* ctl, unsigned long long handle, cudaStream_t s, int wide = 0);
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, double* part, int to_final,
                             cudaStream_t s);
-cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s);
+cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s,
+                              int wide = 0);
 template <typename T>
 cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                               const GhostDev* G, double* part, int restart_only, const LoopCtl* ctl, int ninst,
                               cudaStream_t s);
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
-                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s);
+                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s, int wide = 0);
 // Finest-level Krylov phases take rows = 1 (32x8 tiles) or MG_ROWS_WIDE (32x32 tiles).
 template <typename T>
 cudaError_t launch_bicg_p(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
@@ -52,7 +55,7 @@ template <typename T>
 cudaError_t launch_bicg_dir_smooth(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                                    const GhostDev* G, int which, int rows, cudaStream_t s);
 cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
-                               cudaStream_t s);
+                               cudaStream_t s, int wide = 0);
 template <typename T>
 cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,
                           int rows, cudaStream_t s);

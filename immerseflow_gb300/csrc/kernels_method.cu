@@ -116,15 +116,17 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<float>(R)) k_pred_refr
     const int nvb = ntiles + (ng + TILE_THREADS - 1) / TILE_THREADS;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) b_pred_refresh<R>(tiles, ntiles, G, ng, I, S, stage, finalize, vb);
 }
+template <bool W>
 __global__ void k_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
-                              unsigned long long handle) { b_pred_reduce(I, S, part, parity, ctl, handle, blockIdx.x); }
+                              unsigned long long handle) { b_pred_reduce<W>(I, S, part, parity, ctl, handle, blockIdx.x); }
 __global__ void __launch_bounds__(TILE_THREADS, 8) k_face_rhs(const Tile* __restrict__ tiles, const InstDev* __restrict__ I,
                            const InstState* __restrict__ S, double* __restrict__ part, int to_final) {
     b_face_rhs(tiles, I, S, part, to_final, blockIdx.x);
 }
+template <bool W>
 __global__ void k_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
-                             const double* __restrict__ part) { b_rhs_reduce(I, S, part, blockIdx.x); }
+                             const double* __restrict__ part) { b_rhs_reduce<W>(I, S, part, blockIdx.x); }
 // restart_only: for a chunk of blockDim instances at a time, every block forms
 // the exclusive prefix sum of the finest-level tile counts of the instances
 // whose restart is due (others count 0; each instance's tiles are contiguous
@@ -174,9 +176,10 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB) k_bicg_start(const Tile* _
         __syncthreads();
     }
 }
+template <bool W>
 __global__ void k_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                 const double* __restrict__ part, int start, int mixed, LoopCtl* ctl,
-                                unsigned long long handle) { b_bicg_reduce_r(I, S, part, start, mixed, ctl, handle, blockIdx.x); }
+                                unsigned long long handle) { b_bicg_reduce_r<W>(I, S, part, start, mixed, ctl, handle, blockIdx.x); }
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_p(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_p<T, R>(tiles, LV, I, S, blockIdx.x); }
@@ -193,8 +196,9 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB) k_bicg_apply(const Tile* _
     pdl_trigger();
     b_bicg_apply<T, R>(tiles, LV, I, S, G, part, e_alt, which, blockIdx.x);
 }
+template <bool W>
 __global__ void k_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
-                              const double* __restrict__ part, int which) { b_bicg_scalar(I, S, part, which, blockIdx.x); }
+                              const double* __restrict__ part, int which) { b_bicg_scalar<W>(I, S, part, which, blockIdx.x); }
 template <typename T, int R>
 __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<T>(R)) k_bicg_s(const Tile* __restrict__ tiles, const LevelDev* __restrict__ LV,
                          const InstDev* __restrict__ I, const InstState* __restrict__ S) { b_bicg_s<T, R>(tiles, LV, I, S, blockIdx.x); }
@@ -348,16 +352,19 @@ cudaError_t launch_pred_refresh(const Tile* t, int nt, const GhostDev* G, int ng
     return cudaGetLastError();
 }
 cudaError_t launch_pred_reduce(const InstDev* I, InstState* S, const double* part, int ninst, int parity,
-                               LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
-    return launch_pdl(k_pred_reduce, ninst, 256, 0, s, I, S, part, parity, ctl, handle);
+                               LoopCtl* ctl, unsigned long long handle, cudaStream_t s, int wide) {
+    if (wide) return launch_pdl(k_pred_reduce<true>, ninst, 256, 0, s, I, S, part, parity, ctl, handle);
+    return launch_pdl(k_pred_reduce<false>, ninst, 256, 0, s, I, S, part, parity, ctl, handle);
 }
 cudaError_t launch_face_rhs(const Tile* t, int nt, const InstDev* I, const InstState* S, double* part, int to_final,
                             cudaStream_t s) {
     k_face_rhs<<<nt, TILE_THREADS, 0, s>>>(t, I, S, part, to_final);
     return cudaGetLastError();
 }
-cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s) {
-    k_rhs_reduce<<<ninst, 256, 0, s>>>(I, S, part);
+cudaError_t launch_rhs_reduce(const InstDev* I, InstState* S, const double* part, int ninst, cudaStream_t s,
+                              int wide) {
+    if (wide) k_rhs_reduce<true><<<ninst, 256, 0, s>>>(I, S, part);
+    else k_rhs_reduce<false><<<ninst, 256, 0, s>>>(I, S, part);
     return cudaGetLastError();
 }
 template <typename T>
@@ -370,8 +377,9 @@ cudaError_t launch_bicg_start(const Tile* t, int nt, const LevelDev* LV, const I
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_reduce_r(const InstDev* I, InstState* S, const double* part, int ninst, int start,
-                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s) {
-    return launch_pdl(k_bicg_reduce_r, ninst, 256, 0, s, I, S, part, start, mixed, ctl, handle);
+                                 int mixed, LoopCtl* ctl, unsigned long long handle, cudaStream_t s, int wide) {
+    if (wide) return launch_pdl(k_bicg_reduce_r<true>, ninst, 256, 0, s, I, S, part, start, mixed, ctl, handle);
+    return launch_pdl(k_bicg_reduce_r<false>, ninst, 256, 0, s, I, S, part, start, mixed, ctl, handle);
 }
 // Finest-level Krylov phases: rows = 1 on 32x8 tiles, MG_ROWS_WIDE on 32x32 tiles.
 template <typename T>
@@ -402,8 +410,9 @@ cudaError_t launch_bicg_apply(const Tile* t, int nt, const LevelDev* LV, const I
     return cudaGetLastError();
 }
 cudaError_t launch_bicg_scalar(const InstDev* I, InstState* S, const double* part, int ninst, int which,
-                               cudaStream_t s) {
-    return launch_pdl(k_bicg_scalar, ninst, 256, 0, s, I, S, part, which);
+                               cudaStream_t s, int wide) {
+    if (wide) return launch_pdl(k_bicg_scalar<true>, ninst, 256, 0, s, I, S, part, which);
+    return launch_pdl(k_bicg_scalar<false>, ninst, 256, 0, s, I, S, part, which);
 }
 template <typename T>
 cudaError_t launch_bicg_s(const Tile* t, int nt, const LevelDev* LV, const InstDev* I, const InstState* S,

@@ -150,14 +150,38 @@ __device__ __forceinline__ double block_max(double v) {
 }
 
 // Per-instance sum of the level-0 tile partials, fixed order; valid in all threads.
-template <int NV>
+// A thread adds rows t, t + B, t + 2B, ... (B threads).  WIDE (instances of
+// thousands of tiles): the loads of four rows are issued before their sums, so
+// the block waits for a quarter of the round trips (same additions in the same
+// order); the plain loop keeps the code of the common case short (a one-block
+// kernel fetches its code cold at every launch).
+template <int NV, bool WIDE = false>
 __device__ __forceinline__ void inst_sum(const double* part, int beg, int cnt, double (&res)[NV]) {
     double acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) acc[k] = 0.0;
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x)
+    if constexpr (WIDE) {
+        const int B = (int)blockDim.x;
+        int t = (int)threadIdx.x;
+        for (; t + 3 * B < cnt; t += 4 * B) {
+            double v[4][NV];
 #pragma unroll
-        for (int k = 0; k < NV; k++) acc[k] += part[(size_t)(beg + t) * NPART + k];
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int k = 0; k < NV; k++) v[u][k] = part[(size_t)(beg + t + u * B) * NPART + k];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int k = 0; k < NV; k++) acc[k] += v[u][k];
+        }
+        for (; t < cnt; t += B)
+#pragma unroll
+            for (int k = 0; k < NV; k++) acc[k] += part[(size_t)(beg + t) * NPART + k];
+    } else {
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x)
+#pragma unroll
+            for (int k = 0; k < NV; k++) acc[k] += part[(size_t)(beg + t) * NPART + k];
+    }
     __shared__ double out[NV];
     block_sum<NV>(acc, out);
 #pragma unroll
@@ -564,6 +588,7 @@ __device__ __forceinline__ void b_pred_sweep(const Tile* __restrict__ tiles, int
     }
 }
 
+template <bool WIDE = false>
 __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int parity, LoopCtl* ctl,
                               unsigned long long handle, int vb) {
@@ -574,7 +599,7 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
     bool active = false, due = false;
     if (st == ST_ACTIVE) {
         double r[1];
-        inst_sum<1>(part, beg, cnt, r);
+        inst_sum<1, WIDE>(part, beg, cnt, r);
         if (threadIdx.x == 0) {
             const int it = S[k].pred_iters + 1;
             S[k].pred_iters = it;
@@ -856,13 +881,14 @@ __device__ __forceinline__ void b_face_rhs(const Tile* __restrict__ tiles, const
     if (threadIdx.x == 0) part[(size_t)vb * NPART] = in.singular ? out[0] : 0.0;
 }
 
+template <bool WIDE = false>
 __device__ __forceinline__ void b_rhs_reduce(const InstDev* __restrict__ I, InstState* __restrict__ S,
                              const double* __restrict__ part, int vb) {
     const int k = vb;
     const InstDev& in = I[k];
     if (in.retired) return;
     double r[1];
-    inst_sum<1>(part, in.tile_beg, in.tile_cnt, r);
+    inst_sum<1, WIDE>(part, in.tile_beg, in.tile_cnt, r);
     if (threadIdx.x == 0) S[k].bmean = in.singular ? r[0] / in.area : 0.0;
 }
 
@@ -945,6 +971,7 @@ __device__ __forceinline__ void b_bicg_start(const Tile* __restrict__ tiles, con
 // the recursive FP32 residual is never accepted; a restart is scheduled when
 // it fell by in.restart_drop (or below the tolerance) since the last one, or
 // after in.restart_every iterations.
+template <bool WIDE = false>
 __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, InstState* __restrict__ S,
                                                 const double* __restrict__ part, int start, int mixed,
                                                 LoopCtl* ctl, unsigned long long handle, int vb) {
@@ -957,7 +984,7 @@ __device__ __forceinline__ void b_bicg_reduce_r(const InstDev* __restrict__ I, I
     pdl_wait();  // the partials of the phase before; every write below
     if (run) {
         double r[4];
-        inst_sum<4>(part, beg, cnt, r);
+        inst_sum<4, WIDE>(part, beg, cnt, r);
         if (threadIdx.x == 0) {
             InstState& st = S[k];
             if (start == 1) {
@@ -1102,6 +1129,7 @@ __device__ __forceinline__ void b_bicg_apply(const Tile* __restrict__ tiles, con
 }
 
 // alpha = rho / (rh, v)   (which = 0)   or   omega = (t, s) / (t, t)   (which = 1)
+template <bool WIDE = false>
 __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, InstState* __restrict__ S,
                               const double* __restrict__ part, int which, int vb) {
     const int k = vb;
@@ -1110,7 +1138,7 @@ __device__ __forceinline__ void b_bicg_scalar(const InstDev* __restrict__ I, Ins
     const int beg = in.tile_beg, cnt = in.tile_cnt;
     pdl_wait();  // the operator apply's partials
     double r[2];
-    inst_sum<2>(part, beg, cnt, r);
+    inst_sum<2, WIDE>(part, beg, cnt, r);
     if (threadIdx.x == 0) {
         if (which == 0) S[k].alpha = r[0] != 0.0 ? S[k].rho / r[0] : 0.0;
         else S[k].omega = r[1] != 0.0 ? r[0] / r[1] : 0.0;

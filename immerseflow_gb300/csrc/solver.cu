@@ -1012,6 +1012,7 @@ ifx_status create_method(ifx_solver* S, int n, const ifx_config* cfgs, const dou
             if (l == 0) {
                 I.tile_beg = (int)hT0.size();
                 I.tile_cnt = (int)tl.size();
+                if (I.tile_cnt >= 4 * 256) S->wide_sums = 1;  // four rows per thread of a 256-thread reduction
                 hT0.insert(hT0.end(), tl.begin(), tl.end());
                 hT0W.insert(hT0W.end(), tw.begin(), tw.end());
             } else {
@@ -1378,14 +1379,14 @@ void seq_pred_body(Seq& q, unsigned long long h) {
         q.add(launch_pred_refresh(t0, nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, S->dCtl, R, st));
         for (int par = 0; par < 2; par++) {
             q.add(launch_pred_sweep32(t0, nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, R, st));
-            q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st));
+            q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st, S->wide_sums));
         }
         return;
     }
     q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 0, st));
-    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st));
+    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 0, S->dCtl, h, st, S->wide_sums));
     q.add(launch_pred_sweep(S->dT0, S->nt0, S->dG, S->ng, S->dI, S->dS, S->dPart, 1, st));
-    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 1, S->dCtl, h, st));
+    q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, 1, S->dCtl, h, st, S->wide_sums));
 }
 
 template <typename T>
@@ -1400,9 +1401,9 @@ void seq_mid(Seq& q) {
     q.add(launch_ghost_fill(S->dG, S->ng, S->dI, 3, S->dGval, st));
     q.n++;
     q.add(launch_face_rhs(S->dT0, S->nt0, S->dI, S->dS, S->dPart, 0, st));
-    q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st));
+    q.add(launch_rhs_reduce(S->dI, S->dS, S->dPart, n, st, S->wide_sums));
     q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 0, nullptr, n, st));
-    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 1, mixed_of<T>(), S->dCtl, 0ull, st, S->wide_sums));
 }
 
 // One BiCGSTAB iteration with two V-cycle preconditioner applications.
@@ -1418,7 +1419,7 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     if (mixed_of<T>()) {
         // FP64 true residual and restart for the instances whose FP32 recursion ran its course
         q.add(launch_bicg_start<T>(S->dT0, S->nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, 1, S->dCtl, n, st));
-        q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st));
+        q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 2, 1, S->dCtl, 0ull, st, S->wide_sums));
     }
     // direction updates fused with the first sweep of the tile V-cycle
     const bool fuse = !S->cmg_use;
@@ -1426,14 +1427,14 @@ void seq_ppe_body(Seq& q, unsigned long long h) {
     else q.add(launch_bicg_p<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
     int e1 = seq_vcycle<T>(q, fuse);
     q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e1, 0, R, st));
-    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 0, st));
+    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 0, st, S->wide_sums));
     if (fuse) q.add(launch_bicg_dir_smooth<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, 1, R, st));
     else q.add(launch_bicg_s<T>(t0, nt0, S->dLV, S->dI, S->dS, R, st));
     int e2 = seq_vcycle<T>(q, fuse);
     q.add(launch_bicg_apply<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dG, S->dPart, e2, 1, R, st));
-    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st));
+    q.add(launch_bicg_scalar(S->dI, S->dS, S->dPart, n, 1, st, S->wide_sums));
     q.add(launch_bicg_x<T>(t0, nt0, S->dLV, S->dI, S->dS, S->dPart, R, st));
-    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, mixed_of<T>(), S->dCtl, h, st));
+    q.add(launch_bicg_reduce_r(S->dI, S->dS, S->dPart, n, 0, mixed_of<T>(), S->dCtl, h, st, S->wide_sums));
 }
 
 void seq_post(Seq& q) {
