@@ -51,22 +51,31 @@ __global__ void k_mark_ghosts(const InstDev* __restrict__ I, int inst, uint8_t* 
     if (g) type[id] = T_GHOST;
 }
 
-// Closest point on x^2/e0^2 + y^2/e1^2 = 1 (e0 >= e1) to (y0, y1) >= 0:
-// bisection of D. Eberly, "Distance from a point to an ellipse, an
-// ellipsoid, or a hyperellipsoid" (Geometric Tools, 2013).
+// Closest point on x^2/e0^2 + y^2/e1^2 = 1 (e0 >= e1) to (y0, y1) >= 0, after
+// D. Eberly, "Distance from a point to an ellipse, an ellipsoid, or a
+// hyperellipsoid" (Geometric Tools, 2013): the root s of
+// G(s) = (r0 z0 / (s + r0))^2 + (z1 / (s + 1))^2 - 1 in Eberly's bracket, by
+// Newton's method from s = 0 (G convex and decreasing: monotone from the left
+// of the root, one step from the right lands left of it), a step outside the
+// bracket replaced by bisection.  A few steps with three divisions each instead
+// of ~60 halvings with two; the same operations as the CPU restatement.
 __device__ double ell_root(double r0, double z0, double z1, double g) {
     const double n0 = r0 * z0;
     double s0 = z1 - 1.0;
     double s1 = (g < 0.0 ? 0.0 : sqrt(n0 * n0 + z1 * z1) - 1.0);
     double s = 0.0;
     for (int k = 0; k < 200; k++) {
-        s = 0.5 * (s0 + s1);
-        if (s == s0 || s == s1) break;
-        const double ra = n0 / (s + r0), rb = z1 / (s + 1.0);
+        const double i0 = 1.0 / (s + r0), i1 = 1.0 / (s + 1.0);
+        const double ra = n0 * i0, rb = z1 * i1;
         const double gg = ra * ra + rb * rb - 1.0;
         if (gg > 0.0) s0 = s;
         else if (gg < 0.0) s1 = s;
         else break;
+        const double dg = -2.0 * (ra * ra * i0 + rb * rb * i1);
+        double sn = s - gg / dg;
+        if (!(sn > s0 && sn < s1)) sn = 0.5 * (s0 + s1);  // outside the bracket (or not a number)
+        if (sn == s || sn == s0 || sn == s1) break;
+        s = sn;
     }
     return s;
 }

@@ -365,22 +365,33 @@ enum { B_E = 1, B_W = 2, B_N = 4, B_S = 8 };
 inline double rcp_approx(double d) { return (double)(1.0f / (float)d); }
 
 // Closest point on the axis-aligned ellipse x^2/e0^2 + y^2/e1^2 = 1 (e0 >= e1)
-// to (y0, y1) in the first quadrant: the bisection method of D. Eberly,
-// "Distance from a point to an ellipse, an ellipsoid, or a hyperellipsoid"
-// (Geometric Tools, 2013).  The CUDA path runs the same bisection.
+// to (y0, y1) in the first quadrant, after D. Eberly, "Distance from a point to
+// an ellipse, an ellipsoid, or a hyperellipsoid" (Geometric Tools, 2013): the
+// root s of G(s) = (r0 z0 / (s + r0))^2 + (z1 / (s + 1))^2 - 1 in Eberly's
+// bracket [z1 - 1, s1].  G is convex and decreasing there, so Newton's method
+// from a point left of the root climbs to it monotonically, and from the right
+// its first step lands left of it; a step that leaves the bracket is replaced by
+// the bisection of the bracket.  Starts at s = 0, where G = g (the points are
+// within a few cells of the boundary, so the root is near 0): a few steps
+// instead of the ~60 halvings of plain bisection.  The CUDA path runs the same
+// operations (IEEE division and square root, no contraction).
 double ell_root(double r0, double z0, double z1, double g) {
     double n0 = r0 * z0;
     double s0 = z1 - 1.0;
     double s1 = (g < 0.0 ? 0.0 : std::sqrt(n0 * n0 + z1 * z1) - 1.0);
     double s = 0.0;
     for (int k = 0; k < 200; k++) {
-        s = 0.5 * (s0 + s1);
-        if (s == s0 || s == s1) break;
-        double ra = n0 / (s + r0), rb = z1 / (s + 1.0);
+        double i0 = 1.0 / (s + r0), i1 = 1.0 / (s + 1.0);
+        double ra = n0 * i0, rb = z1 * i1;
         double gg = ra * ra + rb * rb - 1.0;
         if (gg > 0.0) s0 = s;
         else if (gg < 0.0) s1 = s;
         else break;
+        double dg = -2.0 * (ra * ra * i0 + rb * rb * i1);
+        double sn = s - gg / dg;
+        if (!(sn > s0 && sn < s1)) sn = 0.5 * (s0 + s1);  // outside the bracket (or not a number)
+        if (sn == s || sn == s0 || sn == s1) break;
+        s = sn;
     }
     return s;
 }
