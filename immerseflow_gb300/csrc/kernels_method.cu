@@ -74,8 +74,11 @@ __global__ void __launch_bounds__(TILE_THREADS, mg_blocks<double>(1)) k_pred_swe
     pdl_trigger();
     b_pred_sweep(tiles, ntiles, G, ng, I, S, part, parity, blockIdx.x);
 }
+// one-row variant: five blocks per SM (48 registers), as before the inner
+// cycle's FP64 defect moved into the sweep (its branch runs one sweep in
+// mixed_inner and may spill)
 template <int R>
-__global__ void __launch_bounds__(TILE_THREADS, mg_blocks<float>(R)) k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
+__global__ void __launch_bounds__(TILE_THREADS, R == 1 ? 5 : mg_blocks<float>(R)) k_pred_sweep32(const Tile* __restrict__ tiles, int ntiles, const GhostDev* __restrict__ G, int ng,
                                const LevelDev* __restrict__ LV, const InstDev* __restrict__ I,
                                const InstState* __restrict__ S, double* __restrict__ part, int parity) {
     pdl_trigger();

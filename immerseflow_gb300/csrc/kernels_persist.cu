@@ -33,16 +33,6 @@ __device__ __forceinline__ bool any_pred_active(const InstState* S, int n) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) a |= (*(const volatile int*)&S[k].pred_state == ST_ACTIVE);
     return __syncthreads_or(a) != 0;
 }
-__device__ __forceinline__ bool any_pred_refresh_due(const InstDev* I, const InstState* S, int n) {
-    int a = 0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        InstState s;
-        s.pred_state = *(const volatile int*)&S[k].pred_state;
-        s.pred_iters = *(const volatile int*)&S[k].pred_iters;
-        a |= pred_refresh_due(I[k], s);
-    }
-    return __syncthreads_or(a) != 0;
-}
 __device__ __forceinline__ bool any_restart_due(const InstState* S, int n) {
     int a = 0;
     for (int k = threadIdx.x; k < n; k += blockDim.x)
@@ -135,12 +125,7 @@ __device__ bool one_step(const PersistPlan& P, unsigned long long& ep) {
     constexpr bool mixed32 = sizeof(T) == 4;
     for (int pair = 0; pair < P.pred_pairs; pair++) {
         if (mixed32) {
-            if (any_pred_refresh_due(P.I, P.S, n)) {
-                FOR_VB(npred) b_pred_refresh(P.t0, P.nt0, P.G, P.ng, P.I, P.S, 0, 0, vb);
-                BAR();
-                FOR_VB(npred) b_pred_refresh(P.t0, P.nt0, P.G, P.ng, P.I, P.S, 1, 0, vb);
-                BAR();
-            }
+            // the FP64 refresh of each inner cycle runs inside the sweeps that start and end it
             for (int par = 0; par < 2; par++) {
                 FOR_VB(npred) b_pred_sweep32(P.t0, P.nt0, P.G, P.ng, P.LV, P.I, P.S, P.part, par, vb);
                 BAR();

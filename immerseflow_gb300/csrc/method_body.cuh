@@ -624,6 +624,11 @@ __device__ __forceinline__ void b_pred_reduce(const InstDev* __restrict__ I, Ins
 // mixed_inner sweeps q0 absorbs d and r0 is recomputed in FP64 (defect
 // correction): rounding never accumulates into the state.  The sweep metric
 // (sum |update|) and the stop rule are those of the FP64 path.
+// The refresh is folded into the sweeps (mixed_inner >= 2): the sweep that
+// ends an inner cycle stores q0 + d instead of d (and d = 0), the sweep that
+// starts the next one forms r0 from q0 first (its own cell; q0 is not written
+// in that launch).  The first sweep of a step starts a cycle with d = 0 (the
+// step before ended with q = q0 + d, d = 0).
 
 __device__ __forceinline__ bool pred_refresh_due(const InstDev& in, const InstState& s) {
     return s.pred_state == ST_ACTIVE && s.pred_iters % (in.mixed_inner > 0 ? in.mixed_inner : 8) == 0;
@@ -734,6 +739,15 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
                 }
             return;
         }
+        // inner cycle of mixed_inner sweeps: this sweep starts one (FP64 defect
+        // of q0 first) and / or ends one (q0 absorbs the new correction)
+        const int mi = in.mixed_inner > 0 ? in.mixed_inner : 8, it = S[t.inst].pred_iters;
+        const bool cyc_start = it % mi == 0, cyc_end = (it + 1) % mi == 0;
+        if (cyc_start) {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                if (fl[r]) pred_refresh_cell(in, id[r], nullptr, 1, 0);
+        }
         const float dtre = (float)in.dtre;
         const float ixi = __ldg(&L.ixf[ic]);
         const float aE = dtre * (__ldg(&L.kxf[ic]) * ixi), aW = dtre * (__ldg(&L.kxf[ic - 1]) * ixi);
@@ -751,8 +765,16 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
                               aP * sv[q]) * di;
             m[r][0] = 0.0f;
             if (fl[r]) {
-                du[q] = su[q] + dU;
-                dv[q] = sv[q] + dV;
+                const float nu = su[q] + dU, nv = sv[q] + dV;
+                if (cyc_end) {
+                    in.u[q] += (double)nu;
+                    in.v[q] += (double)nv;
+                    du[q] = 0.0f;
+                    dv[q] = 0.0f;
+                } else {
+                    du[q] = nu;
+                    dv[q] = nv;
+                }
                 m[r][0] = fabsf(dU) + fabsf(dV);
             }
         }
@@ -774,14 +796,23 @@ __device__ __forceinline__ void b_pred_sweep32(const Tile* __restrict__ tiles, i
             dv[gh.cell] = sv[gh.cell];
             return;
         }
+        const int mi = in.mixed_inner > 0 ? in.mixed_inner : 8, it = S[gh.inst].pred_iters;
+        if (it % mi == 0) pred_refresh_cell(in, gh.cell, &gh, 1, 0);
         float au = in.rfu[gh.cell], av = in.rfv[gh.cell];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             au += (float)gh.wu[k] * su[gh.nb[k]];
             av += (float)gh.wv[k] * sv[gh.nb[k]];
         }
-        du[gh.cell] = au;
-        dv[gh.cell] = av;
+        if ((it + 1) % mi == 0) {
+            in.u[gh.cell] += (double)au;
+            in.v[gh.cell] += (double)av;
+            du[gh.cell] = 0.0f;
+            dv[gh.cell] = 0.0f;
+        } else {
+            du[gh.cell] = au;
+            dv[gh.cell] = av;
+        }
     }
 }
 

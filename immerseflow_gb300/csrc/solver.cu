@@ -651,7 +651,7 @@ ifx_status validate(const ifx_config* c) {
     if (c->mg_pre < 1 || c->mg_post < 1) return set_error(IFX_ERR_ARG, "multigrid sweeps must be >= 1");
     if (!(c->mg_omega > 0 && c->mg_omega < 2)) return set_error(IFX_ERR_ARG, "multigrid omega must lie in (0, 2)");
     if (c->coarse_sweeps < 1 || c->coarse_sweeps > 10000) return set_error(IFX_ERR_ARG, "coarse sweeps must lie in 1..10000");
-    if (c->mixed_inner < 1) return set_error(IFX_ERR_ARG, "mixed_inner must be >= 1");
+    if (c->mixed_inner < 2) return set_error(IFX_ERR_ARG, "mixed_inner must be >= 2");
     if (!(c->restart_drop > 0 && c->restart_drop < 1) || c->restart_every < 1)
         return set_error(IFX_ERR_ARG, "defect correction: restart_drop in (0, 1), restart_every >= 1");
     if (c->ad_itermax < 1 || c->ppe_itermax < 0) return set_error(IFX_ERR_ARG, "bad iteration caps");
@@ -1375,8 +1375,7 @@ void seq_pred_body(Seq& q, unsigned long long h) {
         const int R = S->mg_rows;
         const Tile* t0 = R == MG_ROWS_WIDE ? S->dT0W : S->dT0;
         const int nt0 = R == MG_ROWS_WIDE ? S->nt0W : S->nt0;
-        q.add(launch_pred_refresh(t0, nt0, S->dG, S->ng, S->dI, S->dS, 0, 0, S->dCtl, R, st));
-        q.add(launch_pred_refresh(t0, nt0, S->dG, S->ng, S->dI, S->dS, 1, 0, S->dCtl, R, st));
+        // the FP64 refresh of each inner cycle runs inside the sweeps that start and end it
         for (int par = 0; par < 2; par++) {
             q.add(launch_pred_sweep32(t0, nt0, S->dG, S->ng, S->dLV, S->dI, S->dS, S->dPart, par, R, st));
             q.add(launch_pred_reduce(S->dI, S->dS, S->dPart, n, par, S->dCtl, h, st, S->wide_sums));
@@ -2306,7 +2305,7 @@ ifx_status check_schedule(const ifx_schedule* s) {
     if (!(s->mg_omega > 0 && s->mg_omega < 2)) return set_error(IFX_ERR_ARG, "schedule: omega must lie in (0, 2)");
     if (s->coarse_sweeps < 1 || s->coarse_sweeps > 10000)
         return set_error(IFX_ERR_ARG, "schedule: coarse sweeps must lie in 1..10000");
-    if (s->mixed_inner < 1) return set_error(IFX_ERR_ARG, "schedule: mixed_inner must be >= 1");
+    if (s->mixed_inner < 2) return set_error(IFX_ERR_ARG, "schedule: mixed_inner must be >= 2");
     if (!(s->restart_drop > 0 && s->restart_drop < 1) || s->restart_every < 1)
         return set_error(IFX_ERR_ARG, "schedule: restart_drop in (0, 1), restart_every >= 1");
     return IFX_OK;

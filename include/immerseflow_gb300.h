@@ -128,7 +128,8 @@ typedef struct ifx_config {
     double ad_tol;                 /* method mode: mean |Jacobi update| bound   */
     int    mg_pre, mg_post;        /* multigrid smoothing sweeps                */
     double mg_omega;               /* weighted-Jacobi factor                    */
-    int    mixed_inner;            /* FP32 predictor sweeps per FP64 residual   */
+    int    mixed_inner;            /* FP32 predictor sweeps per FP64 residual
+                                      (at least 2)                              */
     double force_ref_u, force_ref_len;   /* drag/lift normalisation          */
     int    ppe_method;             /* IFX_PPE_*: REFERENCE-mode pressure solve  */
     double relax_ad, relax_ppe;    /* w-AD, w-PPE as read (0 or 1: none)        */
@@ -263,7 +264,7 @@ typedef struct ifx_schedule {
     double mg_omega;               /* weighted-Jacobi factor                    */
     int    coarse_sweeps;          /* red-black SOR sweeps on the coarsest level */
     int    mixed_inner;            /* mixed path: FP32 predictor sweeps per FP64
-                                      defect                                    */
+                                      defect (at least 2)                       */
     double restart_drop;           /* mixed path: FP32 Krylov recursion restarted
                                       from the FP64 true residual after this drop */
     int    restart_every;          /* ... or after this many iterations         */
