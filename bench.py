@@ -199,11 +199,12 @@ def measured_peak():
 
 
 def committed_traffic():
-    """DRAM bytes of one cylinder step (L2 flushed before it, as before every
-    timed step) from the committed ncu launch list of the step's kernels: the
-    sum of dram__bytes_read.sum + dram__bytes_write.sum over its launches."""
+    """DRAM bytes of one cylinder step past the impulsive start (step 201, L2
+    flushed before it, as before every timed step) from the committed ncu launch
+    list of the step's kernels: the sum of dram__bytes_read.sum +
+    dram__bytes_write.sum over its launches."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "launch_list_cylinder_384x256_host.md")):
+        for line in open(os.path.join(ROOT, "profiles", "launch_list_cylinder_384x256_step201.md")):
             if line.startswith("traffic_bytes_per_step:"):
                 return float(line.split(":")[1])
     except Exception:
