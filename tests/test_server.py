@@ -48,7 +48,7 @@ def test_reference_mode_case_is_refused():
 
 
 @pytest.mark.parametrize("field,value", [("re", -1.0), ("dt", 0.0), ("mg_pre", 0), ("ppe_method", capi.PPE_LINE_SOR),
-                                         ("nx", 1 << 28), ("closed_box_body", None)])
+                                         ("nx", 1 << 28), ("closed_box_body", None), ("mixed_inner", 1)])
 def test_invalid_request_refused_at_submit(field, value):
     """A configuration the solver would refuse is refused at submit, not when its
     cohort is created (which would fail the requests admitted with it)."""
