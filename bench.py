@@ -18,8 +18,8 @@ value     : interior cells x steps / device time of the timed steps (CUDA
 e2e       : same metric through the C ABI with the state copied from pinned
             host buffers and the result copied back every step, wall clock
             (ifx_step_state: copies in, the step and copies out in one call
-            that waits once; three_calls_value: the same through
-            ifx_set_state, ifx_step and ifx_get_state);
+            that waits once; three_calls_value: the same steps again, from
+            a checkpoint, through ifx_set_state, ifx_step and ifx_get_state);
 plain_fp64: the same steps with every kernel in FP64;
 roofline  : the step's kernels as the autotuner runs them (one CUDA-graph
             launch per step, or the persistent per-step kernel); achieved =
@@ -878,6 +878,7 @@ def main():
     nx, ny = s.grid_dims()
     host = tuple(torch.empty(nx * ny, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3))
     s.get_state(out=host)
+    snap = s.checkpoint()  # the three-call timing below repeats the same steps
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -887,7 +888,9 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * cells * args.steps / e2e_s / 1e6
     nbytes = 3 * nx * ny * 8
-    # the same exchange through three calls, each waiting (ifx_set_state, ifx_step, ifx_get_state)
+    # the same steps through three calls, each waiting (ifx_set_state, ifx_step, ifx_get_state)
+    s.restore(snap)
+    s.get_state(out=host)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
