@@ -876,7 +876,9 @@ def main():
 
     # end to end through the C ABI: pinned host state in, result out, every step
     nx, ny = s.grid_dims()
-    host = tuple(torch.empty(nx * ny, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3))
+    # u, v, p back to back in one pinned allocation: one copy each way per step
+    pinned = torch.empty(3 * nx * ny, dtype=torch.float64, pin_memory=True).numpy()
+    host = tuple(pinned[k * nx * ny:(k + 1) * nx * ny] for k in range(3))
     s.get_state(out=host)
     snap = s.checkpoint()  # the three-call timing below repeats the same steps
     barrier()

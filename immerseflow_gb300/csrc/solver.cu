@@ -2601,6 +2601,30 @@ ifx_status state_stage(ifx_solver* S, double** out) {
     return IFX_OK;
 }
 
+// Host copies of u, v, p (n values each; NULL: skip that field) to or from the
+// dense staging buffer: one copy when the three lie back to back in one host
+// allocation (v = u + n, p = v + n), as in the staging buffer, else one each.
+cudaError_t copy_state_in(double* stage, const double* const h[3], size_t n, cudaStream_t st) {
+    if (h[0] && h[1] == h[0] + n && h[2] == h[1] + n)
+        return cudaMemcpyAsync(stage, h[0], 3 * n * 8, cudaMemcpyHostToDevice, st);
+    for (int k = 0; k < 3; k++)
+        if (h[k]) {
+            const cudaError_t e = cudaMemcpyAsync(stage + k * n, h[k], n * 8, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+cudaError_t copy_state_out(double* const h[3], const double* stage, size_t n, cudaStream_t st) {
+    if (h[0] && h[1] == h[0] + n && h[2] == h[1] + n)
+        return cudaMemcpyAsync(h[0], stage, 3 * n * 8, cudaMemcpyDeviceToHost, st);
+    for (int k = 0; k < 3; k++)
+        if (h[k]) {
+            const cudaError_t e = cudaMemcpyAsync(h[k], stage + k * n, n * 8, cudaMemcpyDeviceToHost, st);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
 // The device arrays of u, v, p of one instance and their row pitch.
 void state_arrays(ifx_solver* S, const Instance& I, double* (&f)[3], size_t& pitch) {
     if (S->mode == IFX_MODE_REFERENCE) {
@@ -2632,10 +2656,8 @@ extern "C" ifx_status ifx_set_state(ifx_solver* S, int inst, const double* u, co
     IFX_TRY(state_stage(S, &stage));
     const double* h[3] = {u, v, p};
     double* dst[3];
-    for (int k = 0; k < 3; k++) {
-        dst[k] = h[k] ? f[k] : nullptr;
-        if (h[k]) CUDA_TRY(cudaMemcpyAsync(stage + k * n, h[k], n * 8, cudaMemcpyHostToDevice, S->stream));
-    }
+    for (int k = 0; k < 3; k++) dst[k] = h[k] ? f[k] : nullptr;
+    CUDA_TRY(copy_state_in(stage, h, n, S->stream));
     CUDA_TRY(launch_state_unpack(stage, dst[0], dst[1], dst[2], I.nx, I.ny, (int)pitch, S->stream));
     S->launches++;
     CUDA_TRY(cudaStreamSynchronize(S->stream));
@@ -2659,8 +2681,7 @@ extern "C" ifx_status ifx_get_state(ifx_solver* S, int inst, double* u, double* 
     for (int k = 0; k < 3; k++) src[k] = h[k] ? f[k] : nullptr;
     CUDA_TRY(launch_state_pack(src[0], src[1], src[2], stage, I.nx, I.ny, (int)pitch, S->stream));
     S->launches++;
-    for (int k = 0; k < 3; k++)
-        if (h[k]) CUDA_TRY(cudaMemcpyAsync(h[k], stage + k * n, n * 8, cudaMemcpyDeviceToHost, S->stream));
+    CUDA_TRY(copy_state_out(h, stage, n, S->stream));
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     return IFX_OK;
 }
@@ -2690,10 +2711,8 @@ extern "C" ifx_status ifx_step_state(ifx_solver* S, int inst, const double* u_in
     const double* hi[3] = {u_in, v_in, p_in};
     if (u_in || v_in || p_in) {
         double* dst[3];
-        for (int k = 0; k < 3; k++) {
-            dst[k] = hi[k] ? f[k] : nullptr;
-            if (hi[k]) CUDA_TRY(cudaMemcpyAsync(stage + k * n, hi[k], n * 8, cudaMemcpyHostToDevice, S->stream));
-        }
+        for (int k = 0; k < 3; k++) dst[k] = hi[k] ? f[k] : nullptr;
+        CUDA_TRY(copy_state_in(stage, hi, n, S->stream));
         CUDA_TRY(launch_state_unpack(stage, dst[0], dst[1], dst[2], I.nx, I.ny, (int)pitch, S->stream));
         S->launches++;
     }
@@ -2711,8 +2730,7 @@ extern "C" ifx_status ifx_step_state(ifx_solver* S, int inst, const double* u_in
         for (int k = 0; k < 3; k++) src[k] = ho[k] ? f[k] : nullptr;
         CUDA_TRY(launch_state_pack(src[0], src[1], src[2], stage, I.nx, I.ny, (int)pitch, S->stream));
         S->launches++;
-        for (int k = 0; k < 3; k++)
-            if (ho[k]) CUDA_TRY(cudaMemcpyAsync(ho[k], stage + k * n, n * 8, cudaMemcpyDeviceToHost, S->stream));
+        CUDA_TRY(copy_state_out(ho, stage, n, S->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(S->stream));
     return step_finish(S);  // the steps' status (its wait has already passed)

@@ -376,6 +376,20 @@ def test_step_state_equals_separate_calls(mode):
             assert np.array_equal(u, w.ravel())
         assert a.stats().last_ppe_iters == b.stats().last_ppe_iters
         state = ra
+    # u, v, p back to back in one allocation (one copy each way), against the separate calls
+    big = np.concatenate(state)
+    views = tuple(big[k * nx * ny:(k + 1) * nx * ny] for k in range(3))
+    a.set_state(*state)
+    a.step(1)
+    ra = [f.ravel().copy() for f in a.get_state()]
+    b.step_state(*views, n=1, out=views)
+    for u, w in zip(ra, views):
+        assert np.array_equal(u, w)
+    got = tuple(np.zeros(nx * ny) for _ in range(3))
+    b.set_state(*views)  # contiguous in, separate out
+    b.get_state(out=got)
+    assert all(np.array_equal(u, w) for u, w in zip(views, got))
+    state = ra
     # outputs only, and inputs only
     out = tuple(np.zeros(nx * ny) for _ in range(3))
     assert b.step_state(None, None, None, n=0, out=out) is not None
